@@ -1,0 +1,113 @@
+/* dmsc.h -- C ABI of the GB300 grid Morse-Smale complex library (libdmsc.so).
+ *
+ * The reference (nithins/mscomplex) has no plugin or FFI API: its hot path is
+ * the C++ class GridDataset (dmsc/include/grid_dataset.h) driven by
+ * GridDataManager (dmsc/src/grid_datamanager.cpp), with an OpenCL backend
+ * selected by a bool.  Every entry point below replaces one of those calls;
+ * the citation on each names the reference interface it stands in for.
+ *
+ * Conventions
+ *  - Every function returns DMSC_OK (0) or a DMSC_ERR_* code; the message of
+ *    the last error of the calling thread is dmsc_last_error().
+ *  - Cell ids are (x, y) pairs of int16 in the reference's refined-grid
+ *    coordinates: vertex (i, j) is cell (2i, 2j), cell dimension is
+ *    (x & 1) + (y & 1).  A rect is {left, bottom, right, top} in cell coords.
+ *  - `stream` is a cudaStream_t (NULL = the context's own stream).  Export
+ *    functions write HOST buffers and return after the copy completes.
+ *  - Inputs containing NaN are outside the supported domain (the reference's
+ *    vertex comparison is not a strict weak order on NaN) and are rejected
+ *    with DMSC_ERR_INPUT.
+ */
+#ifndef DMSC_H_
+#define DMSC_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct dmsc_ctx dmsc_ctx;
+typedef struct dmsc_dataset dmsc_dataset;
+typedef struct dmsc_msc dmsc_msc;
+
+enum {
+  DMSC_OK = 0,
+  DMSC_ERR_BAD_ARG = 1,        /* invalid argument (null pointer, bad rect) */
+  DMSC_ERR_OOM = 2,            /* device allocation failed */
+  DMSC_ERR_CUDA = 3,           /* CUDA runtime error */
+  DMSC_ERR_INT16_OVERFLOW = 4, /* grid exceeds the int16 cell-id range (16384 vertices per side) */
+  DMSC_ERR_DEVICE_TIMEOUT = 5, /* a bounded device loop ran out of iterations */
+  DMSC_ERR_INVARIANT = 6,      /* a reference std::logic_error condition */
+  DMSC_ERR_INPUT = 7,          /* input outside the supported domain (NaN heights) */
+  DMSC_ERR_STATE = 8           /* call out of order (e.g. export before work) */
+};
+
+/* Message of the calling thread's last error ("" if none). */
+const char *dmsc_last_error(void);
+
+/* GridDataset::init_opencl() -- process-wide device setup
+ * (dmsc/include/grid_dataset.h:236, dmsc/src/grid_dataset.cpp:186-226). */
+int dmsc_init(int device, dmsc_ctx **out);
+/* GridDataset::stop_opencl() (dmsc/include/grid_dataset.h:238). */
+int dmsc_shutdown(dmsc_ctx *ctx);
+
+/* GridDataset::GridDataset(const rect_t &r, const rect_t &e)
+ * (dmsc/src/grid_dataset.cpp:1429-1441). */
+int dmsc_dataset_create(dmsc_ctx *ctx, const int16_t rect[4], const int16_t ext[4], dmsc_dataset **out);
+/* GridDataset::clear() / ~GridDataset() (dmsc/src/grid_dataset.cpp:1456-1509). */
+int dmsc_dataset_destroy(dmsc_dataset *ds);
+/* GridDataset::init(cell_fn_t *) (dmsc/src/grid_dataset.cpp:1461-1484): the
+ * heights of the ext window, x fastest, `pitch` elements between rows.
+ * on_device = 0: host pointer (copied); 1: device pointer (borrowed, must stay
+ * valid until the dataset is destroyed or re-initialised). */
+int dmsc_dataset_init(dmsc_dataset *ds, const float *heights, int64_t pitch, int on_device, void *stream);
+/* GridDataset::work() / work_ocl() (dmsc/src/grid_dataset.cpp:1734-1741,
+ * 353-399): gradient, critical-cell collation and owner extrema. */
+int dmsc_dataset_work(dmsc_dataset *ds, void *stream);
+/* m_critical_cells.size() (dmsc/include/grid_dataset.h:81). */
+int dmsc_dataset_num_critical(dmsc_dataset *ds, int64_t *n);
+/* m_cell_flags, m_cell_pairs, m_cell_own (dmsc/include/grid_dataset.h:78-80)
+ * in the reference layout: C order [x][y] over ext (y fastest); flags int8,
+ * pairs and own as (x, y) int16 pairs, (-1,-1) where unset.  Any output
+ * pointer may be NULL. */
+int dmsc_dataset_export_cells(dmsc_dataset *ds, int8_t *flags, int16_t *pairs, int16_t *own, void *stream);
+/* m_critical_cells (dmsc/src/grid_dataset.cpp:1822-1832): (x, y) int16 pairs in
+ * collation (row-major) order. */
+int dmsc_dataset_export_critical(dmsc_dataset *ds, int16_t *cellids, void *stream);
+/* GridDataset::writeout_connectivity(mscomplex_t *) (dmsc/src/grid_dataset.cpp:
+ * 1858-1907) / writeout_connectivity_ocl (:1250-1283): a new complex. */
+int dmsc_dataset_writeout_connectivity(dmsc_dataset *ds, dmsc_msc **out, void *stream);
+
+/* GridMSComplex::clear() (dmsc/src/grid_mscomplex.cpp:324-329). */
+int dmsc_msc_destroy(dmsc_msc *msc);
+/* Sizes of a complex: [0] critical points, [1] asc entries, [2] des entries,
+ * [3] asc_disc cells, [4] des_disc cells. */
+int dmsc_msc_sizes(dmsc_msc *msc, int64_t sizes[5]);
+/* MSComplex<cellid_t> (dmsc/include/discreteMorseDS.h:78-143) in flat form:
+ * rect_ext = m_rect then m_ext_rect; per critical point its cell id, m_cp_fns
+ * value, pair_idx, flags (bit0 isCancelled, bit1 isOnStrangulationPath,
+ * bit2 isBoundryCancelable); the asc/des multisets as CSR (offsets have
+ * ncp+1 entries, each segment ascending with multiplicity); asc_disc/des_disc
+ * as CSR of (x, y) cell ids.  Any output pointer may be NULL. */
+int dmsc_msc_export(dmsc_msc *msc, int16_t rect_ext[8], int16_t *cellid, float *fn, uint32_t *pair_idx,
+                    uint8_t *flags, uint32_t *asc_off, uint32_t *asc, uint32_t *des_off, uint32_t *des,
+                    uint32_t *adisc_off, int16_t *adisc, uint32_t *ddisc_off, int16_t *ddisc, void *stream);
+
+/* Tracing: the reference's compile-time _LOG_TIMINGS stage timers
+ * (dmsc/src/grid_dataset.cpp:19-34, 357-390).  When enabled, CUDA events are
+ * recorded on the launching stream around every stage of work and
+ * writeout_connectivity. */
+int dmsc_set_timing(dmsc_ctx *ctx, int enable);
+/* Stage times in ms of the dataset's last work + writeout_connectivity:
+ * [0] gradient, [1] collation scan, [2] border resolve, [3] owner labels and
+ * arcs, [4] connectivity CSR.  Writes min(n, 5) floats. */
+int dmsc_dataset_stage_times(dmsc_dataset *ds, float *ms, int n);
+/* Kernels launched by this library so far in this process. */
+int dmsc_kernel_launches(uint64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DMSC_H_ */

@@ -1,0 +1,86 @@
+"""ctypes binding of libdmsc.so (include/dmsc.h).
+
+The library is the only implementation of the hot path: if it is missing or
+fails to load, every call raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+DMSC_OK = 0
+ERRORS = {
+    1: "BAD_ARG", 2: "OOM", 3: "CUDA", 4: "INT16_OVERFLOW", 5: "DEVICE_TIMEOUT",
+    6: "INVARIANT", 7: "INPUT", 8: "STATE",
+}
+
+# Every extern "C" entry point declared in include/dmsc.h, with its argument types.
+_vp, _i64, _i32, _f64 = C.c_void_p, C.c_int64, C.c_int, C.c_double
+SIGNATURES = {
+    "dmsc_last_error": ([], C.c_char_p),
+    "dmsc_init": ([_i32, _vp], _i32),
+    "dmsc_shutdown": ([_vp], _i32),
+    "dmsc_dataset_create": ([_vp, _vp, _vp, _vp], _i32),
+    "dmsc_dataset_destroy": ([_vp], _i32),
+    "dmsc_dataset_init": ([_vp, _vp, _i64, _i32, _vp], _i32),
+    "dmsc_dataset_work": ([_vp, _vp], _i32),
+    "dmsc_dataset_num_critical": ([_vp, _vp], _i32),
+    "dmsc_dataset_export_cells": ([_vp, _vp, _vp, _vp, _vp], _i32),
+    "dmsc_dataset_export_critical": ([_vp, _vp, _vp], _i32),
+    "dmsc_dataset_writeout_connectivity": ([_vp, _vp, _vp], _i32),
+    "dmsc_msc_destroy": ([_vp], _i32),
+    "dmsc_msc_sizes": ([_vp, _vp], _i32),
+    "dmsc_msc_export": ([_vp] * 15, _i32),
+    "dmsc_set_timing": ([_vp, _i32], _i32),
+    "dmsc_dataset_stage_times": ([_vp, _vp, _i32], _i32),
+    "dmsc_kernel_launches": ([_vp], _i32),
+}
+
+
+class DmscError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"dmsc error {ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libdmsc.so, building it first when it is missing (needs nvcc)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if build_if_missing:
+            path = _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError(f"libdmsc.so not found at {path}; run mscomplex_gb300.build.build()")
+        L = C.CDLL(path)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(L, name, None)
+            if fn is None:
+                continue
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+        return L
+
+
+def check(rc: int):
+    if rc != DMSC_OK:
+        raise DmscError(rc, load().dmsc_last_error().decode())
+
+
+def kernel_launches() -> int:
+    n = C.c_uint64()
+    check(load().dmsc_kernel_launches(C.byref(n)))
+    return n.value

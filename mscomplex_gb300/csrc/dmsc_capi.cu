@@ -1,0 +1,389 @@
+// dmsc_capi.cu -- extern "C" boundary of libdmsc.so (declared in include/dmsc.h).
+//
+// Host-side objects mirror the reference's C++ classes: dmsc_dataset is a
+// GridDataset (dmsc/include/grid_dataset.h:35-240) whose cell arrays live in
+// device memory, dmsc_msc is a GridMSComplex (dmsc/include/grid_mscomplex.h)
+// held as flat device arrays.  There is no CPU fallback: every computation
+// here is a CUDA kernel launch.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dmsc.h"
+#include "dmsc_internal.h"
+#include "grid_types.h"
+
+using namespace dmsc;
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char *where) {
+  cudaGetLastError();  // clear sticky-free errors
+  std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+  return fail(e == cudaErrorMemoryAllocation ? DMSC_ERR_OOM : DMSC_ERR_CUDA, m);
+}
+}  // namespace
+
+#define CK(call)                                             \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);      \
+  } while (0)
+
+static cudaStream_t pick(dmsc_ctx *c, void *s) { return s ? (cudaStream_t)s : c->stream; }
+
+// Maps the device status word to an error code.
+static int status_to_error(uint32_t st) {
+  if (!st) return DMSC_OK;
+  if (st & ST_NAN_INPUT) return fail(DMSC_ERR_INPUT, "NaN height in input (outside the supported domain)");
+  if (st & (ST_RESOLVE_LIMIT | ST_SIMPLIFY_LIMIT))
+    return fail(DMSC_ERR_DEVICE_TIMEOUT, "a bounded device loop ran out of iterations (status " + std::to_string(st) + ")");
+  return fail(DMSC_ERR_INVARIANT, "device invariant violated (status " + std::to_string(st) + ")");
+}
+
+extern "C" {
+
+const char *dmsc_last_error(void) { return g_err.c_str(); }
+
+int dmsc_init(int device, dmsc_ctx **out) {
+  if (!out) return fail(DMSC_ERR_BAD_ARG, "out is null");
+  int n = 0;
+  CK(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) return fail(DMSC_ERR_BAD_ARG, "no such device");
+  CK(cudaSetDevice(device));
+  dmsc_ctx *c = new dmsc_ctx;
+  c->device = device;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaStreamCreate"); }
+  *out = c;
+  return DMSC_OK;
+}
+
+int dmsc_shutdown(dmsc_ctx *c) {
+  if (!c) return fail(DMSC_ERR_BAD_ARG, "ctx is null");
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return DMSC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// dataset
+// ---------------------------------------------------------------------------
+int dmsc_dataset_create(dmsc_ctx *ctx, const int16_t rect[4], const int16_t ext[4], dmsc_dataset **out) {
+  if (!ctx || !rect || !ext || !out) return fail(DMSC_ERR_BAD_ARG, "null argument");
+  for (int i = 0; i < 4; ++i) {
+    if (rect[i] < 0 || ext[i] < 0) return fail(DMSC_ERR_BAD_ARG, "negative coordinate");
+    if ((rect[i] & 1) || (ext[i] & 1)) return fail(DMSC_ERR_BAD_ARG, "rect and ext corners must be vertices (even coordinates)");
+  }
+  if (rect[0] > rect[2] || rect[1] > rect[3] || ext[0] > ext[2] || ext[1] > ext[3])
+    return fail(DMSC_ERR_BAD_ARG, "rect corners out of order");
+  if (rect[0] < ext[0] || rect[1] < ext[1] || rect[2] > ext[2] || rect[3] > ext[3])
+    return fail(DMSC_ERR_BAD_ARG, "ext must contain rect");
+  if (ext[2] - ext[0] < 2 || ext[3] - ext[1] < 2) return fail(DMSC_ERR_BAD_ARG, "ext needs at least 2x2 vertices");
+  if (ext[2] > 32766 || ext[3] > 32766) return fail(DMSC_ERR_INT16_OVERFLOW, "cell ids exceed int16");
+  dmsc_dataset *d = new dmsc_dataset;
+  d->ctx = ctx;
+  std::memcpy(d->rect, rect, 8);
+  std::memcpy(d->ext, ext, 8);
+  GridGeom &g = d->g;
+  g.ex0 = ext[0]; g.ey0 = ext[1];
+  g.vnx = (ext[2] - ext[0]) / 2 + 1; g.vny = (ext[3] - ext[1]) / 2 + 1;
+  g.cx = 2 * (g.vnx - 1); g.cy = 2 * (g.vny - 1);
+  g.rx0 = rect[0] - ext[0]; g.ry0 = rect[1] - ext[1]; g.rx1 = rect[2] - ext[0]; g.ry1 = rect[3] - ext[1];
+  g.ntx = (g.vnx + TX - 1) / TX; g.nty = (g.vny + TY - 1) / TY;
+  g.pitch = g.vnx;
+  *out = d;
+  return DMSC_OK;
+}
+
+int dmsc_dataset_destroy(dmsc_dataset *d) {
+  if (!d) return fail(DMSC_ERR_BAD_ARG, "dataset is null");
+  cudaSetDevice(d->ctx->device);
+  cudaStreamSynchronize(d->ctx->stream);
+  delete d;
+  return DMSC_OK;
+}
+
+int dmsc_dataset_init(dmsc_dataset *d, const float *heights, int64_t pitch, int on_device, void *stream) {
+  if (!d || !heights) return fail(DMSC_ERR_BAD_ARG, "null argument");
+  GridGeom &g = d->g;
+  if (pitch < g.vnx) return fail(DMSC_ERR_BAD_ARG, "pitch smaller than the ext window width");
+  CK(cudaSetDevice(d->ctx->device));
+  cudaStream_t st = pick(d->ctx, stream);
+  if (on_device) {
+    d->hgt = heights;
+    g.pitch = pitch;
+  } else {
+    CK(d->hown.ensure((size_t)g.vnx * g.vny));
+    CK(cudaMemcpy2DAsync(d->hown.p, sizeof(float) * g.vnx, heights, sizeof(float) * pitch, sizeof(float) * g.vnx,
+                         g.vny, cudaMemcpyHostToDevice, st));
+    d->hgt = d->hown.p;
+    g.pitch = g.vnx;
+  }
+  d->worked = false;
+  return DMSC_OK;
+}
+
+// Runs K1 (gradient) -> scan -> K3 (resolve) -> K4 (labels) on `st`.
+// Returns after the device status is known.
+int dmsc_dataset_work(dmsc_dataset *d, void *stream) {
+  if (!d) return fail(DMSC_ERR_BAD_ARG, "dataset is null");
+  if (!d->hgt) return fail(DMSC_ERR_STATE, "dataset has no heights (call dmsc_dataset_init first)");
+  CK(cudaSetDevice(d->ctx->device));
+  cudaStream_t st = pick(d->ctx, stream);
+  int rc = d->alloc_cells();
+  if (rc) return rc;
+  const GridGeom &g = d->g;
+  const bool tm = d->ctx->timing;
+  if (tm && !d->ev_ready) {
+    for (auto &e : d->ev) CK(cudaEventCreate(&e));
+    d->ev_ready = true;
+  }
+  CK(cudaMemsetAsync(d->scal.p, 0, sizeof(uint32_t) * 4, st));
+  if (tm) CK(cudaEventRecord(d->ev[0], st));
+  CK(launch_gradient(d->hgt, g, d->codes.p, d->rowcnt.p, d->table.p, d->scal.p, st));
+  if (tm) CK(cudaEventRecord(d->ev[1], st));
+  CK(scan_exclusive_u8(d->rowcnt.p, (long long)(g.cy + 1) * g.ntx, d->offsets.p, d->scal.p + 1, st));
+  if (tm) CK(cudaEventRecord(d->ev[2], st));
+  CK(launch_resolve(d->table.p, d->nslots(), d->offsets.p, d->scal.p, st));
+  if (tm) CK(cudaEventRecord(d->ev[3], st));
+  if (d->cap <= 0) d->cap = (long long)g.vnx * g.vny / 16 + 4096;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    rc = d->alloc_cps(d->cap);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(d->cp_acnt.p, 0, sizeof(uint32_t) * d->cap, st));
+    CK(cudaMemsetAsync(d->cp_dcnt.p, 0, sizeof(uint32_t) * d->cap, st));
+    CpOut cp{d->cp_cellid.p, d->cp_fn.p, d->cp_flags.p, d->cp_pair_cell.p, d->cp_des2.p,
+             d->cp_asc2.p, d->cp_acnt.p, d->cp_dcnt.p, d->cap};
+    if (tm) CK(cudaEventRecord(d->ev[3], st));
+    CK(launch_labels(d->codes.p, d->hgt, g, d->offsets.p, d->table.p, d->labels.p, cp, d->scal.p, st));
+    if (tm) CK(cudaEventRecord(d->ev[4], st));
+    CK(cudaMemcpyAsync(d->host_scal, d->scal.p, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    d->ncp = d->host_scal[1];
+    if (!(d->host_scal[0] & ST_CAPACITY)) break;
+    d->cap = d->ncp + d->ncp / 8 + 1024;
+    uint32_t clear = d->host_scal[0] & ~ST_CAPACITY;
+    CK(cudaMemcpyAsync(d->scal.p, &clear, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  }
+  if (d->host_scal[0] & ST_CAPACITY) return fail(DMSC_ERR_INVARIANT, "critical-point capacity could not be met");
+  rc = status_to_error(d->host_scal[0]);
+  if (rc) return rc;
+  // pair_idx of critical cells that keep a pair (boundary rule; only with rect != ext)
+  CK(d->cp_pair_idx.ensure(d->cap));
+  if (d->rect_is_ext()) {
+    if (d->ncp) CK(cudaMemsetAsync(d->cp_pair_idx.p, 0xFF, sizeof(uint32_t) * d->ncp, st));
+  } else {
+    CK(launch_pair_index(d->ncp, d->cp_cellid.p, d->cp_flags.p, d->cp_pair_cell.p, d->cp_pair_idx.p, d->scal.p, st));
+    CK(cudaMemcpyAsync(d->host_scal, d->scal.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    rc = status_to_error(d->host_scal[0]);
+    if (rc) return rc;
+  }
+  d->worked = true;
+  return DMSC_OK;
+}
+
+int dmsc_dataset_num_critical(dmsc_dataset *d, int64_t *n) {
+  if (!d || !n) return fail(DMSC_ERR_BAD_ARG, "null argument");
+  if (!d->worked) return fail(DMSC_ERR_STATE, "dataset_work has not run");
+  *n = d->ncp;
+  return DMSC_OK;
+}
+
+int dmsc_dataset_export_cells(dmsc_dataset *d, int8_t *flags, int16_t *pairs, int16_t *own, void *stream) {
+  if (!d) return fail(DMSC_ERR_BAD_ARG, "dataset is null");
+  if (!d->worked) return fail(DMSC_ERR_STATE, "dataset_work has not run");
+  CK(cudaSetDevice(d->ctx->device));
+  cudaStream_t st = pick(d->ctx, stream);
+  const GridGeom &g = d->g;
+  size_t n = (size_t)(g.cx + 1) * (g.cy + 1);
+  DevBuf<int8_t> f;
+  DevBuf<int16_t> p, o;
+  if (flags) CK(f.ensure(n));
+  if (pairs) CK(p.ensure(2 * n));
+  if (own) CK(o.ensure(2 * n));
+  CK(launch_export_cells(g, d->codes.p, d->labels.p, d->cp_cellid.p, d->ncp, f.p, p.p, o.p, st));
+  if (flags) CK(cudaMemcpyAsync(flags, f.p, n, cudaMemcpyDeviceToHost, st));
+  if (pairs) CK(cudaMemcpyAsync(pairs, p.p, 4 * n, cudaMemcpyDeviceToHost, st));
+  if (own) CK(cudaMemcpyAsync(own, o.p, 4 * n, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return DMSC_OK;
+}
+
+int dmsc_dataset_export_critical(dmsc_dataset *d, int16_t *cellids, void *stream) {
+  if (!d || !cellids) return fail(DMSC_ERR_BAD_ARG, "null argument");
+  if (!d->worked) return fail(DMSC_ERR_STATE, "dataset_work has not run");
+  CK(cudaSetDevice(d->ctx->device));
+  cudaStream_t st = pick(d->ctx, stream);
+  if (d->ncp) CK(cudaMemcpyAsync(cellids, d->cp_cellid.p, 4 * d->ncp, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return DMSC_OK;
+}
+
+int dmsc_dataset_writeout_connectivity(dmsc_dataset *d, dmsc_msc **out, void *stream) {
+  if (!d || !out) return fail(DMSC_ERR_BAD_ARG, "null argument");
+  if (!d->worked) return fail(DMSC_ERR_STATE, "dataset_work has not run");
+  CK(cudaSetDevice(d->ctx->device));
+  cudaStream_t st = pick(d->ctx, stream);
+  dmsc_msc *m = new dmsc_msc;
+  m->ctx = d->ctx;
+  std::memcpy(m->rect, d->rect, 8);
+  std::memcpy(m->ext, d->ext, 8);
+  if (d->ctx->timing && d->ev_ready) CK(cudaEventRecord(d->ev[5], st));
+  int rc = m->writeout_from(*d, st);
+  if (rc) { delete m; return rc; }
+  if (d->ctx->timing && d->ev_ready) CK(cudaEventRecord(d->ev[6], st));
+  *out = m;
+  return DMSC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// complex
+// ---------------------------------------------------------------------------
+int dmsc_msc_destroy(dmsc_msc *m) {
+  if (!m) return fail(DMSC_ERR_BAD_ARG, "complex is null");
+  cudaSetDevice(m->ctx->device);
+  cudaStreamSynchronize(m->ctx->stream);
+  delete m;
+  return DMSC_OK;
+}
+
+int dmsc_msc_sizes(dmsc_msc *m, int64_t sizes[5]) {
+  if (!m || !sizes) return fail(DMSC_ERR_BAD_ARG, "null argument");
+  sizes[0] = m->ncp; sizes[1] = m->nasc; sizes[2] = m->ndes; sizes[3] = m->nadisc; sizes[4] = m->nddisc;
+  return DMSC_OK;
+}
+
+int dmsc_msc_export(dmsc_msc *m, int16_t rect_ext[8], int16_t *cellid, float *fn, uint32_t *pair_idx, uint8_t *flags,
+                    uint32_t *asc_off, uint32_t *asc, uint32_t *des_off, uint32_t *des, uint32_t *adisc_off,
+                    int16_t *adisc, uint32_t *ddisc_off, int16_t *ddisc, void *stream) {
+  if (!m) return fail(DMSC_ERR_BAD_ARG, "complex is null");
+  CK(cudaSetDevice(m->ctx->device));
+  cudaStream_t st = pick(m->ctx, stream);
+  if (rect_ext) { std::memcpy(rect_ext, m->rect, 8); std::memcpy(rect_ext + 4, m->ext, 8); }
+  size_t n = (size_t)m->ncp;
+  auto cp = [&](void *dst, const void *src, size_t bytes) -> cudaError_t {
+    if (!dst || !bytes) return cudaSuccess;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
+  };
+  CK(cp(cellid, m->cellid.p, 4 * n));
+  CK(cp(fn, m->fn.p, 4 * n));
+  CK(cp(pair_idx, m->pair_idx.p, 4 * n));
+  CK(cp(flags, m->flags.p, n));
+  CK(cp(asc_off, m->aoff.p, 4 * (n + 1)));
+  CK(cp(asc, m->asc.p, 4 * (size_t)m->nasc));
+  CK(cp(des_off, m->doff.p, 4 * (n + 1)));
+  CK(cp(des, m->des.p, 4 * (size_t)m->ndes));
+  CK(cp(adisc_off, m->adoff.p, m->adoff.p ? 4 * (n + 1) : 0));
+  CK(cp(adisc, m->adisc.p, 4 * (size_t)m->nadisc));
+  CK(cp(ddisc_off, m->ddoff.p, m->ddoff.p ? 4 * (n + 1) : 0));
+  CK(cp(ddisc, m->ddisc.p, 4 * (size_t)m->nddisc));
+  CK(cudaStreamSynchronize(st));
+  if (adisc_off && !m->adoff.p) std::memset(adisc_off, 0, 4 * (n + 1));
+  if (ddisc_off && !m->ddoff.p) std::memset(ddisc_off, 0, 4 * (n + 1));
+  return DMSC_OK;
+}
+
+int dmsc_set_timing(dmsc_ctx *ctx, int enable) {
+  if (!ctx) return fail(DMSC_ERR_BAD_ARG, "ctx is null");
+  ctx->timing = enable != 0;
+  return DMSC_OK;
+}
+
+int dmsc_dataset_stage_times(dmsc_dataset *d, float *ms, int n) {
+  if (!d || !ms) return fail(DMSC_ERR_BAD_ARG, "null argument");
+  if (!d->ev_ready) return fail(DMSC_ERR_STATE, "timing was not enabled for the last run");
+  CK(cudaSetDevice(d->ctx->device));
+  const int pairs[5][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 4}, {5, 6}};
+  for (int i = 0; i < n && i < 5; ++i) {
+    CK(cudaEventSynchronize(d->ev[pairs[i][1]]));
+    float t = 0;
+    if (cudaEventElapsedTime(&t, d->ev[pairs[i][0]], d->ev[pairs[i][1]]) != cudaSuccess) { cudaGetLastError(); t = -1; }
+    ms[i] = t;
+  }
+  return DMSC_OK;
+}
+
+int dmsc_kernel_launches(uint64_t *count) {
+  if (!count) return fail(DMSC_ERR_BAD_ARG, "null argument");
+  *count = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
+  return DMSC_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// member functions of the handle types
+// ---------------------------------------------------------------------------
+int dmsc_dataset::alloc_cells() {
+  size_t nv = (size_t)g.vnx * g.vny;
+  CK(codes.ensure(nv));
+  CK(labels.ensure(nv));
+  CK(rowcnt.ensure((size_t)(g.cy + 1) * g.ntx));
+  CK(offsets.ensure((size_t)(g.cy + 1) * g.ntx));
+  CK(table.ensure((size_t)nslots()));
+  CK(scal.ensure(4));
+  if (!host_scal) CK(cudaMallocHost((void **)&host_scal, sizeof(uint32_t) * 4));
+  return DMSC_OK;
+}
+
+int dmsc_dataset::alloc_cps(long long n) {
+  CK(cp_cellid.ensure(n));
+  CK(cp_fn.ensure(n));
+  CK(cp_flags.ensure(n));
+  CK(cp_pair_cell.ensure(n));
+  CK(cp_des2.ensure(2 * n));
+  CK(cp_asc2.ensure(2 * n));
+  CK(cp_acnt.ensure(n));
+  CK(cp_dcnt.ensure(n));
+  return DMSC_OK;
+}
+
+dmsc_dataset::~dmsc_dataset() {
+  if (host_scal) cudaFreeHost(host_scal);
+  if (ev_ready)
+    for (auto &e : ev) cudaEventDestroy(e);
+}
+
+int dmsc_msc::writeout_from(const dmsc_dataset &d, cudaStream_t st) {
+  ncp = d.ncp;
+  size_t n = (size_t)ncp;
+  CK(cellid.ensure(n + 1));
+  CK(fn.ensure(n + 1));
+  CK(pair_idx.ensure(n + 1));
+  CK(flags.ensure(n + 1));
+  CK(aoff.ensure(n + 1));
+  CK(doff.ensure(n + 1));
+  CK(asc.ensure(4 * n + 1));
+  CK(des.ensure(4 * n + 1));
+  if (n) {
+    CK(cudaMemcpyAsync(cellid.p, d.cp_cellid.p, 4 * n, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(fn.p, d.cp_fn.p, 4 * n, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(pair_idx.p, d.cp_pair_idx.p, 4 * n, cudaMemcpyDeviceToDevice, st));
+    CK(launch_msc_flags(ncp, d.cp_flags.p, flags.p, st));
+  }
+  CK(scan_exclusive_u32(d.cp_acnt.p, ncp, aoff.p, aoff.p + n, st));
+  CK(scan_exclusive_u32(d.cp_dcnt.p, ncp, doff.p, doff.p + n, st));
+  CK(cudaMemsetAsync(d.scal.p, 0, sizeof(uint32_t), st));
+  CK(build_csr(ncp, d.cp_cellid.p, d.cp_des2.p, d.cp_asc2.p, aoff.p, doff.p, asc.p, des.p, 4 * (long long)n + 1,
+               d.scal.p, st));
+  uint32_t tot[3] = {0, 0, 0};
+  CK(cudaMemcpyAsync(&tot[0], aoff.p + n, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&tot[1], doff.p + n, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&tot[2], d.scal.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  nasc = tot[0];
+  ndes = tot[1];
+  if (tot[2]) return status_to_error(tot[2]);
+  if (nasc > 4 * (long long)n || ndes > 4 * (long long)n) return fail(DMSC_ERR_INVARIANT, "arc count exceeds its bound");
+  return DMSC_OK;
+}

@@ -1,0 +1,48 @@
+// dmsc_internal.h -- launchers shared between the CUDA translation units.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "dmsc_common.cuh"
+
+namespace dmsc {
+
+// Number of kernels this library has launched (process-wide, all devices).
+extern unsigned long long g_kernel_launches;
+#define DMSC_LAUNCHED(n) __atomic_fetch_add(&::dmsc::g_kernel_launches, (unsigned long long)(n), __ATOMIC_RELAXED)
+
+// Critical-point outputs of the label kernel (one entry per cp index).
+struct CpOut {
+  uint32_t *cellid;   // packed global (x | y<<16)
+  float *fn;
+  uint8_t *flags;     // bit0 PAIRED (isBoundryCancelable after writeout)
+  uint32_t *pair_cell;// packed global cellid of the pair (paired critical cells only)
+  uint32_t *des2;     // saddles: 2 facet (minimum) labels, ascending, LABEL_NONE padded
+  uint32_t *asc2;     // saddles: 2 cofacet (maximum) labels
+  uint32_t *acnt;     // per cp: |asc| (saddles written, minima counted atomically)
+  uint32_t *dcnt;     // per cp: |des|
+  long long cap;      // capacity of every array above (in critical points)
+};
+
+size_t grad_smem_bytes();
+size_t label_smem_bytes();
+cudaError_t launch_gradient(const float *hgt, const GridGeom &g, uint32_t *codes, uint8_t *rowcnt, uint64_t *table,
+                            uint32_t *status, cudaStream_t st);
+cudaError_t launch_resolve(uint64_t *table, long long nslots, const uint32_t *offsets, uint32_t *status,
+                           cudaStream_t st);
+cudaError_t launch_labels(const uint32_t *codes, const float *hgt, const GridGeom &g, const uint32_t *offsets,
+                          const uint64_t *table, uint4 *labels, const CpOut &cp, uint32_t *status, cudaStream_t st);
+
+cudaError_t scan_exclusive_u8(const uint8_t *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st);
+cudaError_t scan_exclusive_u32(const uint32_t *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st);
+cudaError_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *ktmp, uint32_t *vtmp, long long n, int nbits,
+                             cudaStream_t st);
+cudaError_t build_csr(long long ncp, const uint32_t *cellid, const uint32_t *des2, const uint32_t *asc2,
+                      const uint32_t *aoff, const uint32_t *doff, uint32_t *asc, uint32_t *des, long long out_cap,
+                      uint32_t *status, cudaStream_t st);
+cudaError_t launch_pair_index(long long ncp, const uint32_t *cellid, const uint8_t *flags, const uint32_t *pair_cell,
+                              uint32_t *pair_idx, uint32_t *status, cudaStream_t st);
+cudaError_t launch_msc_flags(long long ncp, const uint8_t *cpflags, uint8_t *out, cudaStream_t st);
+cudaError_t launch_export_cells(const GridGeom &g, const uint32_t *codes, const uint4 *labels, const uint32_t *cp_cellid,
+                                long long ncp, int8_t *flags, int16_t *pairs, int16_t *own, cudaStream_t st);
+
+}  // namespace dmsc

@@ -1,0 +1,660 @@
+// grid_kernels.cu -- discrete gradient, critical-cell collation and owner
+// labels for one piece of a 2D grid, hand-written for sm_103a.
+//
+// Restates, as data-parallel tile kernels, the reference CPU path
+//   GridDataset::assignGradients        dmsc/src/grid_dataset.cpp:1743-1820
+//   lowestPairableCoFacet               dmsc/src/grid_dataset.cpp:1314-1373
+//   compareCells / ptLt                 grid_dataset.cpp:1519-1536, grid_dataset.h:158-167
+//   GridDataset::collateCriticalPoints  grid_dataset.cpp:1822-1832
+//   assignCellOwnerExtrema + BFS        grid_dataset.cpp:1376-1427, 1835-1856
+//   writeout_connectivity (arcs, fns)   grid_dataset.cpp:1538-1552, 1858-1907
+//
+// Exactness argument for the parallel gradient.  The reference pairs cells in
+// row-major order and skips cells already marked.  A cell c can only be chosen
+// by its unique maximal facet (the "usable" test requires the chooser to be
+// the compareCells-maximum of the cofacet's facets), so every cell has at most
+// one chooser.  If a vertex v chooses edge e = (w,v), w is the lowest usable
+// lower neighbour of v, and then e is never the maximal edge of either face of
+// e (the face edge (v,y) is always larger than e in the ascending-sort order),
+// so e has no candidate face and the row-major order never matters.  Hence:
+// pair(v) = cand(v); pair(e) = its choosing vertex, else cand(e); pair(f) =
+// its choosing edge.  ST_PAIR_CONFLICT flags the (impossible) mixed case.
+//
+// Owner labels.  own() of a non-critical vertex is own() of the far end of
+// its paired edge; of a non-critical face, own() of the face across its
+// paired edge; of a non-critical edge, own() of its pair.  Critical cells own
+// themselves and non-critical exterior cells are never reached (LABEL_NONE).
+// The V-paths are followed by pointer jumping in shared memory inside a tile;
+// paths that leave the tile end at a border cell whose global resolution is
+// done once over the much smaller border table (resolve kernel).
+#include "dmsc_common.cuh"
+#include "dmsc_internal.h"
+
+namespace dmsc {
+
+// ---------------------------------------------------------------------------
+// shared helpers
+// ---------------------------------------------------------------------------
+struct EdgeKey {
+  uint64_t lo, hi;
+};
+__device__ __forceinline__ EdgeKey mk_edge(uint64_t a, uint64_t b) {
+  EdgeKey e;
+  e.lo = a < b ? a : b;
+  e.hi = a < b ? b : a;
+  return e;
+}
+__device__ __forceinline__ bool edge_less(const EdgeKey &a, const EdgeKey &b) {
+  return a.lo < b.lo || (a.lo == b.lo && a.hi < b.hi);
+}
+__device__ __forceinline__ void sort4(uint64_t k[4]) {
+#define CSWAP(a, b) { uint64_t x_ = k[a] < k[b] ? k[a] : k[b]; uint64_t y_ = k[a] < k[b] ? k[b] : k[a]; k[a] = x_; k[b] = y_; }
+  CSWAP(0, 1) CSWAP(2, 3) CSWAP(0, 2) CSWAP(1, 3) CSWAP(1, 2)
+#undef CSWAP
+}
+// Lexicographic compare of ascending-sorted vertex keys (compareCells on faces).
+__device__ __forceinline__ bool face_less(uint64_t a[4], uint64_t b[4]) {
+  sort4(a);
+  sort4(b);
+  for (int i = 0; i < 4; ++i) {
+    if (a[i] < b[i]) return true;
+    if (b[i] < a[i]) return false;
+  }
+  return false;
+}
+
+__device__ __forceinline__ bool in_rect(const GridGeom &g, int x, int y) {
+  return x >= g.rx0 && x <= g.rx1 && y >= g.ry0 && y <= g.ry1;
+}
+// True if cell (x,y) (relative to ext) has a cofacet inside ext but outside
+// rect.  Only meaningful for cells inside rect (isCellExterior, :1708-1711).
+__device__ __forceinline__ bool has_ext_cofacet(const GridGeom &g, int x, int y) {
+  int kind = (x & 1) | ((y & 1) << 1);
+  bool up = (y == g.ry1 && y + 1 <= g.cy), dn = (y == g.ry0 && y >= 1);
+  bool lf = (x == g.rx0 && x >= 1), rt = (x == g.rx1 && x + 1 <= g.cx);
+  switch (kind) {
+    case 0: return up || dn || lf || rt;  // vertex: four edges
+    case 1: return up || dn;              // horizontal edge: faces above/below
+    case 2: return lf || rt;              // vertical edge: faces left/right
+    default: return false;                // face: no cofacets
+  }
+}
+__device__ __forceinline__ int dir_dx(uint32_t d) { return d == DIR_PX ? 1 : (d == DIR_MX ? -1 : 0); }
+__device__ __forceinline__ int dir_dy(uint32_t d) { return d == DIR_PY ? 1 : (d == DIR_MY ? -1 : 0); }
+
+// Critical bit of a cell after the pairing (assignGradients steps 2 and 3).
+__device__ __forceinline__ uint32_t finish_code(const GridGeom &g, int x, int y, uint32_t dir, bool paired) {
+  bool inr = in_rect(g, x, y);
+  bool crit = inr && !paired;
+  if (paired) {
+    if (inr && has_ext_cofacet(g, x, y)) crit = true;  // B(c)
+    int px = x + dir_dx(dir), py = y + dir_dy(dir);
+    if (in_rect(g, px, py) && has_ext_cofacet(g, px, py)) crit = true;  // B(pair(c))
+  }
+  return (paired ? (CODE_PAIRED | dir) : 0u) | (crit ? CODE_CRIT : 0u);
+}
+
+// pointer-jumping words (uint16): tag in bits 14-15, local index below
+constexpr uint16_t PJ_PTR = 0x0000, PJ_ROOT = 0x4000, PJ_EXIT = 0x8000, PJ_INVALID = 0xC000;
+constexpr uint16_t PJ_TAG = 0xC000, PJ_IDX = 0x0FFF;
+
+// Jump every pointer of pv[0..TX*TY) and pf[...] to its terminal.  Returns
+// true if any path failed to terminate (a cycle).
+__device__ __forceinline__ bool pointer_jump(uint16_t *pv, uint16_t *pf) {
+  const int n = TX * TY;
+  for (int round = 0; round < 16; ++round) {  // log2(4096) + 4
+    int changed = 0;
+    for (int e = threadIdx.x; e < 2 * n; e += blockDim.x) {
+      uint16_t *p = e < n ? pv : pf;
+      int c = e < n ? e : e - n;
+      uint16_t v = p[c];
+      if ((v & PJ_TAG) == PJ_PTR) {
+        uint16_t w = p[v & PJ_IDX];
+        p[c] = w;
+        changed |= ((w & PJ_TAG) == PJ_PTR);
+      }
+    }
+    if (!__syncthreads_or(changed)) return false;
+  }
+  bool bad = false;
+  for (int e = threadIdx.x; e < 2 * n; e += blockDim.x) {
+    uint16_t *p = e < n ? pv : pf;
+    int c = e < n ? e : e - n;
+    if ((p[c] & PJ_TAG) == PJ_PTR) { p[c] = PJ_INVALID; bad = true; }
+  }
+  __syncthreads();
+  return bad;
+}
+
+// Per-row ranks of critical cells inside the tile's row segments.
+// rankA[j][i]: critical cells of cell row 2j before vertex i (V,H interleaved);
+// rankB[j][i]: same for cell row 2j+1 (Vt,F).  Returns row totals via cntA/cntB.
+__device__ __forceinline__ void row_ranks(const uint32_t (*code)[TX], uint8_t (*rankA)[TX], uint8_t (*rankB)[TX],
+                                          uint8_t *cntA, uint8_t *cntB, int w, int h) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j = warp; j < h; j += nw) {
+    uint32_t c0 = lane < w ? code[j][lane] : 0u;
+    uint32_t c1 = lane + 32 < w ? code[j][lane + 32] : 0u;
+    uint32_t a0 = ((c0 >> 3) & 1) + ((c0 >> 11) & 1), a1 = ((c1 >> 3) & 1) + ((c1 >> 11) & 1);
+    uint32_t b0 = ((c0 >> 19) & 1) + ((c0 >> 27) & 1), b1 = ((c1 >> 19) & 1) + ((c1 >> 27) & 1);
+    uint32_t sa0 = a0, sa1 = a1, sb0 = b0, sb1 = b1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t0 = __shfl_up_sync(0xffffffffu, sa0, o), t1 = __shfl_up_sync(0xffffffffu, sa1, o);
+      uint32_t u0 = __shfl_up_sync(0xffffffffu, sb0, o), u1 = __shfl_up_sync(0xffffffffu, sb1, o);
+      if (lane >= o) { sa0 += t0; sa1 += t1; sb0 += u0; sb1 += u1; }
+    }
+    uint32_t ta = __shfl_sync(0xffffffffu, sa0, 31), tb = __shfl_sync(0xffffffffu, sb0, 31);
+    rankA[j][lane] = (uint8_t)(sa0 - a0);
+    rankA[j][lane + 32] = (uint8_t)(ta + sa1 - a1);
+    rankB[j][lane] = (uint8_t)(sb0 - b0);
+    rankB[j][lane + 32] = (uint8_t)(tb + sb1 - b1);
+    if (lane == 31) {
+      cntA[j] = (uint8_t)(ta + sa1);
+      cntB[j] = (uint8_t)(tb + sb1);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K1: gradient + in-tile tracing + critical counts + border table
+// ---------------------------------------------------------------------------
+struct GradSmem {
+  uint32_t hv[TY + 3][TX + 3];  // ordered heights of vertex (tx0-1+ii, ty0-1+jj)
+  uint8_t candV[TY + 1][TX + 1];
+  uint8_t candH[TY + 1][TX];
+  uint8_t candVt[TY][TX + 1];
+  uint32_t code[TY][TX];
+  uint16_t pv[TY * TX];
+  uint16_t pf[TY * TX];
+  uint8_t rankA[TY][TX];
+  uint8_t rankB[TY][TX];
+  uint8_t cntA[TY], cntB[TY];
+};
+
+__device__ __forceinline__ uint64_t vkey(const GradSmem &s, int i, int j, int tx0, int ty0) {
+  return ((uint64_t)s.hv[j + 1][i + 1] << 32) | ((uint32_t)(tx0 + i) << 16) | (uint32_t)(ty0 + j);
+}
+// Is edge e the compareCells-maximum facet of the face whose lower-left
+// vertex is local (fi,fj)?  ("usable" test of lowestPairableCoFacet, :1344-1351)
+__device__ __forceinline__ bool max_edge_of_face(const GradSmem &s, const EdgeKey &e, int fi, int fj, int tx0, int ty0) {
+  uint64_t a = vkey(s, fi, fj, tx0, ty0), b = vkey(s, fi + 1, fj, tx0, ty0);
+  uint64_t c = vkey(s, fi, fj + 1, tx0, ty0), d = vkey(s, fi + 1, fj + 1, tx0, ty0);
+  if (edge_less(e, mk_edge(a, b))) return false;
+  if (edge_less(e, mk_edge(c, d))) return false;
+  if (edge_less(e, mk_edge(a, c))) return false;
+  if (edge_less(e, mk_edge(b, d))) return false;
+  return true;
+}
+__device__ __forceinline__ void face_keys(const GradSmem &s, int fi, int fj, int tx0, int ty0, uint64_t k[4]) {
+  k[0] = vkey(s, fi, fj, tx0, ty0);
+  k[1] = vkey(s, fi + 1, fj, tx0, ty0);
+  k[2] = vkey(s, fi, fj + 1, tx0, ty0);
+  k[3] = vkey(s, fi + 1, fj + 1, tx0, ty0);
+}
+
+__global__ void __launch_bounds__(GRAD_THREADS, 3)
+k_gradient(const float *__restrict__ hgt, GridGeom g, uint32_t *__restrict__ codes, uint8_t *__restrict__ rowcnt,
+           uint64_t *__restrict__ table, uint32_t *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  GradSmem &s = *reinterpret_cast<GradSmem *>(smem_raw);
+  const int bx = blockIdx.x, by = blockIdx.y;
+  const int tx0 = bx * TX, ty0 = by * TY;
+  int w, h, wf, hf;
+  tile_extent(g, bx, by, 0, w, h);
+  tile_extent(g, bx, by, 1, wf, hf);
+  uint32_t st = 0;
+
+  // 1. heights with a 1-vertex halo below/left and 2 above/right
+  for (int e = threadIdx.x; e < (TX + 3) * (TY + 3); e += blockDim.x) {
+    int jj = e / (TX + 3), ii = e - jj * (TX + 3);
+    int vi = tx0 - 1 + ii, vj = ty0 - 1 + jj;
+    uint32_t v = 0;
+    if (vi >= 0 && vi < g.vnx && vj >= 0 && vj < g.vny) {
+      float f = __ldg(hgt + (long long)vj * g.pitch + vi);
+      if ((__float_as_uint(f) & 0x7fffffffu) > 0x7f800000u) st |= ST_NAN_INPUT;
+      v = ord_key(f);
+    }
+    s.hv[jj][ii] = v;
+  }
+  __syncthreads();
+
+  // 2. lowest pairable cofacet of vertices and edges (only cells in rect choose)
+  for (int e = threadIdx.x; e < (TX + 1) * (TY + 1); e += blockDim.x) {
+    int j = e / (TX + 1), i = e - j * (TX + 1);
+    int vi = tx0 + i, vj = ty0 + j;
+    uint8_t best = CAND_NONE;
+    if (vi < g.vnx && vj < g.vny && in_rect(g, 2 * vi, 2 * vj)) {
+      uint64_t kv = vkey(s, i, j, tx0, ty0), bk = ~0ull;
+      bool tbv = vi == 0 || vi == g.vnx - 1 || vj == 0 || vj == g.vny - 1;
+      bool tbvert = vi == 0 || vi == g.vnx - 1;  // vertical edges of v on the ext boundary
+      bool tbhorz = vj == 0 || vj == g.vny - 1;  // horizontal edges of v on the ext boundary
+      // cofacet order of getCellCofacets (:1626-1629): up, down, left, right
+      if (vj + 1 < g.vny && (!tbv || tbvert)) { uint64_t k = vkey(s, i, j + 1, tx0, ty0); if (k < kv && k < bk) { bk = k; best = DIR_PY; } }
+      if (vj >= 1 && (!tbv || tbvert)) { uint64_t k = vkey(s, i, j - 1, tx0, ty0); if (k < kv && k < bk) { bk = k; best = DIR_MY; } }
+      if (vi >= 1 && (!tbv || tbhorz)) { uint64_t k = vkey(s, i - 1, j, tx0, ty0); if (k < kv && k < bk) { bk = k; best = DIR_MX; } }
+      if (vi + 1 < g.vnx && (!tbv || tbhorz)) { uint64_t k = vkey(s, i + 1, j, tx0, ty0); if (k < kv && k < bk) { bk = k; best = DIR_PX; } }
+    }
+    s.candV[j][i] = best;
+  }
+  for (int e = threadIdx.x; e < TX * (TY + 1); e += blockDim.x) {
+    int j = e / TX, i = e - j * TX;  // H(i,j)
+    int hi = tx0 + i, hj = ty0 + j;
+    uint8_t best = CAND_NONE;
+    if (hi + 1 < g.vnx && hj < g.vny && in_rect(g, 2 * hi + 1, 2 * hj) && hj != 0 && hj != g.vny - 1) {
+      EdgeKey ek = mk_edge(vkey(s, i + 1, j, tx0, ty0), vkey(s, i, j, tx0, ty0));
+      bool u0 = max_edge_of_face(s, ek, i, j, tx0, ty0);      // cf[0]: face above
+      bool u1 = max_edge_of_face(s, ek, i, j - 1, tx0, ty0);  // cf[1]: face below
+      if (u0 && u1) {
+        uint64_t ka[4], kb[4];
+        face_keys(s, i, j, tx0, ty0, ka);
+        face_keys(s, i, j - 1, tx0, ty0, kb);
+        best = face_less(kb, ka) ? DIR_MY : DIR_PY;
+      } else if (u0) best = DIR_PY;
+      else if (u1) best = DIR_MY;
+    }
+    s.candH[j][i] = best;
+  }
+  for (int e = threadIdx.x; e < (TX + 1) * TY; e += blockDim.x) {
+    int j = e / (TX + 1), i = e - j * (TX + 1);  // Vt(i,j)
+    int vi = tx0 + i, vj = ty0 + j;
+    uint8_t best = CAND_NONE;
+    if (vi < g.vnx && vj + 1 < g.vny && in_rect(g, 2 * vi, 2 * vj + 1) && vi != 0 && vi != g.vnx - 1) {
+      EdgeKey ek = mk_edge(vkey(s, i, j + 1, tx0, ty0), vkey(s, i, j, tx0, ty0));
+      bool u0 = max_edge_of_face(s, ek, i, j, tx0, ty0);      // cf[0]: face right
+      bool u1 = max_edge_of_face(s, ek, i - 1, j, tx0, ty0);  // cf[1]: face left
+      if (u0 && u1) {
+        uint64_t ka[4], kb[4];
+        face_keys(s, i, j, tx0, ty0, ka);
+        face_keys(s, i - 1, j, tx0, ty0, kb);
+        best = face_less(kb, ka) ? DIR_MX : DIR_PX;
+      } else if (u0) best = DIR_PX;
+      else if (u1) best = DIR_MX;
+    }
+    s.candVt[j][i] = best;
+  }
+  __syncthreads();
+
+  // 3. final codes of the tile's own cells
+  for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
+    int j = e / TX, i = e - j * TX;
+    uint32_t packed = 0;
+    if (i < w && j < h) {
+      int vi = tx0 + i, vj = ty0 + j, x = 2 * vi, y = 2 * vj;
+      uint8_t cv = s.candV[j][i];
+      packed |= finish_code(g, x, y, cv, cv != CAND_NONE);
+      if (vi + 1 < g.vnx) {  // H(i,j)
+        uint32_t d = CAND_NONE;
+        int nch = 0;
+        if (cv == DIR_PX) { d = DIR_MX; ++nch; }
+        if (s.candV[j][i + 1] == DIR_MX) { d = DIR_PX; ++nch; }
+        uint8_t ce = s.candH[j][i];
+        if (ce != CAND_NONE) { if (nch) st |= ST_PAIR_CONFLICT; else d = ce; }
+        packed |= finish_code(g, x + 1, y, d & 3, d != CAND_NONE) << 8;
+      }
+      if (vj + 1 < g.vny) {  // Vt(i,j)
+        uint32_t d = CAND_NONE;
+        int nch = 0;
+        if (cv == DIR_PY) { d = DIR_MY; ++nch; }
+        if (s.candV[j + 1][i] == DIR_MY) { d = DIR_PY; ++nch; }
+        uint8_t ce = s.candVt[j][i];
+        if (ce != CAND_NONE) { if (nch) st |= ST_PAIR_CONFLICT; else d = ce; }
+        packed |= finish_code(g, x, y + 1, d & 3, d != CAND_NONE) << 16;
+      }
+      if (vi + 1 < g.vnx && vj + 1 < g.vny) {  // F(i,j): chosen by at most one edge
+        uint32_t d = CAND_NONE;
+        if (s.candH[j][i] == DIR_PY) d = DIR_MY;
+        if (s.candH[j + 1][i] == DIR_MY) d = DIR_PY;
+        if (s.candVt[j][i] == DIR_PX) d = DIR_MX;
+        if (s.candVt[j][i + 1] == DIR_MX) d = DIR_PX;
+        packed |= finish_code(g, x + 1, y + 1, d & 3, d != CAND_NONE) << 24;
+      }
+      codes[(long long)vj * g.vnx + vi] = packed;
+    }
+    s.code[j][i] = packed;
+  }
+  __syncthreads();
+
+  // 4. in-tile tracing: vertices follow their paired edge to the next vertex,
+  //    faces follow their paired edge to the face across it.
+  for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
+    int j = e / TX, i = e - j * TX;
+    uint16_t pvv = PJ_INVALID, pff = PJ_INVALID;
+    uint32_t c = s.code[j][i];
+    if (i < w && j < h) {
+      uint32_t cvv = c & 0xff;
+      if (cvv & CODE_CRIT) pvv = PJ_ROOT | e;
+      else if (in_rect(g, 2 * (tx0 + i), 2 * (ty0 + j))) {
+        uint32_t d = cvv & 3;
+        int ni = i + dir_dx(d), nj = j + dir_dy(d);
+        pvv = (ni >= 0 && ni < w && nj >= 0 && nj < h) ? (uint16_t)(PJ_PTR | (nj * TX + ni)) : (uint16_t)(PJ_EXIT | e);
+      }
+    }
+    if (i < wf && j < hf) {
+      uint32_t cf = c >> 24;
+      if (cf & CODE_CRIT) pff = PJ_ROOT | e;
+      else if (in_rect(g, 2 * (tx0 + i) + 1, 2 * (ty0 + j) + 1)) {
+        uint32_t d = cf & 3;
+        int ni = i + dir_dx(d), nj = j + dir_dy(d);
+        pff = (ni >= 0 && ni < wf && nj >= 0 && nj < hf) ? (uint16_t)(PJ_PTR | (nj * TX + ni)) : (uint16_t)(PJ_EXIT | e);
+      }
+    }
+    s.pv[e] = pvv;
+    s.pf[e] = pff;
+  }
+  row_ranks(s.code, s.rankA, s.rankB, s.cntA, s.cntB, w, h);
+  __syncthreads();
+  if (pointer_jump(s.pv, s.pf)) st |= ST_CYCLE;
+
+  // 5. per (cell row, tile) critical counts
+  for (int j = threadIdx.x; j < h; j += blockDim.x) {
+    int y = 2 * (ty0 + j);
+    rowcnt[(long long)y * g.ntx + bx] = s.cntA[j];
+    if (y + 1 <= g.cy) rowcnt[(long long)(y + 1) * g.ntx + bx] = s.cntB[j];
+  }
+
+  // 6. border table: where each border cell's path ends inside this tile
+  long long tile_base = ((long long)by * g.ntx + bx) * SLOTS_PER_TILE;
+  for (int e = threadIdx.x; e < 2 * SLOTS_SIDE; e += blockDim.x) {
+    int kind = e / SLOTS_SIDE, b = e - kind * SLOTS_SIDE;
+    int W = kind ? wf : w, H = kind ? hf : h;
+    // invert border_index
+    int i, j;
+    if (b < TX) { i = b; j = 0; }
+    else if (b < 2 * TX) { i = b - TX; j = H - 1; }
+    else if (b < 2 * TX + TY) { i = 0; j = b - 2 * TX; }
+    else { i = W - 1; j = b - 2 * TX - TY; }
+    if (W <= 0 || H <= 0 || i < 0 || i >= W || j < 0 || j >= H) continue;
+    if (border_index(i, j, W, H) != b) continue;  // slot not used by this tile shape
+    uint16_t p = kind ? s.pf[j * TX + i] : s.pv[j * TX + i];
+    uint64_t entry = BT_INVALID;
+    int k = p & PJ_IDX, ki = k % TX, kj = k / TX;
+    if ((p & PJ_TAG) == PJ_ROOT) {
+      int y = 2 * (ty0 + kj) + kind;
+      uint32_t rank = kind ? (uint32_t)s.rankB[kj][ki] + ((s.code[kj][ki] >> 19) & 1) : s.rankA[kj][ki];
+      entry = BT_ROOT | ((uint64_t)((long long)y * g.ntx + bx) << 8) | rank;
+    } else if ((p & PJ_TAG) == PJ_EXIT) {
+      uint32_t d = (kind ? (s.code[kj][ki] >> 24) : s.code[kj][ki]) & 3;
+      int gi = tx0 + ki + dir_dx(d), gj = ty0 + kj + dir_dy(d);
+      if (gi >= 0 && gj >= 0 && gi < g.vnx - kind && gj < g.vny - kind) entry = BT_EXIT | (uint64_t)border_slot(g, kind, gi, gj);
+      else st |= ST_CYCLE;  // a path leaving the window: never expected
+    }
+    table[tile_base + kind * SLOTS_SIDE + b] = entry;
+  }
+  if (st) atomicOr(status, st);
+}
+
+// ---------------------------------------------------------------------------
+// K3: resolve the border table.  Every EXIT chain is followed to its root;
+// pointers are compressed in place (any value a reader sees is a valid
+// pointer along the same chain), so no grid-wide barrier is needed.
+// ---------------------------------------------------------------------------
+__global__ void k_resolve(uint64_t *table, long long nslots, const uint32_t *__restrict__ offsets,
+                          uint32_t *__restrict__ status) {
+  for (long long sidx = blockIdx.x * (long long)blockDim.x + threadIdx.x; sidx < nslots;
+       sidx += (long long)gridDim.x * blockDim.x) {
+    volatile uint64_t *vt = table;
+    uint64_t e = vt[sidx];
+    long long iter = 0;
+    while (bt_tag(e) == BT_EXIT) {
+      if ((long long)bt_payload(e) >= nslots) { e = BT_INVALID; atomicOr(status, ST_RESOLVE_LIMIT); break; }
+      uint64_t t = vt[bt_payload(e)];
+      e = t;
+      if (bt_tag(e) == BT_EXIT) vt[sidx] = e;
+      if (++iter > nslots) { e = BT_INVALID; atomicOr(status, ST_RESOLVE_LIMIT); break; }
+    }
+    if (bt_tag(e) == BT_ROOT) {
+      uint64_t pl = bt_payload(e);
+      e = BT_FINAL | (uint64_t)(offsets[pl >> 8] + (uint32_t)(pl & 0xff));
+    }
+    vt[sidx] = e;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K4: owner labels, critical-point records and saddle arcs.
+// ---------------------------------------------------------------------------
+struct LabelSmem {
+  uint32_t code[TY][TX];
+  uint32_t labV[TY][TX];
+  uint32_t labF[TY][TX];
+  uint16_t pv[TY * TX];
+  uint16_t pf[TY * TX];
+  uint8_t rankA[TY][TX];
+  uint8_t rankB[TY][TX];
+  uint8_t cntA[TY], cntB[TY];
+  uint32_t offA[TY], offB[TY];
+};
+
+__device__ __forceinline__ uint32_t slot_label(const uint64_t *table, const GridGeom &g, int kind, int gi, int gj) {
+  uint64_t e = table[border_slot(g, kind, gi, gj)];
+  return bt_tag(e) == BT_FINAL ? (uint32_t)bt_payload(e) : LABEL_NONE;
+}
+__device__ __forceinline__ float hat(const float *hgt, const GridGeom &g, int vi, int vj) {
+  return __ldg(hgt + (long long)vj * g.pitch + vi);
+}
+// get_cell_fn (:1538-1552): float sum in getCellPoints order, then / count.
+__device__ __forceinline__ float cell_fn(const float *hgt, const GridGeom &g, int kind, int vi, int vj) {
+  float fn = 0.0f;
+  switch (kind) {
+    case 0: fn = __fadd_rn(fn, hat(hgt, g, vi, vj)); return __fdiv_rn(fn, 1.0f);
+    case 1: fn = __fadd_rn(fn, hat(hgt, g, vi + 1, vj)); fn = __fadd_rn(fn, hat(hgt, g, vi, vj)); return __fdiv_rn(fn, 2.0f);
+    case 2: fn = __fadd_rn(fn, hat(hgt, g, vi, vj + 1)); fn = __fadd_rn(fn, hat(hgt, g, vi, vj)); return __fdiv_rn(fn, 2.0f);
+    default:
+      fn = __fadd_rn(fn, hat(hgt, g, vi + 1, vj + 1));
+      fn = __fadd_rn(fn, hat(hgt, g, vi + 1, vj));
+      fn = __fadd_rn(fn, hat(hgt, g, vi, vj));
+      fn = __fadd_rn(fn, hat(hgt, g, vi, vj + 1));
+      return __fdiv_rn(fn, 4.0f);
+  }
+}
+
+
+
+__global__ void __launch_bounds__(GRAD_THREADS, 3)
+k_labels(const uint32_t *__restrict__ codes, const float *__restrict__ hgt, GridGeom g,
+         const uint32_t *__restrict__ offsets, const uint64_t *__restrict__ table, uint4 *__restrict__ labels,
+         CpOut cp, uint32_t *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  LabelSmem &s = *reinterpret_cast<LabelSmem *>(smem_raw);
+  const int bx = blockIdx.x, by = blockIdx.y;
+  const int tx0 = bx * TX, ty0 = by * TY;
+  int w, h, wf, hf;
+  tile_extent(g, bx, by, 0, w, h);
+  tile_extent(g, bx, by, 1, wf, hf);
+  uint32_t st = 0;
+
+  for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
+    int j = e / TX, i = e - j * TX;
+    s.code[j][i] = (i < w && j < h) ? codes[(long long)(ty0 + j) * g.vnx + tx0 + i] : 0u;
+  }
+  for (int j = threadIdx.x; j < h; j += blockDim.x) {
+    int y = 2 * (ty0 + j);
+    s.offA[j] = offsets[(long long)y * g.ntx + bx];
+    s.offB[j] = (y + 1 <= g.cy) ? offsets[(long long)(y + 1) * g.ntx + bx] : 0u;
+  }
+  __syncthreads();
+  row_ranks(s.code, s.rankA, s.rankB, s.cntA, s.cntB, w, h);
+  for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
+    int j = e / TX, i = e - j * TX;
+    uint16_t pvv = PJ_INVALID, pff = PJ_INVALID;
+    uint32_t c = s.code[j][i];
+    if (i < w && j < h) {
+      uint32_t cvv = c & 0xff;
+      if (cvv & CODE_CRIT) pvv = PJ_ROOT | e;
+      else if (in_rect(g, 2 * (tx0 + i), 2 * (ty0 + j))) {
+        if (on_tile_border(i, j, w, h)) pvv = PJ_EXIT | e;  // resolved through the border table
+        else { uint32_t d = cvv & 3; pvv = PJ_PTR | ((j + dir_dy(d)) * TX + i + dir_dx(d)); }
+      }
+    }
+    if (i < wf && j < hf) {
+      uint32_t cf = c >> 24;
+      if (cf & CODE_CRIT) pff = PJ_ROOT | e;
+      else if (in_rect(g, 2 * (tx0 + i) + 1, 2 * (ty0 + j) + 1)) {
+        if (on_tile_border(i, j, wf, hf)) pff = PJ_EXIT | e;
+        else { uint32_t d = cf & 3; pff = PJ_PTR | ((j + dir_dy(d)) * TX + i + dir_dx(d)); }
+      }
+    }
+    s.pv[e] = pvv;
+    s.pf[e] = pff;
+  }
+  __syncthreads();
+  if (pointer_jump(s.pv, s.pf)) st |= ST_CYCLE;
+
+  // terminal -> cp index
+  for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
+    int j = e / TX, i = e - j * TX;
+    uint32_t lv = LABEL_NONE, lf = LABEL_NONE;
+    uint16_t p = s.pv[e];
+    int k = p & PJ_IDX, ki = k % TX, kj = k / TX;
+    if ((p & PJ_TAG) == PJ_ROOT) lv = s.offA[kj] + s.rankA[kj][ki];
+    else if ((p & PJ_TAG) == PJ_EXIT) lv = slot_label(table, g, 0, tx0 + ki, ty0 + kj);
+    p = s.pf[e];
+    k = p & PJ_IDX; ki = k % TX; kj = k / TX;
+    if ((p & PJ_TAG) == PJ_ROOT) lf = s.offB[kj] + s.rankB[kj][ki] + ((s.code[kj][ki] >> 19) & 1);
+    else if ((p & PJ_TAG) == PJ_EXIT) lf = slot_label(table, g, 1, tx0 + ki, ty0 + kj);
+    s.labV[j][i] = (i < w && j < h) ? lv : LABEL_NONE;
+    s.labF[j][i] = (i < wf && j < hf) ? lf : LABEL_NONE;
+  }
+  __syncthreads();
+
+  for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
+    int j = e / TX, i = e - j * TX;
+    if (i >= w || j >= h) continue;
+    const int vi = tx0 + i, vj = ty0 + j, x = 2 * vi, y = 2 * vj;
+    const uint32_t c = s.code[j][i];
+    // neighbour labels that may live in the next tile
+    auto labV_at = [&](int ii, int jj) -> uint32_t {
+      if (ii >= 0 && ii < w && jj >= 0 && jj < h) return s.labV[jj][ii];
+      return slot_label(table, g, 0, tx0 + ii, ty0 + jj);
+    };
+    auto labF_at = [&](int ii, int jj) -> uint32_t {
+      if (ii >= 0 && ii < wf && jj >= 0 && jj < hf) return s.labF[jj][ii];
+      return slot_label(table, g, 1, tx0 + ii, ty0 + jj);
+    };
+    uint32_t L[4];
+    L[0] = s.labV[j][i];
+    L[3] = s.labF[j][i];
+    uint32_t idxH = s.offA[j] + s.rankA[j][i] + ((c >> 3) & 1);
+    uint32_t idxVt = s.offB[j] + s.rankB[j][i];
+    // H(i,j)
+    L[1] = LABEL_NONE;
+    uint32_t ch = (c >> 8) & 0xff;
+    if (vi + 1 < g.vnx) {
+      if (ch & CODE_CRIT) L[1] = idxH;
+      else if ((ch & CODE_PAIRED) && in_rect(g, x + 1, y)) {
+        switch (ch & 3) {
+          case DIR_MX: L[1] = s.labV[j][i]; break;
+          case DIR_PX: L[1] = labV_at(i + 1, j); break;
+          case DIR_PY: L[1] = labF_at(i, j); break;
+          default: L[1] = labF_at(i, j - 1); break;
+        }
+      }
+    }
+    // Vt(i,j)
+    L[2] = LABEL_NONE;
+    uint32_t cvt = (c >> 16) & 0xff;
+    if (vj + 1 < g.vny) {
+      if (cvt & CODE_CRIT) L[2] = idxVt;
+      else if ((cvt & CODE_PAIRED) && in_rect(g, x, y + 1)) {
+        switch (cvt & 3) {
+          case DIR_MY: L[2] = s.labV[j][i]; break;
+          case DIR_PY: L[2] = labV_at(i, j + 1); break;
+          case DIR_PX: L[2] = labF_at(i, j); break;
+          default: L[2] = labF_at(i - 1, j); break;
+        }
+      }
+    }
+    labels[(long long)vj * g.vnx + vi] = make_uint4(L[0], L[1], L[2], L[3]);
+
+    // critical-point records
+#pragma unroll
+    for (int kind = 0; kind < 4; ++kind) {
+      uint32_t cc = (c >> (8 * kind)) & 0xff;
+      if (!(cc & CODE_CRIT)) continue;
+      int cxr = x + (kind & 1), cyr = y + (kind >> 1);
+      uint32_t k = kind == 0 ? L[0] : kind == 1 ? idxH : kind == 2 ? idxVt : L[3];
+      if ((long long)k >= cp.cap) { st |= ST_CAPACITY; continue; }
+      cp.cellid[k] = pack_cellid(g.ex0 + cxr, g.ey0 + cyr);
+      cp.fn[k] = cell_fn(hgt, g, kind, vi, vj);
+      cp.flags[k] = (cc & CODE_PAIRED) ? 1 : 0;
+      if (cc & CODE_PAIRED) {
+        uint32_t d = cc & 3;
+        cp.pair_cell[k] = pack_cellid(g.ex0 + cxr + dir_dx(d), g.ey0 + cyr + dir_dy(d));
+      }
+      if (kind == 1 || kind == 2) {
+        // facets f[0..1] and ext-filtered cofacets (writeout_connectivity, :1876-1898)
+        uint32_t f0, f1, q0 = LABEL_NONE, q1 = LABEL_NONE;
+        if (kind == 1) {
+          f0 = labV_at(i + 1, j); f1 = L[0];
+          if (vj + 1 < g.vny) q0 = labF_at(i, j);
+          if (vj >= 1) q1 = labF_at(i, j - 1);
+        } else {
+          f0 = labV_at(i, j + 1); f1 = L[0];
+          if (vi + 1 < g.vnx) q0 = labF_at(i, j);
+          if (vi >= 1) q1 = labF_at(i - 1, j);
+        }
+        uint32_t dlo = min(f0, f1), dhi = max(f0, f1), alo = min(q0, q1), ahi = max(q0, q1);
+        cp.des2[2 * k] = dlo; cp.des2[2 * k + 1] = dhi;
+        cp.asc2[2 * k] = alo; cp.asc2[2 * k + 1] = ahi;
+        cp.dcnt[k] = (dlo != LABEL_NONE) + (dhi != LABEL_NONE);
+        cp.acnt[k] = (alo != LABEL_NONE) + (ahi != LABEL_NONE);
+        if (dlo != LABEL_NONE && dlo < cp.cap) atomicAdd(cp.acnt + dlo, 1u);
+        if (dhi != LABEL_NONE && dhi < cp.cap) atomicAdd(cp.acnt + dhi, 1u);
+        if (alo != LABEL_NONE && alo < cp.cap) atomicAdd(cp.dcnt + alo, 1u);
+        if (ahi != LABEL_NONE && ahi < cp.cap) atomicAdd(cp.dcnt + ahi, 1u);
+      } else {
+        cp.des2[2 * k] = cp.des2[2 * k + 1] = LABEL_NONE;
+        cp.asc2[2 * k] = cp.asc2[2 * k + 1] = LABEL_NONE;
+      }
+    }
+  }
+  if (st) atomicOr(status, st);
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+size_t grad_smem_bytes() { return sizeof(GradSmem); }
+size_t label_smem_bytes() { return sizeof(LabelSmem); }
+
+cudaError_t launch_gradient(const float *hgt, const GridGeom &g, uint32_t *codes, uint8_t *rowcnt, uint64_t *table,
+                            uint32_t *status, cudaStream_t st) {
+  static bool init = false;
+  if (!init) {
+    cudaError_t e = cudaFuncSetAttribute(k_gradient, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradSmem));
+    if (e != cudaSuccess) return e;
+    init = true;
+  }
+  dim3 grid(g.ntx, g.nty);
+  k_gradient<<<grid, GRAD_THREADS, sizeof(GradSmem), st>>>(hgt, g, codes, rowcnt, table, status);
+  DMSC_LAUNCHED(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_resolve(uint64_t *table, long long nslots, const uint32_t *offsets, uint32_t *status,
+                           cudaStream_t st) {
+  int threads = 256;
+  long long blocks = (nslots + threads - 1) / threads;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  k_resolve<<<(unsigned)blocks, threads, 0, st>>>(table, nslots, offsets, status);
+  DMSC_LAUNCHED(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_labels(const uint32_t *codes, const float *hgt, const GridGeom &g, const uint32_t *offsets,
+                          const uint64_t *table, uint4 *labels, const CpOut &cp, uint32_t *status, cudaStream_t st) {
+  static bool init = false;
+  if (!init) {
+    cudaError_t e = cudaFuncSetAttribute(k_labels, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LabelSmem));
+    if (e != cudaSuccess) return e;
+    init = true;
+  }
+  dim3 grid(g.ntx, g.nty);
+  k_labels<<<grid, GRAD_THREADS, sizeof(LabelSmem), st>>>(codes, hgt, g, offsets, table, labels, cp, status);
+  DMSC_LAUNCHED(1);
+  return cudaGetLastError();
+}
+
+}  // namespace dmsc

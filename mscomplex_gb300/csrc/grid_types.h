@@ -1,0 +1,83 @@
+// grid_types.h -- host-side handle types behind the C ABI (device-resident data).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "dmsc.h"
+#include "dmsc_common.cuh"
+
+// Grow-only device buffer.
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  cudaError_t ensure(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    release();
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)&p, sizeof(T) * count);
+    if (e != cudaSuccess) { p = nullptr; n = 0; return e; }
+    n = count;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+// GridDataset (dmsc/include/grid_dataset.h:35-240) with device-resident cell arrays.
+struct dmsc_dataset {
+  dmsc_ctx *ctx = nullptr;
+  int16_t rect[4], ext[4];
+  dmsc::GridGeom g;
+  const float *hgt = nullptr;  // heights on the device (owned copy or borrowed)
+  DevBuf<float> hown;
+  DevBuf<uint32_t> codes;      // uchar4 gradient codes per vertex
+  DevBuf<uint4> labels;        // owner labels (cp indices) of the 4 cells of each vertex
+  DevBuf<uint8_t> rowcnt;      // critical cells per (cell row, tile column)
+  DevBuf<uint32_t> offsets;    // exclusive scan of rowcnt: first cp index of each segment
+  DevBuf<uint64_t> table;      // border table
+  DevBuf<uint32_t> scal;       // [0] status word, [1] number of critical points
+  uint32_t *host_scal = nullptr;
+  long long cap = 0;           // capacity of the cp arrays
+  long long ncp = 0;
+  bool worked = false;
+  DevBuf<uint32_t> cp_cellid, cp_pair_cell, cp_des2, cp_asc2, cp_acnt, cp_dcnt, cp_pair_idx;
+  DevBuf<float> cp_fn;
+  DevBuf<uint8_t> cp_flags;
+  cudaEvent_t ev[8] = {};     // stage events (only when the context has timing enabled)
+  bool ev_ready = false;
+
+  long long nslots() const { return (long long)g.ntx * g.nty * dmsc::SLOTS_PER_TILE; }
+  bool rect_is_ext() const {
+    return rect[0] == ext[0] && rect[1] == ext[1] && rect[2] == ext[2] && rect[3] == ext[3];
+  }
+  int alloc_cells();
+  int alloc_cps(long long n);
+  ~dmsc_dataset();
+};
+
+// GridMSComplex (dmsc/include/grid_mscomplex.h:48-84) as flat device arrays.
+struct dmsc_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool timing = false;
+};
+
+struct dmsc_msc {
+  dmsc_ctx *ctx = nullptr;
+  int16_t rect[4], ext[4];
+  long long ncp = 0, nasc = 0, ndes = 0, nadisc = 0, nddisc = 0;
+  DevBuf<uint32_t> cellid, pair_idx, aoff, asc, doff, des, adoff, ddoff;
+  DevBuf<uint32_t> adisc, ddisc;  // packed cell ids
+  DevBuf<float> fn;
+  DevBuf<uint8_t> flags;  // bit0 isCancelled, bit1 isOnStrangulationPath, bit2 isBoundryCancelable
+
+  int writeout_from(const dmsc_dataset &d, cudaStream_t st);
+};

@@ -1,0 +1,390 @@
+// primitives.cu -- device-wide exclusive scan, stable LSD radix sort and the
+// kernels that assemble the Morse-Smale complex in CSR form.
+//
+// The reference's scan is the OpenCL PrefixScan (dmsc/src/prefix_scan.cpp:
+// 340-465, kernels absent: dmsc/resources/scan_kernel.cl is empty) and its
+// sort slot is an unused bitonic sort (dmsc/src/bitonic_sort.cpp).  Both are
+// written here from scratch: the scan is reduce-then-scan with no inter-CTA
+// waiting, the radix sort is a stable 8-bit LSD sort (histogram, scan,
+// match_any-ranked scatter).
+#include "dmsc_common.cuh"
+#include "dmsc_internal.h"
+
+namespace dmsc {
+
+unsigned long long g_kernel_launches = 0;
+
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_CHUNK = SCAN_THREADS * SCAN_ITEMS;
+
+// Block-wide exclusive scan of one value per thread; returns the block total.
+__device__ __forceinline__ uint32_t block_exscan(uint32_t v, uint32_t &excl) {
+  __shared__ uint32_t wsum[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t s = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, s, o);
+    if (lane >= o) s += t;
+  }
+  if (lane == 31) wsum[warp] = s;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t ws = lane < nw ? wsum[lane] : 0u;
+    uint32_t ss = ws;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, ss, o);
+      if (lane >= o) ss += t;
+    }
+    if (lane < nw) wsum[lane] = ss - ws;
+    if (lane == 31) wsum[31] = ss;  // total (nw <= 32)
+  }
+  __syncthreads();
+  excl = wsum[warp] + s - v;
+  uint32_t total = wsum[31];
+  __syncthreads();
+  return total;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const T *__restrict__ in, long long n, uint32_t *partial) {
+  long long base = (long long)blockIdx.x * SCAN_CHUNK + (long long)threadIdx.x * SCAN_ITEMS;
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k)
+    if (base + k < n) s += (uint32_t)in[base + k];
+  uint32_t ex;
+  uint32_t tot = block_exscan(s, ex);
+  if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const T *__restrict__ in, long long n,
+                                                            const uint32_t *__restrict__ block_off,
+                                                            uint32_t *__restrict__ out, uint32_t *total) {
+  long long base = (long long)blockIdx.x * SCAN_CHUNK + (long long)threadIdx.x * SCAN_ITEMS;
+  uint32_t v[SCAN_ITEMS];
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    v[k] = (base + k < n) ? (uint32_t)in[base + k] : 0u;
+    s += v[k];
+  }
+  uint32_t ex;
+  uint32_t tot = block_exscan(s, ex);
+  uint32_t run = (block_off ? block_off[blockIdx.x] : 0u) + ex;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    if (base + k < n) out[base + k] = run;
+    run += v[k];
+  }
+  if (total && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total = (block_off ? block_off[blockIdx.x] : 0u) + tot;
+}
+
+template <typename T>
+cudaError_t scan_exclusive_t(const T *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st) {
+  if (n <= 0) {
+    if (total) return cudaMemsetAsync(total, 0, sizeof(uint32_t), st);
+    return cudaSuccess;
+  }
+  long long nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+  if (nb == 1) {
+    k_scan_down<T><<<1, SCAN_THREADS, 0, st>>>(in, n, nullptr, out, total);
+    DMSC_LAUNCHED(1);
+    return cudaGetLastError();
+  }
+  uint32_t *part = nullptr, *poff = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&part, sizeof(uint32_t) * nb * 2, st);
+  if (e != cudaSuccess) return e;
+  poff = part + nb;
+  k_scan_reduce<T><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, part);
+  DMSC_LAUNCHED(1);
+  e = scan_exclusive_t<uint32_t>(part, nb, poff, nullptr, st);
+  if (e == cudaSuccess) {
+    k_scan_down<T><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, poff, out, total);
+    DMSC_LAUNCHED(1);
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(part, st);
+  return e;
+}
+
+cudaError_t scan_exclusive_u8(const uint8_t *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st) {
+  return scan_exclusive_t<uint8_t>(in, n, out, total, st);
+}
+cudaError_t scan_exclusive_u32(const uint32_t *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st) {
+  return scan_exclusive_t<uint32_t>(in, n, out, total, st);
+}
+
+// ---------------------------------------------------------------------------
+// stable LSD radix sort of (key, value) pairs on key bits [0, nbits)
+// ---------------------------------------------------------------------------
+constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_ROUNDS = 8;
+constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;  // each warp owns a contiguous run of 256 items
+
+__global__ void __launch_bounds__(RS_THREADS) k_radix_hist(const uint32_t *__restrict__ keys, long long n, int shift,
+                                                           uint32_t *__restrict__ hist, long long nb) {
+  __shared__ uint32_t cnt[256];
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  long long base = (long long)blockIdx.x * RS_TILE;
+  for (int k = threadIdx.x; k < RS_TILE; k += RS_THREADS) {
+    long long i = base + k;
+    if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[(long long)threadIdx.x * nb + blockIdx.x] = cnt[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
+                                                              long long n, int shift, const uint32_t *__restrict__ hoff,
+                                                              long long nb, uint32_t *__restrict__ kout,
+                                                              uint32_t *__restrict__ vout) {
+  __shared__ uint32_t wcnt[RS_WARPS][256];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = threadIdx.x; k < RS_WARPS * 256; k += RS_THREADS) (&wcnt[0][0])[k] = 0;
+  __syncthreads();
+  long long base = (long long)blockIdx.x * RS_TILE + warp * (32 * RS_ROUNDS);
+  uint32_t key[RS_ROUNDS], val[RS_ROUNDS], rank[RS_ROUNDS];
+  const uint32_t lt_mask = (1u << lane) - 1u;
+#pragma unroll
+  for (int r = 0; r < RS_ROUNDS; ++r) {
+    long long i = base + r * 32 + lane;
+    bool valid = i < n;
+    key[r] = valid ? kin[i] : 0u;
+    val[r] = valid ? vin[i] : 0u;
+    uint32_t d = valid ? ((key[r] >> shift) & 255u) : 256u;
+    uint32_t peers = __match_any_sync(0xffffffffu, d);
+    uint32_t before = valid ? wcnt[warp][d] : 0u;
+    rank[r] = before + __popc(peers & lt_mask);
+    __syncwarp();
+    if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  {
+    uint32_t d = threadIdx.x, run = 0;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; ++w) { uint32_t t = wcnt[w][d]; wcnt[w][d] = run; run += t; }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < RS_ROUNDS; ++r) {
+    long long i = base + r * 32 + lane;
+    if (i < n) {
+      uint32_t d = (key[r] >> shift) & 255u;
+      uint32_t pos = hoff[(long long)d * nb + blockIdx.x] + wcnt[warp][d] + rank[r];
+      kout[pos] = key[r];
+      vout[pos] = val[r];
+    }
+  }
+}
+
+// Sorts in place (keys/vals) using caller scratch of the same size.
+cudaError_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *ktmp, uint32_t *vtmp, long long n, int nbits,
+                             cudaStream_t st) {
+  if (n <= 1 || nbits <= 0) return cudaSuccess;
+  long long nb = (n + RS_TILE - 1) / RS_TILE;
+  uint32_t *hist = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&hist, sizeof(uint32_t) * 256 * nb * 2, st);
+  if (e != cudaSuccess) return e;
+  uint32_t *hoff = hist + 256 * nb;
+  uint32_t *ka = keys, *va = vals, *kb = ktmp, *vb = vtmp;
+  for (int shift = 0; shift < nbits; shift += 8) {
+    k_radix_hist<<<(unsigned)nb, RS_THREADS, 0, st>>>(ka, n, shift, hist, nb);
+    DMSC_LAUNCHED(1);
+    e = scan_exclusive_u32(hist, 256 * nb, hoff, nullptr, st);
+    if (e != cudaSuccess) break;
+    k_radix_scatter<<<(unsigned)nb, RS_THREADS, 0, st>>>(ka, va, n, shift, hoff, nb, kb, vb);
+    DMSC_LAUNCHED(1);
+    std::swap(ka, kb);
+    std::swap(va, vb);
+  }
+  if (e == cudaSuccess && ka != keys) {
+    cudaMemcpyAsync(keys, ka, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(vals, va, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+  }
+  cudaFreeAsync(hist, st);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// complex assembly (writeout_connectivity, dmsc/src/grid_dataset.cpp:1858-1907)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int cell_dim(uint32_t packed) {
+  return (int)(packed & 1u) + (int)((packed >> 16) & 1u);
+}
+
+// Saddle segments come straight from the 2+2 staged labels; every staged
+// (extremum label, saddle) arc also becomes a sort item for the extremum side.
+__global__ void k_fill_saddles(long long ncp, const uint32_t *__restrict__ cellid, const uint32_t *__restrict__ des2,
+                               const uint32_t *__restrict__ asc2, const uint32_t *__restrict__ aoff,
+                               const uint32_t *__restrict__ doff, uint32_t *__restrict__ asc, uint32_t *__restrict__ des,
+                               uint32_t *__restrict__ kmin, uint32_t *__restrict__ kmax, uint32_t *__restrict__ vidx) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < ncp; k += (long long)gridDim.x * blockDim.x) {
+    bool sad = cell_dim(cellid[k]) == 1;
+    uint32_t d0 = sad ? des2[2 * k] : LABEL_NONE, d1 = sad ? des2[2 * k + 1] : LABEL_NONE;
+    uint32_t a0 = sad ? asc2[2 * k] : LABEL_NONE, a1 = sad ? asc2[2 * k + 1] : LABEL_NONE;
+    if (sad) {
+      uint32_t p = doff[k], pe = doff[k + 1];
+      if (d0 != LABEL_NONE && p < pe) des[p++] = d0;
+      if (d1 != LABEL_NONE && p < pe) des[p++] = d1;
+      p = aoff[k]; pe = aoff[k + 1];
+      if (a0 != LABEL_NONE && p < pe) asc[p++] = a0;
+      if (a1 != LABEL_NONE && p < pe) asc[p++] = a1;
+    }
+    uint32_t none = (uint32_t)ncp;
+    kmin[2 * k] = d0 == LABEL_NONE ? none : d0;
+    kmin[2 * k + 1] = d1 == LABEL_NONE ? none : d1;
+    kmax[2 * k] = a0 == LABEL_NONE ? none : a0;
+    kmax[2 * k + 1] = a1 == LABEL_NONE ? none : a1;
+    vidx[2 * k] = (uint32_t)k;
+    vidx[2 * k + 1] = (uint32_t)k;
+  }
+}
+
+__global__ void k_run_starts(long long n, long long ncp, const uint32_t *__restrict__ keys, uint32_t *__restrict__ start) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    uint32_t k = keys[p];
+    if (k < (uint32_t)ncp && (p == 0 || keys[p - 1] != k)) start[k] = (uint32_t)p;
+  }
+}
+__global__ void k_scatter_runs(long long n, long long ncp, const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
+                               const uint32_t *__restrict__ start, const uint32_t *__restrict__ off,
+                               uint32_t *__restrict__ out, long long out_cap, uint32_t *__restrict__ status) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    uint32_t k = keys[p];
+    if (k >= (uint32_t)ncp) continue;
+    uint32_t r = (uint32_t)p - start[k];
+    long long pos = (long long)off[k] + r;
+    if (r < off[k + 1] - off[k] && pos < out_cap) out[pos] = vals[p];
+    else atomicOr(status, ST_INVARIANT);
+  }
+}
+
+static unsigned grid_for(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  if (b > 152 * 32) b = 152 * 32;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+cudaError_t build_csr(long long ncp, const uint32_t *cellid, const uint32_t *des2, const uint32_t *asc2,
+                      const uint32_t *aoff, const uint32_t *doff, uint32_t *asc, uint32_t *des, long long out_cap,
+                      uint32_t *status, cudaStream_t st) {
+  if (ncp <= 0) return cudaSuccess;
+  long long n = 2 * ncp;
+  uint32_t *buf = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&buf, sizeof(uint32_t) * (n * 6 + ncp), st);
+  if (e != cudaSuccess) return e;
+  uint32_t *kmin = buf, *kmax = buf + n, *vmin = buf + 2 * n, *vmax = buf + 3 * n, *kt = buf + 4 * n, *vt = buf + 5 * n;
+  uint32_t *start = buf + 6 * n;
+  k_fill_saddles<<<grid_for(ncp, 256), 256, 0, st>>>(ncp, cellid, des2, asc2, aoff, doff, asc, des, kmin, kmax, vmin);
+  DMSC_LAUNCHED(1);
+  cudaMemcpyAsync(vmax, vmin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+  int nbits = 1;
+  while ((1ll << nbits) <= ncp) ++nbits;
+  // minima: asc side; maxima: des side -- ascending saddle index within each run (stable sort)
+  e = radix_sort_pairs(kmin, vmin, kt, vt, n, nbits, st);
+  if (e == cudaSuccess) {
+    k_run_starts<<<grid_for(n, 256), 256, 0, st>>>(n, ncp, kmin, start);
+    DMSC_LAUNCHED(1);
+    k_scatter_runs<<<grid_for(n, 256), 256, 0, st>>>(n, ncp, kmin, vmin, start, aoff, asc, out_cap, status);
+    DMSC_LAUNCHED(1);
+    e = radix_sort_pairs(kmax, vmax, kt, vt, n, nbits, st);
+  }
+  if (e == cudaSuccess) {
+    k_run_starts<<<grid_for(n, 256), 256, 0, st>>>(n, ncp, kmax, start);
+    DMSC_LAUNCHED(1);
+    k_scatter_runs<<<grid_for(n, 256), 256, 0, st>>>(n, ncp, kmax, vmax, start, doff, des, out_cap, status);
+    DMSC_LAUNCHED(1);
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(buf, st);
+  return e;
+}
+
+// pair_idx of paired critical cells: binary search of the pair's cell id in
+// the row-major (y, then x) sorted cp list.
+__global__ void k_pair_index(long long ncp, const uint32_t *__restrict__ cellid, const uint8_t *__restrict__ flags,
+                             const uint32_t *__restrict__ pair_cell, uint32_t *__restrict__ pair_idx,
+                             uint32_t *__restrict__ status) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < ncp; k += (long long)gridDim.x * blockDim.x) {
+    if (!(flags[k] & 1)) { pair_idx[k] = 0xFFFFFFFFu; continue; }
+    uint32_t tk = pair_cell[k];  // packed x | y<<16 sorts in (y, x) order for non-negative coordinates
+    long long lo = 0, hi = ncp;
+    while (lo < hi) {
+      long long mid = (lo + hi) >> 1;
+      if (cellid[mid] < tk) lo = mid + 1; else hi = mid;
+    }
+    if (lo < ncp && cellid[lo] == tk) pair_idx[k] = (uint32_t)lo;
+    else { pair_idx[k] = 0xFFFFFFFFu; atomicOr(status, ST_INVARIANT); }
+  }
+}
+
+cudaError_t launch_pair_index(long long ncp, const uint32_t *cellid, const uint8_t *flags, const uint32_t *pair_cell,
+                              uint32_t *pair_idx, uint32_t *status, cudaStream_t st) {
+  if (ncp <= 0) return cudaSuccess;
+  k_pair_index<<<grid_for(ncp, 256), 256, 0, st>>>(ncp, cellid, flags, pair_cell, pair_idx, status);
+  DMSC_LAUNCHED(1);
+  return cudaGetLastError();
+}
+
+// Complex flags after writeout: only isBoundryCancelable (bit 2) can be set.
+__global__ void k_msc_flags(long long ncp, const uint8_t *__restrict__ cpflags, uint8_t *__restrict__ out) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < ncp; k += (long long)gridDim.x * blockDim.x)
+    out[k] = (cpflags[k] & 1) ? 4 : 0;
+}
+cudaError_t launch_msc_flags(long long ncp, const uint8_t *cpflags, uint8_t *out, cudaStream_t st) {
+  if (ncp <= 0) return cudaSuccess;
+  k_msc_flags<<<grid_for(ncp, 256), 256, 0, st>>>(ncp, cpflags, out);
+  DMSC_LAUNCHED(1);
+  return cudaGetLastError();
+}
+
+// Reference-layout export of the per-cell arrays: C order [x][y] over ext
+// (grid_dataset.cpp:1468-1483), flags int8, pairs/own as (x,y) int16 pairs.
+__global__ void k_export_cells(GridGeom g, const uint32_t *__restrict__ codes, const uint4 *__restrict__ labels,
+                               const uint32_t *__restrict__ cp_cellid, long long ncp, int8_t *__restrict__ flags,
+                               int16_t *__restrict__ pairs, int16_t *__restrict__ own) {
+  const long long cny = g.cy + 1, n = (long long)(g.cx + 1) * cny;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    int x = (int)(t / cny), y = (int)(t - (long long)x * cny);
+    long long v = (long long)(y >> 1) * g.vnx + (x >> 1);
+    int kind = (x & 1) | ((y & 1) << 1);
+    uint32_t c = (codes[v] >> (8 * kind)) & 0xff;
+    uint4 L4 = labels[v];
+    uint32_t lab = kind == 0 ? L4.x : kind == 1 ? L4.y : kind == 2 ? L4.z : L4.w;
+    if (flags) flags[t] = (int8_t)((c >> 2) & 3);
+    if (pairs) {
+      int16_t px = -1, py = -1;
+      if (c & CODE_PAIRED) {
+        uint32_t d = c & 3;
+        px = (int16_t)(g.ex0 + x + (d == DIR_PX ? 1 : d == DIR_MX ? -1 : 0));
+        py = (int16_t)(g.ey0 + y + (d == DIR_PY ? 1 : d == DIR_MY ? -1 : 0));
+      }
+      pairs[2 * t] = px;
+      pairs[2 * t + 1] = py;
+    }
+    if (own) {
+      int16_t ox = -1, oy = -1;
+      if (lab < (uint32_t)ncp) { uint32_t cc = cp_cellid[lab]; ox = (int16_t)(cc & 0xffff); oy = (int16_t)(cc >> 16); }
+      own[2 * t] = ox;
+      own[2 * t + 1] = oy;
+    }
+  }
+}
+
+cudaError_t launch_export_cells(const GridGeom &g, const uint32_t *codes, const uint4 *labels, const uint32_t *cp_cellid,
+                                long long ncp, int8_t *flags, int16_t *pairs, int16_t *own, cudaStream_t st) {
+  long long n = (long long)(g.cx + 1) * (g.cy + 1);
+  k_export_cells<<<grid_for(n, 256), 256, 0, st>>>(g, codes, labels, cp_cellid, ncp, flags, pairs, own);
+  DMSC_LAUNCHED(1);
+  return cudaGetLastError();
+}
+
+}  // namespace dmsc

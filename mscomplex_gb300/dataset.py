@@ -1,0 +1,175 @@
+"""Host-side mirror of the reference's grid interfaces over libdmsc.so.
+
+``GridDataset`` mirrors dmsc/include/grid_dataset.h (constructor from
+rect/ext, ``init``, ``work``, ``writeout_connectivity``, and access to the
+cell flags / pairs / owners and the critical-cell list); ``GridMSComplex``
+mirrors dmsc/include/grid_mscomplex.h.  Names and argument meaning follow the
+reference; errors raise ``DmscError`` (the reference throws std::logic_error /
+std::runtime_error).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+import numpy as np
+
+from ._native import check, load
+
+_ctx_lock = threading.Lock()
+_ctx = {}
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """GridDataset::init_opencl / stop_opencl equivalent: one per device."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        check(self.lib.dmsc_init(device, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    def set_timing(self, enable: bool = True):
+        check(self.lib.dmsc_set_timing(self.h, int(enable)))
+
+    def close(self):
+        if self.h:
+            check(self.lib.dmsc_shutdown(self.h))
+            self.h = None
+
+
+def default_context(device: int = 0) -> Context:
+    with _ctx_lock:
+        if device not in _ctx:
+            _ctx[device] = Context(device)
+        return _ctx[device]
+
+
+def _rect(r) -> np.ndarray:
+    a = np.asarray(r, dtype=np.int16).reshape(4)
+    return np.ascontiguousarray(a)
+
+
+class GridDataset:
+    """One piece of the grid: rect (owned cells) inside ext (rect plus halo),
+    both as (left, bottom, right, top) in cell coordinates."""
+
+    def __init__(self, rect, ext=None, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.lib = self.ctx.lib
+        self.rect = _rect(rect)
+        self.ext = _rect(ext if ext is not None else rect)
+        h = C.c_void_p()
+        check(self.lib.dmsc_dataset_create(self.ctx.h, _ptr(self.rect), _ptr(self.ext), C.byref(h)))
+        self.h = h
+        self.cnx = int(self.ext[2] - self.ext[0]) + 1
+        self.cny = int(self.ext[3] - self.ext[1]) + 1
+        self.vnx = self.cnx // 2 + 1
+        self.vny = self.cny // 2 + 1
+        self._keep = None
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.dmsc_dataset_destroy(self.h)
+            self.h = None
+
+    def init(self, heights, stream=None):
+        """GridDataset::init: heights of the ext window, shape (vny, vnx), x fastest.
+        A numpy array is copied to the device; a CUDA tensor is borrowed."""
+        if hasattr(heights, "is_cuda") and heights.is_cuda:
+            t = heights
+            if t.dtype.__repr__() != "torch.float32" or t.dim() != 2 or t.stride(1) != 1:
+                raise ValueError("device heights must be a 2D float32 tensor with unit x stride")
+            if tuple(t.shape) != (self.vny, self.vnx):
+                raise ValueError(f"heights shape {tuple(t.shape)} != ext window {(self.vny, self.vnx)}")
+            self._keep = t
+            check(self.lib.dmsc_dataset_init(self.h, C.c_void_p(t.data_ptr()), t.stride(0), 1, stream))
+        else:
+            a = np.ascontiguousarray(heights, dtype=np.float32)
+            if a.shape != (self.vny, self.vnx):
+                raise ValueError(f"heights shape {a.shape} != ext window {(self.vny, self.vnx)}")
+            self._keep = a
+            check(self.lib.dmsc_dataset_init(self.h, _ptr(a), a.shape[1], 0, stream))
+        return self
+
+    def work(self, stream=None):
+        """Gradient, critical-cell collation and owner extrema (GridDataset::work)."""
+        check(self.lib.dmsc_dataset_work(self.h, stream))
+        return self
+
+    @property
+    def num_critical(self) -> int:
+        n = C.c_int64()
+        check(self.lib.dmsc_dataset_num_critical(self.h, C.byref(n)))
+        return n.value
+
+    def cells(self):
+        """(flags int8, pairs int16[...,2], own int16[...,2]) in the reference
+        layout [x][y] over ext (shape (cnx, cny))."""
+        n = self.cnx * self.cny
+        flags = np.zeros(n, np.int8)
+        pairs = np.zeros((n, 2), np.int16)
+        own = np.zeros((n, 2), np.int16)
+        check(self.lib.dmsc_dataset_export_cells(self.h, _ptr(flags), _ptr(pairs), _ptr(own), None))
+        sh = (self.cnx, self.cny)
+        return flags.reshape(sh), pairs.reshape(sh + (2,)), own.reshape(sh + (2,))
+
+    def critical_cells(self) -> np.ndarray:
+        n = self.num_critical
+        out = np.zeros((n, 2), np.int16)
+        if n:
+            check(self.lib.dmsc_dataset_export_critical(self.h, _ptr(out), None))
+        return out
+
+    STAGES = ("gradient", "collate_scan", "border_resolve", "labels_arcs", "connectivity")
+
+    def stage_times(self) -> dict:
+        ms = np.zeros(5, np.float32)
+        check(self.lib.dmsc_dataset_stage_times(self.h, _ptr(ms), 5))
+        return dict(zip(self.STAGES, (float(v) for v in ms)))
+
+    def writeout_connectivity(self, stream=None) -> "GridMSComplex":
+        h = C.c_void_p()
+        check(self.lib.dmsc_dataset_writeout_connectivity(self.h, C.byref(h), stream))
+        return GridMSComplex(h, self.ctx)
+
+
+class GridMSComplex:
+    """A Morse-Smale complex held on the device (handle to dmsc_msc)."""
+
+    def __init__(self, handle, ctx: Context):
+        self.h = handle
+        self.ctx = ctx
+        self.lib = ctx.lib
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.dmsc_msc_destroy(self.h)
+            self.h = None
+
+    def sizes(self):
+        s = np.zeros(5, np.int64)
+        check(self.lib.dmsc_msc_sizes(self.h, _ptr(s)))
+        return [int(v) for v in s]
+
+    def export(self) -> dict:
+        """Flat arrays with the same keys as the oracle's complex dump."""
+        n, na, nd, nad, ndd = self.sizes()
+        d = dict(
+            rect_ext=np.zeros(8, np.int16),
+            cellid=np.zeros((n, 2), np.int16), fn=np.zeros(n, np.float32),
+            pair_idx=np.zeros(n, np.uint32), flags=np.zeros(n, np.uint8),
+            asc_off=np.zeros(n + 1, np.uint32), asc=np.zeros(na, np.uint32),
+            des_off=np.zeros(n + 1, np.uint32), des=np.zeros(nd, np.uint32),
+            adisc_off=np.zeros(n + 1, np.uint32), adisc=np.zeros((nad, 2), np.int16),
+            ddisc_off=np.zeros(n + 1, np.uint32), ddisc=np.zeros((ndd, 2), np.int16),
+        )
+        keys = ("rect_ext", "cellid", "fn", "pair_idx", "flags", "asc_off", "asc", "des_off", "des",
+                "adisc_off", "adisc", "ddisc_off", "ddisc")
+        check(self.lib.dmsc_msc_export(self.h, *(_ptr(d[k]) for k in keys), None))
+        return d
