@@ -153,7 +153,7 @@ int dmsc_dataset_work(dmsc_dataset *d, void *stream) {
   if (tm) CK(cudaEventRecord(d->ev[1], st));
   CK(scan_exclusive_u8(d->rowcnt.p, (long long)(g.cy + 1) * g.ntx, d->offsets.p, d->scal.p + 1, st));
   if (tm) CK(cudaEventRecord(d->ev[2], st));
-  CK(launch_resolve(d->table.p, d->nslots(), d->offsets.p, d->scal.p, st));
+  CK(launch_resolve(d->table.p, d->nslots(), d->offsets.p, (long long)(g.cy + 1) * g.ntx, d->scal.p, st));
   if (tm) CK(cudaEventRecord(d->ev[3], st));
   if (d->cap <= 0) d->cap = (long long)g.vnx * g.vny / 16 + 4096;
   for (int attempt = 0; attempt < 2; ++attempt) {

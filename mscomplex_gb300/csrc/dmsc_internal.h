@@ -27,7 +27,7 @@ size_t grad_smem_bytes();
 size_t label_smem_bytes();
 cudaError_t launch_gradient(const float *hgt, const GridGeom &g, uint32_t *codes, uint8_t *rowcnt, uint64_t *table,
                             uint32_t *status, cudaStream_t st);
-cudaError_t launch_resolve(uint64_t *table, long long nslots, const uint32_t *offsets, uint32_t *status,
+cudaError_t launch_resolve(uint64_t *table, long long nslots, const uint32_t *offsets, long long nseg, uint32_t *status,
                            cudaStream_t st);
 cudaError_t launch_labels(const uint32_t *codes, const float *hgt, const GridGeom &g, const uint32_t *offsets,
                           const uint64_t *table, uint4 *labels, const CpOut &cp, uint32_t *status, cudaStream_t st);

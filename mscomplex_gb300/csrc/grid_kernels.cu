@@ -364,8 +364,10 @@ k_gradient(const float *__restrict__ hgt, GridGeom g, uint32_t *__restrict__ cod
     else if (b < 2 * TX) { i = b - TX; j = H - 1; }
     else if (b < 2 * TX + TY) { i = 0; j = b - 2 * TX; }
     else { i = W - 1; j = b - 2 * TX - TY; }
-    if (W <= 0 || H <= 0 || i < 0 || i >= W || j < 0 || j >= H) continue;
-    if (border_index(i, j, W, H) != b) continue;  // slot not used by this tile shape
+    if (W <= 0 || H <= 0 || i < 0 || i >= W || j < 0 || j >= H || border_index(i, j, W, H) != b) {
+      table[tile_base + kind * SLOTS_SIDE + b] = BT_INVALID;  // slot not used by this tile shape
+      continue;
+    }
     uint16_t p = kind ? s.pf[j * TX + i] : s.pv[j * TX + i];
     uint64_t entry = BT_INVALID;
     int k = p & PJ_IDX, ki = k % TX, kj = k / TX;
@@ -389,7 +391,7 @@ k_gradient(const float *__restrict__ hgt, GridGeom g, uint32_t *__restrict__ cod
 // pointers are compressed in place (any value a reader sees is a valid
 // pointer along the same chain), so no grid-wide barrier is needed.
 // ---------------------------------------------------------------------------
-__global__ void k_resolve(uint64_t *table, long long nslots, const uint32_t *__restrict__ offsets,
+__global__ void k_resolve(uint64_t *table, long long nslots, const uint32_t *__restrict__ offsets, long long nseg,
                           uint32_t *__restrict__ status) {
   for (long long sidx = blockIdx.x * (long long)blockDim.x + threadIdx.x; sidx < nslots;
        sidx += (long long)gridDim.x * blockDim.x) {
@@ -405,7 +407,8 @@ __global__ void k_resolve(uint64_t *table, long long nslots, const uint32_t *__r
     }
     if (bt_tag(e) == BT_ROOT) {
       uint64_t pl = bt_payload(e);
-      e = BT_FINAL | (uint64_t)(offsets[pl >> 8] + (uint32_t)(pl & 0xff));
+      if ((long long)(pl >> 8) < nseg) e = BT_FINAL | (uint64_t)(offsets[pl >> 8] + (uint32_t)(pl & 0xff));
+      else { e = BT_INVALID; atomicOr(status, ST_RESOLVE_LIMIT); }
     }
     vt[sidx] = e;
   }
@@ -632,13 +635,13 @@ cudaError_t launch_gradient(const float *hgt, const GridGeom &g, uint32_t *codes
   return cudaGetLastError();
 }
 
-cudaError_t launch_resolve(uint64_t *table, long long nslots, const uint32_t *offsets, uint32_t *status,
+cudaError_t launch_resolve(uint64_t *table, long long nslots, const uint32_t *offsets, long long nseg, uint32_t *status,
                            cudaStream_t st) {
   int threads = 256;
   long long blocks = (nslots + threads - 1) / threads;
   if (blocks > 152 * 16) blocks = 152 * 16;
   if (blocks < 1) blocks = 1;
-  k_resolve<<<(unsigned)blocks, threads, 0, st>>>(table, nslots, offsets, status);
+  k_resolve<<<(unsigned)blocks, threads, 0, st>>>(table, nslots, offsets, nseg, status);
   DMSC_LAUNCHED(1);
   return cudaGetLastError();
 }
