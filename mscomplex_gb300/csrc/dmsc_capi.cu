@@ -149,7 +149,7 @@ int dmsc_dataset_work(dmsc_dataset *d, void *stream) {
   }
   CK(cudaMemsetAsync(d->scal.p, 0, sizeof(uint32_t) * 4, st));
   if (tm) CK(cudaEventRecord(d->ev[0], st));
-  CK(launch_gradient(d->hgt, g, d->codes.p, d->rowcnt.p, d->table.p, d->scal.p, st));
+  CK(launch_gradient(d->hgt, g, d->codes.p, d->terms.p, d->rowcnt.p, d->table.p, d->scal.p, st));
   if (tm) CK(cudaEventRecord(d->ev[1], st));
   CK(scan_exclusive_u8(d->rowcnt.p, (long long)(g.cy + 1) * g.ntx, d->offsets.p, d->scal.p + 1, st));
   if (tm) CK(cudaEventRecord(d->ev[2], st));
@@ -164,7 +164,7 @@ int dmsc_dataset_work(dmsc_dataset *d, void *stream) {
     CpOut cp{d->cp_cellid.p, d->cp_fn.p, d->cp_flags.p, d->cp_pair_cell.p, d->cp_des2.p,
              d->cp_asc2.p, d->cp_acnt.p, d->cp_dcnt.p, d->cap};
     if (tm) CK(cudaEventRecord(d->ev[3], st));
-    CK(launch_labels(d->codes.p, d->hgt, g, d->offsets.p, d->table.p, d->labels.p, cp, d->scal.p, st));
+    CK(launch_labels(d->codes.p, d->terms.p, d->hgt, g, d->offsets.p, d->table.p, d->labels.p, cp, d->scal.p, st));
     if (tm) CK(cudaEventRecord(d->ev[4], st));
     CK(cudaMemcpyAsync(d->host_scal, d->scal.p, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -327,6 +327,7 @@ int dmsc_kernel_launches(uint64_t *count) {
 int dmsc_dataset::alloc_cells() {
   size_t nv = (size_t)g.vnx * g.vny;
   CK(codes.ensure(nv));
+  CK(terms.ensure(nv));
   CK(labels.ensure(nv));
   CK(rowcnt.ensure((size_t)(g.cy + 1) * g.ntx));
   CK(offsets.ensure((size_t)(g.cy + 1) * g.ntx));

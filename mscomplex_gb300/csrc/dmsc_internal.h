@@ -25,12 +25,13 @@ struct CpOut {
 
 size_t grad_smem_bytes();
 size_t label_smem_bytes();
-cudaError_t launch_gradient(const float *hgt, const GridGeom &g, uint32_t *codes, uint8_t *rowcnt, uint64_t *table,
-                            uint32_t *status, cudaStream_t st);
+cudaError_t launch_gradient(const float *hgt, const GridGeom &g, uint32_t *codes, uint32_t *terms, uint8_t *rowcnt,
+                            uint64_t *table, uint32_t *status, cudaStream_t st);
 cudaError_t launch_resolve(uint64_t *table, long long nslots, const uint32_t *offsets, long long nseg, uint32_t *status,
                            cudaStream_t st);
-cudaError_t launch_labels(const uint32_t *codes, const float *hgt, const GridGeom &g, const uint32_t *offsets,
-                          const uint64_t *table, uint4 *labels, const CpOut &cp, uint32_t *status, cudaStream_t st);
+cudaError_t launch_labels(const uint32_t *codes, const uint32_t *terms, const float *hgt, const GridGeom &g,
+                          const uint32_t *offsets, const uint64_t *table, uint4 *labels, const CpOut &cp,
+                          uint32_t *status, cudaStream_t st);
 
 cudaError_t scan_exclusive_u8(const uint8_t *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st);
 cudaError_t scan_exclusive_u32(const uint32_t *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st);

@@ -9,59 +9,37 @@
 //   assignCellOwnerExtrema + BFS        grid_dataset.cpp:1376-1427, 1835-1856
 //   writeout_connectivity (arcs, fns)   grid_dataset.cpp:1538-1552, 1858-1907
 //
-// Exactness argument for the parallel gradient.  The reference pairs cells in
-// row-major order and skips cells already marked.  A cell c can only be chosen
-// by its unique maximal facet (the "usable" test requires the chooser to be
-// the compareCells-maximum of the cofacet's facets), so every cell has at most
-// one chooser.  If a vertex v chooses edge e = (w,v), w is the lowest usable
-// lower neighbour of v, and then e is never the maximal edge of either face of
-// e (the face edge (v,y) is always larger than e in the ascending-sort order),
-// so e has no candidate face and the row-major order never matters.  Hence:
-// pair(v) = cand(v); pair(e) = its choosing vertex, else cand(e); pair(f) =
-// its choosing edge.  ST_PAIR_CONFLICT flags the (impossible) mixed case.
+// Vertex order.  ptLt compares values, then cell ids lexicographically; a
+// vertex key is (order-preserving value bits << 32 | x << 16 | y), so ptLt is
+// a 64-bit integer compare.  compareCells sorts cell vertices ASCENDING and
+// compares lexicographically; two closed forms replace the sorts:
+//   * two faces sharing an edge differ in two vertices each, and ascending-
+//     sorted lexicographic order puts first the face holding the smallest
+//     vertex of the symmetric difference;
+//   * edge e=(P,Q) is >= every edge of a face whose other corners are U
+//     (adjacent to P) and W (adjacent to Q) iff U<Q, W<P and min(U,W) <
+//     min(P,Q) ("usable" test of lowestPairableCoFacet, :1344-1351).
+//
+// Exactness of the parallel gradient.  The reference pairs cells in row-major
+// order and skips cells already marked.  A cell can only be chosen by its
+// unique maximal facet, and a vertex v choosing edge e=(w,v) (w its lowest
+// usable lower neighbour) makes e fail the usable test for both of its faces
+// (the face edge (v,y) beats e), so no cell is both chosen and choosing and
+// row-major order never matters: pair(v) = cand(v); pair(e) = its choosing
+// vertex, else cand(e); pair(f) = its choosing edge.  ST_PAIR_CONFLICT flags
+// the (impossible) mixed case.
 //
 // Owner labels.  own() of a non-critical vertex is own() of the far end of
 // its paired edge; of a non-critical face, own() of the face across its
 // paired edge; of a non-critical edge, own() of its pair.  Critical cells own
-// themselves and non-critical exterior cells are never reached (LABEL_NONE).
-// The V-paths are followed by pointer jumping in shared memory inside a tile;
-// paths that leave the tile end at a border cell whose global resolution is
-// done once over the much smaller border table (resolve kernel).
+// themselves; non-critical exterior cells are never reached (LABEL_NONE).
+// K1 follows the V-paths by pointer jumping in shared memory inside a tile
+// and writes each cell's in-tile terminal; paths leaving the tile end at a
+// border cell, and only the border table is resolved globally (K3).
 #include "dmsc_common.cuh"
 #include "dmsc_internal.h"
 
 namespace dmsc {
-
-// ---------------------------------------------------------------------------
-// shared helpers
-// ---------------------------------------------------------------------------
-struct EdgeKey {
-  uint64_t lo, hi;
-};
-__device__ __forceinline__ EdgeKey mk_edge(uint64_t a, uint64_t b) {
-  EdgeKey e;
-  e.lo = a < b ? a : b;
-  e.hi = a < b ? b : a;
-  return e;
-}
-__device__ __forceinline__ bool edge_less(const EdgeKey &a, const EdgeKey &b) {
-  return a.lo < b.lo || (a.lo == b.lo && a.hi < b.hi);
-}
-__device__ __forceinline__ void sort4(uint64_t k[4]) {
-#define CSWAP(a, b) { uint64_t x_ = k[a] < k[b] ? k[a] : k[b]; uint64_t y_ = k[a] < k[b] ? k[b] : k[a]; k[a] = x_; k[b] = y_; }
-  CSWAP(0, 1) CSWAP(2, 3) CSWAP(0, 2) CSWAP(1, 3) CSWAP(1, 2)
-#undef CSWAP
-}
-// Lexicographic compare of ascending-sorted vertex keys (compareCells on faces).
-__device__ __forceinline__ bool face_less(uint64_t a[4], uint64_t b[4]) {
-  sort4(a);
-  sort4(b);
-  for (int i = 0; i < 4; ++i) {
-    if (a[i] < b[i]) return true;
-    if (b[i] < a[i]) return false;
-  }
-  return false;
-}
 
 __device__ __forceinline__ bool in_rect(const GridGeom &g, int x, int y) {
   return x >= g.rx0 && x <= g.rx1 && y >= g.ry0 && y <= g.ry1;
@@ -82,53 +60,74 @@ __device__ __forceinline__ bool has_ext_cofacet(const GridGeom &g, int x, int y)
 __device__ __forceinline__ int dir_dx(uint32_t d) { return d == DIR_PX ? 1 : (d == DIR_MX ? -1 : 0); }
 __device__ __forceinline__ int dir_dy(uint32_t d) { return d == DIR_PY ? 1 : (d == DIR_MY ? -1 : 0); }
 
-// Critical bit of a cell after the pairing (assignGradients steps 2 and 3).
-__device__ __forceinline__ uint32_t finish_code(const GridGeom &g, int x, int y, uint32_t dir, bool paired) {
+// Gradient code of a cell after the pairing (assignGradients steps 2 and 3):
+// unmarked rect cells are critical; the boundary rule marks a paired rect
+// cell with an exterior cofacet, and its pair, critical as well.
+__device__ __forceinline__ uint32_t finish_code(const GridGeom &g, bool piece, int x, int y, uint32_t dir, bool paired) {
   bool inr = in_rect(g, x, y);
   bool crit = inr && !paired;
-  if (paired) {
-    if (inr && has_ext_cofacet(g, x, y)) crit = true;  // B(c)
+  if (piece && paired) {
+    if (inr && has_ext_cofacet(g, x, y)) crit = true;
     int px = x + dir_dx(dir), py = y + dir_dy(dir);
-    if (in_rect(g, px, py) && has_ext_cofacet(g, px, py)) crit = true;  // B(pair(c))
+    if (in_rect(g, px, py) && has_ext_cofacet(g, px, py)) crit = true;
   }
   return (paired ? (CODE_PAIRED | dir) : 0u) | (crit ? CODE_CRIT : 0u);
 }
 
-// pointer-jumping words (uint16): tag in bits 14-15, local index below
+// usable test of an edge (P,Q) for the face whose other corners are U (next
+// to P) and W (next to Q)
+__device__ __forceinline__ bool usable_face(uint64_t P, uint64_t Q, uint64_t U, uint64_t W) {
+  return U < Q && W < P && min(U, W) < min(P, Q);
+}
+
+// pointer-jumping words (uint16): tag in bits 14-15, local cell index below
 constexpr uint16_t PJ_PTR = 0x0000, PJ_ROOT = 0x4000, PJ_EXIT = 0x8000, PJ_INVALID = 0xC000;
 constexpr uint16_t PJ_TAG = 0xC000, PJ_IDX = 0x0FFF;
 
-// Jump every pointer of pv[0..TX*TY) and pf[...] to its terminal.  Returns
-// true if any path failed to terminate (a cycle).
+// Jumps every pointer of pv[0..TX*TY) and pf[...] to its terminal.  Each
+// thread keeps a bit mask of its still-active entries.  Returns true if a
+// path failed to terminate (a cycle).
 __device__ __forceinline__ bool pointer_jump(uint16_t *pv, uint16_t *pf) {
-  const int n = TX * TY;
+  constexpr int n = TX * TY;
+  constexpr int PER = 2 * n / GRAD_THREADS;  // 16 entries per thread
+  uint32_t active = 0;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    int e = threadIdx.x + k * GRAD_THREADS;
+    uint16_t v = e < n ? pv[e] : pf[e - n];
+    if ((v & PJ_TAG) == PJ_PTR) active |= 1u << k;
+  }
   for (int round = 0; round < 16; ++round) {  // log2(4096) + 4
-    int changed = 0;
-    for (int e = threadIdx.x; e < 2 * n; e += blockDim.x) {
+    if (!__syncthreads_or(active != 0)) return false;
+    uint32_t still = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      if (!(active & (1u << k))) continue;
+      int e = threadIdx.x + k * GRAD_THREADS;
       uint16_t *p = e < n ? pv : pf;
       int c = e < n ? e : e - n;
-      uint16_t v = p[c];
-      if ((v & PJ_TAG) == PJ_PTR) {
-        uint16_t w = p[v & PJ_IDX];
-        p[c] = w;
-        changed |= ((w & PJ_TAG) == PJ_PTR);
-      }
+      uint16_t w = p[p[c] & PJ_IDX];
+      p[c] = w;
+      if ((w & PJ_TAG) == PJ_PTR) still |= 1u << k;
     }
-    if (!__syncthreads_or(changed)) return false;
+    active = still;
   }
-  bool bad = false;
-  for (int e = threadIdx.x; e < 2 * n; e += blockDim.x) {
-    uint16_t *p = e < n ? pv : pf;
-    int c = e < n ? e : e - n;
-    if ((p[c] & PJ_TAG) == PJ_PTR) { p[c] = PJ_INVALID; bad = true; }
+  bool bad = __syncthreads_or(active != 0);
+  if (bad) {
+#pragma unroll
+    for (int k = 0; k < PER; ++k)
+      if (active & (1u << k)) {
+        int e = threadIdx.x + k * GRAD_THREADS;
+        if (e < n) pv[e] = PJ_INVALID; else pf[e - n] = PJ_INVALID;
+      }
+    __syncthreads();
   }
-  __syncthreads();
   return bad;
 }
 
 // Per-row ranks of critical cells inside the tile's row segments.
 // rankA[j][i]: critical cells of cell row 2j before vertex i (V,H interleaved);
-// rankB[j][i]: same for cell row 2j+1 (Vt,F).  Returns row totals via cntA/cntB.
+// rankB[j][i]: same for cell row 2j+1 (Vt,F).  Row totals in cntA/cntB.
 __device__ __forceinline__ void row_ranks(const uint32_t (*code)[TX], uint8_t (*rankA)[TX], uint8_t (*rankB)[TX],
                                           uint8_t *cntA, uint8_t *cntB, int w, int h) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -137,21 +136,23 @@ __device__ __forceinline__ void row_ranks(const uint32_t (*code)[TX], uint8_t (*
     uint32_t c1 = lane + 32 < w ? code[j][lane + 32] : 0u;
     uint32_t a0 = ((c0 >> 3) & 1) + ((c0 >> 11) & 1), a1 = ((c1 >> 3) & 1) + ((c1 >> 11) & 1);
     uint32_t b0 = ((c0 >> 19) & 1) + ((c0 >> 27) & 1), b1 = ((c1 >> 19) & 1) + ((c1 >> 27) & 1);
-    uint32_t sa0 = a0, sa1 = a1, sb0 = b0, sb1 = b1;
+    uint32_t v0 = a0 | (b0 << 16), v1 = a1 | (b1 << 16);  // two 16-bit scans at once
+    uint32_t sa0 = v0, sa1 = v1;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       uint32_t t0 = __shfl_up_sync(0xffffffffu, sa0, o), t1 = __shfl_up_sync(0xffffffffu, sa1, o);
-      uint32_t u0 = __shfl_up_sync(0xffffffffu, sb0, o), u1 = __shfl_up_sync(0xffffffffu, sb1, o);
-      if (lane >= o) { sa0 += t0; sa1 += t1; sb0 += u0; sb1 += u1; }
+      if (lane >= o) { sa0 += t0; sa1 += t1; }
     }
-    uint32_t ta = __shfl_sync(0xffffffffu, sa0, 31), tb = __shfl_sync(0xffffffffu, sb0, 31);
-    rankA[j][lane] = (uint8_t)(sa0 - a0);
-    rankA[j][lane + 32] = (uint8_t)(ta + sa1 - a1);
-    rankB[j][lane] = (uint8_t)(sb0 - b0);
-    rankB[j][lane + 32] = (uint8_t)(tb + sb1 - b1);
+    uint32_t t = __shfl_sync(0xffffffffu, sa0, 31);
+    uint32_t x0 = sa0 - v0, x1 = t + sa1 - v1;
+    rankA[j][lane] = (uint8_t)(x0 & 0xffff);
+    rankB[j][lane] = (uint8_t)(x0 >> 16);
+    rankA[j][lane + 32] = (uint8_t)(x1 & 0xffff);
+    rankB[j][lane + 32] = (uint8_t)(x1 >> 16);
     if (lane == 31) {
-      cntA[j] = (uint8_t)(ta + sa1);
-      cntB[j] = (uint8_t)(tb + sb1);
+      uint32_t tot = t + sa1;
+      cntA[j] = (uint8_t)(tot & 0xffff);
+      cntB[j] = (uint8_t)(tot >> 16);
     }
   }
 }
@@ -159,120 +160,104 @@ __device__ __forceinline__ void row_ranks(const uint32_t (*code)[TX], uint8_t (*
 // ---------------------------------------------------------------------------
 // K1: gradient + in-tile tracing + critical counts + border table
 // ---------------------------------------------------------------------------
-struct GradSmem {
-  uint32_t hv[TY + 3][TX + 3];  // ordered heights of vertex (tx0-1+ii, ty0-1+jj)
+struct GradPhase1 {
+  uint64_t key[TY + 3][TX + 3];  // vertex (tx0-1+ii, ty0-1+jj)
   uint8_t candV[TY + 1][TX + 1];
   uint8_t candH[TY + 1][TX];
   uint8_t candVt[TY][TX + 1];
-  uint32_t code[TY][TX];
+};
+struct GradPhase2 {
   uint16_t pv[TY * TX];
   uint16_t pf[TY * TX];
   uint8_t rankA[TY][TX];
   uint8_t rankB[TY][TX];
   uint8_t cntA[TY], cntB[TY];
 };
-
-__device__ __forceinline__ uint64_t vkey(const GradSmem &s, int i, int j, int tx0, int ty0) {
-  return ((uint64_t)s.hv[j + 1][i + 1] << 32) | ((uint32_t)(tx0 + i) << 16) | (uint32_t)(ty0 + j);
-}
-// Is edge e the compareCells-maximum facet of the face whose lower-left
-// vertex is local (fi,fj)?  ("usable" test of lowestPairableCoFacet, :1344-1351)
-__device__ __forceinline__ bool max_edge_of_face(const GradSmem &s, const EdgeKey &e, int fi, int fj, int tx0, int ty0) {
-  uint64_t a = vkey(s, fi, fj, tx0, ty0), b = vkey(s, fi + 1, fj, tx0, ty0);
-  uint64_t c = vkey(s, fi, fj + 1, tx0, ty0), d = vkey(s, fi + 1, fj + 1, tx0, ty0);
-  if (edge_less(e, mk_edge(a, b))) return false;
-  if (edge_less(e, mk_edge(c, d))) return false;
-  if (edge_less(e, mk_edge(a, c))) return false;
-  if (edge_less(e, mk_edge(b, d))) return false;
-  return true;
-}
-__device__ __forceinline__ void face_keys(const GradSmem &s, int fi, int fj, int tx0, int ty0, uint64_t k[4]) {
-  k[0] = vkey(s, fi, fj, tx0, ty0);
-  k[1] = vkey(s, fi + 1, fj, tx0, ty0);
-  k[2] = vkey(s, fi, fj + 1, tx0, ty0);
-  k[3] = vkey(s, fi + 1, fj + 1, tx0, ty0);
-}
+struct GradSmem {
+  union {
+    GradPhase1 a;
+    GradPhase2 b;
+  } u;
+  uint32_t code[TY][TX];
+};
 
 __global__ void __launch_bounds__(GRAD_THREADS, 3)
-k_gradient(const float *__restrict__ hgt, GridGeom g, uint32_t *__restrict__ codes, uint8_t *__restrict__ rowcnt,
-           uint64_t *__restrict__ table, uint32_t *__restrict__ status) {
+k_gradient(const float *__restrict__ hgt, GridGeom g, uint32_t *__restrict__ codes, uint32_t *__restrict__ terms,
+           uint8_t *__restrict__ rowcnt, uint64_t *__restrict__ table, uint32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   GradSmem &s = *reinterpret_cast<GradSmem *>(smem_raw);
+  GradPhase1 &A = s.u.a;
   const int bx = blockIdx.x, by = blockIdx.y;
   const int tx0 = bx * TX, ty0 = by * TY;
   int w, h, wf, hf;
   tile_extent(g, bx, by, 0, w, h);
   tile_extent(g, bx, by, 1, wf, hf);
+  const bool piece = !(g.rx0 == 0 && g.ry0 == 0 && g.rx1 == g.cx && g.ry1 == g.cy);
   uint32_t st = 0;
 
-  // 1. heights with a 1-vertex halo below/left and 2 above/right
+  // 1. vertex keys with a 1-vertex halo below/left and 2 above/right
   for (int e = threadIdx.x; e < (TX + 3) * (TY + 3); e += blockDim.x) {
     int jj = e / (TX + 3), ii = e - jj * (TX + 3);
     int vi = tx0 - 1 + ii, vj = ty0 - 1 + jj;
-    uint32_t v = 0;
+    uint64_t k = 0;
     if (vi >= 0 && vi < g.vnx && vj >= 0 && vj < g.vny) {
       float f = __ldg(hgt + (long long)vj * g.pitch + vi);
       if ((__float_as_uint(f) & 0x7fffffffu) > 0x7f800000u) st |= ST_NAN_INPUT;
-      v = ord_key(f);
+      k = ((uint64_t)ord_key(f) << 32) | ((uint32_t)vi << 16) | (uint32_t)vj;
     }
-    s.hv[jj][ii] = v;
+    A.key[jj][ii] = k;
   }
   __syncthreads();
+#define KEY(i, j) A.key[(j) + 1][(i) + 1]
 
-  // 2. lowest pairable cofacet of vertices and edges (only cells in rect choose)
+  // 2. lowest pairable cofacet of vertices and edges (only rect cells choose)
   for (int e = threadIdx.x; e < (TX + 1) * (TY + 1); e += blockDim.x) {
     int j = e / (TX + 1), i = e - j * (TX + 1);
     int vi = tx0 + i, vj = ty0 + j;
     uint8_t best = CAND_NONE;
     if (vi < g.vnx && vj < g.vny && in_rect(g, 2 * vi, 2 * vj)) {
-      uint64_t kv = vkey(s, i, j, tx0, ty0), bk = ~0ull;
+      uint64_t kv = KEY(i, j), bk = kv;
       bool tbv = vi == 0 || vi == g.vnx - 1 || vj == 0 || vj == g.vny - 1;
-      bool tbvert = vi == 0 || vi == g.vnx - 1;  // vertical edges of v on the ext boundary
-      bool tbhorz = vj == 0 || vj == g.vny - 1;  // horizontal edges of v on the ext boundary
-      // cofacet order of getCellCofacets (:1626-1629): up, down, left, right
-      if (vj + 1 < g.vny && (!tbv || tbvert)) { uint64_t k = vkey(s, i, j + 1, tx0, ty0); if (k < kv && k < bk) { bk = k; best = DIR_PY; } }
-      if (vj >= 1 && (!tbv || tbvert)) { uint64_t k = vkey(s, i, j - 1, tx0, ty0); if (k < kv && k < bk) { bk = k; best = DIR_MY; } }
-      if (vi >= 1 && (!tbv || tbhorz)) { uint64_t k = vkey(s, i - 1, j, tx0, ty0); if (k < kv && k < bk) { bk = k; best = DIR_MX; } }
-      if (vi + 1 < g.vnx && (!tbv || tbhorz)) { uint64_t k = vkey(s, i + 1, j, tx0, ty0); if (k < kv && k < bk) { bk = k; best = DIR_PX; } }
+      bool okv = !tbv || vi == 0 || vi == g.vnx - 1;  // vertical edges usable
+      bool okh = !tbv || vj == 0 || vj == g.vny - 1;  // horizontal edges usable
+      // cofacet order of getCellCofacets (:1626-1629): up, down, left, right;
+      // minimum over lower neighbours (keys are distinct, order is irrelevant)
+      if (okv && vj + 1 < g.vny) { uint64_t k = KEY(i, j + 1); if (k < bk) { bk = k; best = DIR_PY; } }
+      if (okv && vj >= 1) { uint64_t k = KEY(i, j - 1); if (k < bk) { bk = k; best = DIR_MY; } }
+      if (okh && vi >= 1) { uint64_t k = KEY(i - 1, j); if (k < bk) { bk = k; best = DIR_MX; } }
+      if (okh && vi + 1 < g.vnx) { uint64_t k = KEY(i + 1, j); if (k < bk) { bk = k; best = DIR_PX; } }
     }
-    s.candV[j][i] = best;
+    A.candV[j][i] = best;
   }
   for (int e = threadIdx.x; e < TX * (TY + 1); e += blockDim.x) {
-    int j = e / TX, i = e - j * TX;  // H(i,j)
+    int j = e / TX, i = e - j * TX;  // H(i,j): P = V(i,j), Q = V(i+1,j)
     int hi = tx0 + i, hj = ty0 + j;
     uint8_t best = CAND_NONE;
     if (hi + 1 < g.vnx && hj < g.vny && in_rect(g, 2 * hi + 1, 2 * hj) && hj != 0 && hj != g.vny - 1) {
-      EdgeKey ek = mk_edge(vkey(s, i + 1, j, tx0, ty0), vkey(s, i, j, tx0, ty0));
-      bool u0 = max_edge_of_face(s, ek, i, j, tx0, ty0);      // cf[0]: face above
-      bool u1 = max_edge_of_face(s, ek, i, j - 1, tx0, ty0);  // cf[1]: face below
-      if (u0 && u1) {
-        uint64_t ka[4], kb[4];
-        face_keys(s, i, j, tx0, ty0, ka);
-        face_keys(s, i, j - 1, tx0, ty0, kb);
-        best = face_less(kb, ka) ? DIR_MY : DIR_PY;
-      } else if (u0) best = DIR_PY;
+      uint64_t P = KEY(i, j), Q = KEY(i + 1, j);
+      uint64_t Ua = KEY(i, j + 1), Wa = KEY(i + 1, j + 1), Ub = KEY(i, j - 1), Wb = KEY(i + 1, j - 1);
+      bool u0 = usable_face(P, Q, Ua, Wa), u1 = usable_face(P, Q, Ub, Wb);  // cf[0] above, cf[1] below
+      if (u0 && u1) best = min(Ub, Wb) < min(Ua, Wa) ? DIR_MY : DIR_PY;
+      else if (u0) best = DIR_PY;
       else if (u1) best = DIR_MY;
     }
-    s.candH[j][i] = best;
+    A.candH[j][i] = best;
   }
   for (int e = threadIdx.x; e < (TX + 1) * TY; e += blockDim.x) {
-    int j = e / (TX + 1), i = e - j * (TX + 1);  // Vt(i,j)
+    int j = e / (TX + 1), i = e - j * (TX + 1);  // Vt(i,j): P = V(i,j), Q = V(i,j+1)
     int vi = tx0 + i, vj = ty0 + j;
     uint8_t best = CAND_NONE;
     if (vi < g.vnx && vj + 1 < g.vny && in_rect(g, 2 * vi, 2 * vj + 1) && vi != 0 && vi != g.vnx - 1) {
-      EdgeKey ek = mk_edge(vkey(s, i, j + 1, tx0, ty0), vkey(s, i, j, tx0, ty0));
-      bool u0 = max_edge_of_face(s, ek, i, j, tx0, ty0);      // cf[0]: face right
-      bool u1 = max_edge_of_face(s, ek, i - 1, j, tx0, ty0);  // cf[1]: face left
-      if (u0 && u1) {
-        uint64_t ka[4], kb[4];
-        face_keys(s, i, j, tx0, ty0, ka);
-        face_keys(s, i - 1, j, tx0, ty0, kb);
-        best = face_less(kb, ka) ? DIR_MX : DIR_PX;
-      } else if (u0) best = DIR_PX;
+      uint64_t P = KEY(i, j), Q = KEY(i, j + 1);
+      uint64_t Ur = KEY(i + 1, j), Wr = KEY(i + 1, j + 1), Ul = KEY(i - 1, j), Wl = KEY(i - 1, j + 1);
+      bool u0 = usable_face(P, Q, Ur, Wr), u1 = usable_face(P, Q, Ul, Wl);  // cf[0] right, cf[1] left
+      if (u0 && u1) best = min(Ul, Wl) < min(Ur, Wr) ? DIR_MX : DIR_PX;
+      else if (u0) best = DIR_PX;
       else if (u1) best = DIR_MX;
     }
-    s.candVt[j][i] = best;
+    A.candVt[j][i] = best;
   }
+#undef KEY
   __syncthreads();
 
   // 3. final codes of the tile's own cells
@@ -281,39 +266,38 @@ k_gradient(const float *__restrict__ hgt, GridGeom g, uint32_t *__restrict__ cod
     uint32_t packed = 0;
     if (i < w && j < h) {
       int vi = tx0 + i, vj = ty0 + j, x = 2 * vi, y = 2 * vj;
-      uint8_t cv = s.candV[j][i];
-      packed |= finish_code(g, x, y, cv, cv != CAND_NONE);
+      uint8_t cv = A.candV[j][i];
+      packed |= finish_code(g, piece, x, y, cv, cv != CAND_NONE);
       if (vi + 1 < g.vnx) {  // H(i,j)
         uint32_t d = CAND_NONE;
-        int nch = 0;
-        if (cv == DIR_PX) { d = DIR_MX; ++nch; }
-        if (s.candV[j][i + 1] == DIR_MX) { d = DIR_PX; ++nch; }
-        uint8_t ce = s.candH[j][i];
-        if (ce != CAND_NONE) { if (nch) st |= ST_PAIR_CONFLICT; else d = ce; }
-        packed |= finish_code(g, x + 1, y, d & 3, d != CAND_NONE) << 8;
+        if (cv == DIR_PX) d = DIR_MX;
+        if (A.candV[j][i + 1] == DIR_MX) d = DIR_PX;
+        uint8_t ce = A.candH[j][i];
+        if (ce != CAND_NONE) { if (d != CAND_NONE) st |= ST_PAIR_CONFLICT; else d = ce; }
+        packed |= finish_code(g, piece, x + 1, y, d & 3, d != CAND_NONE) << 8;
       }
       if (vj + 1 < g.vny) {  // Vt(i,j)
         uint32_t d = CAND_NONE;
-        int nch = 0;
-        if (cv == DIR_PY) { d = DIR_MY; ++nch; }
-        if (s.candV[j + 1][i] == DIR_MY) { d = DIR_PY; ++nch; }
-        uint8_t ce = s.candVt[j][i];
-        if (ce != CAND_NONE) { if (nch) st |= ST_PAIR_CONFLICT; else d = ce; }
-        packed |= finish_code(g, x, y + 1, d & 3, d != CAND_NONE) << 16;
+        if (cv == DIR_PY) d = DIR_MY;
+        if (A.candV[j + 1][i] == DIR_MY) d = DIR_PY;
+        uint8_t ce = A.candVt[j][i];
+        if (ce != CAND_NONE) { if (d != CAND_NONE) st |= ST_PAIR_CONFLICT; else d = ce; }
+        packed |= finish_code(g, piece, x, y + 1, d & 3, d != CAND_NONE) << 16;
       }
       if (vi + 1 < g.vnx && vj + 1 < g.vny) {  // F(i,j): chosen by at most one edge
         uint32_t d = CAND_NONE;
-        if (s.candH[j][i] == DIR_PY) d = DIR_MY;
-        if (s.candH[j + 1][i] == DIR_MY) d = DIR_PY;
-        if (s.candVt[j][i] == DIR_PX) d = DIR_MX;
-        if (s.candVt[j][i + 1] == DIR_MX) d = DIR_PX;
-        packed |= finish_code(g, x + 1, y + 1, d & 3, d != CAND_NONE) << 24;
+        if (A.candH[j][i] == DIR_PY) d = DIR_MY;
+        if (A.candH[j + 1][i] == DIR_MY) d = DIR_PY;
+        if (A.candVt[j][i] == DIR_PX) d = DIR_MX;
+        if (A.candVt[j][i + 1] == DIR_MX) d = DIR_PX;
+        packed |= finish_code(g, piece, x + 1, y + 1, d & 3, d != CAND_NONE) << 24;
       }
       codes[(long long)vj * g.vnx + vi] = packed;
     }
     s.code[j][i] = packed;
   }
-  __syncthreads();
+  __syncthreads();  // phase-1 arrays are dead from here on (phase 2 aliases them)
+  GradPhase2 &B = s.u.b;
 
   // 4. in-tile tracing: vertices follow their paired edge to the next vertex,
   //    faces follow their paired edge to the face across it.
@@ -339,18 +323,21 @@ k_gradient(const float *__restrict__ hgt, GridGeom g, uint32_t *__restrict__ cod
         pff = (ni >= 0 && ni < wf && nj >= 0 && nj < hf) ? (uint16_t)(PJ_PTR | (nj * TX + ni)) : (uint16_t)(PJ_EXIT | e);
       }
     }
-    s.pv[e] = pvv;
-    s.pf[e] = pff;
+    B.pv[e] = pvv;
+    B.pf[e] = pff;
   }
-  row_ranks(s.code, s.rankA, s.rankB, s.cntA, s.cntB, w, h);
-  __syncthreads();
-  if (pointer_jump(s.pv, s.pf)) st |= ST_CYCLE;
+  row_ranks(s.code, B.rankA, B.rankB, B.cntA, B.cntB, w, h);
+  if (pointer_jump(B.pv, B.pf)) st |= ST_CYCLE;  // (begins with a barrier)
 
-  // 5. per (cell row, tile) critical counts
+  // 5. in-tile terminals of every vertex and face, per (cell row, tile) counts
+  for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
+    int j = e / TX, i = e - j * TX;
+    if (i < w && j < h) terms[(long long)(ty0 + j) * g.vnx + tx0 + i] = (uint32_t)B.pv[e] | ((uint32_t)B.pf[e] << 16);
+  }
   for (int j = threadIdx.x; j < h; j += blockDim.x) {
     int y = 2 * (ty0 + j);
-    rowcnt[(long long)y * g.ntx + bx] = s.cntA[j];
-    if (y + 1 <= g.cy) rowcnt[(long long)(y + 1) * g.ntx + bx] = s.cntB[j];
+    rowcnt[(long long)y * g.ntx + bx] = B.cntA[j];
+    if (y + 1 <= g.cy) rowcnt[(long long)(y + 1) * g.ntx + bx] = B.cntB[j];
   }
 
   // 6. border table: where each border cell's path ends inside this tile
@@ -358,28 +345,25 @@ k_gradient(const float *__restrict__ hgt, GridGeom g, uint32_t *__restrict__ cod
   for (int e = threadIdx.x; e < 2 * SLOTS_SIDE; e += blockDim.x) {
     int kind = e / SLOTS_SIDE, b = e - kind * SLOTS_SIDE;
     int W = kind ? wf : w, H = kind ? hf : h;
-    // invert border_index
-    int i, j;
+    int i, j;  // invert border_index
     if (b < TX) { i = b; j = 0; }
     else if (b < 2 * TX) { i = b - TX; j = H - 1; }
     else if (b < 2 * TX + TY) { i = 0; j = b - 2 * TX; }
     else { i = W - 1; j = b - 2 * TX - TY; }
-    if (W <= 0 || H <= 0 || i < 0 || i >= W || j < 0 || j >= H || border_index(i, j, W, H) != b) {
-      table[tile_base + kind * SLOTS_SIDE + b] = BT_INVALID;  // slot not used by this tile shape
-      continue;
-    }
-    uint16_t p = kind ? s.pf[j * TX + i] : s.pv[j * TX + i];
     uint64_t entry = BT_INVALID;
-    int k = p & PJ_IDX, ki = k % TX, kj = k / TX;
-    if ((p & PJ_TAG) == PJ_ROOT) {
-      int y = 2 * (ty0 + kj) + kind;
-      uint32_t rank = kind ? (uint32_t)s.rankB[kj][ki] + ((s.code[kj][ki] >> 19) & 1) : s.rankA[kj][ki];
-      entry = BT_ROOT | ((uint64_t)((long long)y * g.ntx + bx) << 8) | rank;
-    } else if ((p & PJ_TAG) == PJ_EXIT) {
-      uint32_t d = (kind ? (s.code[kj][ki] >> 24) : s.code[kj][ki]) & 3;
-      int gi = tx0 + ki + dir_dx(d), gj = ty0 + kj + dir_dy(d);
-      if (gi >= 0 && gj >= 0 && gi < g.vnx - kind && gj < g.vny - kind) entry = BT_EXIT | (uint64_t)border_slot(g, kind, gi, gj);
-      else st |= ST_CYCLE;  // a path leaving the window: never expected
+    if (W > 0 && H > 0 && i >= 0 && i < W && j >= 0 && j < H && border_index(i, j, W, H) == b) {
+      uint16_t p = kind ? B.pf[j * TX + i] : B.pv[j * TX + i];
+      int k = p & PJ_IDX, ki = k % TX, kj = k / TX;
+      if ((p & PJ_TAG) == PJ_ROOT) {
+        int y = 2 * (ty0 + kj) + kind;
+        uint32_t rank = kind ? (uint32_t)B.rankB[kj][ki] + ((s.code[kj][ki] >> 19) & 1) : B.rankA[kj][ki];
+        entry = BT_ROOT | ((uint64_t)((long long)y * g.ntx + bx) << 8) | rank;
+      } else if ((p & PJ_TAG) == PJ_EXIT) {
+        uint32_t d = (kind ? (s.code[kj][ki] >> 24) : s.code[kj][ki]) & 3;
+        int gi = tx0 + ki + dir_dx(d), gj = ty0 + kj + dir_dy(d);
+        if (gi >= 0 && gj >= 0 && gi < g.vnx - kind && gj < g.vny - kind) entry = BT_EXIT | (uint64_t)border_slot(g, kind, gi, gj);
+        else st |= ST_CYCLE;  // a path leaving the window: never expected
+      }
     }
     table[tile_base + kind * SLOTS_SIDE + b] = entry;
   }
@@ -421,8 +405,6 @@ struct LabelSmem {
   uint32_t code[TY][TX];
   uint32_t labV[TY][TX];
   uint32_t labF[TY][TX];
-  uint16_t pv[TY * TX];
-  uint16_t pf[TY * TX];
   uint8_t rankA[TY][TX];
   uint8_t rankB[TY][TX];
   uint8_t cntA[TY], cntB[TY];
@@ -452,10 +434,8 @@ __device__ __forceinline__ float cell_fn(const float *hgt, const GridGeom &g, in
   }
 }
 
-
-
 __global__ void __launch_bounds__(GRAD_THREADS, 3)
-k_labels(const uint32_t *__restrict__ codes, const float *__restrict__ hgt, GridGeom g,
+k_labels(const uint32_t *__restrict__ codes, const uint32_t *__restrict__ terms, const float *__restrict__ hgt, GridGeom g,
          const uint32_t *__restrict__ offsets, const uint64_t *__restrict__ table, uint4 *__restrict__ labels,
          CpOut cp, uint32_t *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -478,46 +458,27 @@ k_labels(const uint32_t *__restrict__ codes, const float *__restrict__ hgt, Grid
   }
   __syncthreads();
   row_ranks(s.code, s.rankA, s.rankB, s.cntA, s.cntB, w, h);
-  for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
-    int j = e / TX, i = e - j * TX;
-    uint16_t pvv = PJ_INVALID, pff = PJ_INVALID;
-    uint32_t c = s.code[j][i];
-    if (i < w && j < h) {
-      uint32_t cvv = c & 0xff;
-      if (cvv & CODE_CRIT) pvv = PJ_ROOT | e;
-      else if (in_rect(g, 2 * (tx0 + i), 2 * (ty0 + j))) {
-        if (on_tile_border(i, j, w, h)) pvv = PJ_EXIT | e;  // resolved through the border table
-        else { uint32_t d = cvv & 3; pvv = PJ_PTR | ((j + dir_dy(d)) * TX + i + dir_dx(d)); }
-      }
-    }
-    if (i < wf && j < hf) {
-      uint32_t cf = c >> 24;
-      if (cf & CODE_CRIT) pff = PJ_ROOT | e;
-      else if (in_rect(g, 2 * (tx0 + i) + 1, 2 * (ty0 + j) + 1)) {
-        if (on_tile_border(i, j, wf, hf)) pff = PJ_EXIT | e;
-        else { uint32_t d = cf & 3; pff = PJ_PTR | ((j + dir_dy(d)) * TX + i + dir_dx(d)); }
-      }
-    }
-    s.pv[e] = pvv;
-    s.pf[e] = pff;
-  }
   __syncthreads();
-  if (pointer_jump(s.pv, s.pf)) st |= ST_CYCLE;
 
-  // terminal -> cp index
+  // vertex / face labels from the in-tile terminals written by K1
   for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
     int j = e / TX, i = e - j * TX;
     uint32_t lv = LABEL_NONE, lf = LABEL_NONE;
-    uint16_t p = s.pv[e];
-    int k = p & PJ_IDX, ki = k % TX, kj = k / TX;
-    if ((p & PJ_TAG) == PJ_ROOT) lv = s.offA[kj] + s.rankA[kj][ki];
-    else if ((p & PJ_TAG) == PJ_EXIT) lv = slot_label(table, g, 0, tx0 + ki, ty0 + kj);
-    p = s.pf[e];
-    k = p & PJ_IDX; ki = k % TX; kj = k / TX;
-    if ((p & PJ_TAG) == PJ_ROOT) lf = s.offB[kj] + s.rankB[kj][ki] + ((s.code[kj][ki] >> 19) & 1);
-    else if ((p & PJ_TAG) == PJ_EXIT) lf = slot_label(table, g, 1, tx0 + ki, ty0 + kj);
-    s.labV[j][i] = (i < w && j < h) ? lv : LABEL_NONE;
-    s.labF[j][i] = (i < wf && j < hf) ? lf : LABEL_NONE;
+    if (i < w && j < h) {
+      uint32_t t2 = terms[(long long)(ty0 + j) * g.vnx + tx0 + i];
+      uint16_t p = (uint16_t)(t2 & 0xffff);
+      int k = p & PJ_IDX, ki = k % TX, kj = k / TX;
+      if ((p & PJ_TAG) == PJ_ROOT) lv = s.offA[kj] + s.rankA[kj][ki];
+      else if ((p & PJ_TAG) == PJ_EXIT) lv = slot_label(table, g, 0, tx0 + ki, ty0 + kj);
+      if (i < wf && j < hf) {
+        p = (uint16_t)(t2 >> 16);
+        k = p & PJ_IDX; ki = k % TX; kj = k / TX;
+        if ((p & PJ_TAG) == PJ_ROOT) lf = s.offB[kj] + s.rankB[kj][ki] + ((s.code[kj][ki] >> 19) & 1);
+        else if ((p & PJ_TAG) == PJ_EXIT) lf = slot_label(table, g, 1, tx0 + ki, ty0 + kj);
+      }
+    }
+    s.labV[j][i] = lv;
+    s.labF[j][i] = lf;
   }
   __syncthreads();
 
@@ -526,7 +487,7 @@ k_labels(const uint32_t *__restrict__ codes, const float *__restrict__ hgt, Grid
     if (i >= w || j >= h) continue;
     const int vi = tx0 + i, vj = ty0 + j, x = 2 * vi, y = 2 * vj;
     const uint32_t c = s.code[j][i];
-    // neighbour labels that may live in the next tile
+    // neighbour labels that may live in the next tile (that tile's border cells)
     auto labV_at = [&](int ii, int jj) -> uint32_t {
       if (ii >= 0 && ii < w && jj >= 0 && jj < h) return s.labV[jj][ii];
       return slot_label(table, g, 0, tx0 + ii, ty0 + jj);
@@ -571,6 +532,7 @@ k_labels(const uint32_t *__restrict__ codes, const float *__restrict__ hgt, Grid
     labels[(long long)vj * g.vnx + vi] = make_uint4(L[0], L[1], L[2], L[3]);
 
     // critical-point records
+    if (!(c & 0x08080808u)) continue;
 #pragma unroll
     for (int kind = 0; kind < 4; ++kind) {
       uint32_t cc = (c >> (8 * kind)) & 0xff;
@@ -621,8 +583,8 @@ k_labels(const uint32_t *__restrict__ codes, const float *__restrict__ hgt, Grid
 size_t grad_smem_bytes() { return sizeof(GradSmem); }
 size_t label_smem_bytes() { return sizeof(LabelSmem); }
 
-cudaError_t launch_gradient(const float *hgt, const GridGeom &g, uint32_t *codes, uint8_t *rowcnt, uint64_t *table,
-                            uint32_t *status, cudaStream_t st) {
+cudaError_t launch_gradient(const float *hgt, const GridGeom &g, uint32_t *codes, uint32_t *terms, uint8_t *rowcnt,
+                            uint64_t *table, uint32_t *status, cudaStream_t st) {
   static bool init = false;
   if (!init) {
     cudaError_t e = cudaFuncSetAttribute(k_gradient, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradSmem));
@@ -630,7 +592,7 @@ cudaError_t launch_gradient(const float *hgt, const GridGeom &g, uint32_t *codes
     init = true;
   }
   dim3 grid(g.ntx, g.nty);
-  k_gradient<<<grid, GRAD_THREADS, sizeof(GradSmem), st>>>(hgt, g, codes, rowcnt, table, status);
+  k_gradient<<<grid, GRAD_THREADS, sizeof(GradSmem), st>>>(hgt, g, codes, terms, rowcnt, table, status);
   DMSC_LAUNCHED(1);
   return cudaGetLastError();
 }
@@ -646,8 +608,9 @@ cudaError_t launch_resolve(uint64_t *table, long long nslots, const uint32_t *of
   return cudaGetLastError();
 }
 
-cudaError_t launch_labels(const uint32_t *codes, const float *hgt, const GridGeom &g, const uint32_t *offsets,
-                          const uint64_t *table, uint4 *labels, const CpOut &cp, uint32_t *status, cudaStream_t st) {
+cudaError_t launch_labels(const uint32_t *codes, const uint32_t *terms, const float *hgt, const GridGeom &g,
+                          const uint32_t *offsets, const uint64_t *table, uint4 *labels, const CpOut &cp,
+                          uint32_t *status, cudaStream_t st) {
   static bool init = false;
   if (!init) {
     cudaError_t e = cudaFuncSetAttribute(k_labels, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LabelSmem));
@@ -655,7 +618,7 @@ cudaError_t launch_labels(const uint32_t *codes, const float *hgt, const GridGeo
     init = true;
   }
   dim3 grid(g.ntx, g.nty);
-  k_labels<<<grid, GRAD_THREADS, sizeof(LabelSmem), st>>>(codes, hgt, g, offsets, table, labels, cp, status);
+  k_labels<<<grid, GRAD_THREADS, sizeof(LabelSmem), st>>>(codes, terms, hgt, g, offsets, table, labels, cp, status);
   DMSC_LAUNCHED(1);
   return cudaGetLastError();
 }

@@ -39,6 +39,7 @@ struct dmsc_dataset {
   const float *hgt = nullptr;  // heights on the device (owned copy or borrowed)
   DevBuf<float> hown;
   DevBuf<uint32_t> codes;      // uchar4 gradient codes per vertex
+  DevBuf<uint32_t> terms;      // in-tile path terminals of the vertex and face of each vertex (2 x uint16)
   DevBuf<uint4> labels;        // owner labels (cp indices) of the 4 cells of each vertex
   DevBuf<uint8_t> rowcnt;      // critical cells per (cell row, tile column)
   DevBuf<uint32_t> offsets;    // exclusive scan of rowcnt: first cp index of each segment
