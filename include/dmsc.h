@@ -94,6 +94,23 @@ int dmsc_msc_export(dmsc_msc *msc, int16_t rect_ext[8], int16_t *cellid, float *
                     uint8_t *flags, uint32_t *asc_off, uint32_t *asc, uint32_t *des_off, uint32_t *des,
                     uint32_t *adisc_off, int16_t *adisc, uint32_t *ddisc_off, int16_t *ddisc, void *stream);
 
+/* PrefixScan::PreScanBuffer(out, in, n, queue) (dmsc/include/prefix_scan.h:105-109,
+ * dmsc/src/prefix_scan.cpp:457-464): exclusive prefix sum of n uint32 values
+ * in device memory, out[i] = in[0] + ... + in[i-1] (wrapping modulo 2^32).
+ * d_total (device pointer, may be NULL) receives the sum of all n values.
+ * Scratch for block partial sums comes from the stream-ordered allocator.
+ * d_out may equal d_in. */
+int dmsc_prefix_scan(dmsc_ctx *ctx, uint32_t *d_out, const uint32_t *d_in, int64_t n, uint32_t *d_total,
+                     void *stream);
+/* BitonicSortProgram::bitonicSort(queue, dstKey, dstVal, srcKey, srcVal,
+ * batch, arrayLength, dir) (dmsc/include/bitonic_sort.h:30-39): sorts `batch`
+ * consecutive arrays of `array_length` (key, value) uint32 pairs each, in
+ * device memory, ascending (dir = 1) or descending (dir = 0) by key.  Unlike
+ * the bitonic network this sort is stable and takes any array length.  The
+ * destination may alias the source. */
+int dmsc_sort_pairs(dmsc_ctx *ctx, uint32_t *d_dst_key, uint32_t *d_dst_val, const uint32_t *d_src_key,
+                    const uint32_t *d_src_val, uint32_t batch, uint32_t array_length, uint32_t dir, void *stream);
+
 /* Tracing: the reference's compile-time _LOG_TIMINGS stage timers
  * (dmsc/src/grid_dataset.cpp:19-34, 357-390).  When enabled, CUDA events are
  * recorded on the launching stream around every stage of work and

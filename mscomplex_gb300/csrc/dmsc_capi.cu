@@ -313,6 +313,29 @@ int dmsc_dataset_stage_times(dmsc_dataset *d, float *ms, int n) {
   return DMSC_OK;
 }
 
+int dmsc_prefix_scan(dmsc_ctx *ctx, uint32_t *d_out, const uint32_t *d_in, int64_t n, uint32_t *d_total,
+                     void *stream) {
+  if (!ctx || n < 0 || (n > 0 && (!d_out || !d_in))) return fail(DMSC_ERR_BAD_ARG, "bad argument");
+  if (n > (int64_t)INT32_MAX * 32) return fail(DMSC_ERR_BAD_ARG, "n too large");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = pick(ctx, stream);
+  CK(scan_exclusive_u32(d_in, n, d_out, d_total, st));
+  CK(cudaStreamSynchronize(st));
+  return DMSC_OK;
+}
+
+int dmsc_sort_pairs(dmsc_ctx *ctx, uint32_t *d_dst_key, uint32_t *d_dst_val, const uint32_t *d_src_key,
+                    const uint32_t *d_src_val, uint32_t batch, uint32_t array_length, uint32_t dir, void *stream) {
+  if (!ctx || !d_dst_key || !d_dst_val || !d_src_key || !d_src_val) return fail(DMSC_ERR_BAD_ARG, "null argument");
+  if (dir > 1) return fail(DMSC_ERR_BAD_ARG, "dir must be 0 (descending) or 1 (ascending)");
+  if ((uint64_t)batch * array_length > (1ull << 31)) return fail(DMSC_ERR_BAD_ARG, "batch * array_length too large");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = pick(ctx, stream);
+  CK(sort_pairs_batched(d_dst_key, d_dst_val, d_src_key, d_src_val, batch, array_length, dir, st));
+  CK(cudaStreamSynchronize(st));
+  return DMSC_OK;
+}
+
 int dmsc_kernel_launches(uint64_t *count) {
   if (!count) return fail(DMSC_ERR_BAD_ARG, "null argument");
   *count = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);

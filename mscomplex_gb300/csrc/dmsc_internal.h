@@ -37,6 +37,8 @@ cudaError_t scan_exclusive_u8(const uint8_t *in, long long n, uint32_t *out, uin
 cudaError_t scan_exclusive_u32(const uint32_t *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st);
 cudaError_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *ktmp, uint32_t *vtmp, long long n, int nbits,
                              cudaStream_t st);
+cudaError_t sort_pairs_batched(uint32_t *dk, uint32_t *dv, const uint32_t *sk, const uint32_t *sv, uint32_t batch,
+                               uint32_t len, uint32_t dir, cudaStream_t st);
 cudaError_t build_csr(long long ncp, const uint32_t *cellid, const uint32_t *des2, const uint32_t *asc2,
                       const uint32_t *aoff, const uint32_t *doff, uint32_t *asc, uint32_t *des, long long out_cap,
                       uint32_t *status, cudaStream_t st);

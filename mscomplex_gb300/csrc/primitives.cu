@@ -213,6 +213,85 @@ cudaError_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *ktmp, uin
   return cudaGetLastError();
 }
 
+// Batched key/value sort (the BitonicSortProgram slot): arrays [b*len, (b+1)*len)
+// sorted independently, ascending or descending, stably.  Implemented as one
+// stable LSD sort on the (possibly inverted) key followed by a stable sort on
+// the array index.
+__global__ void k_sort_prepare(long long n, uint32_t len, uint32_t dir, const uint32_t *__restrict__ ks,
+                               const uint32_t *__restrict__ vs, uint32_t *__restrict__ k, uint32_t *__restrict__ v,
+                               uint32_t *__restrict__ seg) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    uint32_t key = ks[i];
+    k[i] = dir ? key : ~key;
+    v[i] = vs[i];
+    seg[i] = (uint32_t)(i / len);
+  }
+}
+__global__ void k_sort_finish(long long n, uint32_t dir, const uint32_t *__restrict__ k, uint32_t *__restrict__ kout) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    kout[i] = dir ? k[i] : ~k[i];
+}
+// (seg, key) pairs: after sorting by key, a stable sort by segment keeps the
+// key order inside each segment.  Values travel through an index permutation.
+__global__ void k_gather_u32(long long n, const uint32_t *__restrict__ idx, const uint32_t *__restrict__ src,
+                             uint32_t *__restrict__ dst) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = src[idx[i]];
+}
+__global__ void k_iota(long long n, uint32_t *__restrict__ a) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a[i] = (uint32_t)i;
+}
+
+static unsigned grid_for(long long n, int threads);
+
+cudaError_t sort_pairs_batched(uint32_t *dk, uint32_t *dv, const uint32_t *sk, const uint32_t *sv, uint32_t batch,
+                               uint32_t len, uint32_t dir, cudaStream_t st) {
+  long long n = (long long)batch * len;
+  if (n == 0) return cudaSuccess;
+  uint32_t *buf = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&buf, sizeof(uint32_t) * n * 7, st);
+  if (e != cudaSuccess) return e;
+  uint32_t *k = buf, *v = buf + n, *seg = buf + 2 * n, *perm = buf + 3 * n, *t1 = buf + 4 * n, *t2 = buf + 5 * n,
+           *t3 = buf + 6 * n;
+  unsigned gb = grid_for(n, 256);
+  k_sort_prepare<<<gb, 256, 0, st>>>(n, len, dir, sk, sv, k, v, seg);
+  DMSC_LAUNCHED(1);
+  k_iota<<<gb, 256, 0, st>>>(n, perm);
+  DMSC_LAUNCHED(1);
+  // 1) stable by key, carrying the original index
+  e = radix_sort_pairs(k, perm, t1, t2, n, 32, st);
+  if (e == cudaSuccess && batch > 1) {
+    // 2) stable by segment of the original index: seg of perm[i]
+    k_gather_u32<<<gb, 256, 0, st>>>(n, perm, seg, t3);
+    DMSC_LAUNCHED(1);
+    int sbits = 1;
+    while ((1ll << sbits) < (long long)batch) ++sbits;
+    // sort (segment, position-in-key-order) carrying the key-sorted position
+    k_iota<<<gb, 256, 0, st>>>(n, t1);
+    DMSC_LAUNCHED(1);
+    e = radix_sort_pairs(t3, t1, seg, t2, n, sbits, st);
+    if (e == cudaSuccess) {
+      k_gather_u32<<<gb, 256, 0, st>>>(n, t1, k, t2);  // keys in final order
+      DMSC_LAUNCHED(1);
+      k_gather_u32<<<gb, 256, 0, st>>>(n, t1, perm, t3);  // original indices in final order
+      DMSC_LAUNCHED(1);
+      cudaMemcpyAsync(k, t2, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+      cudaMemcpyAsync(perm, t3, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+    }
+  }
+  if (e == cudaSuccess) {
+    k_gather_u32<<<gb, 256, 0, st>>>(n, perm, v, t2);  // values (v holds the source values)
+    DMSC_LAUNCHED(1);
+    k_sort_finish<<<gb, 256, 0, st>>>(n, dir, k, dk);
+    DMSC_LAUNCHED(1);
+    cudaMemcpyAsync(dv, t2, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(buf, st);
+  return e;
+}
+
 // ---------------------------------------------------------------------------
 // complex assembly (writeout_connectivity, dmsc/src/grid_dataset.cpp:1858-1907)
 // ---------------------------------------------------------------------------
