@@ -102,6 +102,24 @@ int dmsc_msc_export(dmsc_msc *msc, int16_t rect_ext[8], int16_t *cellid, float *
  * d_out may equal d_in. */
 int dmsc_prefix_scan(dmsc_ctx *ctx, uint32_t *d_out, const uint32_t *d_in, int64_t n, uint32_t *d_total,
                      void *stream);
+/* No counterpart in the reference.  The same exclusive scan as
+ * dmsc_prefix_scan, for callers that cannot let a library allocate device
+ * memory: a host runtime that has reserved the GPU's memory for its own pool,
+ * or a latency-bound serving loop where cudaMalloc (it synchronises the
+ * device) and cudaFree must not appear.  It calls no allocator; its scratch
+ * is a fixed array of about 128 KiB compiled into libdmsc.so, held by every
+ * GPU that loads the library until the process exits.
+ *  - n may be at most 67,108,864 (2^26); larger n fails with
+ *    DMSC_ERR_BAD_ARG and a message naming the limit.
+ *  - The first call on a device looks up the scratch array's device address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture.
+ *  - All calls share the one scratch array: calls that overlap on the GPU
+ *    (concurrent streams, or threads) race and corrupt each other's result.
+ *  - The call only enqueues work on `stream`; the result is ready once that
+ *    stream reaches it. */
+int dmsc_prefix_scan_noalloc(dmsc_ctx *ctx, uint32_t *d_out, const uint32_t *d_in, int64_t n, uint32_t *d_total,
+                             void *stream);
 /* BitonicSortProgram::bitonicSort(queue, dstKey, dstVal, srcKey, srcVal,
  * batch, arrayLength, dir) (dmsc/include/bitonic_sort.h:30-39): sorts `batch`
  * consecutive arrays of `array_length` (key, value) uint32 pairs each, in

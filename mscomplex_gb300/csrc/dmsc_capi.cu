@@ -30,6 +30,8 @@ int cuda_fail(cudaError_t e, const char *where) {
 }
 }  // namespace
 
+int dmsc::set_last_error(int code, const char *msg) { return fail(code, msg); }
+
 #define CK(call)                                             \
   do {                                                       \
     cudaError_t e_ = (call);                                 \

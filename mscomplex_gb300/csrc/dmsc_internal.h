@@ -35,6 +35,11 @@ cudaError_t launch_labels(const uint32_t *codes, const uint32_t *terms, const fl
 
 cudaError_t scan_exclusive_u8(const uint8_t *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st);
 cudaError_t scan_exclusive_u32(const uint32_t *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st);
+long long scan_scratch_words(long long n);
+cudaError_t scan_exclusive_u32_scratch(const uint32_t *in, long long n, uint32_t *out, uint32_t *total,
+                                       uint32_t *scratch, cudaStream_t st);
+// Records the calling thread's last error message (dmsc_last_error) and returns `code`.
+int set_last_error(int code, const char *msg);
 cudaError_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *ktmp, uint32_t *vtmp, long long n, int nbits,
                              cudaStream_t st);
 cudaError_t sort_pairs_batched(uint32_t *dk, uint32_t *dv, const uint32_t *sk, const uint32_t *sv, uint32_t batch,

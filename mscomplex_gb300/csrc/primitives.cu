@@ -118,6 +118,37 @@ cudaError_t scan_exclusive_u32(const uint32_t *in, long long n, uint32_t *out, u
   return scan_exclusive_t<uint32_t>(in, n, out, total, st);
 }
 
+// Same scan with caller-provided scratch instead of the stream-ordered
+// allocator: `scratch` must hold scan_scratch_words(n) uint32 words.
+long long scan_scratch_words(long long n) {
+  long long words = 0;
+  for (long long nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK; nb > 1; nb = (nb + SCAN_CHUNK - 1) / SCAN_CHUNK)
+    words += 2 * nb;
+  return words;
+}
+
+cudaError_t scan_exclusive_u32_scratch(const uint32_t *in, long long n, uint32_t *out, uint32_t *total,
+                                       uint32_t *scratch, cudaStream_t st) {
+  if (n <= 0) {
+    if (total) return cudaMemsetAsync(total, 0, sizeof(uint32_t), st);
+    return cudaSuccess;
+  }
+  long long nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+  if (nb == 1) {
+    k_scan_down<uint32_t><<<1, SCAN_THREADS, 0, st>>>(in, n, nullptr, out, total);
+    DMSC_LAUNCHED(1);
+    return cudaGetLastError();
+  }
+  uint32_t *part = scratch, *poff = scratch + nb;
+  k_scan_reduce<uint32_t><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, part);
+  DMSC_LAUNCHED(1);
+  cudaError_t e = scan_exclusive_u32_scratch(part, nb, poff, nullptr, scratch + 2 * nb, st);
+  if (e != cudaSuccess) return e;
+  k_scan_down<uint32_t><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, poff, out, total);
+  DMSC_LAUNCHED(1);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // stable LSD radix sort of (key, value) pairs on key bits [0, nbits)
 // ---------------------------------------------------------------------------
