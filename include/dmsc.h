@@ -94,6 +94,18 @@ int dmsc_msc_export(dmsc_msc *msc, int16_t rect_ext[8], int16_t *cellid, float *
                     uint8_t *flags, uint32_t *asc_off, uint32_t *asc, uint32_t *des_off, uint32_t *des,
                     uint32_t *adisc_off, int16_t *adisc, uint32_t *ddisc_off, int16_t *ddisc, void *stream);
 
+/* GridMSComplex::simplify_un_simplify(tresh) (dmsc/src/grid_mscomplex.cpp:
+ * 384-535): persistence cancellation in the reference's exact pop order,
+ * then every cancellation undone, leaving isBoundryCancelable / pair_idx as
+ * the record of the simplified complex.  The reference heap's order among
+ * equal persistences is replayed exactly, so the pass is sequential: it stops
+ * with DMSC_ERR_DEVICE_TIMEOUT (complex unchanged) after max_ops heap pops
+ * and cross-connections (max_ops <= 0: 20,000,000). */
+int dmsc_msc_simplify_un_simplify(dmsc_msc *msc, double tresh, int64_t max_ops, void *stream);
+/* Counters of the last simplification: [0] heap pushes, [1] pops,
+ * [2] cancellations, [3] operations, [4] device status. */
+int dmsc_msc_simplify_stats(dmsc_msc *msc, uint64_t stats[5]);
+
 /* PrefixScan::PreScanBuffer(out, in, n, queue) (dmsc/include/prefix_scan.h:105-109,
  * dmsc/src/prefix_scan.cpp:457-464): exclusive prefix sum of n uint32 values
  * in device memory, out[i] = in[0] + ... + in[i-1] (wrapping modulo 2^32).

@@ -315,6 +315,47 @@ int dmsc_dataset_stage_times(dmsc_dataset *d, float *ms, int n) {
   return DMSC_OK;
 }
 
+int dmsc_msc_simplify_un_simplify(dmsc_msc *m, double tresh, int64_t max_ops, void *stream) {
+  if (!m) return fail(DMSC_ERR_BAD_ARG, "complex is null");
+  if (!(tresh >= 0.0)) return fail(DMSC_ERR_BAD_ARG, "threshold must be >= 0");
+  CK(cudaSetDevice(m->ctx->device));
+  cudaStream_t st = pick(m->ctx, stream);
+  unsigned long long *hs = nullptr;
+  CK(cudaMallocHost((void **)&hs, sizeof(unsigned long long) * 5));
+  SimplifyIO io;
+  io.ncp = m->ncp; io.nasc = m->nasc; io.ndes = m->ndes;
+  io.cellid = m->cellid.p; io.fn = m->fn.p; io.flags = m->flags.p; io.pair_idx = m->pair_idx.p;
+  io.aoff = m->aoff.p; io.asc = m->asc.p; io.doff = m->doff.p; io.des = m->des.p;
+  for (int i = 0; i < 4; ++i) io.rect[i] = m->rect[i];
+  io.tresh = tresh;
+  io.max_ops = max_ops > 0 ? (unsigned long long)max_ops : 20000000ull;
+  io.host_stats = hs;
+  cudaError_t e = simplify_run(io, st);
+  int rc = DMSC_OK;
+  if (e != cudaSuccess) rc = cuda_fail(e, "simplify_run");
+  else if (hs[4] != 0) rc = status_to_error((uint32_t)hs[4]);
+  if (rc == DMSC_OK) {
+    // grow the CSR arrays if needed, then write the new lists
+    if ((size_t)io.nasc_out + 1 > m->asc.n) e = m->asc.ensure(io.nasc_out + io.nasc_out / 4 + 16);
+    if (e == cudaSuccess && (size_t)io.ndes_out + 1 > m->des.n) e = m->des.ensure(io.ndes_out + io.ndes_out / 4 + 16);
+    if (e == cudaSuccess) e = simplify_emit(io, m->asc.p, m->des.p, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "simplify_emit");
+    else { m->nasc = io.nasc_out; m->ndes = io.ndes_out; }
+  }
+  for (int i = 0; i < 5; ++i) m->simp_stats[i] = hs[i];
+  simplify_release(io, st);
+  cudaStreamSynchronize(st);
+  cudaFreeHost(hs);
+  return rc;
+}
+
+int dmsc_msc_simplify_stats(dmsc_msc *m, uint64_t stats[5]) {
+  if (!m || !stats) return fail(DMSC_ERR_BAD_ARG, "null argument");
+  for (int i = 0; i < 5; ++i) stats[i] = m->simp_stats[i];
+  return DMSC_OK;
+}
+
 int dmsc_prefix_scan(dmsc_ctx *ctx, uint32_t *d_out, const uint32_t *d_in, int64_t n, uint32_t *d_total,
                      void *stream) {
   if (!ctx || n < 0 || (n > 0 && (!d_out || !d_in))) return fail(DMSC_ERR_BAD_ARG, "bad argument");

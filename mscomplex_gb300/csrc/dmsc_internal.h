@@ -53,4 +53,25 @@ cudaError_t launch_msc_flags(long long ncp, const uint8_t *cpflags, uint8_t *out
 cudaError_t launch_export_cells(const GridGeom &g, const uint32_t *codes, const uint4 *labels, const uint32_t *cp_cellid,
                                 long long ncp, int8_t *flags, int16_t *pairs, int16_t *own, cudaStream_t st);
 
+// Persistence simplification (simplify.cu): run, then emit the new CSR into
+// buffers of nasc_out / ndes_out entries, then release.
+struct SimplifyIO {
+  long long ncp = 0, nasc = 0, ndes = 0;
+  const uint32_t *cellid = nullptr;
+  const float *fn = nullptr;
+  uint8_t *flags = nullptr;      // updated by simplify_emit
+  uint32_t *pair_idx = nullptr;  // updated by simplify_emit
+  uint32_t *aoff = nullptr, *asc = nullptr, *doff = nullptr, *des = nullptr;  // offsets rewritten by simplify_run
+  int rect[4] = {0, 0, 0, 0};
+  double tresh = 0;
+  unsigned long long max_ops = 0;
+  unsigned long long heap_cap = 0, tmp_cap = 0, pool_extra = 0;  // 0 = defaults
+  unsigned long long *host_stats = nullptr;  // [0] pushes [1] pops [2] cancels [3] ops [4] status
+  long long nasc_out = 0, ndes_out = 0;
+  void *work = nullptr;
+};
+cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st);
+cudaError_t simplify_emit(SimplifyIO &io, uint32_t *asc, uint32_t *des, cudaStream_t st);
+void simplify_release(SimplifyIO &io, cudaStream_t st);
+
 }  // namespace dmsc

@@ -79,6 +79,7 @@ struct dmsc_msc {
   DevBuf<uint32_t> adisc, ddisc;  // packed cell ids
   DevBuf<float> fn;
   DevBuf<uint8_t> flags;  // bit0 isCancelled, bit1 isOnStrangulationPath, bit2 isBoundryCancelable
+  unsigned long long simp_stats[5] = {0, 0, 0, 0, 0};
 
   int writeout_from(const dmsc_dataset &d, cudaStream_t st);
 };

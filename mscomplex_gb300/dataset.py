@@ -152,6 +152,19 @@ class GridMSComplex:
             self.lib.dmsc_msc_destroy(self.h)
             self.h = None
 
+    def simplify_un_simplify(self, tresh: float, max_ops: int = 0, stream=None) -> dict:
+        """GridMSComplex::simplify_un_simplify: persistence cancellation at
+        `tresh` (fraction of the value range) in the reference's exact order."""
+        rc = self.lib.dmsc_msc_simplify_un_simplify(self.h, float(tresh), int(max_ops), stream)
+        st = self.simplify_stats()
+        check(rc)
+        return st
+
+    def simplify_stats(self) -> dict:
+        a = np.zeros(5, np.uint64)
+        check(self.lib.dmsc_msc_simplify_stats(self.h, _ptr(a)))
+        return dict(zip(("pushes", "pops", "cancels", "ops", "status"), (int(v) for v in a)))
+
     def sizes(self):
         s = np.zeros(5, np.int64)
         check(self.lib.dmsc_msc_sizes(self.h, _ptr(s)))
