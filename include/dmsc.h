@@ -106,6 +106,19 @@ int dmsc_msc_simplify_un_simplify(dmsc_msc *msc, double tresh, int64_t max_ops, 
  * [2] cancellations, [3] operations, [4] device status. */
 int dmsc_msc_simplify_stats(dmsc_msc *msc, uint64_t stats[5]);
 
+/* GridDataset::postMergeFillDiscs(mscomplex_t *) (dmsc/src/grid_dataset.cpp:
+ * 1044-1231): fills the asc/des manifold discs of the complex's surviving
+ * critical points from the dataset's gradient and owners (dataset_work must
+ * have run on the piece the complex belongs to).  The dataset's owner labels
+ * of cancelled extrema are redirected as in the reference, on a copy: the
+ * dataset itself is not modified. */
+int dmsc_dataset_fill_discs(dmsc_dataset *ds, dmsc_msc *msc, void *stream);
+/* GridMSComplex::write_discs(prefix) (dmsc/src/grid_mscomplex.cpp:542-590):
+ * for every critical point that is not boundary-cancelable, appends its
+ * non-empty asc / des disc (x, y int16 pairs) to the file prefix + "asc_" /
+ * "des_" + "(x,y)" (binary, append mode, as the reference). */
+int dmsc_msc_write_discs(dmsc_msc *msc, const char *prefix);
+
 /* PrefixScan::PreScanBuffer(out, in, n, queue) (dmsc/include/prefix_scan.h:105-109,
  * dmsc/src/prefix_scan.cpp:457-464): exclusive prefix sum of n uint32 values
  * in device memory, out[i] = in[0] + ... + in[i-1] (wrapping modulo 2^32).

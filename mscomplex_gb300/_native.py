@@ -42,6 +42,8 @@ SIGNATURES = {
     "dmsc_kernel_launches": ([_vp], _i32),
     "dmsc_msc_simplify_un_simplify": ([_vp, _f64, _i64, _vp], _i32),
     "dmsc_msc_simplify_stats": ([_vp, _vp], _i32),
+    "dmsc_dataset_fill_discs": ([_vp, _vp, _vp], _i32),
+    "dmsc_msc_write_discs": ([_vp, C.c_char_p], _i32),
     "dmsc_prefix_scan": ([_vp, _vp, _vp, _i64, _vp, _vp], _i32),
     "dmsc_prefix_scan_noalloc": ([_vp, _vp, _vp, _i64, _vp, _vp], _i32),
     "dmsc_sort_pairs": ([_vp, _vp, _vp, _vp, _vp, C.c_uint32, C.c_uint32, C.c_uint32, _vp], _i32),

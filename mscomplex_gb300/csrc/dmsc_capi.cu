@@ -356,6 +356,70 @@ int dmsc_msc_simplify_stats(dmsc_msc *m, uint64_t stats[5]) {
   return DMSC_OK;
 }
 
+int dmsc_dataset_fill_discs(dmsc_dataset *d, dmsc_msc *m, void *stream) {
+  if (!d || !m) return fail(DMSC_ERR_BAD_ARG, "null argument");
+  if (!d->worked) return fail(DMSC_ERR_STATE, "dataset_work has not run");
+  if (m->ncp < d->ncp) return fail(DMSC_ERR_BAD_ARG, "complex does not hold the dataset's critical points");
+  CK(cudaSetDevice(d->ctx->device));
+  cudaStream_t st = pick(d->ctx, stream);
+  const size_t n = (size_t)m->ncp;
+  CK(m->adoff.ensure(n + 1));
+  CK(m->ddoff.ensure(n + 1));
+  DiscIO io;
+  io.g = d->g; io.codes = d->codes.p; io.labels = d->labels.p; io.ncp_ds = d->ncp;
+  io.ncp = m->ncp; io.nasc = m->nasc; io.ndes = m->ndes;
+  io.cellid = m->cellid.p; io.flags = m->flags.p; io.pair_idx = m->pair_idx.p;
+  io.aoff = m->aoff.p; io.asc = m->asc.p; io.doff = m->doff.p; io.des = m->des.p;
+  io.adoff = m->adoff.p; io.ddoff = m->ddoff.p; io.adisc = &m->adisc; io.ddisc = &m->ddisc;
+  io.status = d->scal.p;
+  // a gradient path visits each cell at most once: bounds every chain of a disc
+  io.limit = (unsigned long long)(d->g.cx + 1) * (d->g.cy + 1) + 16;
+  CK(cudaMemsetAsync(d->scal.p, 0, sizeof(uint32_t), st));
+  CK(fill_discs(io, st));
+  uint32_t stw = 0;
+  CK(cudaMemcpyAsync(&stw, d->scal.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (stw) return status_to_error(stw);
+  m->nadisc = io.nadisc;
+  m->nddisc = io.nddisc;
+  return DMSC_OK;
+}
+
+int dmsc_msc_write_discs(dmsc_msc *m, const char *prefix) {
+  if (!m || !prefix) return fail(DMSC_ERR_BAD_ARG, "null argument");
+  if (!m->adoff.p || !m->ddoff.p) return fail(DMSC_ERR_STATE, "the complex has no discs (fill_discs has not run)");
+  CK(cudaSetDevice(m->ctx->device));
+  size_t n = (size_t)m->ncp;
+  std::vector<uint32_t> cell(n), ao(n + 1), dofs(n + 1), ad(m->nadisc), dd(m->nddisc);
+  std::vector<uint8_t> fl(n);
+  if (n) {
+    CK(cudaMemcpy(cell.data(), m->cellid.p, 4 * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(fl.data(), m->flags.p, n, cudaMemcpyDeviceToHost));
+  }
+  CK(cudaMemcpy(ao.data(), m->adoff.p, 4 * (n + 1), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(dofs.data(), m->ddoff.p, 4 * (n + 1), cudaMemcpyDeviceToHost));
+  if (m->nadisc) CK(cudaMemcpy(ad.data(), m->adisc.p, 4 * m->nadisc, cudaMemcpyDeviceToHost));
+  if (m->nddisc) CK(cudaMemcpy(dd.data(), m->ddisc.p, 4 * m->nddisc, cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < n; ++i) {
+    if (fl[i] & 4) continue;
+    const int16_t x = (int16_t)(cell[i] & 0xffff), y = (int16_t)(cell[i] >> 16);
+    for (int k = 0; k < 2; ++k) {
+      const std::vector<uint32_t> &off = k ? dofs : ao;
+      const std::vector<uint32_t> &v = k ? dd : ad;
+      if (off[i + 1] == off[i]) continue;
+      std::string fn = std::string(prefix) + (k ? "des_" : "asc_") + "(" + std::to_string(x) + "," + std::to_string(y) + ")";
+      FILE *f = fopen(fn.c_str(), "ab");
+      if (!f) return fail(DMSC_ERR_BAD_ARG, "asc/des disc file not writeable: " + fn);
+      // each packed cell id is (x, y) as two little-endian int16, the layout of cellid_t
+      size_t cnt = off[i + 1] - off[i];
+      size_t wrote = fwrite(v.data() + off[i], 4, cnt, f);
+      fclose(f);
+      if (wrote != cnt) return fail(DMSC_ERR_BAD_ARG, "short write to " + fn);
+    }
+  }
+  return DMSC_OK;
+}
+
 int dmsc_prefix_scan(dmsc_ctx *ctx, uint32_t *d_out, const uint32_t *d_in, int64_t n, uint32_t *d_total,
                      void *stream) {
   if (!ctx || n < 0 || (n > 0 && (!d_out || !d_in))) return fail(DMSC_ERR_BAD_ARG, "bad argument");

@@ -71,7 +71,29 @@ struct SimplifyIO {
   void *work = nullptr;
 };
 cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st);
+
 cudaError_t simplify_emit(SimplifyIO &io, uint32_t *asc, uint32_t *des, cudaStream_t st);
 void simplify_release(SimplifyIO &io, cudaStream_t st);
+
+}  // namespace dmsc
+template <typename T> struct DevBuf;
+namespace dmsc {
+// Manifold discs (discs.cu): postMergeFillDiscs of one dataset into its complex.
+struct DiscIO {
+  GridGeom g;
+  const uint32_t *codes = nullptr;
+  const uint4 *labels = nullptr;
+  long long ncp_ds = 0, ncp = 0, nasc = 0, ndes = 0;
+  const uint32_t *cellid = nullptr;
+  const uint8_t *flags = nullptr;
+  const uint32_t *pair_idx = nullptr;
+  const uint32_t *aoff = nullptr, *asc = nullptr, *doff = nullptr, *des = nullptr;
+  uint32_t *adoff = nullptr, *ddoff = nullptr;  // ncp+1 each (outputs)
+  DevBuf<uint32_t> *adisc = nullptr, *ddisc = nullptr;
+  uint32_t *status = nullptr;
+  unsigned long long limit = 1ull << 31;  // bound on one gradient chain (cells of the window)
+  long long nadisc = 0, nddisc = 0;
+};
+cudaError_t fill_discs(DiscIO &io, cudaStream_t st);
 
 }  // namespace dmsc

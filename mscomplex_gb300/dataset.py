@@ -133,6 +133,11 @@ class GridDataset:
         check(self.lib.dmsc_dataset_stage_times(self.h, _ptr(ms), 5))
         return dict(zip(self.STAGES, (float(v) for v in ms)))
 
+    def post_merge_fill_discs(self, msc: "GridMSComplex", stream=None) -> "GridMSComplex":
+        """GridDataset::postMergeFillDiscs: the manifold discs of `msc`."""
+        check(self.lib.dmsc_dataset_fill_discs(self.h, msc.h, stream))
+        return msc
+
     def writeout_connectivity(self, stream=None) -> "GridMSComplex":
         h = C.c_void_p()
         check(self.lib.dmsc_dataset_writeout_connectivity(self.h, C.byref(h), stream))
@@ -164,6 +169,10 @@ class GridMSComplex:
         a = np.zeros(5, np.uint64)
         check(self.lib.dmsc_msc_simplify_stats(self.h, _ptr(a)))
         return dict(zip(("pushes", "pops", "cancels", "ops", "status"), (int(v) for v in a)))
+
+    def write_discs(self, prefix: str):
+        """GridMSComplex::write_discs: one binary file per disc, appended."""
+        check(self.lib.dmsc_msc_write_discs(self.h, prefix.encode()))
 
     def sizes(self):
         s = np.zeros(5, np.int64)

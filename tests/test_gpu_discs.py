@@ -1,0 +1,69 @@
+"""GPU parity of the manifold discs (postMergeFillDiscs, dmsc/src/grid_dataset.cpp:
+1044-1231) against the oracle: every asc/des disc, cell by cell and in order."""
+import numpy as np
+import pytest
+
+from helpers import assert_same_complex, full_rect, smooth_field, tie_field
+
+pytestmark = pytest.mark.gpu
+
+
+def check_discs(M, oracle, f, tresh, what):
+    r = full_rect(f)
+    want = oracle.Dataset(f, r, r, tresh=tresh, fill_discs=True).msc()
+    ds = M.GridDataset(r, r).init(f).work()
+    msc = ds.writeout_connectivity()
+    if tresh > 0:
+        msc.simplify_un_simplify(tresh)
+    ds.post_merge_fill_discs(msc)
+    assert_same_complex(msc.export(), want, what)
+
+
+@pytest.mark.parametrize("tresh", [0.0, 0.05, 0.3])
+def test_discs_smooth(gpu_lib, oracle, tresh):
+    check_discs(gpu_lib, oracle, smooth_field(70, 90, 5), tresh, f"smooth t={tresh}")
+
+
+# (seed, threshold) pairs whose reference discs stay bounded: on tie fields
+# un_simplify multiplies arc multiplicities, and postMergeFillDiscs pushes a
+# cancelled saddle once per occurrence (seed 2 at 0.1 yields 617K disc cells;
+# seed 1 at 0.1 exhausts gigabytes in the reference algorithm itself).
+@pytest.mark.parametrize("seed,tresh", [(0, 0.05), (1, 0.05), (2, 0.05), (0, 0.25), (2, 0.1)])
+def test_discs_ties(gpu_lib, oracle, seed, tresh):
+    check_discs(gpu_lib, oracle, tie_field(30 + 9 * seed, 41 + 4 * seed, 4, seed), tresh, f"ties seed={seed} t={tresh}")
+
+
+def test_discs_bumps256(gpu_lib, oracle):
+    from mscomplex_gb300 import synth
+    check_discs(gpu_lib, oracle, synth.bumps256(), 0.0, "bumps256")
+
+
+def test_discs_quantized_simplified(gpu_lib, oracle):
+    from mscomplex_gb300 import synth
+    check_discs(gpu_lib, oracle, synth.bumps4096q(n=256), 0.01, "bumps256q t=0.01")
+
+
+def test_discs_multi_tile(gpu_lib, oracle):
+    check_discs(gpu_lib, oracle, smooth_field(150, 133, 9), 0.02, "smooth 150x133 t=0.02")
+
+
+def test_write_discs_files(gpu_lib, oracle, tmp_path):
+    from mscomplex_gb300 import synth
+    f = synth.bumps256()
+    r = full_rect(f)
+    ds = gpu_lib.GridDataset(r, r).init(f).work()
+    msc = ds.writeout_connectivity()
+    msc.simplify_un_simplify(0.05)
+    ds.post_merge_fill_discs(msc)
+    msc.write_discs(str(tmp_path / "dp__disc_"))
+    P = oracle.Pipeline(f, levels=0, tresh=0.05)
+    want = P.disc_files()
+    got = {}
+    for p in tmp_path.iterdir():
+        name = p.name[len("dp__disc_"):]
+        kind = 0 if name.startswith("asc_") else 1
+        x, y = (int(v) for v in name[5:-1].split(","))
+        got[(kind, x, y)] = np.fromfile(p, np.int16).reshape(-1, 2)
+    assert set(got) == set(want)
+    for k in want:
+        assert np.array_equal(got[k], want[k]), k
