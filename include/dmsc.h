@@ -119,6 +119,35 @@ int dmsc_dataset_fill_discs(dmsc_dataset *ds, dmsc_msc *msc, void *stream);
  * "des_" + "(x,y)" (binary, append mode, as the reference). */
 int dmsc_msc_write_discs(dmsc_msc *msc, const char *prefix);
 
+/* ---- the whole piece pipeline ----
+ * GridDataManager (dmsc/src/grid_datamanager.cpp): createPieces_quadtree
+ * (:40-89), computeSubdomainMsgraphs (:493-528), mergePiecesUp (:258-306),
+ * simplify_un_simplify at the root (:651-652), mergePiecesDown +
+ * finalMergeDownPiecesInRange (:308-395) and collectSubdomainManifolds
+ * (:454-490) on one GPU.  The grid (size_x x size_y vertices, row pitch in
+ * floats) is split `levels` times into 2^levels pieces with a one-vertex
+ * halo; split2d = 0 splits along y as the reference (split_axes = 1,
+ * :50-51), split2d = 1 alternates y and x.  tresh <= 0 skips simplification.
+ * On success every piece holds its merged-down complex with manifold discs.
+ * The pipeline owns the pieces' datasets and complexes. */
+typedef struct dmsc_pipeline dmsc_pipeline;
+int dmsc_pipeline_run(dmsc_ctx *ctx, const float *heights, int64_t pitch, int on_device, int size_x, int size_y,
+                      int levels, double tresh, int split2d, dmsc_pipeline **out, void *stream);
+int dmsc_pipeline_destroy(dmsc_pipeline *p);
+int dmsc_pipeline_num_pieces(dmsc_pipeline *p, int64_t *n);
+/* Node i of the piece tree: i < num_pieces is a leaf (order of
+ * createPieces_quadtree), num_pieces <= i < 2 num_pieces - 1 is the merge of
+ * nodes 2(i - num_pieces) and 2(i - num_pieces) + 1 (the last is the root),
+ * in its state after merge_down.  Returns its complex and, for a leaf, its
+ * dataset (NULL for inner nodes); either output pointer may be NULL.  Both
+ * stay owned by the pipeline. */
+int dmsc_pipeline_piece(dmsc_pipeline *p, int64_t i, dmsc_msc **msc, dmsc_dataset **ds);
+/* write_discs of every piece in leaf order, as collectSubdomainManifolds. */
+int dmsc_pipeline_write_discs(dmsc_pipeline *p, const char *prefix);
+/* Host wall time (ms) of the last run's stages: pieces, merge up, simplify,
+ * merge down, discs. */
+int dmsc_pipeline_stage_times(dmsc_pipeline *p, double ms[5]);
+
 /* PrefixScan::PreScanBuffer(out, in, n, queue) (dmsc/include/prefix_scan.h:105-109,
  * dmsc/src/prefix_scan.cpp:457-464): exclusive prefix sum of n uint32 values
  * in device memory, out[i] = in[0] + ... + in[i-1] (wrapping modulo 2^32).

@@ -44,6 +44,12 @@ SIGNATURES = {
     "dmsc_msc_simplify_stats": ([_vp, _vp], _i32),
     "dmsc_dataset_fill_discs": ([_vp, _vp, _vp], _i32),
     "dmsc_msc_write_discs": ([_vp, C.c_char_p], _i32),
+    "dmsc_pipeline_run": ([_vp, _vp, _i64, _i32, _i32, _i32, _i32, C.c_double, _i32, _vp, _vp], _i32),
+    "dmsc_pipeline_destroy": ([_vp], _i32),
+    "dmsc_pipeline_num_pieces": ([_vp, _vp], _i32),
+    "dmsc_pipeline_piece": ([_vp, _i64, _vp, _vp], _i32),
+    "dmsc_pipeline_write_discs": ([_vp, C.c_char_p], _i32),
+    "dmsc_pipeline_stage_times": ([_vp, _vp], _i32),
     "dmsc_prefix_scan": ([_vp, _vp, _vp, _i64, _vp, _vp], _i32),
     "dmsc_prefix_scan_noalloc": ([_vp, _vp, _vp, _i64, _vp, _vp], _i32),
     "dmsc_sort_pairs": ([_vp, _vp, _vp, _vp, _vp, C.c_uint32, C.c_uint32, C.c_uint32, _vp], _i32),

@@ -96,4 +96,25 @@ struct DiscIO {
 };
 cudaError_t fill_discs(DiscIO &io, cudaStream_t st);
 
+// Piece merges (merge.cu).  MGraphHost is host-side storage of a device
+// MGraph (a complex as a mutable graph with its cell-id hash).
+struct MGraphHost {
+  uint32_t *buf = nullptr;
+  alignas(16) unsigned char raw[320];
+};
+
+}  // namespace dmsc
+
+struct dmsc_msc;
+namespace dmsc {
+cudaError_t mgraph_alloc(MGraphHost &h, const dmsc_msc &src, uint32_t cap, unsigned long long pool, cudaStream_t st);
+void mgraph_free(MGraphHost &h, cudaStream_t st);
+void mgraph_set_rects(MGraphHost &h, const int rect[4], const int ext[4]);
+uint32_t mgraph_ncp(const MGraphHost &h);
+unsigned long long mgraph_pool_used(const MGraphHost &h);
+cudaError_t mgraph_to_csr(const MGraphHost &h, dmsc_msc &out, cudaStream_t st);
+// One tree level: jobs are (a, b, c) graph indices -- merge up: out c = a + b;
+// merge down: parent a into children b and c; ixn4: the shared 1-manifold (l,b,r,t).
+cudaError_t merge_level(bool up, MGraphHost *hosts, int ngraphs, const int *jobs3, const int *ixn4, int njobs,
+                        uint32_t *status, cudaStream_t st);
 }  // namespace dmsc

@@ -1,0 +1,442 @@
+// merge.cu -- piece merges of Morse-Smale complexes on the device:
+// GridMSComplex::merge_up and merge_down (dmsc/src/grid_mscomplex.cpp:7-322).
+//
+// A complex being merged is a mutable graph (msc_graph.cuh) plus a hash table
+// from cell id to critical-point index standing in for m_id_cp_map (std::map).
+// Both merges are restated step by step, including the reference's
+// std::map::operator[] (a missing key is inserted with index 0).  Each merge
+// runs on one thread; independent merges of one tree level run in separate
+// blocks of one launch.
+#include "dmsc_common.cuh"
+#include "dmsc_internal.h"
+#include "msc_graph.cuh"
+#include "grid_types.h"
+
+namespace dmsc {
+
+constexpr uint32_t HASH_EMPTY = 0xFFFFFFFFu;
+constexpr uint32_t NO_CP = 0xFFFFFFFFu;
+
+struct CRect {  // rect_t (dmsc/include/rectangle_complex.h:108-308), global cell coordinates
+  int l, b, r, t;
+  __host__ __device__ bool contains(int x, int y) const { return x >= l && y >= b && x <= r && y <= t; }
+  __host__ __device__ bool interior(int x, int y) const { return x > l && y > b && x < r && y < t; }
+  __host__ __device__ bool boundary(int x, int y) const { return contains(x, y) && !interior(x, y); }
+};
+
+struct MGraph {
+  Graph G;           // G.ncp is the current number of critical points
+  float *fn;
+  uint32_t cap;      // capacity of the per-cp arrays
+  uint32_t *hkey, *hval;
+  uint32_t hmask;    // hash capacity - 1 (power of two)
+  CRect rect, ext;
+
+  __host__ __device__ static uint32_t hash(uint32_t k) {
+    k ^= k >> 16; k *= 0x7feb352du; k ^= k >> 15; k *= 0x846ca68bu; k ^= k >> 16;
+    return k;
+  }
+  __host__ __device__ uint32_t find(uint32_t cid) const {
+    uint32_t h = hash(cid) & hmask;
+    for (uint32_t probe = 0; probe <= hmask; ++probe) {
+      uint32_t k = hkey[h];
+      if (k == cid) return hval[h];
+      if (k == HASH_EMPTY) return NO_CP;
+      h = (h + 1) & hmask;
+    }
+    return NO_CP;
+  }
+  __host__ __device__ bool put(uint32_t cid, uint32_t idx) {
+    uint32_t h = hash(cid) & hmask;
+    for (uint32_t probe = 0; probe <= hmask; ++probe) {
+      if (hkey[h] == HASH_EMPTY || hkey[h] == cid) { hkey[h] = cid; hval[h] = idx; return true; }
+      h = (h + 1) & hmask;
+    }
+    G.fail = true;
+    return false;
+  }
+  // std::map::operator[]: inserts index 0 for a missing key
+  __host__ __device__ uint32_t at(uint32_t cid) {
+    uint32_t i = find(cid);
+    if (i != NO_CP) return i;
+    put(cid, 0);
+    return 0;
+  }
+  // shallow_replicate_cp (grid_mscomplex.cpp:7-22): flags copied, pair unset
+  __host__ __device__ uint32_t add(uint32_t cid, uint8_t fl, float f) {
+    if (G.ncp >= cap) { G.fail = true; return 0; }
+    uint32_t k = G.ncp++;
+    G.cellid[k] = cid;
+    G.flags[k] = fl & (F_CANCELLED | F_STRANG | F_BCANCEL);
+    G.pair_idx[k] = NO_CP;
+    fn[k] = f;
+    for (int w = 0; w < 2; ++w) {
+      G.L.off[2 * k + w] = 0; G.L.nrun[2 * k + w] = 0; G.L.cap[2 * k + w] = 0; G.L.total[2 * k + w] = 0;
+    }
+    put(cid, k);
+    return k;
+  }
+};
+
+__host__ __device__ __forceinline__ void set_status(uint32_t *s, uint32_t v) {
+#ifdef __CUDA_ARCH__
+  atomicOr(s, v);
+#else
+  *s |= v;
+#endif
+}
+
+__host__ __device__ __forceinline__ int px_(uint32_t c) { return (int16_t)(c & 0xffff); }
+__host__ __device__ __forceinline__ int py_(uint32_t c) { return (int16_t)(c >> 16); }
+
+// merge_up (grid_mscomplex.cpp:24-156); out starts empty.
+__host__ __device__ void merge_up_one(MGraph *in[2], MGraph &out, CRect ixn, uint32_t *status) {
+  // union of the critical points (:56-75)
+  for (int i = 0; i < 2; ++i) {
+    MGraph &M = *in[i];
+    for (uint32_t j = 0; j < M.G.ncp && !out.G.fail; ++j) {
+      uint32_t cid = M.G.cellid[j];
+      if (i == 1 && out.find(cid) != NO_CP) continue;
+      if (M.G.flags[j] & F_CANCELLED) continue;
+      out.add(cid, M.G.flags[j], M.fn[j]);
+    }
+  }
+  // connectivity (:77-122)
+  for (int i = 0; i < 2 && !out.G.fail; ++i) {
+    MGraph &M = *in[i];
+    for (uint32_t j = 0; j < M.G.ncp && !out.G.fail; ++j) {
+      if (M.G.flags[j] & F_CANCELLED) continue;
+      uint32_t cid = M.G.cellid[j];
+      uint32_t d = out.find(cid);
+      if (d == NO_CP) { set_status(status, ST_INVARIANT); return; }
+      if (M.G.flags[j] & F_BCANCEL) {
+        uint32_t p = M.G.pair_idx[j];
+        if (p >= M.G.ncp) { set_status(status, ST_INVARIANT); return; }
+        out.G.pair_idx[d] = out.at(M.G.cellid[p]);
+      }
+      bool cmn = ixn.contains(px_(cid), py_(cid)) && i == 1;
+      for (int k = 0; k < 2; ++k) {
+        uint32_t l = 2 * j + k;
+        for (uint32_t q = 0; q < M.G.L.nrun[l]; ++q) {
+          uint2 r = M.G.runs(l)[q];
+          uint32_t cc = M.G.cellid[r.x];
+          if (cmn && ixn.contains(px_(cc), py_(cc))) continue;
+          if (M.G.flags[r.x] & F_CANCELLED) continue;
+          out.G.insert(2 * d + k, out.at(cc), r.y);
+        }
+      }
+    }
+  }
+  // cancellation along the shared boundary (:124-153)
+  for (int y = ixn.b; y <= ixn.t && !out.G.fail; ++y)
+    for (int x = ixn.l; x <= ixn.r && !out.G.fail; ++x) {
+      uint32_t si = out.find(pack_cellid(x, y));
+      if (si == NO_CP) { set_status(status, ST_INVARIANT); return; }  // "missing common bndry cp"
+      if ((out.G.flags[si] & F_CANCELLED) || !(out.G.flags[si] & F_BCANCEL)) continue;
+      uint32_t pi = out.G.pair_idx[si];
+      if (pi >= out.G.ncp) { set_status(status, ST_INVARIANT); return; }
+      uint32_t p = out.G.cellid[pi];
+      if (!out.rect.interior(x, y) && !out.ext.boundary(x, y)) continue;
+      if (!out.rect.interior(px_(p), py_(p)) && !out.ext.boundary(px_(p), py_(p))) continue;
+      uint32_t a = si, b = pi;
+      out.G.cancel_pairs(a, b);
+    }
+}
+
+// merge_down (grid_mscomplex.cpp:158-322) of parent P into one child C; the
+// boundary uncancellation on P is done once by the caller.
+__host__ __device__ void merge_down_child(MGraph &P, MGraph &C, uint32_t *status) {
+  Graph &G = C.G;
+  // cancelable critical points of the parent (:207-281)
+  for (uint32_t j = 0; j < P.G.ncp && !G.fail; ++j) {
+    if (P.G.flags[j] & F_CANCELLED) { set_status(status, ST_INVARIANT); return; }  // "all cps ought to be uncancelled"
+    if (!(P.G.flags[j] & F_BCANCEL)) continue;
+    uint32_t sp = P.G.pair_idx[j];
+    if (sp >= P.G.ncp) { set_status(status, ST_INVARIANT); return; }
+    uint32_t scid = P.G.cellid[j], spcid = P.G.cellid[sp];
+    bool s_in = C.find(scid) != NO_CP, sp_in = C.find(spcid) != NO_CP;
+    if (!s_in && !sp_in) continue;
+    if (!s_in) C.add(scid, P.G.flags[j], P.fn[j]);
+    if (!sp_in) C.add(spcid, P.G.flags[sp], P.fn[sp]);
+    uint32_t di = C.at(scid);
+    if (!s_in || !sp_in || !(G.flags[di] & F_BCANCEL)) {
+      uint32_t dpi = C.at(spcid);
+      G.flags[di] |= F_BCANCEL;
+      G.flags[dpi] |= F_BCANCEL;
+      G.pair_idx[di] = dpi;
+      G.pair_idx[dpi] = di;
+    }
+    for (int k = 0; k < 2 && !G.fail; ++k) {
+      uint32_t l = 2 * j + k;
+      unsigned long long n = 0;
+      for (uint32_t q = 0; q < P.G.L.nrun[l]; ++q) {
+        uint2 r = P.G.runs(l)[q];
+        if (P.G.flags[r.x] & F_BCANCEL) { set_status(status, ST_INVARIANT); return; }  // "only non cancellable cps"
+        uint32_t cc = P.G.cellid[r.x];
+        if (C.find(cc) == NO_CP) C.add(cc, P.G.flags[r.x], P.fn[r.x]);
+        if (n >= G.tmp_cap) { G.fail = true; return; }
+        G.tmp[n++] = make_uint2(C.at(cc), r.y);
+      }
+      G.set_list_from_tmp(2 * di + k, n);
+    }
+  }
+  // the other critical points the child holds (:283-320)
+  for (uint32_t j = 0; j < P.G.ncp && !G.fail; ++j) {
+    if (P.G.flags[j] & F_BCANCEL) continue;
+    uint32_t di = C.find(P.G.cellid[j]);
+    if (di == NO_CP) continue;
+    for (int k = 0; k < 2 && !G.fail; ++k) {
+      uint32_t l = 2 * j + k;
+      unsigned long long n = 0;
+      for (uint32_t q = 0; q < P.G.L.nrun[l]; ++q) {
+        uint2 r = P.G.runs(l)[q];
+        uint32_t ci = C.find(P.G.cellid[r.x]);
+        if (ci == NO_CP) continue;
+        if (n >= G.tmp_cap) { G.fail = true; return; }
+        G.tmp[n++] = make_uint2(ci, r.y);
+      }
+      G.set_list_from_tmp(2 * di + k, n);
+    }
+  }
+}
+
+// merge_down's uncancellation along the shared boundary of the children, in
+// reverse row-major order (grid_mscomplex.cpp:172-201), done once on the parent.
+__host__ __device__ void merge_down_boundary(MGraph &P, CRect ixn, uint32_t *status) {
+  for (int y = ixn.t; y >= ixn.b && !P.G.fail; --y)
+    for (int x = ixn.r; x >= ixn.l && !P.G.fail; --x) {
+      uint32_t si = P.find(pack_cellid(x, y));
+      if (si == NO_CP) { set_status(status, ST_INVARIANT); return; }
+      if (!(P.G.flags[si] & F_CANCELLED)) continue;
+      uint32_t pi = P.G.pair_idx[si];
+      if (pi >= P.G.ncp) { set_status(status, ST_INVARIANT); return; }
+      uint32_t p = P.G.cellid[pi];
+      if (!P.rect.interior(x, y) && !P.ext.boundary(x, y)) continue;
+      if (!P.rect.interior(px_(p), py_(p)) && !P.ext.boundary(px_(p), py_(p))) continue;
+      if (!P.G.uncancel_pairs(si, pi)) { set_status(status, ST_INVARIANT); return; }
+    }
+}
+
+// One block per merge of a tree level; thread 0 works.
+__global__ void k_merge_up(MGraph *graphs, const int3 *jobs, const CRect *ixns, int njobs, uint32_t *status) {
+  int b = blockIdx.x;
+  if (b >= njobs || threadIdx.x != 0) return;
+  int3 jb = jobs[b];  // (left child, right child, output)
+  MGraph *in[2] = {&graphs[jb.x], &graphs[jb.y]};
+  merge_up_one(in, graphs[jb.z], ixns[b], status);
+  if (graphs[jb.z].G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+}
+
+__global__ void k_merge_down(MGraph *graphs, const int3 *jobs, const CRect *ixns, int njobs, uint32_t *status) {
+  int b = blockIdx.x;
+  if (b >= njobs || threadIdx.x != 0) return;
+  int3 jb = jobs[b];  // (parent, child 1, child 2)
+  MGraph &P = graphs[jb.x];
+  merge_down_boundary(P, ixns[b], status);
+  if (P.G.fail) { set_status(status, ST_SIMPLIFY_LIMIT); return; }
+  merge_down_child(P, graphs[jb.y], status);
+  if (graphs[jb.y].G.fail) { set_status(status, ST_SIMPLIFY_LIMIT); return; }
+  merge_down_child(P, graphs[jb.z], status);
+  if (graphs[jb.z].G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+}
+
+// ---------------------------------------------------------------------------
+// conversions between a CSR complex and an MGraph (parallel)
+// ---------------------------------------------------------------------------
+__global__ void k_mg_from_csr(MGraph m, uint32_t n, const uint32_t *cellid, const float *fn, const uint8_t *flags,
+                              const uint32_t *pair_idx, const uint32_t *aoff, const uint32_t *asc, const uint32_t *doff,
+                              const uint32_t *des) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    m.G.cellid[i] = cellid[i];
+    m.fn[i] = fn[i];
+    m.G.flags[i] = flags[i];
+    m.G.pair_idx[i] = pair_idx[i];
+    for (int w = 0; w < 2; ++w) {
+      const uint32_t *o = w ? doff : aoff, *src = w ? des : asc;
+      uint32_t b = o[i], e = o[i + 1];
+      // initial lists: asc runs at aoff[i] + i*4, des runs after all asc runs
+      unsigned long long base = w ? (unsigned long long)aoff[n] + 4ull * n + doff[i] + 4ull * i : aoff[i] + 4ull * i;
+      uint32_t r = 0;
+      for (uint32_t k = b; k < e; ++k) {
+        if (r > 0 && m.G.L.pool[base + r - 1].x == src[k]) m.G.L.pool[base + r - 1].y += 1;
+        else m.G.L.pool[base + r++] = make_uint2(src[k], 1u);
+      }
+      m.G.L.off[2 * i + w] = (uint32_t)base; m.G.L.nrun[2 * i + w] = r; m.G.L.cap[2 * i + w] = (e - b) + 4;
+      m.G.L.total[2 * i + w] = e - b;
+    }
+    // hash insert (keys are unique within a complex)
+    uint32_t cid = cellid[i], h = MGraph::hash(cid) & m.hmask;
+    for (uint32_t probe = 0; probe <= m.hmask; ++probe) {
+      uint32_t prev = atomicCAS(m.hkey + h, HASH_EMPTY, cid);
+      if (prev == HASH_EMPTY || prev == cid) { m.hval[h] = i; break; }
+      h = (h + 1) & m.hmask;
+    }
+  }
+}
+
+__global__ void k_mg_totals(MGraph m, int which, uint32_t *out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m.G.ncp; i += gridDim.x * blockDim.x)
+    out[i] = m.G.L.total[2 * i + which];
+}
+__global__ void k_mg_to_csr(MGraph m, int which, const uint32_t *off, uint32_t *out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m.G.ncp; i += gridDim.x * blockDim.x) {
+    uint32_t l = 2 * i + which, o = off[i];
+    const uint2 *p = m.G.L.pool + m.G.L.off[l];
+    for (uint32_t k = 0; k < m.G.L.nrun[l]; ++k)
+      for (uint32_t c = 0; c < p[k].y; ++c) out[o++] = p[k].x;
+  }
+}
+
+static unsigned nblk(long long n) {
+  long long b = (n + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+// Allocates an MGraph with room for `cap` critical points and a list pool of
+// `pool` runs, and fills it from a CSR complex (n critical points, may be 0).
+cudaError_t mgraph_alloc(MGraphHost &h, const dmsc_msc &src, uint32_t cap, unsigned long long pool, cudaStream_t st) {
+  uint32_t n = (uint32_t)src.ncp;
+  if (cap < n) cap = n;
+  uint32_t hcap = 1;
+  while (hcap < 2 * cap + 16) hcap <<= 1;
+  unsigned long long base = (unsigned long long)src.nasc + src.ndes + 8ull * n;
+  if (pool < base + 1024) pool = base + 1024;
+  if (pool > 0xffffffffull) return cudaErrorInvalidValue;
+  unsigned long long tmpc = 1ull << 20;
+  size_t words = 4ull * cap + 8ull * cap + 2ull * hcap + 2 * pool + 2 * tmpc + 64;
+  cudaError_t e = cudaMallocAsync((void **)&h.buf, sizeof(uint32_t) * words, st);
+  if (e != cudaSuccess) return e;
+  uint32_t *p = h.buf;
+  MGraph &m = *reinterpret_cast<MGraph *>(h.raw);
+  static_assert(sizeof(MGraph) <= sizeof(h.raw), "MGraphHost storage");
+  m = MGraph();
+  m.G.cellid = p; p += cap;
+  m.fn = (float *)p; p += cap;
+  m.G.pair_idx = p; p += cap;
+  m.G.flags = (uint8_t *)p; p += cap;  // (1 byte used per word)
+  m.G.L.off = p; p += 2ull * cap;
+  m.G.L.nrun = p; p += 2ull * cap;
+  m.G.L.cap = p; p += 2ull * cap;
+  m.G.L.total = p; p += 2ull * cap;
+  m.hkey = p; p += hcap;
+  m.hval = p; p += hcap;
+  m.G.L.pool = (uint2 *)p; p += 2 * pool;
+  m.G.tmp = (uint2 *)p; p += 2 * tmpc;
+  m.G.tmp_cap = tmpc;
+  m.G.L.top = base;
+  m.G.L.pool_cap = pool;
+  m.G.ncp = n;
+  m.G.max_ops = ~0ull;
+  m.G.ops = 0;
+  m.G.fail = false;
+  m.cap = cap;
+  m.hmask = hcap - 1;
+  m.rect = CRect{src.rect[0], src.rect[1], src.rect[2], src.rect[3]};
+  m.ext = CRect{src.ext[0], src.ext[1], src.ext[2], src.ext[3]};
+  e = cudaMemsetAsync(m.hkey, 0xFF, sizeof(uint32_t) * hcap, st);
+  if (e == cudaSuccess && n) {
+    k_mg_from_csr<<<nblk(n), 256, 0, st>>>(m, n, src.cellid.p, src.fn.p, src.flags.p, src.pair_idx.p, src.aoff.p,
+                                          src.asc.p, src.doff.p, src.des.p);
+    DMSC_LAUNCHED(1);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+void mgraph_free(MGraphHost &h, cudaStream_t st) {
+  if (h.buf) cudaFreeAsync(h.buf, st);
+  h.buf = nullptr;
+}
+
+// Runs one tree level of merges; graphs[] is a device array of MGraph.
+cudaError_t merge_level(bool up, MGraphHost *hosts, int ngraphs, const int *jobs3, const int *ixn4, int njobs,
+                        uint32_t *status, cudaStream_t st) {
+  MGraph *dg = nullptr;
+  int3 *dj = nullptr;
+  CRect *dx = nullptr;
+  size_t bytes = sizeof(MGraph) * ngraphs + sizeof(int3) * njobs + sizeof(CRect) * njobs + 64;
+  char *buf = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&buf, bytes, st);
+  if (e != cudaSuccess) return e;
+  dg = (MGraph *)buf;
+  dj = (int3 *)(buf + sizeof(MGraph) * ngraphs);
+  dx = (CRect *)((char *)dj + sizeof(int3) * njobs);
+  // host images
+  MGraph *hg = new MGraph[ngraphs];
+  for (int i = 0; i < ngraphs; ++i) hg[i] = *reinterpret_cast<MGraph *>(hosts[i].raw);
+  e = cudaMemcpyAsync(dg, hg, sizeof(MGraph) * ngraphs, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dj, jobs3, sizeof(int3) * njobs, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dx, ixn4, sizeof(CRect) * njobs, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    if (up) k_merge_up<<<njobs, 32, 0, st>>>(dg, dj, dx, njobs, status);
+    else k_merge_down<<<njobs, 32, 0, st>>>(dg, dj, dx, njobs, status);
+    DMSC_LAUNCHED(1);
+    e = cudaGetLastError();
+  }
+  // bring back the counts and pool tops the kernels changed
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hg, dg, sizeof(MGraph) * ngraphs, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess)
+    for (int i = 0; i < ngraphs; ++i) *reinterpret_cast<MGraph *>(hosts[i].raw) = hg[i];
+  delete[] hg;
+  cudaFreeAsync(buf, st);
+  return e;
+}
+
+uint32_t mgraph_ncp(const MGraphHost &h) { return reinterpret_cast<const MGraph *>(h.raw)->G.ncp; }
+unsigned long long mgraph_pool_used(const MGraphHost &h) { return reinterpret_cast<const MGraph *>(h.raw)->G.L.top; }
+bool mgraph_failed(const MGraphHost &h) { return reinterpret_cast<const MGraph *>(h.raw)->G.fail; }
+void mgraph_set_rects(MGraphHost &h, const int rect[4], const int ext[4]) {
+  MGraph &m = *reinterpret_cast<MGraph *>(h.raw);
+  m.rect = CRect{rect[0], rect[1], rect[2], rect[3]};
+  m.ext = CRect{ext[0], ext[1], ext[2], ext[3]};
+}
+
+// Writes an MGraph back into a CSR complex (rect/ext are the caller's).
+cudaError_t mgraph_to_csr(const MGraphHost &h, dmsc_msc &out, cudaStream_t st) {
+  const MGraph &m = *reinterpret_cast<const MGraph *>(h.raw);
+  uint32_t n = m.G.ncp;
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = out.cellid.ensure(n + 1);
+  if (e == cudaSuccess) e = out.fn.ensure(n + 1);
+  if (e == cudaSuccess) e = out.pair_idx.ensure(n + 1);
+  if (e == cudaSuccess) e = out.flags.ensure(n + 1);
+  if (e == cudaSuccess) e = out.aoff.ensure(n + 1);
+  if (e == cudaSuccess) e = out.doff.ensure(n + 1);
+  if (e != cudaSuccess) return e;
+  out.ncp = n;
+  if (n) {
+    e = cudaMemcpyAsync(out.cellid.p, m.G.cellid, 4ull * n, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out.fn.p, m.fn, 4ull * n, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out.pair_idx.p, m.G.pair_idx, 4ull * n, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out.flags.p, m.G.flags, n, cudaMemcpyDeviceToDevice, st);
+  }
+  for (int w = 0; w < 2 && e == cudaSuccess; ++w) {
+    uint32_t *tot = nullptr;
+    e = cudaMallocAsync((void **)&tot, 4ull * (n + 1), st);
+    if (e != cudaSuccess) break;
+    uint32_t *off = w ? out.doff.p : out.aoff.p;
+    if (n) {
+      k_mg_totals<<<nblk(n), 256, 0, st>>>(m, w, tot);
+      DMSC_LAUNCHED(1);
+    }
+    e = scan_exclusive_u32(tot, n, off, off + n, st);
+    uint32_t total = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&total, off + n, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    DevBuf<uint32_t> &lb = w ? out.des : out.asc;
+    if (e == cudaSuccess) e = lb.ensure((size_t)total + 1);
+    if (e == cudaSuccess && n) {
+      k_mg_to_csr<<<nblk(n), 256, 0, st>>>(m, w, off, lb.p);
+      DMSC_LAUNCHED(1);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) (w ? out.ndes : out.nasc) = total;
+    cudaFreeAsync(tot, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e;
+}
+
+}  // namespace dmsc

@@ -21,6 +21,7 @@
 // operation budget or a pool runs out, leaving the complex unmodified.
 #include "dmsc_common.cuh"
 #include "dmsc_internal.h"
+#include "msc_graph.cuh"
 
 namespace dmsc {
 
@@ -39,49 +40,24 @@ __host__ __device__ __forceinline__ float fsub_rn(float a, float b) {
 #endif
 }
 
-// flags bits of a critical point (as exported by dmsc_msc_export)
-constexpr uint8_t F_CANCELLED = 1, F_STRANG = 2, F_BCANCEL = 4;
-
-// Multisets are run-length encoded: sorted (value, count) runs, so equal
-// elements stay consecutive exactly as std::multiset iterates them, and a
-// multiplicity of thousands costs one run.
-struct Lists {  // list 2*cp = asc, 2*cp+1 = des
-  uint32_t *off, *nrun, *cap;  // runs of list l live at pool[off[l] .. off[l]+nrun[l])
-  uint32_t *total;             // multiset size (sum of counts)
-  uint2 *pool;                 // .x = value, .y = count
-  unsigned long long top, pool_cap;
-};
-
 struct SimpArgs {
-  uint32_t ncp;
-  const uint32_t *cellid;
+  Graph G;            // the complex as a mutable graph (msc_graph.cuh)
   const float *fn;
-  uint8_t *flags;
-  uint32_t *pair_idx;
-  Lists L;
   HeapEnt *heap;
   unsigned long long heap_cap;
   uint2 *resub;       // resubmit list (capacity heap_cap)
   uint2 *canc;        // cancellation list (capacity ncp)
-  uint2 *tmp;         // new_edges (d, a) / uncancel runs (capacity tmp_cap)
-  unsigned long long tmp_cap;
   int rx0, ry0, rx1, ry1;  // m_rect of the complex (cell coordinates)
   double tresh;
-  unsigned long long max_ops;
   unsigned long long *stats;  // [0] pushes [1] pops [2] cancels [3] ops [4] status
 };
 
 struct Simp {
   SimpArgs A;
-  unsigned long long nheap = 0, nres = 0, ncanc = 0, ops = 0;
-  bool fail = false;
+  unsigned long long nheap = 0, nres = 0, ncanc = 0;
 
-  __host__ __device__ __forceinline__ int dim(uint32_t k) const {
-    uint32_t c = A.cellid[k];
-    return (int)(c & 1u) + (int)((c >> 16) & 1u);
-  }
   __host__ __device__ __forceinline__ bool on_boundary(uint32_t k) const {  // m_rect.isOnBoundry
-    uint32_t c = A.cellid[k];
+    uint32_t c = A.G.cellid[k];
     int x = (int16_t)(c & 0xffff), y = (int16_t)(c >> 16);
     bool contains = x >= A.rx0 && y >= A.ry0 && x <= A.rx1 && y <= A.ry1;
     bool interior = x > A.rx0 && y > A.ry0 && x < A.rx1 && y < A.ry1;
@@ -89,63 +65,6 @@ struct Simp {
   }
   __host__ __device__ __forceinline__ float pers(uint32_t a, uint32_t b) const {
     return fabsf(fsub_rn(A.fn[b], A.fn[a]));
-  }
-  __host__ __device__ __forceinline__ bool tick(unsigned long long n = 1) {
-    ops += n;
-    if (ops > A.max_ops) fail = true;
-    return !fail;
-  }
-
-  // ---- run-length multisets ----
-  __host__ __device__ __forceinline__ uint2 *runs(uint32_t l) const { return A.L.pool + A.L.off[l]; }
-  __host__ __device__ uint32_t find_run(uint32_t l, uint32_t x) const {  // first run with value >= x
-    const uint2 *p = runs(l);
-    uint32_t lo = 0, hi = A.L.nrun[l];
-    while (lo < hi) { uint32_t m = (lo + hi) >> 1; if (p[m].x < x) lo = m + 1; else hi = m; }
-    return lo;
-  }
-  __host__ __device__ uint32_t count(uint32_t l, uint32_t x) const {
-    uint32_t i = find_run(l, x);
-    return (i < A.L.nrun[l] && runs(l)[i].x == x) ? runs(l)[i].y : 0u;
-  }
-  __host__ __device__ bool contains(uint32_t l, uint32_t x) const { return count(l, x) != 0; }
-  __host__ __device__ bool reserve(uint32_t l, uint32_t need) {
-    if (need <= A.L.cap[l]) return true;
-    uint32_t nc = A.L.cap[l] * 2 + 4;
-    while (nc < need) nc *= 2;
-    if (A.L.top + nc > A.L.pool_cap) { fail = true; return false; }
-    uint2 *src = runs(l), *dst = A.L.pool + A.L.top;
-    for (uint32_t i = 0; i < A.L.nrun[l]; ++i) dst[i] = src[i];
-    A.L.off[l] = (uint32_t)A.L.top;
-    A.L.cap[l] = nc;
-    A.L.top += nc;
-    return true;
-  }
-  __host__ __device__ void insert(uint32_t l, uint32_t x, uint32_t c = 1) {  // std::multiset::insert, c times
-    uint32_t i = find_run(l, x), n = A.L.nrun[l];
-    if (i < n && runs(l)[i].x == x) {
-      uint2 &r = runs(l)[i];
-      if (r.y > 0xffffffffu - c) { fail = true; return; }
-      r.y += c;
-    } else {
-      if (!reserve(l, n + 1)) return;
-      uint2 *p = runs(l);
-      for (uint32_t k = n; k > i; --k) p[k] = p[k - 1];
-      p[i] = make_uint2(x, c);
-      A.L.nrun[l] = n + 1;
-      tick(n - i);
-    }
-    if (A.L.total[l] > 0xffffffffu - c) { fail = true; return; }
-    A.L.total[l] += c;
-  }
-  __host__ __device__ void erase(uint32_t l, uint32_t x) {  // std::multiset::erase(key): all copies
-    uint32_t i = find_run(l, x), n = A.L.nrun[l];
-    if (i >= n || runs(l)[i].x != x) return;
-    uint2 *p = runs(l);
-    A.L.total[l] -= p[i].y;
-    for (uint32_t k = i + 1; k < n; ++k) p[k - 1] = p[k];
-    A.L.nrun[l] = n - 1;
-    tick(n - i);
   }
 
   // ---- heap (binary heap of the standard library, comparator d1 > d2) ----
@@ -161,7 +80,7 @@ struct Simp {
     v[hole] = val;
   }
   __host__ __device__ void push(uint32_t a, uint32_t b) {
-    if (nheap >= A.heap_cap) { fail = true; return; }
+    if (nheap >= A.heap_cap) { A.G.fail = true; return; }
     HeapEnt x{pers(a, b), a, b};
     A.heap[nheap] = x;
     push_at(nheap, 0, x);
@@ -194,189 +113,77 @@ struct Simp {
     return top;
   }
 
-  // cancelPairs(msc, cp0, cp1, new_edges) (discreteMorseAlgorithm.h:466-585).
-  // The new edges (d, a) are pushed onto the heap in the reference's order:
-  // every occurrence of a (ascending) times every occurrence of d (ascending).
-  __host__ __device__ void cancel_pairs(uint32_t cp0, uint32_t cp1) {
-    if (!contains(2 * cp0, cp1)) { uint32_t t = cp0; cp0 = cp1; cp1 = t; }
-    if (!contains(2 * cp0, cp1)) return;  // "critical points are not connected"
-    const uint32_t la0 = 2 * cp0, ld1 = 2 * cp1 + 1;
-    // 1. connections: collect (d, a) runs first (the iterated lists do not change)
-    for (uint32_t i = 0; i < A.L.nrun[la0] && !fail; ++i) {
-      uint2 ra = runs(la0)[i];
-      if (ra.x == cp1) continue;
-      for (uint32_t j = 0; j < A.L.nrun[ld1] && !fail; ++j) {
-        uint2 rd = runs(ld1)[j];
-        if (rd.x == cp0) continue;
-        unsigned long long c = (unsigned long long)ra.y * rd.y;
-        if (c > 0xffffffffull) { fail = true; return; }
-        insert(2 * ra.x + 1, rd.x, (uint32_t)c);
-        insert(2 * rd.x, ra.x, (uint32_t)c);
-        if (count(2 * ra.x + 1, rd.x) >= 2) {
-          A.flags[ra.x] |= F_STRANG;
-          A.flags[rd.x] |= F_STRANG;
-        }
-        if (!tick(c)) return;
-      }
-    }
-    // 2. heap pushes of the new edges, in the reference's order
-    for (uint32_t i = 0; i < A.L.nrun[la0] && !fail; ++i) {
-      uint2 ra = runs(la0)[i];
-      if (ra.x == cp1) continue;
-      for (uint32_t ca = 0; ca < ra.y && !fail; ++ca)
-        for (uint32_t j = 0; j < A.L.nrun[ld1] && !fail; ++j) {
-          uint2 rd = runs(ld1)[j];
-          if (rd.x == cp0) continue;
-          for (uint32_t cd = 0; cd < rd.y && !fail; ++cd) push(rd.x, ra.x);
-        }
-    }
-    if (fail) return;
-    // 3. remove the pair from its neighbours
-    for (uint32_t i = 0; i < A.L.nrun[la0]; ++i) {
-      uint32_t a = runs(la0)[i].x;
-      if (a == cp1) continue;
-      erase(2 * a + 1, cp0);
-    }
-    for (uint32_t i = 0; i < A.L.nrun[2 * cp0 + 1]; ++i) erase(2 * runs(2 * cp0 + 1)[i].x, cp0);
-    for (uint32_t i = 0; i < A.L.nrun[2 * cp1]; ++i) erase(2 * runs(2 * cp1)[i].x + 1, cp1);
-    for (uint32_t i = 0; i < A.L.nrun[ld1]; ++i) {
-      uint32_t d = runs(ld1)[i].x;
-      if (d == cp0) continue;
-      erase(2 * d, cp1);
-    }
-    A.flags[cp0] |= F_CANCELLED;
-    A.L.nrun[2 * cp0 + 1] = 0; A.L.total[2 * cp0 + 1] = 0;
-    A.flags[cp1] |= F_CANCELLED;
-    A.L.nrun[2 * cp1] = 0; A.L.total[2 * cp1] = 0;
-  }
-
-  // heap sort of tmp[0..n) by value (in place, O(n log n))
-  __host__ __device__ void sort_runs(unsigned long long n) {
-    uint2 *t = A.tmp;
-    auto sift = [&](unsigned long long root, unsigned long long end) {
-      while (2 * root + 1 < end) {
-        unsigned long long c = 2 * root + 1;
-        if (c + 1 < end && t[c].x < t[c + 1].x) ++c;
-        if (t[root].x < t[c].x) { uint2 q = t[root]; t[root] = t[c]; t[c] = q; root = c; }
-        else return;
-      }
-    };
-    for (unsigned long long s = n / 2; s-- > 0;) sift(s, n);
-    for (unsigned long long e = n; e-- > 1;) { uint2 q = t[0]; t[0] = t[e]; t[e] = q; sift(0, e); }
-  }
-
-  // uncancel_pairs(msc, cp1, cp2) (discreteMorseAlgorithm.h:1006-1089).
-  // Returns false on a reference logic_error condition.
-  __host__ __device__ bool uncancel_pairs(uint32_t c1, uint32_t c2) {
-    if (!contains(2 * c1, c2)) { uint32_t t = c1; c1 = c2; c2 = t; }
-    const uint32_t lists[2] = {2 * c1, 2 * c2 + 1};
-    const uint32_t ids[2] = {c1, c2};
-    for (int i = 0; i < 2; ++i) {
-      uint32_t l = lists[i], other = ids[(i + 1) % 2];
-      if (!contains(l, other)) return false;  // "cancellable pair is not connected"
-      unsigned long long n = 0;
-      for (uint32_t k = 0; k < A.L.nrun[l]; ++k) {
-        uint2 rx = runs(l)[k];
-        if (rx.x == other) continue;
-        if (!(A.flags[rx.x] & F_BCANCEL)) {
-          if (n >= A.tmp_cap) { fail = true; return true; }
-          A.tmp[n++] = rx;
-          continue;
-        }
-        if (A.flags[rx.x] & F_CANCELLED) return false;
-        uint32_t pidx = A.pair_idx[rx.x];
-        if (pidx >= A.ncp || A.pair_idx[pidx] != rx.x) return false;
-        uint32_t pl = 2 * pidx + i;
-        for (uint32_t q = 0; q < A.L.nrun[pl]; ++q) {
-          uint2 ry = runs(pl)[q];
-          if (A.flags[ry.x] & F_BCANCEL) return false;
-          unsigned long long c = (unsigned long long)rx.y * ry.y;
-          if (c > 0xffffffffull || n >= A.tmp_cap) { fail = true; return true; }
-          A.tmp[n++] = make_uint2(ry.x, (uint32_t)c);
-        }
-        if (!tick(1 + A.L.nrun[pl])) return true;
-      }
-      if (!tick(n + 1)) return true;
-      sort_runs(n);
-      // merge equal values into runs
-      unsigned long long m = 0, tot = 0;
-      for (unsigned long long u = 0; u < n; ++u) {
-        if (m > 0 && A.tmp[m - 1].x == A.tmp[u].x) {
-          unsigned long long c = (unsigned long long)A.tmp[m - 1].y + A.tmp[u].y;
-          if (c > 0xffffffffull) { fail = true; return true; }
-          A.tmp[m - 1].y = (uint32_t)c;
-        } else {
-          A.tmp[m++] = A.tmp[u];
-        }
-        tot += A.tmp[u].y;
-      }
-      if (tot > 0xffffffffull || m > 0xffffffffull || !reserve(l, (uint32_t)m)) { fail = true; return true; }
-      uint2 *p = runs(l);
-      for (unsigned long long u = 0; u < m; ++u) p[u] = A.tmp[u];
-      A.L.nrun[l] = (uint32_t)m;
-      A.L.total[l] = (uint32_t)tot;
-    }
-    A.flags[c1] &= ~F_CANCELLED;
-    A.flags[c2] &= ~F_CANCELLED;
-    return true;
-  }
-
   // simplify (grid_mscomplex.cpp:384-512) followed by un_simplify (:514-526)
   __host__ __device__ void run() {
-    const uint32_t n = A.ncp;
+    Graph &G = A.G;
+    const uint32_t n = G.ncp;
     float max_val = 1.17549435e-38f;  // std::numeric_limits<float>::min(), as in the reference (:399)
     float min_val = 3.40282347e+38f;
-    for (uint32_t i = 0; i < n && !fail; ++i) {
-      if (dim(i) == 1) {
+    for (uint32_t i = 0; i < n && !G.fail; ++i) {
+      if (G.dim(i) == 1) {
         for (int j = 0; j < 2; ++j) {
           uint32_t l = 2 * i + j;
-          if (A.L.total[l] != 2) continue;
-          if (runs(l)[0].y == 2) A.flags[i] |= F_STRANG;  // both elements equal
+          if (G.L.total[l] != 2) continue;
+          if (G.runs(l)[0].y == 2) G.flags[i] |= F_STRANG;  // both elements equal
         }
       }
       float f = A.fn[i];
       max_val = (max_val < f) ? f : max_val;  // std::max
       min_val = (f < min_val) ? f : min_val;  // std::min
       const uint32_t ld = 2 * i + 1;
-      for (uint32_t k = 0; k < A.L.nrun[ld] && !fail; ++k)
-        for (uint32_t c = 0; c < runs(ld)[k].y && !fail; ++c) push(i, runs(ld)[k].x);
+      for (uint32_t k = 0; k < G.L.nrun[ld] && !G.fail; ++k)
+        for (uint32_t c = 0; c < G.runs(ld)[k].y && !G.fail; ++c) push(i, G.runs(ld)[k].x);
     }
     const float max_persistence = fsub_rn(max_val, min_val);
-    while (nheap != 0 && !fail) {
-      if (!tick()) break;
+    while (nheap != 0 && !G.fail) {
+      if (!G.tick()) break;
       HeapEnt e = pop();
       uint32_t v1 = e.a, v2 = e.b;
       if ((double)e.d / (double)max_persistence > A.tresh) break;
-      if (dim(v2) == 1) { uint32_t t = v1; v1 = v2; v2 = t; }
-      const int cp2_dim = dim(v2);
-      if ((A.flags[v1] & F_CANCELLED) || (A.flags[v2] & F_CANCELLED)) continue;
+      if (G.dim(v2) == 1) { uint32_t t = v1; v1 = v2; v2 = t; }
+      const int cp2_dim = G.dim(v2);
+      if ((G.flags[v1] & F_CANCELLED) || (G.flags[v2] & F_CANCELLED)) continue;
       bool b1 = on_boundary(v1), b2 = on_boundary(v2);
       if (b1 && !b2) continue;
       if (!b1 && b2) continue;
-      const bool strang = A.flags[v1] & F_STRANG;
-      if (strang && A.L.total[2 * v2 + cp2_dim / 2] != 1) {
-        if (nres >= A.heap_cap) { fail = true; break; }
+      const bool strang = G.flags[v1] & F_STRANG;
+      if (strang && G.L.total[2 * v2 + cp2_dim / 2] != 1) {
+        if (nres >= A.heap_cap) { G.fail = true; break; }
         A.resub[nres++] = make_uint2(e.a, e.b);
         continue;
       }
       if (strang && b1) continue;
-      cancel_pairs(v1, v2);
-      if (fail) break;
-      A.flags[v1] |= F_BCANCEL;
-      A.flags[v2] |= F_BCANCEL;
-      A.pair_idx[v1] = v2;
-      A.pair_idx[v2] = v1;
-      if (ncanc >= n) { fail = true; break; }
+      uint32_t cp0 = v1, cp1 = v2;
+      bool connected = G.cancel_pairs(cp0, cp1);
+      if (G.fail) break;
+      G.flags[v1] |= F_BCANCEL;
+      G.flags[v2] |= F_BCANCEL;
+      G.pair_idx[v1] = v2;
+      G.pair_idx[v2] = v1;
+      if (ncanc >= n) { G.fail = true; break; }
       A.canc[ncanc++] = make_uint2(e.a, e.b);
-      for (unsigned long long i = 0; i < nres && !fail; ++i) push(A.resub[i].x, A.resub[i].y);
+      if (connected) {  // new edges (d, a) in the reference's order
+        const uint32_t la0 = 2 * cp0, ld1 = 2 * cp1 + 1;
+        for (uint32_t i = 0; i < G.L.nrun[la0] && !G.fail; ++i) {
+          uint2 ra = G.runs(la0)[i];
+          if (ra.x == cp1) continue;
+          for (uint32_t ca = 0; ca < ra.y && !G.fail; ++ca)
+            for (uint32_t j = 0; j < G.L.nrun[ld1] && !G.fail; ++j) {
+              uint2 rd = G.runs(ld1)[j];
+              if (rd.x == cp0) continue;
+              for (uint32_t cd = 0; cd < rd.y && !G.fail; ++cd) push(rd.x, ra.x);
+            }
+        }
+      }
+      for (unsigned long long i = 0; i < nres && !G.fail; ++i) push(A.resub[i].x, A.resub[i].y);
       nres = 0;
     }
     A.stats[2] = ncanc;
-    if (fail) return;
+    if (G.fail) return;
     for (unsigned long long k = ncanc; k-- > 0;) {
       uint2 c = A.canc[k];
-      if (!uncancel_pairs(c.x, c.y)) { A.stats[4] |= ST_INVARIANT; return; }
-      if (fail) return;
+      if (!G.uncancel_pairs(c.x, c.y)) { A.stats[4] |= ST_INVARIANT; return; }
+      if (G.fail) return;
     }
   }
 };
@@ -386,8 +193,8 @@ __global__ void k_simplify(SimpArgs a) {
   Simp s;
   s.A = a;
   s.run();
-  a.stats[3] = s.ops;
-  if (s.fail) a.stats[4] |= ST_SIMPLIFY_LIMIT;
+  a.stats[3] = s.A.G.ops;
+  if (s.A.G.fail) a.stats[4] |= ST_SIMPLIFY_LIMIT;
 }
 
 // CSR (expanded, ascending) -> run-length lists.  Capacity of a list is its
@@ -462,38 +269,41 @@ cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st) {
   int si = 0;
   auto take = [&]() { char *r = p; p += rnd(sizes[si++]); return r; };
   SimpArgs &a = w->a;
-  a.ncp = ncp;
-  a.cellid = io.cellid;
+  Graph &G = a.G;
+  G.ncp = ncp;
+  G.cellid = const_cast<uint32_t *>(io.cellid);
   a.fn = io.fn;
-  a.L.off = (uint32_t *)take();
-  a.L.nrun = (uint32_t *)take();
-  a.L.cap = (uint32_t *)take();
-  a.L.total = (uint32_t *)take();
-  a.L.pool = (uint2 *)take();
-  a.L.top = base_top;
-  a.L.pool_cap = pool_cap;
-  a.tmp = (uint2 *)take();
-  a.tmp_cap = tmp_cap;
+  G.L.off = (uint32_t *)take();
+  G.L.nrun = (uint32_t *)take();
+  G.L.cap = (uint32_t *)take();
+  G.L.total = (uint32_t *)take();
+  G.L.pool = (uint2 *)take();
+  G.L.top = base_top;
+  G.L.pool_cap = pool_cap;
+  G.tmp = (uint2 *)take();
+  G.tmp_cap = tmp_cap;
   a.heap = (HeapEnt *)take();
   a.heap_cap = heap_cap;
   a.resub = (uint2 *)take();
   a.canc = (uint2 *)take();
   a.stats = (unsigned long long *)take();
-  a.flags = (uint8_t *)take();
-  a.pair_idx = (uint32_t *)take();
+  G.flags = (uint8_t *)take();
+  G.pair_idx = (uint32_t *)take();
   w->lens = (uint32_t *)take();
   w->flags_in = io.flags;
   w->pair_in = io.pair_idx;
   a.rx0 = io.rect[0]; a.ry0 = io.rect[1]; a.rx1 = io.rect[2]; a.ry1 = io.rect[3];
   a.tresh = io.tresh;
-  a.max_ops = io.max_ops;
+  G.max_ops = io.max_ops;
+  G.ops = 0;
+  G.fail = false;
   e = cudaMemsetAsync(a.stats, 0, sizeof(unsigned long long) * 8, st);
-  if (e == cudaSuccess && ncp) e = cudaMemcpyAsync(a.flags, io.flags, ncp, cudaMemcpyDeviceToDevice, st);
-  if (e == cudaSuccess && ncp) e = cudaMemcpyAsync(a.pair_idx, io.pair_idx, 4ull * ncp, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess && ncp) e = cudaMemcpyAsync(G.flags, io.flags, ncp, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess && ncp) e = cudaMemcpyAsync(G.pair_idx, io.pair_idx, 4ull * ncp, cudaMemcpyDeviceToDevice, st);
   if (e != cudaSuccess) return e;
   if (ncp) {
-    k_lists_from_csr<<<blocks_for(ncp), 256, 0, st>>>(ncp, io.aoff, io.asc, io.doff, io.des, des_base, a.L.off,
-                                                       a.L.nrun, a.L.cap, a.L.total, a.L.pool);
+    k_lists_from_csr<<<blocks_for(ncp), 256, 0, st>>>(ncp, io.aoff, io.asc, io.doff, io.des, des_base, G.L.off,
+                                                       G.L.nrun, G.L.cap, G.L.total, G.L.pool);
     DMSC_LAUNCHED(1);
     k_simplify<<<1, 32, 0, st>>>(a);
     DMSC_LAUNCHED(1);
@@ -504,7 +314,7 @@ cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st) {
   // new CSR offsets (asc, then des) from the list lengths
   for (int which = 0; which < 2 && e == cudaSuccess; ++which) {
     uint32_t *offs = which ? io.doff : io.aoff;
-    k_pick_len<<<blocks_for(ncp), 256, 0, st>>>(ncp, a.L.total, which, w->lens);
+    k_pick_len<<<blocks_for(ncp), 256, 0, st>>>(ncp, G.L.total, which, w->lens);
     DMSC_LAUNCHED(1);
     e = scan_exclusive_u32(w->lens, ncp, offs, offs + ncp, st);
   }
@@ -521,12 +331,12 @@ cudaError_t simplify_emit(SimplifyIO &io, uint32_t *asc, uint32_t *des, cudaStre
   SimplifyWork *w = (SimplifyWork *)io.work;
   const uint32_t ncp = (uint32_t)io.ncp;
   if (!w || !ncp) return cudaSuccess;
-  k_csr_from_lists<<<blocks_for(ncp), 256, 0, st>>>(ncp, w->a.L.off, w->a.L.nrun, w->a.L.pool, 0, io.aoff, asc);
+  k_csr_from_lists<<<blocks_for(ncp), 256, 0, st>>>(ncp, w->a.G.L.off, w->a.G.L.nrun, w->a.G.L.pool, 0, io.aoff, asc);
   DMSC_LAUNCHED(1);
-  k_csr_from_lists<<<blocks_for(ncp), 256, 0, st>>>(ncp, w->a.L.off, w->a.L.nrun, w->a.L.pool, 1, io.doff, des);
+  k_csr_from_lists<<<blocks_for(ncp), 256, 0, st>>>(ncp, w->a.G.L.off, w->a.G.L.nrun, w->a.G.L.pool, 1, io.doff, des);
   DMSC_LAUNCHED(1);
-  cudaError_t e = cudaMemcpyAsync(w->flags_in, w->a.flags, ncp, cudaMemcpyDeviceToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(w->pair_in, w->a.pair_idx, 4ull * ncp, cudaMemcpyDeviceToDevice, st);
+  cudaError_t e = cudaMemcpyAsync(w->flags_in, w->a.G.flags, ncp, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(w->pair_in, w->a.G.pair_idx, 4ull * ncp, cudaMemcpyDeviceToDevice, st);
   if (e == cudaSuccess) e = cudaGetLastError();
   return e;
 }

@@ -147,15 +147,16 @@ class GridDataset:
 class GridMSComplex:
     """A Morse-Smale complex held on the device (handle to dmsc_msc)."""
 
-    def __init__(self, handle, ctx: Context):
+    def __init__(self, handle, ctx: Context, owner=None):
         self.h = handle
         self.ctx = ctx
         self.lib = ctx.lib
+        self._owner = owner  # a Pipeline owns its pieces' complexes
 
     def __del__(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and self._owner is None:
             self.lib.dmsc_msc_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def simplify_un_simplify(self, tresh: float, max_ops: int = 0, stream=None) -> dict:
         """GridMSComplex::simplify_un_simplify: persistence cancellation at
@@ -195,3 +196,61 @@ class GridMSComplex:
                 "adisc_off", "adisc", "ddisc_off", "ddisc")
         check(self.lib.dmsc_msc_export(self.h, *(_ptr(d[k]) for k in keys), None))
         return d
+
+
+class GridDataManager:
+    """The piece pipeline of GridDataManager (dmsc/src/grid_datamanager.cpp):
+    the grid split `levels` times into pieces, one complex per piece, merge up
+    to the root, simplify_un_simplify(tresh) there, merge down, and the
+    manifold discs of every piece.  heights: (size_y, size_x) float32 numpy
+    array (copied to the device) or CUDA tensor (read in place)."""
+
+    STAGES = ("pieces", "merge_up", "simplify", "merge_down", "discs")
+
+    def __init__(self, heights, levels: int = 0, tresh: float = 0.0, split2d: bool = False,
+                 ctx: Context | None = None, stream=None):
+        self.ctx = ctx or default_context()
+        self.lib = self.ctx.lib
+        h = C.c_void_p()
+        if hasattr(heights, "is_cuda") and heights.is_cuda:
+            t = heights
+            if t.dtype.__repr__() != "torch.float32" or t.dim() != 2 or t.stride(1) != 1:
+                raise ValueError("device heights must be a 2D float32 tensor with unit x stride")
+            ny, nx = int(t.shape[0]), int(t.shape[1])
+            self._keep = t
+            rc = self.lib.dmsc_pipeline_run(self.ctx.h, C.c_void_p(t.data_ptr()), t.stride(0), 1, nx, ny,
+                                            int(levels), float(tresh), int(bool(split2d)), C.byref(h), stream)
+        else:
+            a = np.ascontiguousarray(heights, dtype=np.float32)
+            if a.ndim != 2:
+                raise ValueError("heights must be 2D (size_y, size_x)")
+            ny, nx = a.shape
+            self._keep = a
+            rc = self.lib.dmsc_pipeline_run(self.ctx.h, _ptr(a), nx, 0, nx, ny, int(levels), float(tresh),
+                                            int(bool(split2d)), C.byref(h), stream)
+        check(rc)
+        self.h = h
+        n = C.c_int64()
+        check(self.lib.dmsc_pipeline_num_pieces(self.h, C.byref(n)))
+        self.num_pieces = n.value
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.dmsc_pipeline_destroy(self.h)
+            self.h = None
+
+    def piece(self, i: int) -> GridMSComplex:
+        """Node i of the piece tree after merge_down: leaves first (with
+        discs), then the merges, the root last (2 * num_pieces - 2)."""
+        m = C.c_void_p()
+        check(self.lib.dmsc_pipeline_piece(self.h, int(i), C.byref(m), None))
+        return GridMSComplex(m, self.ctx, owner=self)
+
+    def write_discs(self, prefix: str):
+        """collectSubdomainManifolds: write_discs of every piece in leaf order."""
+        check(self.lib.dmsc_pipeline_write_discs(self.h, prefix.encode()))
+
+    def stage_times(self) -> dict:
+        ms = np.zeros(5, np.float64)
+        check(self.lib.dmsc_pipeline_stage_times(self.h, _ptr(ms)))
+        return dict(zip(self.STAGES, (float(v) for v in ms)))
