@@ -1,14 +1,24 @@
 """Benchmark of the GB300 grid Morse-Smale path (one JSON line on rank 0).
 
 Workload: the 4096x4096 float32 field of 512 Gaussian bumps quantised to
-1/256 of its range (seed 1).  A step is one pass of the device pipeline over
-that grid.  ``value`` is Mvertices/s with the heights already in HBM; ``e2e``
-is the same metric through the public API with host (pinned) heights copied
-in and the complex copied out every step.  ``--impl reference`` times the CPU
-restatement of the reference path (the oracle) on the host cores instead.
+1/256 of its range (seed 1).  A step is one pass of the device path over that
+grid: gradient, critical-cell collation, owner labels, connectivity (the
+complex) and the ascending/descending manifold discs of every critical point.
+``value`` is Mvertices/s with the heights already in HBM; ``e2e`` is the same
+step through the public API with host (pinned) heights copied in and the
+complex with its discs copied out every step.
 
-Multi-GPU: the path does not shard (replicas only): every rank processes its
-own grid, value = all vertices processed / max-over-ranks time.
+Persistence cancellation at 1% of the range is not inside the timed step: on
+this field the reference's tie order (its heap) needs ~5.9e9 dependent heap
+operations, which the device replays exactly but sequentially.  It is
+measured beside the step ("simplify": device replay operations per second
+under an operation budget, and the whole-field estimate from the operation
+count).
+
+``--impl reference`` times the CPU restatement of the reference path (the
+oracle) on the host cores instead.  Multi-GPU: the path does not shard
+(replicas only): every rank processes its own grid, value = all vertices
+processed / max-over-ranks time.
 """
 from __future__ import annotations
 
@@ -28,11 +38,48 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Mvert/s at 4096^2 (% HBM roofline)"
 WORKLOAD = ("bumps4096q: 4096x4096 float32, 512 Gaussian bumps (sigma U(4,64)) quantised to 1/256 of the range, "
-            "seed 1; device pipeline: gradient, critical-cell collation, owner labels, connectivity")
-STAGE_BYTES = {  # algorithmic bytes per vertex of each stage
-    "gradient": 8.0,        # 4 B height read + 4 B gradient codes written
-    "labels_arcs": 20.0,    # 4 B gradient codes read + 16 B owner labels written (+12 B/cp, 8 B/arc)
+            "seed 1; step = gradient, critical-cell collation, owner labels, connectivity, manifold discs; "
+            "persistence cancellation at 1% measured separately (see simplify)")
+SIMPLIFY_TRESH = 0.01
+# heap pushes + pops of the reference's simplification of this field at 1%,
+# counted by the oracle (2.956808816e9 pushes, 2.954259461e9 pops)
+SIMPLIFY_HEAP_OPS = 2956808816 + 2954259461
+# Algorithmic bytes of each stage: (per vertex, per critical point, per arc, per disc cell).
+STAGE_BYTES = {
+    "gradient": (8.0, 0, 0, 0),        # 4 B height read + 4 B gradient codes written
+    "labels_arcs": (20.0, 12, 8, 0),   # 4 B codes read + 16 B owner labels written; cp records and arcs
+    "connectivity": (0, 24, 16, 0),    # cp records read/written, arcs sorted into CSR (read + write)
+    "discs": (20.0, 8, 0, 4),          # codes + owner labels read, 4 B per disc cell written
 }
+
+
+def stage_bytes(stage, nverts, ncp, narcs, ndisc):
+    v, c, a, d = STAGE_BYTES.get(stage, (0, 0, 0, 0))
+    return v * nverts + c * ncp + a * narcs + d * ndisc
+
+
+def simplify_rate(M, ds, stream, sh, torch, budget=20_000_000):
+    """Runs the exact device replay of simplify_un_simplify at 1% on a fresh
+    complex of the field until `budget` operations, and reports its rate."""
+    m = ds.writeout_connectivity(stream=sh)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    try:
+        m.simplify_un_simplify(SIMPLIFY_TRESH, max_ops=budget, stream=sh)
+        done = True
+    except M.DmscError:
+        done = False
+    e1.record(stream)
+    e1.synchronize()
+    st = m.simplify_stats()
+    ms = e0.elapsed_time(e1)
+    heap_ops = st["pops"] + st["pushes"]
+    rate = heap_ops / (ms / 1e3) if ms > 0 else None
+    return {"threshold": SIMPLIFY_TRESH, "completed": done, "budget_ops": budget, "ops": st["ops"],
+            "pops": st["pops"], "pushes": st["pushes"], "cancellations": st["cancels"], "ms": round(ms, 3),
+            "heap_ops_per_s": round(rate, 1) if rate else None, "field_heap_ops": SIMPLIFY_HEAP_OPS,
+            "field_est_s": round(SIMPLIFY_HEAP_OPS / rate, 1) if rate else None}
 
 
 def peaks():
@@ -106,19 +153,25 @@ def cpu_sample_field(field: np.ndarray, n: int) -> np.ndarray:
     return np.ascontiguousarray(field[:n, :n])
 
 
+def oracle_step(win: np.ndarray) -> float:
+    """One step of the oracle on a window: init, work, writeout_connectivity and
+    postMergeFillDiscs (the stages of the device step); returns seconds."""
+    from oracle import oracle as O
+    r = (0, 0, 2 * (win.shape[1] - 1), 2 * (win.shape[0] - 1))
+    t0 = time.perf_counter()
+    O.Dataset(win, r, r, tresh=0.0, fill_discs=True)
+    return time.perf_counter() - t0
+
+
 def cpu_baseline(field: np.ndarray, side: int = 1024):
-    """The oracle (single thread) on a window of the same field, stages matching the device pipeline."""
+    """The oracle (single thread) on a window of the same field, same stages as the device step."""
     from oracle import oracle as O
     O.build()
     win = cpu_sample_field(field, side)
-    t0 = time.perf_counter()
-    P = O.Pipeline(win, levels=0, tresh=0.0)
-    wall = time.perf_counter() - t0
-    t = P.times_ms()
-    secs = t["build"] / 1e3
+    secs = oracle_step(win)
     return {"value": round(win.size / secs / 1e6, 3), "unit": "Mvert/s", "cores": 1, "kind": "port",
-            "sample": f"{side}x{side} window of the same field, oracle stages work+writeout_connectivity "
-                      f"({secs:.2f} s; whole oracle run {wall:.2f} s)"}
+            "sample": f"{side}x{side} window of the same field, one oracle step (work, writeout_connectivity, "
+                      f"postMergeFillDiscs) in {secs:.2f} s"}
 
 
 def run_reference(args):
@@ -136,13 +189,19 @@ def run_reference(args):
     nwin = (field.shape[0] // side) * (field.shape[1] // side)
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
+    nx = field.shape[1] // side
+
+    def window(i):
+        y0, x0 = (i // nx) * side, (i % nx) * side
+        return np.ascontiguousarray(field[y0:y0 + side, x0:x0 + side])
+
     with ctx.Pool(cores, initializer=_ref_init) as pool:
         for _ in range(args.warmup):
-            pool.map(_ref_job, [(field, side, i % nwin) for i in range(cores)])
+            pool.map(_ref_job, [window(i % nwin) for i in range(cores)])
         t0 = time.perf_counter()
         verts = 0
         for s in range(args.steps):
-            res = pool.map(_ref_job, [(field, side, (s * cores + i) % nwin) for i in range(cores)])
+            res = pool.map(_ref_job, [window((s * cores + i) % nwin) for i in range(cores)])
             verts += sum(res)
         dt = time.perf_counter() - t0
     value = verts / dt / 1e6
@@ -151,7 +210,7 @@ def run_reference(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
             "config": {"workload": WORKLOAD, "sample": f"{cores} windows of {side}x{side} per step"},
             "cpu_baseline": {"value": round(value, 3), "unit": "Mvert/s", "cores": cores, "kind": "port",
-                             "sample": f"{cores} processes, each the oracle (work+writeout_connectivity+discs) on a "
+                             "sample": f"{cores} processes, each one oracle step (work, writeout_connectivity, postMergeFillDiscs) on a "
                                        f"{side}x{side} window of the field"},
             "e2e": {"value": round(value, 3), "unit": "Mvert/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -161,13 +220,8 @@ def _ref_init():
     sys.path.insert(0, ROOT)
 
 
-def _ref_job(a):
-    field, side, i = a
-    from oracle import oracle as O
-    nx = field.shape[1] // side
-    y0, x0 = (i // nx) * side, (i % nx) * side
-    win = np.ascontiguousarray(field[y0:y0 + side, x0:x0 + side])
-    O.Pipeline(win, levels=0, tresh=0.0)
+def _ref_job(win):
+    oracle_step(win)
     return win.size
 
 
@@ -210,15 +264,21 @@ def main():
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
 
+    disc_ev = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)]
+
     def step():
         ds.init(dev, stream=sh)
         ds.work(stream=sh)
-        return ds.writeout_connectivity(stream=sh)
+        m = ds.writeout_connectivity(stream=sh)
+        disc_ev[0].record(stream)
+        ds.post_merge_fill_discs(m, stream=sh)
+        disc_ev[1].record(stream)
+        return m
 
     for _ in range(max(3, args.warmup)):
         msc = step()
     torch.cuda.synchronize()
-    ncp, nasc, ndes = msc.sizes()[:3]
+    ncp, nasc, ndes, nadisc, nddisc = msc.sizes()
 
     # ---- device-resident timed region ----
     clocks = ClockSampler(local)
@@ -226,7 +286,7 @@ def main():
     barrier()
     torch.cuda.synchronize()
     launches0 = kernel_launches()
-    times, stages = [], {k: [] for k in M.GridDataset.STAGES}
+    times, stages = [], {k: [] for k in M.GridDataset.STAGES + ("discs",)}
     for _ in range(args.steps):
         flush.fill_(1.0)  # evict L2 between steps (outside the timed interval)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -237,6 +297,7 @@ def main():
         times.append(e0.elapsed_time(e1))
         for k, v in ds.stage_times().items():
             stages[k].append(v)
+        stages["discs"].append(disc_ev[0].elapsed_time(disc_ev[1]))
     torch.cuda.synchronize()
     launches = kernel_launches() - launches0
     barrier()
@@ -251,15 +312,17 @@ def main():
     # roofline of the dominant kernel (median stage time, live CUDA events)
     med = {k: statistics.median(v) for k, v in stages.items()}
     dom = max(STAGE_BYTES, key=lambda k: med[k])
-    extra = 12.0 * ncp + 8.0 * (nasc + ndes) if dom == "labels_arcs" else 0.0
-    alg_bytes = STAGE_BYTES[dom] * nverts + extra
+    alg_bytes = stage_bytes(dom, nverts, ncp, nasc + ndes, nadisc + nddisc)
     peak, peak_kind = peaks()
     achieved = alg_bytes / (med[dom] / 1e3) / 1e9
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         traffic = json.load(open(tp)).get(f"{dom}:bumps4096q")
-    pipe_bytes = 24.0 * nverts + 12.0 * ncp + 8.0 * (nasc + ndes)
+    pipe_bytes = sum(stage_bytes(k, nverts, ncp, nasc + ndes, nadisc + nddisc) for k in STAGE_BYTES)
+
+    # ---- persistence cancellation at 1%: device replay rate under an operation budget ----
+    simp = simplify_rate(M, ds, stream, sh, torch)
 
     # ---- end to end through the public API (pinned host heights in, complex out) ----
     host = torch.from_numpy(field).pin_memory()
@@ -274,7 +337,9 @@ def main():
         d = host.to("cuda", non_blocking=True)
         ds.init(d, stream=sh)
         ds.work(stream=sh)
-        out = ds.writeout_connectivity(stream=sh).export()
+        m = ds.writeout_connectivity(stream=sh)
+        ds.post_merge_fill_discs(m, stream=sh)
+        out = m.export()
         e2e_times.append(time.perf_counter() - s0)
         d2h = sum(v.nbytes for v in out.values())
     e2e_total = sum(e2e_times)
@@ -291,7 +356,9 @@ def main():
             "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "grid": [nx, ny], "levels": 0, "critical_points": ncp,
-                       "arcs": [nasc, ndes], "l2": "flushed between steps (256 MB write)",
+                       "arcs": [nasc, ndes], "disc_cells": [nadisc, nddisc],
+                       "simplification": "excluded from the step; measured in simplify",
+                       "l2": "flushed between steps (256 MB write)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "stages_ms": {k: round(v, 4) for k, v in med.items()},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
@@ -299,6 +366,7 @@ def main():
                          "alg_bytes_per_launch": int(alg_bytes), "traffic": traffic},
             "pipeline_roofline": {"alg_bytes": int(pipe_bytes),
                                   "frac": round(pipe_bytes / (total_ms / args.steps / 1e3) / 1e9 / peak, 4)},
+            "simplify": simp,
             "e2e": {"value": round(e2e_value, 3), "unit": "Mvert/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),

@@ -29,8 +29,8 @@ def smooth_field(ny: int, nx: int, seed: int) -> np.ndarray:
     return f.astype(np.float32)
 
 
-def assert_same_complex(got: dict, want: dict, what: str = "complex"):
-    for k in COMPLEX_KEYS:
+def assert_same_complex(got: dict, want: dict, what: str = "complex", keys=None):
+    for k in keys or COMPLEX_KEYS:
         a, b = np.asarray(got[k]), np.asarray(want[k])
         if k == "fn":
             a, b = a.view(np.uint32), b.view(np.uint32)  # bit-exact float compare

@@ -23,7 +23,7 @@ def check_pipeline(M, oracle, f, levels, tresh, split2d, what):
         if i < N:
             assert_same_complex(g, w, f"{what} leaf {i}")
         else:
-            assert_same_complex({k: g[k] for k in GRAPH_KEYS}, {k: w[k] for k in GRAPH_KEYS}, f"{what} node {i}")
+            assert_same_complex(g, w, f"{what} node {i}", keys=GRAPH_KEYS)
             assert len(g["adisc"]) == 0 and len(g["ddisc"]) == 0
     return got, want
 
