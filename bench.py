@@ -261,7 +261,10 @@ def main():
     dev = torch.from_numpy(field).cuda()
     ds = M.GridDataset(rect, rect, ctx=ctx)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > L2 (129 MB)
-    stream = torch.cuda.current_stream()
+    # one non-default stream for everything: the library's kernels, the L2
+    # flush, host copies and the timing events are ordered on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
 
     disc_ev = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)]

@@ -12,8 +12,11 @@
  *  - Cell ids are (x, y) pairs of int16 in the reference's refined-grid
  *    coordinates: vertex (i, j) is cell (2i, 2j), cell dimension is
  *    (x & 1) + (y & 1).  A rect is {left, bottom, right, top} in cell coords.
- *  - `stream` is a cudaStream_t (NULL = the context's own stream).  Export
- *    functions write HOST buffers and return after the copy completes.
+ *  - `stream` is a cudaStream_t (NULL = the context's own stream, which is
+ *    created non-blocking: it does not order with the legacy default
+ *    stream, so a caller that produced device inputs on another stream
+ *    passes that stream or synchronises first).  Export functions write
+ *    HOST buffers and return after the copy completes.
  *  - Inputs containing NaN are outside the supported domain (the reference's
  *    vertex comparison is not a strict weak order on NaN) and are rejected
  *    with DMSC_ERR_INPUT.

@@ -192,11 +192,13 @@ __device__ __forceinline__ void for_seeds(const DiscArgs &a, int kind, uint32_t 
   for (; k < cnt; ++k) f(a.cellid[a.pair_idx[sr.val[st + k]]]);
 }
 
-// pass 1: disc lengths.  Every non-critical path cell has at most one
-// successor, so each seed expands into at most two chains.
-__global__ void k_saddle_disc_count(DiscArgs a, int kind, SeedRuns sr, uint32_t *len, unsigned long long limit) {
+// Serial pass for saddles with more than KMAX chains.  1: disc lengths (every
+// non-critical path cell has at most one successor, so each seed expands into
+// at most two chains).
+__global__ void k_saddle_disc_count(DiscArgs a, int kind, SeedRuns sr, const uint8_t *big, uint32_t *len,
+                                    unsigned long long limit) {
   for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < a.ncp; s += gridDim.x * blockDim.x) {
-    if ((a.flags[s] & F_BCANCEL) || cdim(a.cellid[s]) != 1) { len[s] = 0; continue; }
+    if (!big[s]) continue;
     unsigned long long total = 0;
     bool bad = false;
     for_seeds(a, kind, s, sr, [&](uint32_t seed) {
@@ -223,10 +225,11 @@ __global__ void k_saddle_disc_count(DiscArgs a, int kind, SeedRuns sr, uint32_t 
   }
 }
 
-// pass 2: the reference's breadth-first growth, the output span is the queue
-__global__ void k_saddle_disc_write(DiscArgs a, int kind, SeedRuns sr, const uint32_t *off, uint32_t *out) {
+// 2: the reference's breadth-first growth, the output span is the queue
+__global__ void k_saddle_disc_write(DiscArgs a, int kind, SeedRuns sr, const uint8_t *big, const uint32_t *off,
+                                    uint32_t *out) {
   for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < a.ncp; s += gridDim.x * blockDim.x) {
-    if ((a.flags[s] & F_BCANCEL) || cdim(a.cellid[s]) != 1) continue;
+    if (!big[s]) continue;
     uint32_t o = off[s], cap = off[s + 1] - o, tail = 0;
     uint32_t *q = out + o;
     for_seeds(a, kind, s, sr, [&](uint32_t seed) { if (tail < cap) q[tail++] = seed; });
@@ -241,22 +244,302 @@ __global__ void k_saddle_disc_write(DiscArgs a, int kind, SeedRuns sr, const uin
   }
 }
 
-// 5. per-cp disc lengths of the extrema from the sorted owner keys
-__global__ void k_group_counts(long long n, uint32_t ncp, const uint32_t *key, uint32_t *cnt) {
+// ---------------------------------------------------------------------------
+// 4b. Saddle discs as chains.  A disc's breadth-first queue starts with its
+// level-0 items (the seeds above, m of them); each item has up to two
+// successors, and every later cell exactly one or none (a chain cell is an
+// edge paired with the face (asc) or vertex (des) it was reached from).  So
+// the disc is m items followed by K chains c_1..c_K (successors of item 1 in
+// order, then of item 2, ...) interleaved level by level: the cell at level
+// t >= 1 of chain j sits at
+//     m + sum_j' min(L_j', t - 1) + #{ j' < j : L_j' >= t }
+// where L_j is the length of chain j.  Chains are followed in "hops": per
+// 64x64 vertex tile, in-tile pointer jumping in shared memory gives every
+// edge the number of cells to its tile exit and the edge after it, so a
+// chain's length costs one step per tile crossed, and its cells are written
+// by one thread per (chain, tile) segment.
+// ---------------------------------------------------------------------------
+constexpr int KMAX = 32;                 // saddles with more chains take the serial pass
+constexpr uint32_t HOP_END = 0xFFFFFFFFu;
+constexpr int HOP_THREADS = 512;
+constexpr int HOP_SLOTS = 2 * TX * TY;   // H and Vt edge of every vertex of a tile
+constexpr uint16_t SLOT_NIL = 0xFFFF;
+
+// edge id over the ext window: 2 * vertex index + (0: H edge (2i+1, 2j), 1: Vt edge (2i, 2j+1))
+__host__ __device__ __forceinline__ uint32_t edge_id(const GridGeom &g, int rx, int ry) {
+  return (uint32_t)(((long long)(ry >> 1) * g.vnx + (rx >> 1)) * 2 + (ry & 1));
+}
+__host__ __device__ __forceinline__ void edge_cell(const GridGeom &g, uint32_t e, int &rx, int &ry) {
+  uint32_t v = e >> 1;
+  int vx = (int)(v % (uint32_t)g.vnx), vy = (int)(v / (uint32_t)g.vnx);
+  rx = 2 * vx + ((e & 1) ? 0 : 1);
+  ry = 2 * vy + (int)(e & 1);
+}
+
+// next_cells in ext-local coordinates with a code accessor: up to two
+// successors of edge (rx, ry); returns -1 on a non-critical unpaired rect cell.
+template <class CodeFn>
+__device__ __forceinline__ int succ_local(const GridGeom &g, int kind, int rx, int ry, CodeFn code, int ox[2], int oy[2]) {
+  const int d0 = rx & 1, d1 = ry & 1;
+  int c[2][2];
+  if (kind == 0) { c[0][0] = rx + d1; c[0][1] = ry + d0; c[1][0] = rx - d1; c[1][1] = ry - d0; }
+  else           { c[0][0] = rx + d0; c[0][1] = ry + d1; c[1][0] = rx - d0; c[1][1] = ry - d1; }
+  int n = 0;
+  for (int k = 0; k < 2; ++k) {
+    const int qx = c[k][0], qy = c[k][1];
+    if (qx < 0 || qy < 0 || qx > g.cx || qy > g.cy) continue;
+    const uint32_t qc = code(qx, qy);
+    if (qc & CODE_CRIT) continue;
+    if (qx < g.rx0 || qx > g.rx1 || qy < g.ry0 || qy > g.ry1) continue;
+    if (!(qc & CODE_PAIRED)) return -1;  // every rect cell is paired or critical
+    const uint32_t d = qc & 3;
+    const int px = qx + (d == DIR_PX ? 1 : d == DIR_MX ? -1 : 0), py = qy + (d == DIR_PY ? 1 : d == DIR_MY ? -1 : 0);
+    if (px == rx && py == ry) continue;
+    ox[n] = px; oy[n] = py; ++n;
+  }
+  return n;
+}
+
+struct HopSmem {
+  uint32_t code[(TX + 2) * (TY + 2)];
+  uint16_t nxt[HOP_SLOTS], val[HOP_SLOTS], tail[HOP_SLOTS];
+};
+
+// hop_to[kind][e] / hop_len[kind][e] for every edge: grid (ntx, nty, 2 kinds)
+__global__ void __launch_bounds__(HOP_THREADS)
+k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *to0, uint32_t *to1, uint16_t *len0,
+            uint16_t *len1, uint32_t *status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  HopSmem &S = *reinterpret_cast<HopSmem *>(smem_raw);
+  const int kind = blockIdx.z;
+  const int tx0 = blockIdx.x * TX, ty0 = blockIdx.y * TY;
+  uint32_t *to = kind ? to1 : to0;
+  uint16_t *len = kind ? len1 : len0;
+  for (int e = threadIdx.x; e < (TX + 2) * (TY + 2); e += blockDim.x) {
+    const int jj = e / (TX + 2), ii = e - jj * (TX + 2);
+    const int vx = tx0 - 1 + ii, vy = ty0 - 1 + jj;
+    S.code[e] = (vx >= 0 && vy >= 0 && vx < g.vnx && vy < g.vny) ? codes[(long long)vy * g.vnx + vx] : 0u;
+  }
+  __syncthreads();
+  auto code = [&](int qx, int qy) -> uint32_t {
+    const int ii = (qx >> 1) - tx0 + 1, jj = (qy >> 1) - ty0 + 1;
+    return (S.code[jj * (TX + 2) + ii] >> (8 * ((qx & 1) | ((qy & 1) << 1)))) & 0xff;
+  };
+  auto slot_cell = [&](int sl, int &rx, int &ry) -> bool {  // false: no such edge
+    const int t = sl & 1, v = sl >> 1, li = v % TX, lj = v / TX;
+    const int vx = tx0 + li, vy = ty0 + lj;
+    rx = 2 * vx + (t ? 0 : 1);
+    ry = 2 * vy + t;
+    return vx < g.vnx && vy < g.vny && rx <= g.cx && ry <= g.cy;
+  };
+  uint32_t st = 0;
+  for (int sl = threadIdx.x; sl < HOP_SLOTS; sl += blockDim.x) {
+    int rx, ry, ox[2], oy[2];
+    uint16_t nx = SLOT_NIL;
+    if (slot_cell(sl, rx, ry)) {
+      const int n = succ_local(g, kind, rx, ry, code, ox, oy);
+      if (n < 0) st |= ST_INVARIANT;
+      if (n == 1) {
+        const int vx = ox[0] >> 1, vy = oy[0] >> 1;
+        if (vx >= tx0 && vx < tx0 + TX && vy >= ty0 && vy < ty0 + TY)
+          nx = (uint16_t)((((vy - ty0) * TX + (vx - tx0)) << 1) | (oy[0] & 1));
+      }
+    }
+    S.nxt[sl] = nx;
+    S.val[sl] = 1;
+    S.tail[sl] = (uint16_t)sl;
+  }
+  __syncthreads();
+  // list ranking: 13 rounds cover 2^13 = HOP_SLOTS cells
+  constexpr int PER = HOP_SLOTS / HOP_THREADS;
+  for (int round = 0; round < 13; ++round) {
+    uint16_t nn[PER], nv[PER], nt[PER];
+    int active = 0;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int sl = threadIdx.x + q * HOP_THREADS;
+      const uint16_t n = S.nxt[sl];
+      nn[q] = n; nv[q] = S.val[sl]; nt[q] = S.tail[sl];
+      if (n != SLOT_NIL) { nv[q] = (uint16_t)(nv[q] + S.val[n]); nt[q] = S.tail[n]; nn[q] = S.nxt[n]; active = 1; }
+    }
+    if (!__syncthreads_or(active)) break;  // every list already ranked
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int sl = threadIdx.x + q * HOP_THREADS;
+      S.nxt[sl] = nn[q]; S.val[sl] = nv[q]; S.tail[sl] = nt[q];
+    }
+    __syncthreads();
+  }
+  for (int sl = threadIdx.x; sl < HOP_SLOTS; sl += blockDim.x) {
+    int rx, ry, ox[2], oy[2];
+    if (!slot_cell(sl, rx, ry)) continue;
+    const uint32_t e = edge_id(g, rx, ry);
+    if (S.nxt[sl] != SLOT_NIL) { st |= ST_CYCLE; to[e] = HOP_END; len[e] = 0; continue; }
+    uint32_t dst = HOP_END;
+    int tx, ty;
+    slot_cell(S.tail[sl], tx, ty);
+    const int n = succ_local(g, kind, tx, ty, code, ox, oy);
+    if (n == 1) {
+      const int vx = ox[0] >> 1, vy = oy[0] >> 1;
+      if (!(vx >= tx0 && vx < tx0 + TX && vy >= ty0 && vy < ty0 + TY)) dst = edge_id(g, ox[0], oy[0]);
+    }
+    to[e] = dst;
+    // a cell with two successors ends no chain: length 0 marks it for the walkers
+    len[e] = n == 2 ? 0 : S.val[sl];
+  }
+  if (st) atomicOr(status, st);
+}
+
+struct ChainArgs {
+  const uint32_t *hop_to;
+  const uint16_t *hop_len;
+  uint32_t *kc;         // per cp: chains of a saddle handled here (0 otherwise)
+  uint32_t *mc;         // per cp: level-0 items
+  uint8_t *big;         // per cp: surviving saddle with more than KMAX chains
+  uint32_t *cbase;      // exclusive scan of kc
+  uint32_t *cstart, *csaddle, *clen, *cnseg, *csegoff;  // per chain
+  uint4 *segs;          // (chain, first edge, first level, cells)
+  unsigned long long limit;
+};
+
+__device__ __forceinline__ bool surviving_saddle(const DiscArgs &a, uint32_t s) {
+  return !(a.flags[s] & F_BCANCEL) && cdim(a.cellid[s]) == 1;
+}
+// successors of a level-0 item (a global edge cell) as ext-local edge ids
+__device__ __forceinline__ int item_children(const DiscArgs &a, int kind, uint32_t pc, uint32_t out[2]) {
+  uint32_t nx[2];
+  int n = next_cells(a, kind, pc, nx);
+  for (int b = 0; b < n; ++b) out[b] = edge_id(a.g, cx(nx[b]) - a.g.ex0, cy(nx[b]) - a.g.ey0);
+  return n;
+}
+
+__global__ void k_chain_count(DiscArgs a, int kind, SeedRuns sr, ChainArgs c) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < a.ncp; s += gridDim.x * blockDim.x) {
+    uint32_t m = 0, K = 0;
+    if (surviving_saddle(a, s)) {
+      for_seeds(a, kind, s, sr, [&](uint32_t seed) {
+        uint32_t ch[2];
+        ++m;
+        K += item_children(a, kind, seed, ch);
+      });
+    }
+    const bool big = K > KMAX;
+    c.kc[s] = big ? 0 : K;
+    c.mc[s] = m;
+    c.big[s] = big;
+  }
+}
+
+// chain starts, lengths and segment counts; the disc length of every
+// saddle handled here (0 for other critical points, big saddles untouched)
+__global__ void k_chain_len(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, uint32_t *slen) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < a.ncp; s += gridDim.x * blockDim.x) {
+    if (c.big[s]) continue;
+    if (!surviving_saddle(a, s)) { slen[s] = 0; continue; }
+    unsigned long long total = c.mc[s];
+    uint32_t j = c.cbase[s];
+    bool bad = false;
+    for_seeds(a, kind, s, sr, [&](uint32_t seed) {
+      uint32_t ch[2];
+      const int n = item_children(a, kind, seed, ch);
+      for (int b = 0; b < n; ++b) {
+        unsigned long long L = 0;
+        uint32_t nseg = 0;
+        for (uint32_t e = ch[b]; e != HOP_END; e = c.hop_to[e]) {
+          const uint32_t l = c.hop_len[e];
+          if (l == 0) { atomicOr(a.status, ST_INVARIANT); break; }  // a chain cell never branches
+          L += l;
+          ++nseg;
+          if (L > c.limit) { bad = true; break; }
+        }
+        c.cstart[j] = ch[b]; c.csaddle[j] = s; c.clen[j] = (uint32_t)L; c.cnseg[j] = nseg;
+        ++j;
+        total += L;
+      }
+    });
+    if (bad) { atomicOr(a.status, ST_CYCLE); total = 0; }
+    if (total > 0xffffffffull) { atomicOr(a.status, ST_SIMPLIFY_LIMIT); total = 0; }
+    slen[s] = (uint32_t)total;
+  }
+}
+
+__global__ void k_chain_segs(long long nchains, ChainArgs c) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nchains; k += (long long)gridDim.x * blockDim.x) {
+    uint32_t o = c.csegoff[k], end = c.csegoff[k + 1], T = 1;
+    for (uint32_t e = c.cstart[k]; e != HOP_END && o < end; e = c.hop_to[e]) {
+      const uint32_t l = c.hop_len[e];
+      if (l == 0) break;
+      c.segs[o++] = make_uint4((uint32_t)k, e, T, l);
+      T += l;
+    }
+  }
+}
+
+// level-0 items of the saddles handled here
+__global__ void k_level0(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, const uint32_t *off, uint32_t *out) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < a.ncp; s += gridDim.x * blockDim.x) {
+    if (c.big[s] || !surviving_saddle(a, s)) continue;
+    uint32_t o = off[s], end = off[s + 1];
+    for_seeds(a, kind, s, sr, [&](uint32_t seed) {
+      if (o < end) out[o++] = seed;
+      else atomicOr(a.status, ST_INVARIANT);
+    });
+  }
+}
+
+// one thread per segment: walk its cells (all in one tile) and place them
+__global__ void k_seg_write(DiscArgs a, int kind, ChainArgs c, long long nsegs, const uint32_t *off, uint32_t *out) {
+  const GridGeom &g = a.g;
+  auto gcode = [&](int qx, int qy) -> uint32_t {
+    const uint32_t q = a.codes[(long long)(qy >> 1) * g.vnx + (qx >> 1)];
+    return (q >> (8 * ((qx & 1) | ((qy & 1) << 1)))) & 0xff;
+  };
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nsegs; k += (long long)gridDim.x * blockDim.x) {
+    const uint4 sg = c.segs[k];
+    const uint32_t ch = sg.x, s = c.csaddle[ch], K = c.kc[s], cb = c.cbase[s], j = ch - cb;
+    uint32_t L[KMAX];
+    for (uint32_t q = 0; q < K; ++q) L[q] = c.clen[cb + q];
+    const uint32_t base = off[s] + c.mc[s], end = off[s + 1];
+    int rx, ry;
+    edge_cell(g, sg.y, rx, ry);
+    for (uint32_t i = 0; i < sg.w; ++i) {
+      const uint32_t t = sg.z + i;
+      uint32_t pos = base;
+      for (uint32_t q = 0; q < K; ++q) {
+        pos += L[q] < t - 1 ? L[q] : t - 1;
+        pos += (q < j && L[q] >= t) ? 1u : 0u;
+      }
+      if (pos >= end) { atomicOr(a.status, ST_INVARIANT); break; }
+      out[pos] = pack_cellid(g.ex0 + rx, g.ey0 + ry);
+      if (i + 1 < sg.w) {
+        int ox[2], oy[2];
+        if (succ_local(g, kind, rx, ry, gcode, ox, oy) != 1) { atomicOr(a.status, ST_INVARIANT); break; }
+        rx = ox[0]; ry = oy[0];
+      }
+    }
+  }
+}
+
+// 5. runs of equal sorted keys: the last element of each run writes (or adds)
+// its length, after k_seed_runs has recorded the run starts
+__global__ void k_run_len(long long n, uint32_t ncp, const uint32_t *key, const uint32_t *start, uint32_t *cnt,
+                          int accumulate) {
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     uint32_t k = key[p];
-    if (k < ncp) atomicAdd(cnt + k, 1u);
+    if (k < ncp && (p + 1 == n || key[p + 1] != k)) {
+      uint32_t len = (uint32_t)p + 1 - start[k];
+      cnt[k] = accumulate ? cnt[k] + len : len;
+    }
   }
 }
 __global__ void k_add_counts(uint32_t n, const uint32_t *a, uint32_t *b) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] += a[i];
 }
-__global__ void k_seed_runs(long long n, uint32_t ncp, const uint32_t *key, uint32_t *start, uint32_t *count) {
+// first position of each run of equal sorted keys
+__global__ void k_seed_runs(long long n, uint32_t ncp, const uint32_t *key, uint32_t *start) {
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     uint32_t k = key[p];
-    if (k >= ncp) continue;
-    if (p == 0 || key[p - 1] != k) start[k] = (uint32_t)p;
-    atomicAdd(count + k, 1u);
+    if (k < ncp && (p == 0 || key[p - 1] != k)) start[k] = (uint32_t)p;
   }
 }
 __global__ void k_group_scatter(long long n, uint32_t ncp, const uint32_t *key, const uint32_t *val,
@@ -278,6 +561,14 @@ static int nbits_for(long long n) {
   return b;
 }
 
+static cudaError_t hops_attr() {
+  static bool done = false;
+  if (done) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_disc_hops, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(HopSmem));
+  if (e == cudaSuccess) done = true;
+  return e;
+}
+
 cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   DiscArgs a;
   a.g = io.g; a.codes = io.codes; a.labels = io.labels; a.ncp_ds = (uint32_t)io.ncp_ds; a.ncp = (uint32_t)io.ncp;
@@ -288,21 +579,37 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   const long long nV = (long long)((g.rx1 - g.rx0) / 2 + 1) * ((g.ry1 - g.ry0) / 2 + 1);
   const long long nF = (long long)((g.rx1 - g.rx0) / 2) * ((g.ry1 - g.ry0) / 2);
   const long long nmax = std::max(std::max(nV, nF), std::max(io.nasc, io.ndes)) + 1;
-  size_t words = (size_t)ncp * 7 + 8 + (size_t)nmax * 4 + (size_t)(nV + nF) * 2 + 64;
+  const long long nE = 2ll * g.vnx * g.vny;  // edge ids of the ext window
+  // words: 7 ncp + 8 | 4 nmax | 2 (nV + nF) | 2 ncp (kc, mc) + ncp + 1 (cbase) | ncp / 4 (big) | 3 nE (hops)
+  size_t words = (size_t)ncp * 7 + 8 + (size_t)nmax * 4 + (size_t)(nV + nF) * 2 + (size_t)ncp * 3 + 1 +
+                 (size_t)ncp / 4 + 1 + (size_t)nE * 3 + 64;
   uint32_t *buf = nullptr;
-  cudaError_t e = cudaMallocAsync((void **)&buf, sizeof(uint32_t) * words, st);
+  cudaError_t e = hops_attr();
+  if (e != cudaSuccess) return e;
+  e = cudaMallocAsync((void **)&buf, sizeof(uint32_t) * words, st);
   if (e != cudaSuccess) return e;
   uint32_t *redir = buf, *acnt = buf + ncp, *dcnt = buf + 2 * ncp, *slen = buf + 3 * ncp;
   uint32_t *sstart = buf + 4 * ncp, *scount = buf + 5 * ncp, *soff = buf + 6 * ncp;  // soff: ncp+1
   uint32_t *key = buf + 7 * ncp + 8, *val = key + nmax, *kt = val + nmax, *vt = kt + nmax;
   uint32_t *gkey[2] = {vt + nmax, vt + nmax + nV}, *gval[2] = {vt + nmax + nV + nF, vt + nmax + 2 * nV + nF};
+  uint32_t *kc = gval[1] + nF, *mc = kc + ncp, *cbase = mc + ncp;  // cbase: ncp+1
+  uint8_t *big = (uint8_t *)(cbase + ncp + 1);
+  uint32_t *hop_to[2] = {cbase + ncp + 1 + ncp / 4 + 1, cbase + ncp + 1 + ncp / 4 + 1 + nE};
+  uint16_t *hop_len[2] = {(uint16_t *)(hop_to[1] + nE), (uint16_t *)(hop_to[1] + nE) + nE};
   const long long gn[2] = {nV, nF};
   auto L = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+  uint32_t *chain_buf = nullptr;
+  uint4 *segs = nullptr;
 
   if (ncp) {
     k_redir_init<<<nb(ncp), 256, 0, st>>>((uint32_t)ncp, redir);
-    DMSC_LAUNCHED(1);
     k_redir_saddles<<<nb(ncp), 256, 0, st>>>(a, redir);
+    DMSC_LAUNCHED(2);
+  }
+  {
+    dim3 grid(g.ntx, g.nty, 2);
+    k_disc_hops<<<grid, HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, hop_to[0], hop_to[1], hop_len[0], hop_len[1],
+                                                            io.status);
     DMSC_LAUNCHED(1);
   }
   L(cudaMemsetAsync(acnt, 0, sizeof(uint32_t) * ncp * 2, st));
@@ -314,8 +621,9 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     k_disc_keys<<<nb(n), 256, 0, st>>>(a, redir, kind, gkey[kind], gval[kind]);
     DMSC_LAUNCHED(1);
     L(radix_sort_pairs(gkey[kind], gval[kind], kt, vt, n, nbits_for(ncp), st));
-    k_group_counts<<<nb(n), 256, 0, st>>>(n, (uint32_t)ncp, gkey[kind], kind ? dcnt : acnt);
-    DMSC_LAUNCHED(1);
+    k_seed_runs<<<nb(n), 256, 0, st>>>(n, (uint32_t)ncp, gkey[kind], sstart);
+    k_run_len<<<nb(n), 256, 0, st>>>(n, (uint32_t)ncp, gkey[kind], sstart, kind ? dcnt : acnt, 1);
+    DMSC_LAUNCHED(2);
   }
   // saddle discs
   for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind) {
@@ -335,34 +643,68 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     }
     L(cudaMemsetAsync(scount, 0, sizeof(uint32_t) * ncp, st));
     if (ns) {
-      k_seed_runs<<<nb(ns), 256, 0, st>>>(ns, (uint32_t)ncp, key, sstart, scount);
-      DMSC_LAUNCHED(1);
+      k_seed_runs<<<nb(ns), 256, 0, st>>>(ns, (uint32_t)ncp, key, sstart);
+      k_run_len<<<nb(ns), 256, 0, st>>>(ns, (uint32_t)ncp, key, sstart, scount, 0);
+      DMSC_LAUNCHED(2);
     }
     SeedRuns sr{val, sstart, scount};
-    k_saddle_disc_count<<<nb(ncp), 128, 0, st>>>(a, kind, sr, slen, io.limit);
+    ChainArgs c{};
+    c.hop_to = hop_to[kind]; c.hop_len = hop_len[kind];
+    c.kc = kc; c.mc = mc; c.big = big; c.cbase = cbase; c.limit = io.limit;
+    k_chain_count<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c);
     DMSC_LAUNCHED(1);
+    L(scan_exclusive_u32(kc, ncp, cbase, cbase + ncp, st));
+    uint32_t nch = 0;
+    L(cudaMemcpyAsync(&nch, cbase + ncp, 4, cudaMemcpyDeviceToHost, st));
+    L(cudaStreamSynchronize(st));
+    if (e != cudaSuccess) break;
+    L(cudaMallocAsync((void **)&chain_buf, sizeof(uint32_t) * (6ull * nch + 8), st));
+    if (e != cudaSuccess) break;
+    c.cstart = chain_buf; c.csaddle = chain_buf + nch; c.clen = chain_buf + 2 * nch; c.cnseg = chain_buf + 3 * nch;
+    c.csegoff = chain_buf + 4 * nch;  // nch + 1
+    k_chain_len<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, slen);
+    k_saddle_disc_count<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, slen, io.limit);
     k_add_counts<<<nb(ncp), 256, 0, st>>>((uint32_t)ncp, slen, kind ? dcnt : acnt);
-    DMSC_LAUNCHED(1);
+    DMSC_LAUNCHED(3);
     uint32_t *offs = kind ? io.ddoff : io.adoff;
     L(scan_exclusive_u32(kind ? dcnt : acnt, ncp, offs, offs + ncp, st));
-    uint32_t tot = 0;
-    L(cudaMemcpyAsync(&tot, offs + ncp, 4, cudaMemcpyDeviceToHost, st));
+    L(scan_exclusive_u32(c.cnseg, nch, c.csegoff, c.csegoff + nch, st));
+    uint32_t tot[2] = {0, 0};
+    L(cudaMemcpyAsync(&tot[0], offs + ncp, 4, cudaMemcpyDeviceToHost, st));
+    L(cudaMemcpyAsync(&tot[1], c.csegoff + nch, 4, cudaMemcpyDeviceToHost, st));
     L(cudaStreamSynchronize(st));
     if (e != cudaSuccess) break;
     DevBuf<uint32_t> *ob = kind ? io.ddisc : io.adisc;
-    L(ob->ensure((size_t)tot + 1));
+    L(ob->ensure((size_t)tot[0] + 1));
+    L(cudaMallocAsync((void **)&segs, sizeof(uint4) * ((size_t)tot[1] + 1), st));
     if (e != cudaSuccess) break;
-    k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, offs, ob->p);
-    DMSC_LAUNCHED(1);
+    c.segs = segs;
+    if (nch) {
+      k_chain_segs<<<nb(nch), 128, 0, st>>>(nch, c);
+      DMSC_LAUNCHED(1);
+    }
+    k_level0<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, offs, ob->p);
+    k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);
+    DMSC_LAUNCHED(2);
+    if (tot[1]) {
+      k_seg_write<<<nb(tot[1]), 128, 0, st>>>(a, kind, c, tot[1], offs, ob->p);
+      DMSC_LAUNCHED(1);
+    }
     long long n = gn[kind];
     if (n > 0) {  // extremum groups of this kind
-      k_seed_runs<<<nb(n), 256, 0, st>>>(n, (uint32_t)ncp, gkey[kind], sstart, scount);
+      k_seed_runs<<<nb(n), 256, 0, st>>>(n, (uint32_t)ncp, gkey[kind], sstart);
       DMSC_LAUNCHED(1);
       k_group_scatter<<<nb(n), 256, 0, st>>>(n, (uint32_t)ncp, gkey[kind], gval[kind], sstart, offs, ob->p);
       DMSC_LAUNCHED(1);
     }
-    (kind ? io.nddisc : io.nadisc) = tot;
+    (kind ? io.nddisc : io.nadisc) = tot[0];
+    cudaFreeAsync(segs, st);
+    cudaFreeAsync(chain_buf, st);
+    segs = nullptr;
+    chain_buf = nullptr;
   }
+  if (segs) cudaFreeAsync(segs, st);
+  if (chain_buf) cudaFreeAsync(chain_buf, st);
   cudaFreeAsync(buf, st);
   if (e == cudaSuccess) e = cudaGetLastError();
   return e;

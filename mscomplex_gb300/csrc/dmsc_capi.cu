@@ -512,6 +512,13 @@ int dmsc_msc::writeout_from(const dmsc_dataset &d, cudaStream_t st) {
   CK(cudaMemcpyAsync(&tot[1], doff.p + n, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&tot[2], d.scal.p, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  if (tot[2] == ST_CAPACITY) {  // an extremum segment too long for the in-place sorts
+    CK(cudaMemsetAsync(d.scal.p, 0, sizeof(uint32_t), st));
+    CK(build_csr_radix(ncp, d.cp_cellid.p, d.cp_des2.p, d.cp_asc2.p, aoff.p, doff.p, asc.p, des.p,
+                       4 * (long long)n + 1, d.scal.p, st));
+    CK(cudaMemcpyAsync(&tot[2], d.scal.p, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
   nasc = tot[0];
   ndes = tot[1];
   if (tot[2]) return status_to_error(tot[2]);

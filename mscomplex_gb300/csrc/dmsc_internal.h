@@ -47,6 +47,9 @@ cudaError_t sort_pairs_batched(uint32_t *dk, uint32_t *dv, const uint32_t *sk, c
 cudaError_t build_csr(long long ncp, const uint32_t *cellid, const uint32_t *des2, const uint32_t *asc2,
                       const uint32_t *aoff, const uint32_t *doff, uint32_t *asc, uint32_t *des, long long out_cap,
                       uint32_t *status, cudaStream_t st);
+cudaError_t build_csr_radix(long long ncp, const uint32_t *cellid, const uint32_t *des2, const uint32_t *asc2,
+                      const uint32_t *aoff, const uint32_t *doff, uint32_t *asc, uint32_t *des, long long out_cap,
+                      uint32_t *status, cudaStream_t st);
 cudaError_t launch_pair_index(long long ncp, const uint32_t *cellid, const uint8_t *flags, const uint32_t *pair_cell,
                               uint32_t *pair_idx, uint32_t *status, cudaStream_t st);
 cudaError_t launch_msc_flags(long long ncp, const uint8_t *cpflags, uint8_t *out, cudaStream_t st);

@@ -383,7 +383,140 @@ static unsigned grid_for(long long n, int threads) {
   return (unsigned)(b < 1 ? 1 : b);
 }
 
+// ---- extremum side by atomic scatter + per-segment sort ----
+// Every staged (extremum, saddle) arc is placed into its extremum's CSR
+// segment at an atomically claimed slot; each segment is then sorted by
+// saddle index, which is the ascending iteration order of the reference's
+// multiset (equal saddle indices are indistinguishable, so the result does
+// not depend on the claim order).  Segments of up to SEG_THREAD items are
+// sorted by one thread, up to SEG_BLOCK by one block in shared memory; a
+// longer one sets ST_CAPACITY and the caller falls back to the radix path.
+constexpr uint32_t SEG_THREAD = 32, SEG_BLOCK = 8192;
+
+__global__ void k_ext_scatter(long long ncp, const uint32_t *__restrict__ cellid, const uint32_t *__restrict__ des2,
+                              const uint32_t *__restrict__ asc2, const uint32_t *__restrict__ aoff,
+                              const uint32_t *__restrict__ doff, uint32_t *__restrict__ asc, uint32_t *__restrict__ des,
+                              uint32_t *__restrict__ afill, uint32_t *__restrict__ dfill, uint32_t *__restrict__ status) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < ncp; k += (long long)gridDim.x * blockDim.x) {
+    if (cell_dim(cellid[k]) != 1) continue;
+    for (int q = 0; q < 2; ++q) {
+      const uint32_t x = des2[2 * k + q];  // a minimum: the saddle joins its asc list
+      if (x != LABEL_NONE) {
+        if (x >= (uint32_t)ncp) { atomicOr(status, ST_INVARIANT); continue; }
+        const uint32_t r = atomicAdd(afill + x, 1u);
+        if (r < aoff[x + 1] - aoff[x]) asc[aoff[x] + r] = (uint32_t)k;
+        else atomicOr(status, ST_INVARIANT);
+      }
+      const uint32_t y = asc2[2 * k + q];  // a maximum: the saddle joins its des list
+      if (y != LABEL_NONE) {
+        if (y >= (uint32_t)ncp) { atomicOr(status, ST_INVARIANT); continue; }
+        const uint32_t r = atomicAdd(dfill + y, 1u);
+        if (r < doff[y + 1] - doff[y]) des[doff[y] + r] = (uint32_t)k;
+        else atomicOr(status, ST_INVARIANT);
+      }
+    }
+  }
+}
+
+// the saddle's own lists straight from its 2+2 staged labels
+__global__ void k_saddle_lists(long long ncp, const uint32_t *__restrict__ cellid, const uint32_t *__restrict__ des2,
+                               const uint32_t *__restrict__ asc2, const uint32_t *__restrict__ aoff,
+                               const uint32_t *__restrict__ doff, uint32_t *__restrict__ asc, uint32_t *__restrict__ des) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < ncp; k += (long long)gridDim.x * blockDim.x) {
+    if (cell_dim(cellid[k]) != 1) continue;
+    uint32_t p = doff[k], pe = doff[k + 1];
+    for (int q = 0; q < 2; ++q)
+      if (des2[2 * k + q] != LABEL_NONE && p < pe) des[p++] = des2[2 * k + q];
+    p = aoff[k]; pe = aoff[k + 1];
+    for (int q = 0; q < 2; ++q)
+      if (asc2[2 * k + q] != LABEL_NONE && p < pe) asc[p++] = asc2[2 * k + q];
+  }
+}
+
+// short extremum segments: insertion sort by one thread; longer ones queued
+__global__ void k_seg_sort(long long ncp, const uint32_t *__restrict__ cellid, const uint32_t *__restrict__ aoff,
+                           const uint32_t *__restrict__ doff, uint32_t *__restrict__ asc, uint32_t *__restrict__ des,
+                           uint32_t *__restrict__ longq, uint32_t *__restrict__ nlong, uint32_t *__restrict__ status) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < ncp; k += (long long)gridDim.x * blockDim.x) {
+    const int dim = cell_dim(cellid[k]);
+    if (dim == 1) continue;
+    uint32_t *seg = dim == 0 ? asc + aoff[k] : des + doff[k];
+    const uint32_t n = dim == 0 ? aoff[k + 1] - aoff[k] : doff[k + 1] - doff[k];
+    if (n <= 1) continue;
+    if (n > SEG_THREAD) {
+      if (n > SEG_BLOCK) { atomicOr(status, ST_CAPACITY); continue; }
+      longq[atomicAdd(nlong, 1u)] = (uint32_t)k;
+      continue;
+    }
+    uint32_t v[SEG_THREAD];
+    for (uint32_t i = 0; i < n; ++i) v[i] = seg[i];
+    for (uint32_t i = 1; i < n; ++i) {
+      const uint32_t x = v[i];
+      uint32_t j = i;
+      while (j > 0 && v[j - 1] > x) { v[j] = v[j - 1]; --j; }
+      v[j] = x;
+    }
+    for (uint32_t i = 0; i < n; ++i) seg[i] = v[i];
+  }
+}
+
+// queued segments: one block each, bitonic sort in shared memory
+__global__ void __launch_bounds__(512) k_seg_sort_block(const uint32_t *__restrict__ cellid, const uint32_t *__restrict__ aoff,
+                                                        const uint32_t *__restrict__ doff, uint32_t *__restrict__ asc,
+                                                        uint32_t *__restrict__ des, const uint32_t *__restrict__ longq,
+                                                        const uint32_t *__restrict__ nlong) {
+  __shared__ uint32_t sh[SEG_BLOCK];
+  const uint32_t nq = *nlong;
+  for (uint32_t q = blockIdx.x; q < nq; q += gridDim.x) {
+    const uint32_t k = longq[q];
+    const int dim = cell_dim(cellid[k]);
+    uint32_t *seg = dim == 0 ? asc + aoff[k] : des + doff[k];
+    const uint32_t n = dim == 0 ? aoff[k + 1] - aoff[k] : doff[k + 1] - doff[k];
+    uint32_t p2 = 1;
+    while (p2 < n) p2 <<= 1;
+    for (uint32_t i = threadIdx.x; i < p2; i += blockDim.x) sh[i] = i < n ? seg[i] : 0xFFFFFFFFu;
+    __syncthreads();
+    for (uint32_t size = 2; size <= p2; size <<= 1)
+      for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+        for (uint32_t i = threadIdx.x; i < p2; i += blockDim.x) {
+          const uint32_t j = i ^ stride;
+          if (j > i) {
+            const bool up = (i & size) == 0;
+            const uint32_t a = sh[i], b = sh[j];
+            if ((a > b) == up) { sh[i] = b; sh[j] = a; }
+          }
+        }
+        __syncthreads();
+      }
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) seg[i] = sh[i];
+    __syncthreads();
+  }
+}
+
 cudaError_t build_csr(long long ncp, const uint32_t *cellid, const uint32_t *des2, const uint32_t *asc2,
+                      const uint32_t *aoff, const uint32_t *doff, uint32_t *asc, uint32_t *des, long long out_cap,
+                      uint32_t *status, cudaStream_t st) {
+  if (ncp <= 0) return cudaSuccess;
+  uint32_t *buf = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&buf, sizeof(uint32_t) * (3 * ncp + 8), st);
+  if (e != cudaSuccess) return e;
+  uint32_t *afill = buf, *dfill = buf + ncp, *longq = buf + 2 * ncp, *nlong = buf + 3 * ncp;
+  e = cudaMemsetAsync(afill, 0, sizeof(uint32_t) * 2 * ncp, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(nlong, 0, sizeof(uint32_t), st);
+  if (e == cudaSuccess) {
+    (void)out_cap;  // every write is bounded by its own segment of aoff/doff
+    k_saddle_lists<<<grid_for(ncp, 256), 256, 0, st>>>(ncp, cellid, des2, asc2, aoff, doff, asc, des);
+    k_ext_scatter<<<grid_for(ncp, 256), 256, 0, st>>>(ncp, cellid, des2, asc2, aoff, doff, asc, des, afill, dfill, status);
+    k_seg_sort<<<grid_for(ncp, 128), 128, 0, st>>>(ncp, cellid, aoff, doff, asc, des, longq, nlong, status);
+    k_seg_sort_block<<<152 * 2, 512, 0, st>>>(cellid, aoff, doff, asc, des, longq, nlong);
+    DMSC_LAUNCHED(4);
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(buf, st);
+  return e;
+}
+
+cudaError_t build_csr_radix(long long ncp, const uint32_t *cellid, const uint32_t *des2, const uint32_t *asc2,
                       const uint32_t *aoff, const uint32_t *doff, uint32_t *asc, uint32_t *des, long long out_cap,
                       uint32_t *status, cudaStream_t st) {
   if (ncp <= 0) return cudaSuccess;

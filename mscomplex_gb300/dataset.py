@@ -88,6 +88,10 @@ class GridDataset:
             if tuple(t.shape) != (self.vny, self.vnx):
                 raise ValueError(f"heights shape {tuple(t.shape)} != ext window {(self.vny, self.vnx)}")
             self._keep = t
+            if stream is None:
+                # the library's own stream does not order with torch's streams
+                import torch
+                torch.cuda.current_stream(t.device).synchronize()
             check(self.lib.dmsc_dataset_init(self.h, C.c_void_p(t.data_ptr()), t.stride(0), 1, stream))
         else:
             a = np.ascontiguousarray(heights, dtype=np.float32)
@@ -218,6 +222,9 @@ class GridDataManager:
                 raise ValueError("device heights must be a 2D float32 tensor with unit x stride")
             ny, nx = int(t.shape[0]), int(t.shape[1])
             self._keep = t
+            if stream is None:
+                import torch
+                torch.cuda.current_stream(t.device).synchronize()
             rc = self.lib.dmsc_pipeline_run(self.ctx.h, C.c_void_p(t.data_ptr()), t.stride(0), 1, nx, ny,
                                             int(levels), float(tresh), int(bool(split2d)), C.byref(h), stream)
         else:
