@@ -50,7 +50,10 @@ enum {
 const char *dmsc_last_error(void);
 
 /* GridDataset::init_opencl() -- process-wide device setup
- * (dmsc/include/grid_dataset.h:236, dmsc/src/grid_dataset.cpp:186-226). */
+ * (dmsc/include/grid_dataset.h:236, dmsc/src/grid_dataset.cpp:186-226).
+ * Scratch buffers come from the device's default stream-ordered memory
+ * pool; dmsc_init sets that pool to keep freed memory cached (release
+ * threshold = max) and dmsc_shutdown trims it. */
 int dmsc_init(int device, dmsc_ctx **out);
 /* GridDataset::stop_opencl() (dmsc/include/grid_dataset.h:238). */
 int dmsc_shutdown(dmsc_ctx *ctx);

@@ -59,6 +59,14 @@ int dmsc_init(int device, dmsc_ctx **out) {
   CK(cudaGetDeviceCount(&n));
   if (device < 0 || device >= n) return fail(DMSC_ERR_BAD_ARG, "no such device");
   CK(cudaSetDevice(device));
+  // Scratch comes from the device's default stream-ordered pool.  Its default
+  // release threshold (0) hands freed memory back at every synchronisation,
+  // so each call would map its scratch anew; keep it cached instead
+  // (dmsc_shutdown trims the pool).
+  cudaMemPool_t pool;
+  CK(cudaDeviceGetDefaultMemPool(&pool, device));
+  uint64_t keep = ~0ull;
+  CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
   dmsc_ctx *c = new dmsc_ctx;
   c->device = device;
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
@@ -72,6 +80,8 @@ int dmsc_shutdown(dmsc_ctx *c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   cudaStreamDestroy(c->stream);
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, c->device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
   delete c;
   return DMSC_OK;
 }
