@@ -82,7 +82,10 @@ int dmsc_dataset_export_cells(dmsc_dataset *ds, int8_t *flags, int16_t *pairs, i
  * collation (row-major) order. */
 int dmsc_dataset_export_critical(dmsc_dataset *ds, int16_t *cellids, void *stream);
 /* GridDataset::writeout_connectivity(mscomplex_t *) (dmsc/src/grid_dataset.cpp:
- * 1858-1907) / writeout_connectivity_ocl (:1250-1283): a new complex. */
+ * 1858-1907) / writeout_connectivity_ocl (:1250-1283).  *out == NULL: a new
+ * complex is returned in *out.  *out != NULL: that complex (of the same
+ * context) is overwritten in place, reusing its device buffers, as the
+ * reference fills the mscomplex_t it is given. */
 int dmsc_dataset_writeout_connectivity(dmsc_dataset *ds, dmsc_msc **out, void *stream);
 
 /* GridMSComplex::clear() (dmsc/src/grid_mscomplex.cpp:324-329). */
@@ -153,6 +156,37 @@ int dmsc_pipeline_write_discs(dmsc_pipeline *p, const char *prefix);
 /* Host wall time (ms) of the last run's stages: pieces, merge up, simplify,
  * merge down, discs. */
 int dmsc_pipeline_stage_times(dmsc_pipeline *p, double ms[5]);
+
+/* ---- batches of whole grids ----
+ * No counterpart in the reference, which builds one GridDataset at a time
+ * (GridDataManager::computeMsGraph, dmsc/src/grid_datamanager.cpp:121-140):
+ * ngrids whole grids (rect == ext) of sizes[2g] x sizes[2g+1] vertices, their
+ * heights packed back to back (x fastest, grid after grid; host or device
+ * pointer), each taken through work + writeout_connectivity +
+ * simplify_un_simplify(tresh[g]) (skipped where tresh[g] == 0) in shared
+ * launches.  Every grid's complex is identical to the one-grid path.
+ * *out == NULL: a new batch; otherwise that batch is rerun in place (buffers
+ * reused).  max_ops bounds each grid's simplification (<= 0: 20,000,000). */
+typedef struct dmsc_batch dmsc_batch;
+int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float *heights, int on_device,
+                   const double *tresh, int64_t max_ops, dmsc_batch **out, void *stream);
+int dmsc_batch_destroy(dmsc_batch *b);
+int dmsc_batch_num_grids(dmsc_batch *b, int64_t *n);
+/* [0] critical points, [1] asc entries, [2] des entries of grid i */
+int dmsc_batch_sizes(dmsc_batch *b, int64_t i, int64_t sizes[3]);
+/* simplification counters of grid i, as dmsc_msc_simplify_stats */
+int dmsc_batch_simplify_stats(dmsc_batch *b, int64_t i, uint64_t stats[5]);
+/* grid i's complex in the layout of dmsc_msc_export (no discs) */
+int dmsc_batch_export(dmsc_batch *b, int64_t i, int16_t rect_ext[8], int16_t *cellid, float *fn, uint32_t *pair_idx,
+                      uint8_t *flags, uint32_t *asc_off, uint32_t *asc, uint32_t *des_off, uint32_t *des, void *stream);
+/* [0] critical points, [1] asc entries, [2] des entries of the whole batch */
+int dmsc_batch_totals(dmsc_batch *b, int64_t totals[3]);
+/* every grid at once: per-grid bases (ngrids + 1 each) into the shared arrays;
+ * asc_off / des_off are batch-wide (subtract asc_base[g] / des_base[g]); list
+ * values and pair_idx are local to each grid.  Any pointer may be NULL. */
+int dmsc_batch_export_all(dmsc_batch *b, uint32_t *cp_base, uint32_t *asc_base, uint32_t *des_base, uint32_t *cellid,
+                          float *fn, uint32_t *pair_idx, uint8_t *flags, uint32_t *asc_off, uint32_t *asc,
+                          uint32_t *des_off, uint32_t *des, void *stream);
 
 /* PrefixScan::PreScanBuffer(out, in, n, queue) (dmsc/include/prefix_scan.h:105-109,
  * dmsc/src/prefix_scan.cpp:457-464): exclusive prefix sum of n uint32 values

@@ -50,6 +50,14 @@ SIGNATURES = {
     "dmsc_pipeline_piece": ([_vp, _i64, _vp, _vp], _i32),
     "dmsc_pipeline_write_discs": ([_vp, C.c_char_p], _i32),
     "dmsc_pipeline_stage_times": ([_vp, _vp], _i32),
+    "dmsc_batch_run": ([_vp, _i32, _vp, _vp, _i32, _vp, _i64, _vp, _vp], _i32),
+    "dmsc_batch_destroy": ([_vp], _i32),
+    "dmsc_batch_num_grids": ([_vp, _vp], _i32),
+    "dmsc_batch_sizes": ([_vp, _i64, _vp], _i32),
+    "dmsc_batch_simplify_stats": ([_vp, _i64, _vp], _i32),
+    "dmsc_batch_export": ([_vp, _i64] + [_vp] * 9 + [_vp], _i32),
+    "dmsc_batch_totals": ([_vp, _vp], _i32),
+    "dmsc_batch_export_all": ([_vp] + [_vp] * 11 + [_vp], _i32),
     "dmsc_prefix_scan": ([_vp, _vp, _vp, _i64, _vp, _vp], _i32),
     "dmsc_prefix_scan_noalloc": ([_vp, _vp, _vp, _i64, _vp, _vp], _i32),
     "dmsc_sort_pairs": ([_vp, _vp, _vp, _vp, _vp, C.c_uint32, C.c_uint32, C.c_uint32, _vp], _i32),

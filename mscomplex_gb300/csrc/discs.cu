@@ -254,14 +254,14 @@ __global__ void k_saddle_disc_write(DiscArgs a, int kind, SeedRuns sr, const uin
 // t >= 1 of chain j sits at
 //     m + sum_j' min(L_j', t - 1) + #{ j' < j : L_j' >= t }
 // where L_j is the length of chain j.  Chains are followed in "hops": per
-// 64x64 vertex tile, in-tile pointer jumping in shared memory gives every
-// edge the number of cells to its tile exit and the edge after it, so a
-// chain's length costs one step per tile crossed, and its cells are written
-// by one thread per (chain, tile) segment.
+// 64x64 vertex tile, list ranking in shared memory gives every edge the
+// number of cells to its tile exit, the edge after it and the edge 64 cells
+// ahead, so a chain's length costs one step per tile crossed and its cells
+// are written by one thread per piece of at most 64 cells, into a
+// chain-major buffer that a last pass interleaves.
 // ---------------------------------------------------------------------------
 constexpr int KMAX = 32;                 // saddles with more chains take the serial pass
 constexpr uint32_t HOP_END = 0xFFFFFFFFu;
-constexpr int HOP_THREADS = 512;
 constexpr int HOP_SLOTS = 2 * TX * TY;   // H and Vt edge of every vertex of a tile
 constexpr uint16_t SLOT_NIL = 0xFFFF;
 
@@ -300,21 +300,35 @@ __device__ __forceinline__ int succ_local(const GridGeom &g, int kind, int rx, i
   return n;
 }
 
+// The chain kind of an edge: 0 if it is paired with a face (asc chains),
+// 1 if paired with a vertex (des chains), -1 if critical or unpaired.
+__device__ __forceinline__ int chain_kind(uint32_t code, int rx, int ry) {
+  if ((code & CODE_CRIT) || !(code & CODE_PAIRED)) return -1;
+  const uint32_t d = code & 3;
+  const int px = rx + (d == DIR_PX ? 1 : d == DIR_MX ? -1 : 0), py = ry + (d == DIR_PY ? 1 : d == DIR_MY ? -1 : 0);
+  return ((px & 1) + (py & 1)) == 2 ? 0 : 1;
+}
+
+constexpr int HOP_THREADS = 512;
+constexpr int SEG_MAX = 64;  // cells of a write piece: the jump pointer distance (2^6)
+
 struct HopSmem {
   uint32_t code[(TX + 2) * (TY + 2)];
-  uint16_t nxt[HOP_SLOTS], val[HOP_SLOTS], tail[HOP_SLOTS];
+  uint32_t nv[HOP_SLOTS];     // next slot << 16 | cells counted so far
+  uint16_t tail[HOP_SLOTS];
+  uint16_t jmp[HOP_SLOTS];    // the slot SEG_MAX cells ahead in the tile (SLOT_NIL: none)
 };
 
-// hop_to[kind][e] / hop_len[kind][e] for every edge: grid (ntx, nty, 2 kinds)
+// Per edge, for the chains of its own kind: hop_to (the edge after its
+// in-tile run, HOP_END if the chain ends in the tile), hop_len (cells of the
+// run, 0 for a branching cell) and j64 (the edge SEG_MAX cells ahead in the
+// same run, HOP_END if the run is shorter).  One block per tile.
 __global__ void __launch_bounds__(HOP_THREADS)
-k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *to0, uint32_t *to1, uint16_t *len0,
-            uint16_t *len1, uint32_t *status) {
+k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict__ to, uint16_t *__restrict__ len,
+            uint32_t *__restrict__ j64, uint32_t *status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   HopSmem &S = *reinterpret_cast<HopSmem *>(smem_raw);
-  const int kind = blockIdx.z;
   const int tx0 = blockIdx.x * TX, ty0 = blockIdx.y * TY;
-  uint32_t *to = kind ? to1 : to0;
-  uint16_t *len = kind ? len1 : len0;
   for (int e = threadIdx.x; e < (TX + 2) * (TY + 2); e += blockDim.x) {
     const int jj = e / (TX + 2), ii = e - jj * (TX + 2);
     const int vx = tx0 - 1 + ii, vy = ty0 - 1 + jj;
@@ -332,60 +346,84 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *to0, uint3
     ry = 2 * vy + t;
     return vx < g.vnx && vy < g.vny && rx <= g.cx && ry <= g.cy;
   };
+  auto in_tile = [&](int ox, int oy) {
+    const int vx = ox >> 1, vy = oy >> 1;
+    return vx >= tx0 && vx < tx0 + TX && vy >= ty0 && vy < ty0 + TY;
+  };
   uint32_t st = 0;
+  int active = 0;
   for (int sl = threadIdx.x; sl < HOP_SLOTS; sl += blockDim.x) {
     int rx, ry, ox[2], oy[2];
-    uint16_t nx = SLOT_NIL;
+    uint32_t nx = SLOT_NIL;
     if (slot_cell(sl, rx, ry)) {
-      const int n = succ_local(g, kind, rx, ry, code, ox, oy);
-      if (n < 0) st |= ST_INVARIANT;
-      if (n == 1) {
-        const int vx = ox[0] >> 1, vy = oy[0] >> 1;
-        if (vx >= tx0 && vx < tx0 + TX && vy >= ty0 && vy < ty0 + TY)
-          nx = (uint16_t)((((vy - ty0) * TX + (vx - tx0)) << 1) | (oy[0] & 1));
+      const int kind = chain_kind(code(rx, ry), rx, ry);
+      if (kind >= 0) {
+        const int n = succ_local(g, kind, rx, ry, code, ox, oy);
+        if (n < 0) st |= ST_INVARIANT;
+        if (n == 1 && in_tile(ox[0], oy[0])) {
+          nx = (uint32_t)((((oy[0] >> 1) - ty0) * TX + ((ox[0] >> 1) - tx0)) << 1) | (uint32_t)(oy[0] & 1);
+          active = 1;
+        }
       }
     }
-    S.nxt[sl] = nx;
-    S.val[sl] = 1;
+    S.nv[sl] = (nx << 16) | 1u;
     S.tail[sl] = (uint16_t)sl;
+    S.jmp[sl] = SLOT_NIL;
   }
-  __syncthreads();
-  // list ranking: 13 rounds cover 2^13 = HOP_SLOTS cells
+  // list ranking: at most 13 rounds (2^13 = HOP_SLOTS cells); after round 6
+  // every pointer still inside the tile is exactly SEG_MAX cells ahead
   constexpr int PER = HOP_SLOTS / HOP_THREADS;
-  for (int round = 0; round < 13; ++round) {
-    uint16_t nn[PER], nv[PER], nt[PER];
-    int active = 0;
+  for (int round = 0; round < 14 && __syncthreads_or(active); ++round) {
+    uint32_t nn[PER];
+    uint16_t nt[PER];
+    active = 0;
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
       const int sl = threadIdx.x + q * HOP_THREADS;
-      const uint16_t n = S.nxt[sl];
-      nn[q] = n; nv[q] = S.val[sl]; nt[q] = S.tail[sl];
-      if (n != SLOT_NIL) { nv[q] = (uint16_t)(nv[q] + S.val[n]); nt[q] = S.tail[n]; nn[q] = S.nxt[n]; active = 1; }
-    }
-    if (!__syncthreads_or(active)) break;  // every list already ranked
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int sl = threadIdx.x + q * HOP_THREADS;
-      S.nxt[sl] = nn[q]; S.val[sl] = nv[q]; S.tail[sl] = nt[q];
+      const uint32_t v = S.nv[sl];
+      nn[q] = v; nt[q] = S.tail[sl];
+      const uint32_t n = v >> 16;
+      if (n != SLOT_NIL) {
+        const uint32_t w = S.nv[n];
+        nn[q] = (w & 0xFFFF0000u) | ((v + w) & 0xFFFFu);
+        nt[q] = S.tail[n];
+        active |= (w >> 16) != SLOT_NIL;
+      }
     }
     __syncthreads();
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int sl = threadIdx.x + q * HOP_THREADS;
+      S.nv[sl] = nn[q]; S.tail[sl] = nt[q];
+      if (round == 5) S.jmp[sl] = (uint16_t)(nn[q] >> 16);
+    }
   }
+  __syncthreads();
   for (int sl = threadIdx.x; sl < HOP_SLOTS; sl += blockDim.x) {
     int rx, ry, ox[2], oy[2];
     if (!slot_cell(sl, rx, ry)) continue;
     const uint32_t e = edge_id(g, rx, ry);
-    if (S.nxt[sl] != SLOT_NIL) { st |= ST_CYCLE; to[e] = HOP_END; len[e] = 0; continue; }
-    uint32_t dst = HOP_END;
+    const uint32_t v = S.nv[sl];
+    if ((v >> 16) != SLOT_NIL) { st |= ST_CYCLE; to[e] = HOP_END; len[e] = 0; j64[e] = HOP_END; continue; }
     int tx, ty;
     slot_cell(S.tail[sl], tx, ty);
-    const int n = succ_local(g, kind, tx, ty, code, ox, oy);
-    if (n == 1) {
-      const int vx = ox[0] >> 1, vy = oy[0] >> 1;
-      if (!(vx >= tx0 && vx < tx0 + TX && vy >= ty0 && vy < ty0 + TY)) dst = edge_id(g, ox[0], oy[0]);
+    const int kind = chain_kind(code(tx, ty), tx, ty);
+    uint32_t dst = HOP_END;
+    int n = 0;
+    if (kind >= 0) {
+      n = succ_local(g, kind, tx, ty, code, ox, oy);
+      if (n == 1 && !in_tile(ox[0], oy[0])) dst = edge_id(g, ox[0], oy[0]);
     }
     to[e] = dst;
     // a cell with two successors ends no chain: length 0 marks it for the walkers
-    len[e] = n == 2 ? 0 : S.val[sl];
+    len[e] = n == 2 ? 0 : (uint16_t)(v & 0xFFFFu);
+    uint32_t jv = HOP_END;
+    if (S.jmp[sl] != SLOT_NIL) {
+      int jx, jy;
+      slot_cell(S.jmp[sl], jx, jy);
+      jv = edge_id(g, jx, jy);
+    }
+    j64[e] = jv;
   }
   if (st) atomicOr(status, st);
 }
@@ -393,12 +431,16 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *to0, uint3
 struct ChainArgs {
   const uint32_t *hop_to;
   const uint16_t *hop_len;
+  const uint32_t *j64;
   uint32_t *kc;         // per cp: chains of a saddle handled here (0 otherwise)
   uint32_t *mc;         // per cp: level-0 items
   uint8_t *big;         // per cp: surviving saddle with more than KMAX chains
   uint32_t *cbase;      // exclusive scan of kc
   uint32_t *cstart, *csaddle, *clen, *cnseg, *csegoff;  // per chain
   uint4 *segs;          // (chain, first edge, first level, cells)
+  uint32_t *cofs;       // exclusive scan of clen: each chain's cells in tmp
+  uint32_t *tmp;        // chain-major cells
+  uint4 *blocks;        // per chain slot of a saddle: (first level, last level, alive mask, offset)
   unsigned long long limit;
 };
 
@@ -430,8 +472,8 @@ __global__ void k_chain_count(DiscArgs a, int kind, SeedRuns sr, ChainArgs c) {
   }
 }
 
-// chain starts, lengths and segment counts; the disc length of every
-// saddle handled here (0 for other critical points, big saddles untouched)
+// chain starts, lengths and piece counts; the disc length of every saddle
+// handled here (0 for other critical points, big saddles untouched)
 __global__ void k_chain_len(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, uint32_t *slen) {
   for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < a.ncp; s += gridDim.x * blockDim.x) {
     if (c.big[s]) continue;
@@ -449,7 +491,7 @@ __global__ void k_chain_len(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, uint
           const uint32_t l = c.hop_len[e];
           if (l == 0) { atomicOr(a.status, ST_INVARIANT); break; }  // a chain cell never branches
           L += l;
-          ++nseg;
+          nseg += (l + SEG_MAX - 1) / SEG_MAX;
           if (L > c.limit) { bad = true; break; }
         }
         c.cstart[j] = ch[b]; c.csaddle[j] = s; c.clen[j] = (uint32_t)L; c.cnseg[j] = nseg;
@@ -463,13 +505,19 @@ __global__ void k_chain_len(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, uint
   }
 }
 
+// write pieces of every chain: its hops cut at every SEG_MAX cells
 __global__ void k_chain_segs(long long nchains, ChainArgs c) {
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nchains; k += (long long)gridDim.x * blockDim.x) {
     uint32_t o = c.csegoff[k], end = c.csegoff[k + 1], T = 1;
     for (uint32_t e = c.cstart[k]; e != HOP_END && o < end; e = c.hop_to[e]) {
       const uint32_t l = c.hop_len[e];
       if (l == 0) break;
-      c.segs[o++] = make_uint4((uint32_t)k, e, T, l);
+      uint32_t x = e;
+      for (uint32_t done = 0; done < l && o < end && x != HOP_END; done += SEG_MAX) {
+        const uint32_t w = l - done < (uint32_t)SEG_MAX ? l - done : (uint32_t)SEG_MAX;
+        c.segs[o++] = make_uint4((uint32_t)k, x, T + done, w);
+        if (done + SEG_MAX < l) x = c.j64[x];
+      }
       T += l;
     }
   }
@@ -487,8 +535,9 @@ __global__ void k_level0(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, const u
   }
 }
 
-// one thread per segment: walk its cells (all in one tile) and place them
-__global__ void k_seg_write(DiscArgs a, int kind, ChainArgs c, long long nsegs, const uint32_t *off, uint32_t *out) {
+// one thread per piece (at most SEG_MAX cells of one chain): walk it into
+// the chain's span of tmp
+__global__ void k_seg_write(DiscArgs a, int kind, ChainArgs c, long long nsegs) {
   const GridGeom &g = a.g;
   auto gcode = [&](int qx, int qy) -> uint32_t {
     const uint32_t q = a.codes[(long long)(qy >> 1) * g.vnx + (qx >> 1)];
@@ -496,27 +545,81 @@ __global__ void k_seg_write(DiscArgs a, int kind, ChainArgs c, long long nsegs, 
   };
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nsegs; k += (long long)gridDim.x * blockDim.x) {
     const uint4 sg = c.segs[k];
-    const uint32_t ch = sg.x, s = c.csaddle[ch], K = c.kc[s], cb = c.cbase[s], j = ch - cb;
-    uint32_t L[KMAX];
-    for (uint32_t q = 0; q < K; ++q) L[q] = c.clen[cb + q];
-    const uint32_t base = off[s] + c.mc[s], end = off[s + 1];
+    const uint32_t ch = sg.x;
+    if (sg.z - 1 + sg.w > c.clen[ch]) { atomicOr(a.status, ST_INVARIANT); continue; }
+    uint32_t *dst = c.tmp + c.cofs[ch] + (sg.z - 1);
     int rx, ry;
     edge_cell(g, sg.y, rx, ry);
     for (uint32_t i = 0; i < sg.w; ++i) {
-      const uint32_t t = sg.z + i;
-      uint32_t pos = base;
-      for (uint32_t q = 0; q < K; ++q) {
-        pos += L[q] < t - 1 ? L[q] : t - 1;
-        pos += (q < j && L[q] >= t) ? 1u : 0u;
-      }
-      if (pos >= end) { atomicOr(a.status, ST_INVARIANT); break; }
-      out[pos] = pack_cellid(g.ex0 + rx, g.ey0 + ry);
+      dst[i] = pack_cellid(g.ex0 + rx, g.ey0 + ry);
       if (i + 1 < sg.w) {
         int ox[2], oy[2];
         if (succ_local(g, kind, rx, ry, gcode, ox, oy) != 1) { atomicOr(a.status, ST_INVARIANT); break; }
         rx = ox[0]; ry = oy[0];
       }
     }
+  }
+}
+
+// Per saddle: the level ranges over which the set of alive chains is
+// constant.  Between consecutive distinct chain lengths the disc is a
+// regular interleave of the alive chains.
+__global__ void k_zip_blocks(DiscArgs a, ChainArgs c) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < a.ncp; s += gridDim.x * blockDim.x) {
+    const uint32_t K = c.kc[s], cb = c.cbase[s];
+    if (!K) continue;
+    uint32_t L[KMAX];
+    for (uint32_t q = 0; q < K; ++q) L[q] = c.clen[cb + q];
+    uint32_t prev = 0, P = 0, nb = 0;
+    for (;;) {
+      uint32_t u = 0xFFFFFFFFu, mask = 0;
+      for (uint32_t q = 0; q < K; ++q)
+        if (L[q] > prev) { mask |= 1u << q; u = L[q] < u ? L[q] : u; }
+      if (!mask) break;
+      c.blocks[cb + nb++] = make_uint4(prev + 1, u, mask, P);
+      P += (u - prev) * (uint32_t)__popc(mask);
+      prev = u;
+    }
+    for (; nb < K; ++nb) c.blocks[cb + nb] = make_uint4(1, 0, 0, 0);
+  }
+}
+
+// one warp per block: out[base + P + q] = cell of level t_b + q / a of the
+// (q % a)-th alive chain
+__global__ void __launch_bounds__(256) k_zip(DiscArgs a, ChainArgs c, long long nch, const uint32_t *off, uint32_t *out) {
+  __shared__ uint32_t src[8][KMAX];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long k = w0; k < nch; k += nw) {
+    const uint4 b = c.blocks[k];
+    if (!b.z || b.y < b.x) continue;
+    const uint32_t s = c.csaddle[k], cb = c.cbase[s];
+    const uint32_t na = (uint32_t)__popc(b.z), levels = b.y - b.x + 1;
+    const unsigned long long n64 = (unsigned long long)levels * na;
+    const uint32_t base = off[s] + c.mc[s] + b.w, end = off[s + 1];
+    if ((unsigned long long)base + n64 > end) { if (lane == 0) atomicOr(a.status, ST_INVARIANT); continue; }
+    const uint32_t n = (uint32_t)n64;  // within one disc, whose length fits 32 bits
+    // lane r < na: start in tmp of the r-th alive chain at level t_b
+    if (lane < (int)na) {
+      uint32_t m = b.z;
+      for (int z = 0; z < lane; ++z) m &= m - 1;
+      src[wib][lane] = c.cofs[cb + (uint32_t)__ffs(m) - 1] + b.x - 1;
+    }
+    __syncwarp();
+    uint32_t *o = out + base;
+    if (na == 1) {
+      const uint32_t *p = c.tmp + src[wib][0];
+      for (uint32_t q = lane; q < n; q += 32) o[q] = p[q];
+    } else if (na == 2) {
+      for (uint32_t q = lane; q < n; q += 32) o[q] = c.tmp[src[wib][q & 1] + (q >> 1)];
+    } else {
+      for (uint32_t q = lane; q < n; q += 32) {
+        const uint32_t t = q / na;
+        o[q] = c.tmp[src[wib][q - t * na] + t];
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -580,9 +683,9 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   const long long nF = (long long)((g.rx1 - g.rx0) / 2) * ((g.ry1 - g.ry0) / 2);
   const long long nmax = std::max(std::max(nV, nF), std::max(io.nasc, io.ndes)) + 1;
   const long long nE = 2ll * g.vnx * g.vny;  // edge ids of the ext window
-  // words: 7 ncp + 8 | 4 nmax | 2 (nV + nF) | 2 ncp (kc, mc) + ncp + 1 (cbase) | ncp / 4 (big) | 3 nE (hops)
+  // words: 7 ncp + 8 | 4 nmax | 2 (nV + nF) | 3 ncp + 1 (kc, mc, cbase) | ncp / 4 (big) | 2.5 nE (hops)
   size_t words = (size_t)ncp * 7 + 8 + (size_t)nmax * 4 + (size_t)(nV + nF) * 2 + (size_t)ncp * 3 + 1 +
-                 (size_t)ncp / 4 + 1 + (size_t)nE * 3 + 64;
+                 (size_t)ncp / 4 + 1 + 2 * (size_t)nE + (size_t)nE / 2 + 64;
   uint32_t *buf = nullptr;
   cudaError_t e = hops_attr();
   if (e != cudaSuccess) return e;
@@ -594,24 +697,27 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   uint32_t *gkey[2] = {vt + nmax, vt + nmax + nV}, *gval[2] = {vt + nmax + nV + nF, vt + nmax + 2 * nV + nF};
   uint32_t *kc = gval[1] + nF, *mc = kc + ncp, *cbase = mc + ncp;  // cbase: ncp+1
   uint8_t *big = (uint8_t *)(cbase + ncp + 1);
-  uint32_t *hop_to[2] = {cbase + ncp + 1 + ncp / 4 + 1, cbase + ncp + 1 + ncp / 4 + 1 + nE};
-  uint16_t *hop_len[2] = {(uint16_t *)(hop_to[1] + nE), (uint16_t *)(hop_to[1] + nE) + nE};
+  uint32_t *hop_to = cbase + ncp + 1 + ncp / 4 + 1, *j64 = hop_to + nE;
+  uint16_t *hop_len = (uint16_t *)(j64 + nE);
   const long long gn[2] = {nV, nF};
   auto L = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-  uint32_t *chain_buf = nullptr;
-  uint4 *segs = nullptr;
+  uint32_t *chain_buf = nullptr, *tmp = nullptr;
+  uint4 *segs = nullptr, *blocks = nullptr;
+  auto release = [&]() {
+    if (segs) cudaFreeAsync(segs, st);
+    if (tmp) cudaFreeAsync(tmp, st);
+    if (blocks) cudaFreeAsync(blocks, st);
+    if (chain_buf) cudaFreeAsync(chain_buf, st);
+    segs = nullptr; tmp = nullptr; blocks = nullptr; chain_buf = nullptr;
+  };
 
   if (ncp) {
     k_redir_init<<<nb(ncp), 256, 0, st>>>((uint32_t)ncp, redir);
     k_redir_saddles<<<nb(ncp), 256, 0, st>>>(a, redir);
     DMSC_LAUNCHED(2);
   }
-  {
-    dim3 grid(g.ntx, g.nty, 2);
-    k_disc_hops<<<grid, HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, hop_to[0], hop_to[1], hop_len[0], hop_len[1],
-                                                            io.status);
-    DMSC_LAUNCHED(1);
-  }
+  k_disc_hops<<<dim3(g.ntx, g.nty), HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, hop_to, hop_len, j64, io.status);
+  DMSC_LAUNCHED(1);
   L(cudaMemsetAsync(acnt, 0, sizeof(uint32_t) * ncp * 2, st));
   // extremum discs: vertices -> minima (asc_disc), faces -> maxima (des_disc),
   // grouped by owner with a stable sort (row-major order is the append order)
@@ -649,7 +755,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     }
     SeedRuns sr{val, sstart, scount};
     ChainArgs c{};
-    c.hop_to = hop_to[kind]; c.hop_len = hop_len[kind];
+    c.hop_to = hop_to; c.hop_len = hop_len; c.j64 = j64;
     c.kc = kc; c.mc = mc; c.big = big; c.cbase = cbase; c.limit = io.limit;
     k_chain_count<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c);
     DMSC_LAUNCHED(1);
@@ -658,10 +764,14 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     L(cudaMemcpyAsync(&nch, cbase + ncp, 4, cudaMemcpyDeviceToHost, st));
     L(cudaStreamSynchronize(st));
     if (e != cudaSuccess) break;
+    // per chain: cstart csaddle clen cnseg | csegoff cofs (nch + 1 each)
     L(cudaMallocAsync((void **)&chain_buf, sizeof(uint32_t) * (6ull * nch + 8), st));
+    L(cudaMallocAsync((void **)&blocks, sizeof(uint4) * ((size_t)nch + 1), st));
     if (e != cudaSuccess) break;
     c.cstart = chain_buf; c.csaddle = chain_buf + nch; c.clen = chain_buf + 2 * nch; c.cnseg = chain_buf + 3 * nch;
-    c.csegoff = chain_buf + 4 * nch;  // nch + 1
+    c.csegoff = chain_buf + 4 * nch;      // nch + 1
+    c.cofs = chain_buf + 5 * nch + 1;     // nch + 1
+    c.blocks = blocks;
     k_chain_len<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, slen);
     k_saddle_disc_count<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, slen, io.limit);
     k_add_counts<<<nb(ncp), 256, 0, st>>>((uint32_t)ncp, slen, kind ? dcnt : acnt);
@@ -669,25 +779,34 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     uint32_t *offs = kind ? io.ddoff : io.adoff;
     L(scan_exclusive_u32(kind ? dcnt : acnt, ncp, offs, offs + ncp, st));
     L(scan_exclusive_u32(c.cnseg, nch, c.csegoff, c.csegoff + nch, st));
-    uint32_t tot[2] = {0, 0};
+    L(scan_exclusive_u32(c.clen, nch, c.cofs, c.cofs + nch, st));
+    uint32_t tot[3] = {0, 0, 0};
     L(cudaMemcpyAsync(&tot[0], offs + ncp, 4, cudaMemcpyDeviceToHost, st));
     L(cudaMemcpyAsync(&tot[1], c.csegoff + nch, 4, cudaMemcpyDeviceToHost, st));
+    L(cudaMemcpyAsync(&tot[2], c.cofs + nch, 4, cudaMemcpyDeviceToHost, st));
     L(cudaStreamSynchronize(st));
     if (e != cudaSuccess) break;
     DevBuf<uint32_t> *ob = kind ? io.ddisc : io.adisc;
     L(ob->ensure((size_t)tot[0] + 1));
     L(cudaMallocAsync((void **)&segs, sizeof(uint4) * ((size_t)tot[1] + 1), st));
+    L(cudaMallocAsync((void **)&tmp, sizeof(uint32_t) * ((size_t)tot[2] + 1), st));
     if (e != cudaSuccess) break;
     c.segs = segs;
+    c.tmp = tmp;
     if (nch) {
       k_chain_segs<<<nb(nch), 128, 0, st>>>(nch, c);
       DMSC_LAUNCHED(1);
     }
+    if (tot[1]) {
+      k_seg_write<<<nb(tot[1]), 128, 0, st>>>(a, kind, c, tot[1]);
+      DMSC_LAUNCHED(1);
+    }
+    k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c);
     k_level0<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, offs, ob->p);
     k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);
-    DMSC_LAUNCHED(2);
-    if (tot[1]) {
-      k_seg_write<<<nb(tot[1]), 128, 0, st>>>(a, kind, c, tot[1], offs, ob->p);
+    DMSC_LAUNCHED(3);
+    if (nch) {
+      k_zip<<<nb(32ll * nch), 256, 0, st>>>(a, c, nch, offs, ob->p);
       DMSC_LAUNCHED(1);
     }
     long long n = gn[kind];
@@ -698,13 +817,9 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
       DMSC_LAUNCHED(1);
     }
     (kind ? io.nddisc : io.nadisc) = tot[0];
-    cudaFreeAsync(segs, st);
-    cudaFreeAsync(chain_buf, st);
-    segs = nullptr;
-    chain_buf = nullptr;
+    release();
   }
-  if (segs) cudaFreeAsync(segs, st);
-  if (chain_buf) cudaFreeAsync(chain_buf, st);
+  release();
   cudaFreeAsync(buf, st);
   if (e == cudaSuccess) e = cudaGetLastError();
   return e;

@@ -246,13 +246,23 @@ int dmsc_dataset_writeout_connectivity(dmsc_dataset *d, dmsc_msc **out, void *st
   if (!d->worked) return fail(DMSC_ERR_STATE, "dataset_work has not run");
   CK(cudaSetDevice(d->ctx->device));
   cudaStream_t st = pick(d->ctx, stream);
-  dmsc_msc *m = new dmsc_msc;
+  // a complex passed in is overwritten in place (its device buffers are
+  // reused, growing only when too small); otherwise a new one is made
+  const bool fresh = *out == nullptr;
+  if (!fresh && (*out)->ctx != d->ctx) return fail(DMSC_ERR_BAD_ARG, "complex belongs to another context");
+  dmsc_msc *m = fresh ? new dmsc_msc : *out;
   m->ctx = d->ctx;
   std::memcpy(m->rect, d->rect, 8);
   std::memcpy(m->ext, d->ext, 8);
+  m->nadisc = m->nddisc = 0;
+  for (auto &v : m->simp_stats) v = 0;
   if (d->ctx->timing && d->ev_ready) CK(cudaEventRecord(d->ev[5], st));
   int rc = m->writeout_from(*d, st);
-  if (rc) { delete m; return rc; }
+  if (rc) {
+    if (fresh) delete m;
+    else m->ncp = m->nasc = m->ndes = 0;
+    return rc;
+  }
   if (d->ctx->timing && d->ev_ready) CK(cudaEventRecord(d->ev[6], st));
   *out = m;
   return DMSC_OK;

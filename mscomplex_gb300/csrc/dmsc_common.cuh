@@ -57,6 +57,10 @@ struct GridGeom {
   int rx0, ry0, rx1, ry1; // rect relative to ext (even)
   int ntx, nty;           // tiles of TX x TY vertices
   long long pitch;        // height row pitch in elements (>= vnx)
+  // Offsets of this grid's border slots and row segments in tables shared by
+  // a batch of grids (0 for a grid on its own): the border table's EXIT and
+  // ROOT entries carry batch-wide indices.
+  long long sbase = 0, gbase = 0;
 };
 
 __host__ __device__ __forceinline__ uint32_t pack_cellid(int x, int y) {

@@ -23,6 +23,22 @@ struct CpOut {
   long long cap;      // capacity of every array above (in critical points)
 };
 
+// One grid of a batch: its geometry (with batch-wide slot / segment bases)
+// and its parts of the batch's packed arrays.
+struct BatchGrid {
+  GridGeom g;
+  const float *hgt;
+  uint32_t *codes, *terms;
+  uint4 *labels;
+  uint8_t *rowcnt;
+  uint64_t *table;
+  const uint32_t *offsets;  // the batch's cp offsets from this grid's first row segment on
+  long long tile0;          // first tile of this grid in the batch's tile numbering
+};
+cudaError_t launch_gradient_batch(const BatchGrid *grids, int ngrids, long long ntiles, uint32_t *status, cudaStream_t st);
+cudaError_t launch_labels_batch(const BatchGrid *grids, int ngrids, long long ntiles, const CpOut &cp, uint32_t *status,
+                                cudaStream_t st);
+
 size_t grad_smem_bytes();
 size_t label_smem_bytes();
 cudaError_t launch_gradient(const float *hgt, const GridGeom &g, uint32_t *codes, uint32_t *terms, uint8_t *rowcnt,
@@ -77,6 +93,29 @@ cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st);
 
 cudaError_t simplify_emit(SimplifyIO &io, uint32_t *asc, uint32_t *des, cudaStream_t st);
 void simplify_release(SimplifyIO &io, cudaStream_t st);
+
+// Simplification of many complexes held in shared arrays (a batch): critical
+// points of grid g are [cpb[g], cpb[g+1]) with list values local to the grid;
+// one block per grid with tresh > 0.  flags / pair_idx are edited in place.
+struct BatchSimplifyIO {
+  long long ncp = 0, nasc = 0, ndes = 0;  // batch totals
+  const uint32_t *cellid = nullptr;
+  const float *fn = nullptr;
+  uint8_t *flags = nullptr;
+  uint32_t *pair_idx = nullptr;
+  uint32_t *aoff = nullptr, *asc = nullptr, *doff = nullptr, *des = nullptr;  // offsets rewritten by the run
+  int ngrids = 0;
+  const uint32_t *cpb = nullptr, *abase = nullptr, *dbase = nullptr;  // host, ngrids + 1 each
+  const double *tresh = nullptr;  // host, per grid
+  const int *rect = nullptr;      // host, 4 per grid
+  unsigned long long max_ops = 0;
+  unsigned long long *host_stats = nullptr;  // host, 5 per grid
+  long long nasc_out = 0, ndes_out = 0;
+  void *work = nullptr;
+};
+cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st);
+cudaError_t simplify_batch_emit(BatchSimplifyIO &io, uint32_t *asc, uint32_t *des, cudaStream_t st);
+void simplify_batch_release(BatchSimplifyIO &io, cudaStream_t st);
 
 }  // namespace dmsc
 template <typename T> struct DevBuf;

@@ -36,6 +36,8 @@
 // K1 follows the V-paths by pointer jumping in shared memory inside a tile
 // and writes each cell's in-tile terminal; paths leaving the tile end at a
 // border cell, and only the border table is resolved globally (K3).
+#include <algorithm>
+
 #include "dmsc_common.cuh"
 #include "dmsc_internal.h"
 
@@ -181,13 +183,13 @@ struct GradSmem {
   uint32_t code[TY][TX];
 };
 
-__global__ void __launch_bounds__(GRAD_THREADS, 3)
-k_gradient(const float *__restrict__ hgt, GridGeom g, uint32_t *__restrict__ codes, uint32_t *__restrict__ terms,
-           uint8_t *__restrict__ rowcnt, uint64_t *__restrict__ table, uint32_t *__restrict__ status) {
+// K1 on tile (bx, by) of one grid.
+__device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, const GridGeom &g, uint32_t *__restrict__ codes,
+                                              uint32_t *__restrict__ terms, uint8_t *__restrict__ rowcnt,
+                                              uint64_t *__restrict__ table, uint32_t *__restrict__ status, int bx, int by) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   GradSmem &s = *reinterpret_cast<GradSmem *>(smem_raw);
   GradPhase1 &A = s.u.a;
-  const int bx = blockIdx.x, by = blockIdx.y;
   const int tx0 = bx * TX, ty0 = by * TY;
   int w, h, wf, hf;
   tile_extent(g, bx, by, 0, w, h);
@@ -357,17 +359,44 @@ k_gradient(const float *__restrict__ hgt, GridGeom g, uint32_t *__restrict__ cod
       if ((p & PJ_TAG) == PJ_ROOT) {
         int y = 2 * (ty0 + kj) + kind;
         uint32_t rank = kind ? (uint32_t)B.rankB[kj][ki] + ((s.code[kj][ki] >> 19) & 1) : B.rankA[kj][ki];
-        entry = BT_ROOT | ((uint64_t)((long long)y * g.ntx + bx) << 8) | rank;
+        entry = BT_ROOT | ((uint64_t)((long long)y * g.ntx + bx + g.gbase) << 8) | rank;
       } else if ((p & PJ_TAG) == PJ_EXIT) {
         uint32_t d = (kind ? (s.code[kj][ki] >> 24) : s.code[kj][ki]) & 3;
         int gi = tx0 + ki + dir_dx(d), gj = ty0 + kj + dir_dy(d);
-        if (gi >= 0 && gj >= 0 && gi < g.vnx - kind && gj < g.vny - kind) entry = BT_EXIT | (uint64_t)border_slot(g, kind, gi, gj);
+        if (gi >= 0 && gj >= 0 && gi < g.vnx - kind && gj < g.vny - kind) entry = BT_EXIT | (uint64_t)(border_slot(g, kind, gi, gj) + g.sbase);
         else st |= ST_CYCLE;  // a path leaving the window: never expected
       }
     }
     table[tile_base + kind * SLOTS_SIDE + b] = entry;
   }
   if (st) atomicOr(status, st);
+}
+
+__global__ void __launch_bounds__(GRAD_THREADS, 3)
+k_gradient(const float *__restrict__ hgt, GridGeom g, uint32_t *__restrict__ codes, uint32_t *__restrict__ terms,
+           uint8_t *__restrict__ rowcnt, uint64_t *__restrict__ table, uint32_t *__restrict__ status) {
+  gradient_tile(hgt, g, codes, terms, rowcnt, table, status, blockIdx.x, blockIdx.y);
+}
+
+// The grid of batch tile t (tiles numbered grid after grid).
+__device__ __forceinline__ int batch_grid_of(const BatchGrid *G, int ngrids, long long t) {
+  int lo = 0, hi = ngrids - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (G[mid].tile0 <= t) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// K1 over a batch: a persistent grid of blocks takes (grid, tile) items in order.
+__global__ void __launch_bounds__(GRAD_THREADS, 3)
+k_gradient_batch(const BatchGrid *__restrict__ G, int ngrids, long long ntiles, uint32_t *__restrict__ status) {
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BatchGrid &B = G[batch_grid_of(G, ngrids, t)];
+    const long long lt = t - B.tile0;
+    gradient_tile(B.hgt, B.g, B.codes, B.terms, B.rowcnt, B.table, status, (int)(lt % B.g.ntx), (int)(lt / B.g.ntx));
+    __syncthreads();  // shared memory is reused by the next item
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -434,13 +463,14 @@ __device__ __forceinline__ float cell_fn(const float *hgt, const GridGeom &g, in
   }
 }
 
-__global__ void __launch_bounds__(GRAD_THREADS, 3)
-k_labels(const uint32_t *__restrict__ codes, const uint32_t *__restrict__ terms, const float *__restrict__ hgt, GridGeom g,
-         const uint32_t *__restrict__ offsets, const uint64_t *__restrict__ table, uint4 *__restrict__ labels,
-         CpOut cp, uint32_t *__restrict__ status) {
+// K4 on tile (bx, by) of one grid.
+__device__ __forceinline__ void labels_tile(const uint32_t *__restrict__ codes, const uint32_t *__restrict__ terms,
+                                            const float *__restrict__ hgt, const GridGeom &g,
+                                            const uint32_t *__restrict__ offsets, const uint64_t *__restrict__ table,
+                                            uint4 *__restrict__ labels, const CpOut &cp, uint32_t *__restrict__ status,
+                                            int bx, int by) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   LabelSmem &s = *reinterpret_cast<LabelSmem *>(smem_raw);
-  const int bx = blockIdx.x, by = blockIdx.y;
   const int tx0 = bx * TX, ty0 = by * TY;
   int w, h, wf, hf;
   tile_extent(g, bx, by, 0, w, h);
@@ -577,6 +607,25 @@ k_labels(const uint32_t *__restrict__ codes, const uint32_t *__restrict__ terms,
   if (st) atomicOr(status, st);
 }
 
+__global__ void __launch_bounds__(GRAD_THREADS, 3)
+k_labels(const uint32_t *__restrict__ codes, const uint32_t *__restrict__ terms, const float *__restrict__ hgt, GridGeom g,
+         const uint32_t *__restrict__ offsets, const uint64_t *__restrict__ table, uint4 *__restrict__ labels,
+         CpOut cp, uint32_t *__restrict__ status) {
+  labels_tile(codes, terms, hgt, g, offsets, table, labels, cp, status, blockIdx.x, blockIdx.y);
+}
+
+// K4 over a batch; cp indices (and so labels) are batch-wide.
+__global__ void __launch_bounds__(GRAD_THREADS, 3)
+k_labels_batch(const BatchGrid *__restrict__ G, int ngrids, long long ntiles, CpOut cp, uint32_t *__restrict__ status) {
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BatchGrid &B = G[batch_grid_of(G, ngrids, t)];
+    const long long lt = t - B.tile0;
+    labels_tile(B.codes, B.terms, B.hgt, B.g, B.offsets, B.table, B.labels, cp, status, (int)(lt % B.g.ntx),
+                (int)(lt / B.g.ntx));
+    __syncthreads();
+  }
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -619,6 +668,35 @@ cudaError_t launch_labels(const uint32_t *codes, const uint32_t *terms, const fl
   }
   dim3 grid(g.ntx, g.nty);
   k_labels<<<grid, GRAD_THREADS, sizeof(LabelSmem), st>>>(codes, terms, hgt, g, offsets, table, labels, cp, status);
+  DMSC_LAUNCHED(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gradient_batch(const BatchGrid *grids, int ngrids, long long ntiles, uint32_t *status, cudaStream_t st) {
+  static bool init = false;
+  if (!init) {
+    cudaError_t e = cudaFuncSetAttribute(k_gradient_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradSmem));
+    if (e != cudaSuccess) return e;
+    init = true;
+  }
+  if (ntiles <= 0) return cudaSuccess;
+  const long long blocks = std::min<long long>(ntiles, 152LL * 3);
+  k_gradient_batch<<<(unsigned)blocks, GRAD_THREADS, sizeof(GradSmem), st>>>(grids, ngrids, ntiles, status);
+  DMSC_LAUNCHED(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_labels_batch(const BatchGrid *grids, int ngrids, long long ntiles, const CpOut &cp, uint32_t *status,
+                                cudaStream_t st) {
+  static bool init = false;
+  if (!init) {
+    cudaError_t e = cudaFuncSetAttribute(k_labels_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LabelSmem));
+    if (e != cudaSuccess) return e;
+    init = true;
+  }
+  if (ntiles <= 0) return cudaSuccess;
+  const long long blocks = std::min<long long>(ntiles, 152LL * 3);
+  k_labels_batch<<<(unsigned)blocks, GRAD_THREADS, sizeof(LabelSmem), st>>>(grids, ngrids, ntiles, cp, status);
   DMSC_LAUNCHED(1);
   return cudaGetLastError();
 }

@@ -23,6 +23,8 @@
 #include "dmsc_internal.h"
 #include "msc_graph.cuh"
 
+#include <vector>
+
 namespace dmsc {
 
 struct HeapEnt {
@@ -343,6 +345,163 @@ cudaError_t simplify_emit(SimplifyIO &io, uint32_t *asc, uint32_t *des, cudaStre
 
 void simplify_release(SimplifyIO &io, cudaStream_t st) {
   SimplifyWork *w = (SimplifyWork *)io.work;
+  if (!w) return;
+  if (w->buf) cudaFreeAsync(w->buf, st);
+  delete w;
+  io.work = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// batches: one block per complex to simplify, all in one launch
+// ---------------------------------------------------------------------------
+__global__ void k_simplify_batch(SimpArgs *args, int n) {
+  if (threadIdx.x != 0 || blockIdx.x >= (unsigned)n) return;
+  Simp s;
+  s.A = args[blockIdx.x];
+  s.run();
+  s.A.stats[3] = s.A.G.ops;
+  if (s.A.G.fail) s.A.stats[4] |= ST_SIMPLIFY_LIMIT;
+}
+
+struct BatchSimplifyWork {
+  char *buf = nullptr;
+  uint32_t *off = nullptr, *nrun = nullptr, *lcap = nullptr, *total = nullptr, *lens = nullptr;
+  uint2 *pool = nullptr;
+  SimpArgs *dargs = nullptr;
+  unsigned long long *dstats = nullptr;
+  int nsimp = 0;
+};
+
+cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
+  const uint32_t ncp = (uint32_t)io.ncp;
+  const unsigned long long des_base = (unsigned long long)io.nasc + 4ull * ncp;
+  const unsigned long long base_top = des_base + (unsigned long long)io.ndes + 4ull * ncp;
+  // per simplified grid: pool growth region, heap, resubmits, cancellations, scratch runs
+  std::vector<int> which;
+  unsigned long long grow = 0, heap = 0, canc = 0, tmp = 0;
+  for (int g = 0; g < io.ngrids; ++g) {
+    const unsigned long long n = io.cpb[g + 1] - io.cpb[g];
+    if (!(io.tresh[g] > 0.0) || n == 0) continue;
+    const unsigned long long na = io.abase[g + 1] - io.abase[g], nd = io.dbase[g + 1] - io.dbase[g];
+    which.push_back(g);
+    grow += 2 * (na + nd + 8 * n) + 4096;
+    heap += 4 * nd + 1024;
+    canc += n + 1;
+    tmp += 2 * (na + nd) + 65536;
+  }
+  const unsigned long long pool_cap = base_top + grow;
+  if (pool_cap > 0xffffffffull) return cudaErrorInvalidValue;  // list offsets are 32-bit
+  const int ns = (int)which.size();
+  auto rnd = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t sizes[] = {4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * (ncp + 1),
+                          sizeof(uint2) * pool_cap, sizeof(uint2) * tmp, sizeof(HeapEnt) * heap, sizeof(uint2) * heap,
+                          sizeof(uint2) * canc, sizeof(unsigned long long) * 8 * (size_t)(ns + 1),
+                          sizeof(SimpArgs) * (size_t)(ns + 1)};
+  size_t bytes = 0;
+  for (size_t z : sizes) bytes += rnd(z);
+  BatchSimplifyWork *w = new BatchSimplifyWork;
+  io.work = w;
+  cudaError_t e = cudaMallocAsync((void **)&w->buf, bytes, st);
+  if (e != cudaSuccess) { w->buf = nullptr; return e; }
+  char *p = w->buf;
+  int si = 0;
+  auto take = [&]() { char *r = p; p += rnd(sizes[si++]); return r; };
+  w->off = (uint32_t *)take(); w->nrun = (uint32_t *)take(); w->lcap = (uint32_t *)take(); w->total = (uint32_t *)take();
+  w->lens = (uint32_t *)take();
+  w->pool = (uint2 *)take();
+  uint2 *dtmp = (uint2 *)take();
+  HeapEnt *dheap = (HeapEnt *)take();
+  uint2 *dres = (uint2 *)take();
+  uint2 *dcanc = (uint2 *)take();
+  w->dstats = (unsigned long long *)take();
+  w->dargs = (SimpArgs *)take();
+  w->nsimp = ns;
+  if (ncp) {
+    k_lists_from_csr<<<blocks_for(ncp), 256, 0, st>>>(ncp, io.aoff, io.asc, io.doff, io.des, des_base, w->off, w->nrun,
+                                                       w->lcap, w->total, w->pool);
+    DMSC_LAUNCHED(1);
+  }
+  e = cudaMemsetAsync(w->dstats, 0, sizeof(unsigned long long) * 8 * (size_t)(ns + 1), st);
+  std::vector<SimpArgs> args(ns);
+  unsigned long long top = base_top, ho = 0, co = 0, to = 0;
+  for (int k = 0; k < ns && e == cudaSuccess; ++k) {
+    const int g = which[k];
+    const unsigned long long c0 = io.cpb[g], n = io.cpb[g + 1] - c0;
+    const unsigned long long na = io.abase[g + 1] - io.abase[g], nd = io.dbase[g + 1] - io.dbase[g];
+    SimpArgs &a = args[k];
+    Graph &G = a.G;
+    G = Graph();
+    G.ncp = (uint32_t)n;
+    G.cellid = const_cast<uint32_t *>(io.cellid) + c0;
+    G.flags = io.flags + c0;
+    G.pair_idx = io.pair_idx + c0;
+    G.L.off = w->off + 2 * c0; G.L.nrun = w->nrun + 2 * c0; G.L.cap = w->lcap + 2 * c0; G.L.total = w->total + 2 * c0;
+    G.L.pool = w->pool;
+    G.L.top = top;
+    top += 2 * (na + nd + 8 * n) + 4096;
+    G.L.pool_cap = top;
+    G.tmp = dtmp + to;
+    G.tmp_cap = 2 * (na + nd) + 65536;
+    to += G.tmp_cap;
+    G.max_ops = io.max_ops;
+    G.ops = 0;
+    G.fail = false;
+    a.fn = io.fn + c0;
+    a.heap = dheap + ho;
+    a.resub = dres + ho;
+    a.heap_cap = 4 * nd + 1024;
+    ho += a.heap_cap;
+    a.canc = dcanc + co;
+    co += n + 1;
+    a.rx0 = io.rect[4 * g]; a.ry0 = io.rect[4 * g + 1]; a.rx1 = io.rect[4 * g + 2]; a.ry1 = io.rect[4 * g + 3];
+    a.tresh = io.tresh[g];
+    a.stats = w->dstats + 8 * k;
+  }
+  if (e == cudaSuccess && ns) e = cudaMemcpyAsync(w->dargs, args.data(), sizeof(SimpArgs) * ns, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && ns) {
+    k_simplify_batch<<<ns, 32, 0, st>>>(w->dargs, ns);
+    DMSC_LAUNCHED(1);
+    e = cudaGetLastError();
+  }
+  std::vector<unsigned long long> hs(8 * (size_t)(ns + 1), 0);
+  if (e == cudaSuccess && ns) e = cudaMemcpyAsync(hs.data(), w->dstats, sizeof(unsigned long long) * 8 * ns, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  for (int g = 0; g < io.ngrids; ++g)
+    for (int q = 0; q < 5; ++q) io.host_stats[5 * g + q] = 0;
+  bool bad = false;
+  for (int k = 0; k < ns; ++k) {
+    for (int q = 0; q < 5; ++q) io.host_stats[5 * which[k] + q] = hs[8 * k + q];
+    bad |= hs[8 * k + 4] != 0;
+  }
+  if (bad || !ncp) return cudaSuccess;  // the caller reads the per-grid status
+  for (int wch = 0; wch < 2 && e == cudaSuccess; ++wch) {
+    uint32_t *offs = wch ? io.doff : io.aoff;
+    k_pick_len<<<blocks_for(ncp), 256, 0, st>>>(ncp, w->total, wch, w->lens);
+    DMSC_LAUNCHED(1);
+    e = scan_exclusive_u32(w->lens, ncp, offs, offs + ncp, st);
+  }
+  uint32_t tot[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&tot[0], io.aoff + ncp, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&tot[1], io.doff + ncp, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  io.nasc_out = tot[0];
+  io.ndes_out = tot[1];
+  return e;
+}
+
+cudaError_t simplify_batch_emit(BatchSimplifyIO &io, uint32_t *asc, uint32_t *des, cudaStream_t st) {
+  BatchSimplifyWork *w = (BatchSimplifyWork *)io.work;
+  const uint32_t ncp = (uint32_t)io.ncp;
+  if (!w || !ncp) return cudaSuccess;
+  k_csr_from_lists<<<blocks_for(ncp), 256, 0, st>>>(ncp, w->off, w->nrun, w->pool, 0, io.aoff, asc);
+  k_csr_from_lists<<<blocks_for(ncp), 256, 0, st>>>(ncp, w->off, w->nrun, w->pool, 1, io.doff, des);
+  DMSC_LAUNCHED(2);
+  return cudaGetLastError();
+}
+
+void simplify_batch_release(BatchSimplifyIO &io, cudaStream_t st) {
+  BatchSimplifyWork *w = (BatchSimplifyWork *)io.work;
   if (!w) return;
   if (w->buf) cudaFreeAsync(w->buf, st);
   delete w;

@@ -142,7 +142,13 @@ class GridDataset:
         check(self.lib.dmsc_dataset_fill_discs(self.h, msc.h, stream))
         return msc
 
-    def writeout_connectivity(self, stream=None) -> "GridMSComplex":
+    def writeout_connectivity(self, msc: "GridMSComplex | None" = None, stream=None) -> "GridMSComplex":
+        """GridDataset::writeout_connectivity: the complex of this piece.  With
+        `msc`, that complex is overwritten in place (its buffers are reused)."""
+        if msc is not None:
+            h = C.c_void_p(msc.h.value if isinstance(msc.h, C.c_void_p) else msc.h)
+            check(self.lib.dmsc_dataset_writeout_connectivity(self.h, C.byref(h), stream))
+            return msc
         h = C.c_void_p()
         check(self.lib.dmsc_dataset_writeout_connectivity(self.h, C.byref(h), stream))
         return GridMSComplex(h, self.ctx)
@@ -184,21 +190,33 @@ class GridMSComplex:
         check(self.lib.dmsc_msc_sizes(self.h, _ptr(s)))
         return [int(v) for v in s]
 
-    def export(self) -> dict:
-        """Flat arrays with the same keys as the oracle's complex dump."""
+    EXPORT_KEYS = ("rect_ext", "cellid", "fn", "pair_idx", "flags", "asc_off", "asc", "des_off", "des",
+                   "adisc_off", "adisc", "ddisc_off", "ddisc")
+
+    def export_shapes(self) -> dict:
         n, na, nd, nad, ndd = self.sizes()
-        d = dict(
-            rect_ext=np.zeros(8, np.int16),
-            cellid=np.zeros((n, 2), np.int16), fn=np.zeros(n, np.float32),
-            pair_idx=np.zeros(n, np.uint32), flags=np.zeros(n, np.uint8),
-            asc_off=np.zeros(n + 1, np.uint32), asc=np.zeros(na, np.uint32),
-            des_off=np.zeros(n + 1, np.uint32), des=np.zeros(nd, np.uint32),
-            adisc_off=np.zeros(n + 1, np.uint32), adisc=np.zeros((nad, 2), np.int16),
-            ddisc_off=np.zeros(n + 1, np.uint32), ddisc=np.zeros((ndd, 2), np.int16),
-        )
-        keys = ("rect_ext", "cellid", "fn", "pair_idx", "flags", "asc_off", "asc", "des_off", "des",
-                "adisc_off", "adisc", "ddisc_off", "ddisc")
-        check(self.lib.dmsc_msc_export(self.h, *(_ptr(d[k]) for k in keys), None))
+        return dict(rect_ext=((8,), np.int16), cellid=((n, 2), np.int16), fn=((n,), np.float32),
+                    pair_idx=((n,), np.uint32), flags=((n,), np.uint8), asc_off=((n + 1,), np.uint32),
+                    asc=((na,), np.uint32), des_off=((n + 1,), np.uint32), des=((nd,), np.uint32),
+                    adisc_off=((n + 1,), np.uint32), adisc=((nad, 2), np.int16),
+                    ddisc_off=((n + 1,), np.uint32), ddisc=((ndd, 2), np.int16))
+
+    def export(self, out: dict | None = None) -> dict:
+        """Flat arrays with the same keys as the oracle's complex dump.  `out`
+        may hold preallocated flat host buffers (e.g. pinned) per key, large
+        enough: the result is then views into them."""
+        shapes = self.export_shapes()
+        if out is None:
+            d = {k: np.zeros(sh, dt) for k, (sh, dt) in shapes.items()}
+        else:
+            d = {}
+            for k, (sh, dt) in shapes.items():
+                n = int(np.prod(sh))
+                buf = out[k].view(dt).reshape(-1)
+                if buf.size < n:
+                    raise ValueError(f"export buffer {k} holds {buf.size} < {n} elements")
+                d[k] = buf[:n].reshape(sh)
+        check(self.lib.dmsc_msc_export(self.h, *(_ptr(d[k]) for k in self.EXPORT_KEYS), None))
         return d
 
 
@@ -261,3 +279,99 @@ class GridDataManager:
         ms = np.zeros(5, np.float64)
         check(self.lib.dmsc_pipeline_stage_times(self.h, _ptr(ms)))
         return dict(zip(self.STAGES, (float(v) for v in ms)))
+
+
+class GridBatch:
+    """Many whole grids through work + writeout_connectivity +
+    simplify_un_simplify in shared launches (no reference counterpart: the
+    reference builds one GridDataset at a time).  fields: 2D float32 arrays
+    (size_y, size_x), or one packed 1D array/tensor with `shapes`; tresh: one
+    threshold per grid (0 skips simplification)."""
+
+    GRAPH_KEYS = ("rect_ext", "cellid", "fn", "pair_idx", "flags", "asc_off", "asc", "des_off", "des")
+
+    def __init__(self, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.lib = self.ctx.lib
+        self.h = C.c_void_p()
+        self.n = 0
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.lib.dmsc_batch_destroy(self.h)
+            self.h = None
+
+    @staticmethod
+    def pack(fields):
+        """(packed float32 heights, sizes int32[2n]) of a list of 2D fields."""
+        sizes = np.array([[f.shape[1], f.shape[0]] for f in fields], np.int32).reshape(-1)
+        packed = np.concatenate([np.ascontiguousarray(f, np.float32).reshape(-1) for f in fields])
+        return packed, sizes
+
+    def run(self, fields=None, tresh=0.0, *, packed=None, sizes=None, max_ops: int = 0, stream=None):
+        if fields is not None:
+            packed, sizes = self.pack(fields)
+        sizes = np.ascontiguousarray(sizes, np.int32).reshape(-1)
+        n = sizes.size // 2
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(tresh, np.float64), (n,)))
+        if hasattr(packed, "is_cuda") and packed.is_cuda:
+            if packed.dtype.__repr__() != "torch.float32" or not packed.is_contiguous():
+                raise ValueError("device heights must be a contiguous float32 tensor")
+            if stream is None:
+                import torch
+                torch.cuda.current_stream(packed.device).synchronize()
+            self._keep = packed
+            ptr, on_dev = C.c_void_p(packed.data_ptr()), 1
+        else:
+            packed = np.ascontiguousarray(packed, np.float32)
+            self._keep = packed
+            ptr, on_dev = _ptr(packed), 0
+        check(self.lib.dmsc_batch_run(self.ctx.h, n, _ptr(sizes), ptr, on_dev, _ptr(t), int(max_ops),
+                                      C.byref(self.h), stream))
+        self.n = n
+        self._sizes = sizes
+        return self
+
+    def sizes(self, i: int):
+        s = np.zeros(3, np.int64)
+        check(self.lib.dmsc_batch_sizes(self.h, int(i), _ptr(s)))
+        return [int(v) for v in s]
+
+    def simplify_stats(self, i: int) -> dict:
+        a = np.zeros(5, np.uint64)
+        check(self.lib.dmsc_batch_simplify_stats(self.h, int(i), _ptr(a)))
+        return dict(zip(("pushes", "pops", "cancels", "ops", "status"), (int(v) for v in a)))
+
+    def export(self, i: int) -> dict:
+        n, na, nd = self.sizes(i)
+        d = dict(rect_ext=np.zeros(8, np.int16), cellid=np.zeros((n, 2), np.int16), fn=np.zeros(n, np.float32),
+                 pair_idx=np.zeros(n, np.uint32), flags=np.zeros(n, np.uint8), asc_off=np.zeros(n + 1, np.uint32),
+                 asc=np.zeros(na, np.uint32), des_off=np.zeros(n + 1, np.uint32), des=np.zeros(nd, np.uint32))
+        check(self.lib.dmsc_batch_export(self.h, int(i), *(_ptr(d[k]) for k in self.GRAPH_KEYS), None))
+        return d
+
+    def totals(self):
+        t = np.zeros(3, np.int64)
+        check(self.lib.dmsc_batch_totals(self.h, _ptr(t)))
+        return [int(v) for v in t]
+
+    def export_all(self, out: dict | None = None) -> dict:
+        """All grids at once (shared arrays plus per-grid bases); `out` may
+        hold preallocated flat host buffers per key."""
+        ncp, na, nd = self.totals()
+        g1 = self.n + 1
+        shapes = dict(cp_base=(g1, np.uint32), asc_base=(g1, np.uint32), des_base=(g1, np.uint32),
+                      cellid=(ncp, np.uint32), fn=(ncp, np.float32), pair_idx=(ncp, np.uint32), flags=(ncp, np.uint8),
+                      asc_off=(ncp + 1, np.uint32), asc=(na, np.uint32), des_off=(ncp + 1, np.uint32),
+                      des=(nd, np.uint32))
+        d = {}
+        for k, (m, dt) in shapes.items():
+            if out is None:
+                d[k] = np.zeros(m, dt)
+            else:
+                buf = out[k].view(dt).reshape(-1)
+                if buf.size < m:
+                    raise ValueError(f"export buffer {k} holds {buf.size} < {m} elements")
+                d[k] = buf[:m]
+        check(self.lib.dmsc_batch_export_all(self.h, *(_ptr(d[k]) for k in shapes), None))
+        return d

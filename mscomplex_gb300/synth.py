@@ -76,3 +76,11 @@ def mixed_grid(side: int, seed: int, quantize: int = 0) -> np.ndarray:
     rng = np.random.default_rng(seed)
     nb = max(1, int(round(side * side / 8192)))
     return gaussian_bumps(side, side, nb, 4.0, 32.0, rng, quantize=quantize)
+
+
+def batch_fields(count: int = 1000, seed: int = 3, lo: int = 64, hi: int = 2048) -> list:
+    """The mixed-size batch: sides log-uniform in [lo, hi], each grid a sum of
+    Gaussians (count proportional to area / 8192, sigma U(4, 32)) with its own
+    seed."""
+    sides = mixed_batch_sides(count, seed, lo, hi)
+    return [mixed_grid(int(s), seed * 1000003 + i) for i, s in enumerate(sides)]
