@@ -174,6 +174,81 @@ def cpu_baseline(field: np.ndarray, side: int = 1024):
                       f"postMergeFillDiscs) in {secs:.2f} s"}
 
 
+BATCH_WORKLOAD = ("batch_fields: 1000 grids, sides log-uniform in [64, 2048], each a float32 sum of Gaussians "
+                  "(count = area / 8192, sigma U(4, 32)), seed 3; work + writeout_connectivity + "
+                  "simplify_un_simplify at 2% of each grid's range")
+
+
+def bench_batched(M, torch, stream, sh, steps=2, warmup=1, count=1000):
+    """Mixed-size batch: one batched pass over all grids versus one plain
+    per-grid pass (dataset, work, writeout_connectivity, simplify per grid),
+    both from heights resident in HBM; e2e batch from pinned host heights to
+    every complex in pinned host memory.  Returns the JSON object."""
+    from mscomplex_gb300 import synth
+    fields = synth.batch_fields(count)
+    packed, sizes = M.GridBatch.pack(fields)
+    nverts = int(packed.size)
+    dev = torch.from_numpy(packed).cuda()
+    torch.cuda.synchronize()
+    tresh = 0.02
+    b = M.GridBatch()
+    for _ in range(max(1, warmup)):
+        b.run(packed=dev, sizes=sizes, tresh=tresh, stream=sh)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        b.run(packed=dev, sizes=sizes, tresh=tresh, stream=sh)
+    e1.record(stream)
+    e1.synchronize()
+    batch_s = e0.elapsed_time(e1) / 1e3 / steps
+    # plain: one grid at a time through the per-grid API
+    offs = np.concatenate([[0], np.cumsum(sizes[0::2].astype(np.int64) * sizes[1::2])])
+    views = [dev[offs[i]:offs[i + 1]].view(int(sizes[2 * i + 1]), int(sizes[2 * i])) for i in range(count)]
+    def plain(check_idx=()):
+        outs = {}
+        for i, v in enumerate(views):
+            r = (0, 0, 2 * (v.shape[1] - 1), 2 * (v.shape[0] - 1))
+            ds = M.GridDataset(r, r).init(v, stream=sh).work(stream=sh)
+            m = ds.writeout_connectivity(stream=sh)
+            m.simplify_un_simplify(tresh, stream=sh)
+            if i in check_idx:
+                outs[i] = m.export()
+        return outs
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ref = plain(check_idx=set(range(0, count, max(1, count // 16))))
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    keys = M.GridBatch.GRAPH_KEYS
+    exact = all(all(np.array_equal(np.asarray(b.export(i)[k]).view(np.uint8), np.asarray(ref[i][k]).view(np.uint8))
+                    for k in keys) for i in ref)
+    # e2e: pinned host heights in, every complex out into pinned host memory
+    host = torch.from_numpy(packed).pin_memory()
+    ncp, na, nd = b.totals()
+    pinned = {k: torch.empty(max(16, 4 * (m * 5 // 4 + 16)), dtype=torch.uint8).pin_memory().numpy()
+              for k, m in (("cp_base", count + 1), ("asc_base", count + 1), ("des_base", count + 1), ("cellid", ncp),
+                           ("fn", ncp), ("pair_idx", ncp), ("flags", ncp), ("asc_off", ncp + 1), ("asc", na),
+                           ("des_off", ncp + 1), ("des", nd))}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(steps):
+        d = host.to("cuda", non_blocking=True)
+        b.run(packed=d, sizes=sizes, tresh=tresh, stream=sh)
+        out = b.export_all(pinned)
+        d2h = sum(v.nbytes for v in out.values())
+    e2e_s = (time.perf_counter() - t0) / steps
+    st = [b.simplify_stats(i) for i in range(count)]
+    return {"workload": BATCH_WORKLOAD, "grids": count, "vertices": nverts, "critical_points": ncp,
+            "batched_grids_per_s": round(count / batch_s, 2), "batched_mvert_per_s": round(nverts / batch_s / 1e6, 2),
+            "batched_ms": round(batch_s * 1e3, 3), "plain_grids_per_s": round(count / plain_s, 2),
+            "plain_ms": round(plain_s * 1e3, 3), "speedup_vs_plain": round(plain_s / batch_s, 2),
+            "e2e_grids_per_s": round(count / e2e_s, 2), "e2e_h2d_bytes": int(packed.nbytes), "e2e_d2h_bytes": int(d2h),
+            "bit_exact_vs_plain": bool(exact), "checked_grids": len(ref),
+            "max_simplify_pops": max(x["pops"] for x in st), "total_simplify_pops": sum(x["pops"] for x in st)}
+
+
 def run_reference(args):
     """--impl reference: the oracle on the host cores (all threads via processes)."""
     rank, world, _ = dist_env()
@@ -232,6 +307,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="leave out the mixed-size batch measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -332,8 +408,8 @@ def main():
     host = torch.from_numpy(field).pin_memory()
     # pinned host buffers for the exported complex and discs (sized from the warm-up result, 25% headroom)
     pinned = {}
-    for k, (sh, dt) in msc.export_shapes().items():
-        n = int(np.prod(sh)) * 5 // 4 + 16
+    for k, (shape, dt) in msc.export_shapes().items():
+        n = int(np.prod(shape)) * 5 // 4 + 16
         pinned[k] = torch.empty(n * np.dtype(dt).itemsize, dtype=torch.uint8).pin_memory().numpy()
     h2d = host.numel() * 4
     d2h = 0
@@ -383,6 +459,8 @@ def main():
         }
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(field)
+        if world == 1 and not args.no_batch:
+            line["batched"] = bench_batched(M, torch, stream, sh)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -188,6 +188,33 @@ int dmsc_batch_export_all(dmsc_batch *b, uint32_t *cp_base, uint32_t *asc_base, 
                           float *fn, uint32_t *pair_idx, uint8_t *flags, uint32_t *asc_off, uint32_t *asc,
                           uint32_t *des_off, uint32_t *des, void *stream);
 
+/* ---- request server (continuous batching) ----
+ * No counterpart in the reference.  Requests (one whole grid each, heights
+ * copied at submit) are admitted in arrival order by their device footprint
+ * against arena_bytes and run as batches (dmsc_batch_run) by `lanes` worker
+ * threads, each with its own stream, so one batch is admitted and copied
+ * while another computes.  A request's result equals its grid's complex
+ * computed alone.  max_ops bounds each grid's simplification (<= 0: the
+ * default of dmsc_msc_simplify_un_simplify). */
+typedef struct dmsc_server dmsc_server;
+int dmsc_server_create(dmsc_ctx *ctx, int64_t arena_bytes, int lanes, int max_batch, int64_t max_ops, dmsc_server **out);
+int dmsc_server_submit(dmsc_server *s, const float *heights, int nx, int ny, double tresh, int64_t *id);
+/* waits up to timeout_ms (< 0: without limit); *done = 1 once the request
+ * has completed, *status (may be NULL) is then its DMSC_* result */
+int dmsc_server_wait(dmsc_server *s, int64_t id, int timeout_ms, int *done, int *status);
+/* a completed request: sizes as dmsc_batch_sizes, times (ms since the server
+ * started) of submit, batch start and completion; returns its status */
+int dmsc_server_result(dmsc_server *s, int64_t id, int64_t sizes[3], double times_ms[3], char *error, int error_len);
+/* a completed request's complex in the layout of dmsc_msc_export (no discs) */
+int dmsc_server_export(dmsc_server *s, int64_t id, int16_t *cellid, float *fn, uint32_t *pair_idx, uint8_t *flags,
+                       uint32_t *asc_off, uint32_t *asc, uint32_t *des_off, uint32_t *des);
+/* forgets a completed request */
+int dmsc_server_release(dmsc_server *s, int64_t id);
+/* [0] batches run, [1] grids completed, [2] queued, [3] arena bytes in use */
+int dmsc_server_stats(dmsc_server *s, int64_t stats[4]);
+/* drains the queue, stops the workers */
+int dmsc_server_destroy(dmsc_server *s);
+
 /* PrefixScan::PreScanBuffer(out, in, n, queue) (dmsc/include/prefix_scan.h:105-109,
  * dmsc/src/prefix_scan.cpp:457-464): exclusive prefix sum of n uint32 values
  * in device memory, out[i] = in[0] + ... + in[i-1] (wrapping modulo 2^32).

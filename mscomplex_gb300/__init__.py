@@ -5,6 +5,6 @@ this package is its host-side mirror of the reference interfaces
 (GridDataset / GridMSComplex / GridDataManager of nithins/mscomplex).
 """
 from ._native import DmscError, load
-from .dataset import Context, GridBatch, GridDataManager, GridDataset, GridMSComplex, default_context
+from .dataset import Context, GridBatch, GridDataManager, GridDataset, GridMSComplex, GridServer, default_context
 
-__all__ = ["DmscError", "load", "Context", "GridBatch", "GridDataManager", "GridDataset", "GridMSComplex", "default_context"]
+__all__ = ["DmscError", "load", "Context", "GridBatch", "GridDataManager", "GridDataset", "GridMSComplex", "GridServer", "default_context"]

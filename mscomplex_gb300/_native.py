@@ -58,6 +58,14 @@ SIGNATURES = {
     "dmsc_batch_export": ([_vp, _i64] + [_vp] * 9 + [_vp], _i32),
     "dmsc_batch_totals": ([_vp, _vp], _i32),
     "dmsc_batch_export_all": ([_vp] + [_vp] * 11 + [_vp], _i32),
+    "dmsc_server_create": ([_vp, _i64, _i32, _i32, _i64, _vp], _i32),
+    "dmsc_server_submit": ([_vp, _vp, _i32, _i32, C.c_double, _vp], _i32),
+    "dmsc_server_wait": ([_vp, _i64, _i32, _vp, _vp], _i32),
+    "dmsc_server_result": ([_vp, _i64, _vp, _vp, C.c_char_p, _i32], _i32),
+    "dmsc_server_export": ([_vp, _i64] + [_vp] * 8, _i32),
+    "dmsc_server_release": ([_vp, _i64], _i32),
+    "dmsc_server_stats": ([_vp, _vp], _i32),
+    "dmsc_server_destroy": ([_vp], _i32),
     "dmsc_prefix_scan": ([_vp, _vp, _vp, _i64, _vp, _vp], _i32),
     "dmsc_prefix_scan_noalloc": ([_vp, _vp, _vp, _i64, _vp, _vp], _i32),
     "dmsc_sort_pairs": ([_vp, _vp, _vp, _vp, _vp, C.c_uint32, C.c_uint32, C.c_uint32, _vp], _i32),

@@ -665,11 +665,9 @@ static int nbits_for(long long n) {
 }
 
 static cudaError_t hops_attr() {
-  static bool done = false;
-  if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(k_disc_hops, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(HopSmem));
-  if (e == cudaSuccess) done = true;
-  return e;
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(k_disc_hops, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(HopSmem));
+  return attr;
 }
 
 cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {

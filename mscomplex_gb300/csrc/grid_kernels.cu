@@ -634,12 +634,9 @@ size_t label_smem_bytes() { return sizeof(LabelSmem); }
 
 cudaError_t launch_gradient(const float *hgt, const GridGeom &g, uint32_t *codes, uint32_t *terms, uint8_t *rowcnt,
                             uint64_t *table, uint32_t *status, cudaStream_t st) {
-  static bool init = false;
-  if (!init) {
-    cudaError_t e = cudaFuncSetAttribute(k_gradient, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradSmem));
-    if (e != cudaSuccess) return e;
-    init = true;
-  }
+  // once per process (thread-safe static initialisation)
+  static const cudaError_t attr = cudaFuncSetAttribute(k_gradient, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradSmem));
+  if (attr != cudaSuccess) return attr;
   dim3 grid(g.ntx, g.nty);
   k_gradient<<<grid, GRAD_THREADS, sizeof(GradSmem), st>>>(hgt, g, codes, terms, rowcnt, table, status);
   DMSC_LAUNCHED(1);
@@ -660,12 +657,9 @@ cudaError_t launch_resolve(uint64_t *table, long long nslots, const uint32_t *of
 cudaError_t launch_labels(const uint32_t *codes, const uint32_t *terms, const float *hgt, const GridGeom &g,
                           const uint32_t *offsets, const uint64_t *table, uint4 *labels, const CpOut &cp,
                           uint32_t *status, cudaStream_t st) {
-  static bool init = false;
-  if (!init) {
-    cudaError_t e = cudaFuncSetAttribute(k_labels, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LabelSmem));
-    if (e != cudaSuccess) return e;
-    init = true;
-  }
+  // once per process (thread-safe static initialisation)
+  static const cudaError_t attr = cudaFuncSetAttribute(k_labels, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LabelSmem));
+  if (attr != cudaSuccess) return attr;
   dim3 grid(g.ntx, g.nty);
   k_labels<<<grid, GRAD_THREADS, sizeof(LabelSmem), st>>>(codes, terms, hgt, g, offsets, table, labels, cp, status);
   DMSC_LAUNCHED(1);
@@ -673,12 +667,9 @@ cudaError_t launch_labels(const uint32_t *codes, const uint32_t *terms, const fl
 }
 
 cudaError_t launch_gradient_batch(const BatchGrid *grids, int ngrids, long long ntiles, uint32_t *status, cudaStream_t st) {
-  static bool init = false;
-  if (!init) {
-    cudaError_t e = cudaFuncSetAttribute(k_gradient_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradSmem));
-    if (e != cudaSuccess) return e;
-    init = true;
-  }
+  // once per process (thread-safe static initialisation)
+  static const cudaError_t attr = cudaFuncSetAttribute(k_gradient_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradSmem));
+  if (attr != cudaSuccess) return attr;
   if (ntiles <= 0) return cudaSuccess;
   const long long blocks = std::min<long long>(ntiles, 152LL * 3);
   k_gradient_batch<<<(unsigned)blocks, GRAD_THREADS, sizeof(GradSmem), st>>>(grids, ngrids, ntiles, status);
@@ -688,12 +679,9 @@ cudaError_t launch_gradient_batch(const BatchGrid *grids, int ngrids, long long 
 
 cudaError_t launch_labels_batch(const BatchGrid *grids, int ngrids, long long ntiles, const CpOut &cp, uint32_t *status,
                                 cudaStream_t st) {
-  static bool init = false;
-  if (!init) {
-    cudaError_t e = cudaFuncSetAttribute(k_labels_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LabelSmem));
-    if (e != cudaSuccess) return e;
-    init = true;
-  }
+  // once per process (thread-safe static initialisation)
+  static const cudaError_t attr = cudaFuncSetAttribute(k_labels_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LabelSmem));
+  if (attr != cudaSuccess) return attr;
   if (ntiles <= 0) return cudaSuccess;
   const long long blocks = std::min<long long>(ntiles, 152LL * 3);
   k_labels_batch<<<(unsigned)blocks, GRAD_THREADS, sizeof(LabelSmem), st>>>(grids, ngrids, ntiles, cp, status);

@@ -375,3 +375,62 @@ class GridBatch:
                 d[k] = buf[:m]
         check(self.lib.dmsc_batch_export_all(self.h, *(_ptr(d[k]) for k in shapes), None))
         return d
+
+
+class GridServer:
+    """Request server with continuous batching over GridBatch (no reference
+    counterpart).  submit() copies the heights and returns a request id;
+    result() waits and returns the grid's complex (the GridBatch.export keys)
+    with its submit / start / done times in ms."""
+
+    def __init__(self, arena_bytes: int = 150 << 30, lanes: int = 2, max_batch: int = 256, max_ops: int = 0,
+                 ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.lib = self.ctx.lib
+        h = C.c_void_p()
+        check(self.lib.dmsc_server_create(self.ctx.h, int(arena_bytes), int(lanes), int(max_batch), int(max_ops),
+                                          C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dmsc_server_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def submit(self, heights: np.ndarray, tresh: float = 0.0) -> int:
+        a = np.ascontiguousarray(heights, np.float32)
+        if a.ndim != 2:
+            raise ValueError("heights must be 2D (size_y, size_x)")
+        rid = C.c_int64()
+        check(self.lib.dmsc_server_submit(self.h, _ptr(a), a.shape[1], a.shape[0], float(tresh), C.byref(rid)))
+        return rid.value
+
+    def wait(self, rid: int, timeout_ms: int = -1) -> bool:
+        done, status = C.c_int(), C.c_int()
+        check(self.lib.dmsc_server_wait(self.h, int(rid), int(timeout_ms), C.byref(done), C.byref(status)))
+        return bool(done.value)
+
+    def result(self, rid: int, release: bool = True) -> dict:
+        self.wait(rid)
+        sizes = np.zeros(3, np.int64)
+        times = np.zeros(3, np.float64)
+        err = C.create_string_buffer(512)
+        check(self.lib.dmsc_server_result(self.h, int(rid), _ptr(sizes), _ptr(times), err, 512))
+        n, na, nd = (int(v) for v in sizes)
+        d = dict(cellid=np.zeros((n, 2), np.int16), fn=np.zeros(n, np.float32), pair_idx=np.zeros(n, np.uint32),
+                 flags=np.zeros(n, np.uint8), asc_off=np.zeros(n + 1, np.uint32), asc=np.zeros(na, np.uint32),
+                 des_off=np.zeros(n + 1, np.uint32), des=np.zeros(nd, np.uint32))
+        check(self.lib.dmsc_server_export(self.h, int(rid), *(_ptr(d[k]) for k in
+                                                             ("cellid", "fn", "pair_idx", "flags", "asc_off", "asc",
+                                                              "des_off", "des"))))
+        d["times_ms"] = times
+        if release:
+            check(self.lib.dmsc_server_release(self.h, int(rid)))
+        return d
+
+    def stats(self) -> dict:
+        s = np.zeros(4, np.int64)
+        check(self.lib.dmsc_server_stats(self.h, _ptr(s)))
+        return dict(zip(("batches", "grids_done", "queued", "arena_in_use"), (int(v) for v in s)))
