@@ -249,6 +249,81 @@ def bench_batched(M, torch, stream, sh, steps=2, warmup=1, count=1000):
             "max_simplify_pops": max(x["pops"] for x in st), "total_simplify_pops": sum(x["pops"] for x in st)}
 
 
+SERVE_WORKLOAD = ("served: Poisson arrivals; sides 80% U(128,512), 18% U(1024,2048), 2% 4096; Gaussian sums "
+                  "(10% quantised to 1/256 of the range); tresh U(0, 5%); arena 150 GB; seed 4")
+
+
+def serve_requests(count: int, seed: int = 4):
+    """The served request mix: (field, tresh) pairs."""
+    from mscomplex_gb300 import synth
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(count):
+        u = rng.random()
+        side = int(rng.integers(128, 513)) if u < 0.8 else int(rng.integers(1024, 2049)) if u < 0.98 else 4096
+        quant = 256 if rng.random() < 0.1 else 0
+        reqs.append((synth.mixed_grid(side, seed * 7919 + i, quantize=quant), float(rng.uniform(0.0, 0.05))))
+    return reqs
+
+
+def bench_served(M, torch, count=300, rates=(None, 200.0), max_ops=2_000_000):
+    """The request server under a Poisson stream (rate None = every request
+    submitted at once, i.e. saturation) against plain one-request-at-a-time
+    processing through the per-grid API.  Latency = submit -> result ready."""
+    reqs = serve_requests(count)
+    out = {"workload": SERVE_WORKLOAD, "requests": count, "max_ops_per_request": max_ops, "runs": []}
+    for rate in rates:
+        rng = np.random.default_rng(11)
+        gaps = np.zeros(count) if rate is None else rng.exponential(1.0 / rate, count)
+        srv = M.GridServer(arena_bytes=150 << 30, lanes=2, max_batch=128, max_ops=max_ops)
+        t0 = time.perf_counter()
+        ids = []
+        next_t = 0.0
+        for (f, t), gap in zip(reqs, gaps):
+            next_t += gap
+            while time.perf_counter() - t0 < next_t:
+                time.sleep(0.0002)
+            ids.append(srv.submit(f, t))
+        lat, fails = [], 0
+        for rid in ids:
+            try:
+                r = srv.result(rid)
+                s0, _, d0 = r["times_ms"]
+                lat.append(d0 - s0)
+            except M.DmscError:
+                fails += 1
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        lat = np.array(lat) if lat else np.zeros(1)
+        out["runs"].append({"rate_per_s": rate if rate is not None else "saturation",
+                            "grids_per_s": round(count / wall, 2), "p50_ms": round(float(np.percentile(lat, 50)), 2),
+                            "p99_ms": round(float(np.percentile(lat, 99)), 2), "failed": fails,
+                            "batches": st["batches"]})
+    # plain: one request at a time, each through dataset / writeout / simplify / export
+    t0 = time.perf_counter()
+    lat, fails = [], 0
+    for f, t in reqs:
+        s0 = time.perf_counter()
+        try:
+            r = (0, 0, 2 * (f.shape[1] - 1), 2 * (f.shape[0] - 1))
+            m = M.GridDataset(r, r).init(f).work().writeout_connectivity()
+            if t > 0:
+                m.simplify_un_simplify(t, max_ops=max_ops)
+            m.export()
+        except M.DmscError:
+            fails += 1
+        lat.append((time.perf_counter() - s0) * 1e3)
+    wall = time.perf_counter() - t0
+    lat = np.array(lat)
+    out["plain"] = {"grids_per_s": round(count / wall, 2), "p50_ms": round(float(np.percentile(lat, 50)), 2),
+                    "p99_ms": round(float(np.percentile(lat, 99)), 2), "failed": fails,
+                    "note": "sequential; latency excludes queueing behind earlier requests"}
+    sat = out["runs"][0]["grids_per_s"]
+    out["speedup_vs_plain"] = round(sat / out["plain"]["grids_per_s"], 2)
+    return out
+
+
 def run_reference(args):
     """--impl reference: the oracle on the host cores (all threads via processes)."""
     rank, world, _ = dist_env()
@@ -461,6 +536,7 @@ def main():
             line["cpu_baseline"] = cpu_baseline(field)
         if world == 1 and not args.no_batch:
             line["batched"] = bench_batched(M, torch, stream, sh)
+            line["served"] = bench_served(M, torch)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -119,7 +119,7 @@ int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float 
   B->ngrids = ngrids;
   auto fail = [&](int rc) {
     if (fresh) delete B;
-    else B->ncp = 0;
+    else { B->ncp = 0; B->cpb.clear(); B->abase.clear(); B->dbase.clear(); }
     return rc;
   };
 
@@ -252,16 +252,34 @@ int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float 
     io.tresh = B->tresh.data(); io.rect = B->rect.data();
     io.max_ops = max_ops > 0 ? (unsigned long long)max_ops : 20000000ull;
     io.host_stats = B->stats.data();
-    cudaError_t e = simplify_batch_run(io, st);
     int rc = DMSC_OK;
-    if (e != cudaSuccess) rc = berr(e == cudaErrorMemoryAllocation ? DMSC_ERR_OOM : DMSC_ERR_CUDA,
-                                   std::string("batch simplify: ") + cudaGetErrorString(e));
-    for (int g = 0; g < ngrids && rc == DMSC_OK; ++g) {
-      const unsigned long long s = B->stats[5 * g + 4];
-      if (s & ST_SIMPLIFY_LIMIT)
-        rc = berr(DMSC_ERR_DEVICE_TIMEOUT, "grid " + std::to_string(g) + ": simplification ran out of its operation budget or pool");
-      else if (s)
-        rc = berr(DMSC_ERR_INVARIANT, "grid " + std::to_string(g) + ": simplification status " + std::to_string(s));
+    // a grid that ran out of list pool, heap or scratch (not of its operation
+    // budget) makes the whole simplification rerun with larger capacities;
+    // whole grids start with no flags and no pairs, so the rerun starts clean
+    for (int attempt = 0;; ++attempt) {
+      cudaError_t e = simplify_batch_run(io, st);
+      if (e != cudaSuccess) {
+        rc = berr(e == cudaErrorMemoryAllocation ? DMSC_ERR_OOM : DMSC_ERR_CUDA,
+                  std::string("batch simplify: ") + cudaGetErrorString(e));
+        break;
+      }
+      bool capacity = false;
+      for (int g = 0; g < ngrids && rc == DMSC_OK; ++g) {
+        const unsigned long long s = B->stats[5 * g + 4];
+        if (!s) continue;
+        if (s == ST_SIMPLIFY_LIMIT && B->stats[5 * g + 3] <= io.max_ops && attempt < 3) capacity = true;
+        else if (s & ST_SIMPLIFY_LIMIT)
+          rc = berr(DMSC_ERR_DEVICE_TIMEOUT, "grid " + std::to_string(g) + ": simplification ran out of its operation budget");
+        else
+          rc = berr(DMSC_ERR_INVARIANT, "grid " + std::to_string(g) + ": simplification status " + std::to_string(s));
+      }
+      if (rc != DMSC_OK || !capacity) break;
+      simplify_batch_release(io, st);
+      io.scale *= 4;
+      if (cudaMemsetAsync(B->flags.p, 0, n, st) || cudaMemsetAsync(B->pair_idx.p, 0xFF, 4 * n, st)) {
+        rc = berr(DMSC_ERR_CUDA, "batch simplify reset");
+        break;
+      }
     }
     if (rc == DMSC_OK) {
       if (B->asc.ensure((size_t)io.nasc_out + 1) || B->des.ensure((size_t)io.ndes_out + 1) ||

@@ -109,6 +109,7 @@ struct BatchSimplifyIO {
   const double *tresh = nullptr;  // host, per grid
   const int *rect = nullptr;      // host, 4 per grid
   unsigned long long max_ops = 0;
+  unsigned long long scale = 1;              // multiplies every per-grid capacity
   unsigned long long *host_stats = nullptr;  // host, 5 per grid
   long long nasc_out = 0, ndes_out = 0;
   void *work = nullptr;

@@ -379,15 +379,21 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
   // per simplified grid: pool growth region, heap, resubmits, cancellations, scratch runs
   std::vector<int> which;
   unsigned long long grow = 0, heap = 0, canc = 0, tmp = 0;
+  const unsigned long long sc = io.scale ? io.scale : 1;
+  auto grow_of = [&](unsigned long long na, unsigned long long nd, unsigned long long n) {
+    return sc * (4 * (na + nd + 8 * n) + 16384);
+  };
+  auto heap_of = [&](unsigned long long nd) { return sc * (8 * nd + 16384); };
+  auto tmp_of = [&](unsigned long long na, unsigned long long nd) { return sc * (4 * (na + nd) + 16384); };
   for (int g = 0; g < io.ngrids; ++g) {
     const unsigned long long n = io.cpb[g + 1] - io.cpb[g];
     if (!(io.tresh[g] > 0.0) || n == 0) continue;
     const unsigned long long na = io.abase[g + 1] - io.abase[g], nd = io.dbase[g + 1] - io.dbase[g];
     which.push_back(g);
-    grow += 2 * (na + nd + 8 * n) + 4096;
-    heap += 4 * nd + 1024;
+    grow += grow_of(na, nd, n);
+    heap += heap_of(nd);
     canc += n + 1;
-    tmp += 2 * (na + nd) + 65536;
+    tmp += tmp_of(na, nd);
   }
   const unsigned long long pool_cap = base_top + grow;
   if (pool_cap > 0xffffffffull) return cudaErrorInvalidValue;  // list offsets are 32-bit
@@ -438,10 +444,10 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
     G.L.off = w->off + 2 * c0; G.L.nrun = w->nrun + 2 * c0; G.L.cap = w->lcap + 2 * c0; G.L.total = w->total + 2 * c0;
     G.L.pool = w->pool;
     G.L.top = top;
-    top += 2 * (na + nd + 8 * n) + 4096;
+    top += grow_of(na, nd, n);
     G.L.pool_cap = top;
     G.tmp = dtmp + to;
-    G.tmp_cap = 2 * (na + nd) + 65536;
+    G.tmp_cap = tmp_of(na, nd);
     to += G.tmp_cap;
     G.max_ops = io.max_ops;
     G.ops = 0;
@@ -449,7 +455,7 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
     a.fn = io.fn + c0;
     a.heap = dheap + ho;
     a.resub = dres + ho;
-    a.heap_cap = 4 * nd + 1024;
+    a.heap_cap = heap_of(nd);
     ho += a.heap_cap;
     a.canc = dcanc + co;
     co += n + 1;

@@ -72,10 +72,34 @@ def mixed_batch_sides(count: int = 1000, seed: int = 3, lo: int = 64, hi: int = 
     return np.exp(rng.uniform(math.log(lo), math.log(hi), count)).astype(np.int64)
 
 
+def gaussian_sum(nx: int, ny: int, nbumps: int, sigma_lo: float, sigma_hi: float, rng: np.random.Generator,
+                 quantize: int = 0) -> np.ndarray:
+    """Sum of isotropic Gaussian bumps evaluated everywhere (no window), float64,
+    returned float32 (ny, nx).  A Gaussian is separable, so the sum is the
+    matrix product Gy diag(a) Gx^T.  Without a window the field has no exact
+    zero plateaus between bumps (a windowed sum is exactly 0 wherever no
+    window reaches, which makes large flat ties).  ``quantize=k`` snaps values
+    to k steps of the range."""
+    cx = rng.uniform(0, nx - 1, nbumps)
+    cy = rng.uniform(0, ny - 1, nbumps)
+    sg = rng.uniform(sigma_lo, sigma_hi, nbumps)
+    amp = rng.uniform(-1.0, 1.0, nbumps)
+    gx = np.exp(-0.5 * ((np.arange(nx)[None, :] - cx[:, None]) / sg[:, None]) ** 2)  # (nb, nx)
+    gy = np.exp(-0.5 * ((np.arange(ny)[:, None] - cy[None, :]) / sg[None, :]) ** 2)  # (ny, nb)
+    f = (gy * amp[None, :]) @ gx
+    if quantize:
+        lo, hi = float(f.min()), float(f.max())
+        step = (hi - lo) / quantize if hi > lo else 1.0
+        f = lo + np.round((f - lo) / step) * step
+    return f.astype(np.float32)
+
+
 def mixed_grid(side: int, seed: int, quantize: int = 0) -> np.ndarray:
+    """One grid of the mixed-size workloads: side x side, a sum of
+    area / 8192 Gaussians with sigma U(4, 32) pixels."""
     rng = np.random.default_rng(seed)
     nb = max(1, int(round(side * side / 8192)))
-    return gaussian_bumps(side, side, nb, 4.0, 32.0, rng, quantize=quantize)
+    return gaussian_sum(side, side, nb, 4.0, 32.0, rng, quantize=quantize)
 
 
 def batch_fields(count: int = 1000, seed: int = 3, lo: int = 64, hi: int = 2048) -> list:
