@@ -11,6 +11,13 @@
 // requests that arrive while the GPU is busy join the next free lane
 // (continuous batching).  A request's result is the complex of its grid
 // alone: batching does not change any output.
+//
+// The exact simplification is sequential per grid and can be long on fields
+// with many exact ties (its heap replays the reference's tie order), and a
+// batch completes with its slowest grid.  So requests with tresh > 0 whose
+// heights have more than 1% equal neighbour pairs are "heavy" and queue for
+// lane 0 alone (when there are two or more lanes); the other lanes never wait
+// behind them.
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -37,6 +44,7 @@ struct Request {
   std::vector<float> heights;
   long long footprint = 0;
   double t_submit = 0, t_start = 0, t_done = 0;
+  bool heavy = false;
   int status = -1;  // -1 pending, else DMSC_OK or an error code
   std::string error;
   int64_t sizes[3] = {0, 0, 0};
@@ -66,7 +74,8 @@ struct dmsc_server {
   long long max_ops = 0;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  std::deque<std::shared_ptr<Request>> queue;
+  std::deque<std::shared_ptr<Request>> queue, heavy;  // light and heavy requests
+  int lanes = 1;
   std::unordered_map<int64_t, std::shared_ptr<Request>> all;
   int64_t next_id = 1;
   bool stop = false;
@@ -79,7 +88,8 @@ struct dmsc_server {
 };
 
 void dmsc_server::lane(int k) {
-  (void)k;
+  // lane 0 takes the heavy queue when there are other lanes; a single lane takes both
+  const bool heavy_lane = lanes >= 2 && k == 0, light_lane = lanes == 1 || k != 0;
   cudaSetDevice(ctx->device);
   cudaStream_t st = nullptr;
   cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
@@ -92,16 +102,27 @@ void dmsc_server::lane(int k) {
     long long fp = 0;
     {
       std::unique_lock<std::mutex> lk(mu);
-      cv_work.wait(lk, [&] { return stop || (!queue.empty() && in_use + queue.front()->footprint <= arena) ||
-                                   (!queue.empty() && in_use == 0); });
-      if (stop && queue.empty()) break;
+      auto pick = [&]() -> std::deque<std::shared_ptr<Request>> * {
+        if (light_lane && !queue.empty()) return &queue;
+        if (heavy_lane && !heavy.empty()) return &heavy;
+        if (lanes == 1 && !heavy.empty()) return &heavy;
+        return nullptr;
+      };
+      auto ready = [&] {
+        auto *q = pick();
+        return q && (in_use + q->front()->footprint <= arena || in_use == 0);
+      };
+      cv_work.wait(lk, [&] { return stop || ready(); });
+      auto *q = pick();
+      if (stop && !q) break;
+      if (!q) continue;
       // admit in arrival order while the footprint fits (a request larger than
       // the whole arena is admitted alone once the arena is empty)
-      while (!queue.empty() && (int)take.size() < max_batch) {
-        const long long f = queue.front()->footprint;
+      while (!q->empty() && (int)take.size() < max_batch) {
+        const long long f = q->front()->footprint;
         if (in_use + fp + f > arena && !(take.empty() && in_use == 0)) break;
-        take.push_back(queue.front());
-        queue.pop_front();
+        take.push_back(q->front());
+        q->pop_front();
         fp += f;
       }
       in_use += fp;
@@ -219,6 +240,7 @@ int dmsc_server_create(dmsc_ctx *ctx, int64_t arena_bytes, int lanes, int max_ba
   s->arena = arena_bytes;
   s->max_batch = max_batch;
   s->max_ops = max_ops;
+  s->lanes = lanes;
   for (int k = 0; k < lanes; ++k) s->workers.emplace_back([s, k] { s->lane(k); });
   *out = s;
   return DMSC_OK;
@@ -232,11 +254,21 @@ int dmsc_server_submit(dmsc_server *s, const float *heights, int nx, int ny, dou
   r->nx = nx; r->ny = ny; r->tresh = tresh;
   r->heights.assign(heights, heights + (size_t)nx * ny);
   r->footprint = footprint_of(nx, ny);
+  if (tresh > 0.0) {  // equal neighbour pairs along x and y
+    size_t ties = 0;
+    const float *h = r->heights.data();
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        const size_t i = (size_t)y * nx + x;
+        ties += (x + 1 < nx && h[i] == h[i + 1]) + (y + 1 < ny && h[i] == h[i + nx]);
+      }
+    r->heavy = ties * 100 > (size_t)nx * ny;
+  }
   {
     std::lock_guard<std::mutex> lk(s->mu);
     r->id = s->next_id++;
     r->t_submit = s->now_ms();
-    s->queue.push_back(r);
+    (r->heavy ? s->heavy : s->queue).push_back(r);
     s->all[r->id] = r;
     *id = r->id;
   }
@@ -317,7 +349,8 @@ int dmsc_server_release(dmsc_server *s, int64_t id) {
 int dmsc_server_stats(dmsc_server *s, int64_t stats[4]) {
   if (!s || !stats) return dmsc::set_last_error(DMSC_ERR_BAD_ARG, "null argument");
   std::lock_guard<std::mutex> lk(s->mu);
-  stats[0] = s->batches; stats[1] = s->grids_done; stats[2] = (int64_t)s->queue.size(); stats[3] = s->in_use;
+  stats[0] = s->batches; stats[1] = s->grids_done; stats[2] = (int64_t)(s->queue.size() + s->heavy.size());
+  stats[3] = s->in_use;
   return DMSC_OK;
 }
 
