@@ -316,16 +316,15 @@ struct HopSmem {
   uint32_t code[(TX + 2) * (TY + 2)];
   uint32_t nv[HOP_SLOTS];     // next slot << 16 | cells counted so far
   uint16_t tail[HOP_SLOTS];
-  uint16_t jmp[HOP_SLOTS];    // the slot SEG_MAX cells ahead in the tile (SLOT_NIL: none)
 };
 
 // Per edge, for the chains of its own kind: hop_to (the edge after its
 // in-tile run, HOP_END if the chain ends in the tile), hop_len (cells of the
 // run, 0 for a branching cell) and j64 (the edge SEG_MAX cells ahead in the
 // same run, HOP_END if the run is shorter).  One block per tile.
-__global__ void __launch_bounds__(HOP_THREADS)
+__global__ void __launch_bounds__(HOP_THREADS, 3)
 k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict__ to, uint16_t *__restrict__ len,
-            uint32_t *__restrict__ j64, uint32_t *status) {
+            uint32_t *__restrict__ j64, uint32_t *__restrict__ nextc, uint32_t *status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   HopSmem &S = *reinterpret_cast<HopSmem *>(smem_raw);
   const int tx0 = blockIdx.x * TX, ty0 = blockIdx.y * TY;
@@ -357,23 +356,27 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict
     uint32_t nx = SLOT_NIL;
     if (slot_cell(sl, rx, ry)) {
       const int kind = chain_kind(code(rx, ry), rx, ry);
+      uint32_t succ = HOP_END;
       if (kind >= 0) {
         const int n = succ_local(g, kind, rx, ry, code, ox, oy);
         if (n < 0) st |= ST_INVARIANT;
+        if (n == 1) succ = (uint32_t)ox[0] | ((uint32_t)oy[0] << 16);
         if (n == 1 && in_tile(ox[0], oy[0])) {
           nx = (uint32_t)((((oy[0] >> 1) - ty0) * TX + ((ox[0] >> 1) - tx0)) << 1) | (uint32_t)(oy[0] & 1);
           active = 1;
         }
       }
+      nextc[edge_id(g, rx, ry)] = succ;
     }
     S.nv[sl] = (nx << 16) | 1u;
     S.tail[sl] = (uint16_t)sl;
-    S.jmp[sl] = SLOT_NIL;
   }
   // list ranking: at most 13 rounds (2^13 = HOP_SLOTS cells); after round 6
   // every pointer still inside the tile is exactly SEG_MAX cells ahead
   constexpr int PER = HOP_SLOTS / HOP_THREADS;
+  int rounds = 0;
   for (int round = 0; round < 14 && __syncthreads_or(active); ++round) {
+    rounds = round + 1;
     uint32_t nn[PER];
     uint16_t nt[PER];
     active = 0;
@@ -395,7 +398,15 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict
     for (int q = 0; q < PER; ++q) {
       const int sl = threadIdx.x + q * HOP_THREADS;
       S.nv[sl] = nn[q]; S.tail[sl] = nt[q];
-      if (round == 5) S.jmp[sl] = (uint16_t)(nn[q] >> 16);
+      if (round == 5) {  // pointers now SEG_MAX cells ahead (or none)
+        int rx, ry, jx, jy;
+        if (slot_cell(sl, rx, ry)) {
+          const uint32_t js = nn[q] >> 16;
+          uint32_t jv = HOP_END;
+          if (js != SLOT_NIL) { slot_cell((int)js, jx, jy); jv = edge_id(g, jx, jy); }
+          j64[edge_id(g, rx, ry)] = jv;
+        }
+      }
     }
   }
   __syncthreads();
@@ -404,7 +415,7 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict
     if (!slot_cell(sl, rx, ry)) continue;
     const uint32_t e = edge_id(g, rx, ry);
     const uint32_t v = S.nv[sl];
-    if ((v >> 16) != SLOT_NIL) { st |= ST_CYCLE; to[e] = HOP_END; len[e] = 0; j64[e] = HOP_END; continue; }
+    if ((v >> 16) != SLOT_NIL) { st |= ST_CYCLE; to[e] = HOP_END; len[e] = 0; continue; }
     int tx, ty;
     slot_cell(S.tail[sl], tx, ty);
     const int kind = chain_kind(code(tx, ty), tx, ty);
@@ -417,13 +428,7 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict
     to[e] = dst;
     // a cell with two successors ends no chain: length 0 marks it for the walkers
     len[e] = n == 2 ? 0 : (uint16_t)(v & 0xFFFFu);
-    uint32_t jv = HOP_END;
-    if (S.jmp[sl] != SLOT_NIL) {
-      int jx, jy;
-      slot_cell(S.jmp[sl], jx, jy);
-      jv = edge_id(g, jx, jy);
-    }
-    j64[e] = jv;
+    if (rounds < 6) j64[e] = HOP_END;  // every run in the tile is shorter than SEG_MAX + 1 cells
   }
   if (st) atomicOr(status, st);
 }
@@ -432,6 +437,7 @@ struct ChainArgs {
   const uint32_t *hop_to;
   const uint16_t *hop_len;
   const uint32_t *j64;
+  const uint32_t *nextc;  // per edge: its chain successor (ext-local x | y << 16), HOP_END if none
   uint32_t *kc;         // per cp: chains of a saddle handled here (0 otherwise)
   uint32_t *mc;         // per cp: level-0 items
   uint8_t *big;         // per cp: surviving saddle with more than KMAX chains
@@ -535,14 +541,10 @@ __global__ void k_level0(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, const u
   }
 }
 
-// one thread per piece (at most SEG_MAX cells of one chain): walk it into
-// the chain's span of tmp
-__global__ void k_seg_write(DiscArgs a, int kind, ChainArgs c, long long nsegs) {
+// one thread per piece (at most SEG_MAX cells of one chain): follow the
+// successor cells into the chain's span of tmp
+__global__ void k_seg_write(DiscArgs a, ChainArgs c, long long nsegs) {
   const GridGeom &g = a.g;
-  auto gcode = [&](int qx, int qy) -> uint32_t {
-    const uint32_t q = a.codes[(long long)(qy >> 1) * g.vnx + (qx >> 1)];
-    return (q >> (8 * ((qx & 1) | ((qy & 1) << 1)))) & 0xff;
-  };
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nsegs; k += (long long)gridDim.x * blockDim.x) {
     const uint4 sg = c.segs[k];
     const uint32_t ch = sg.x;
@@ -553,9 +555,9 @@ __global__ void k_seg_write(DiscArgs a, int kind, ChainArgs c, long long nsegs) 
     for (uint32_t i = 0; i < sg.w; ++i) {
       dst[i] = pack_cellid(g.ex0 + rx, g.ey0 + ry);
       if (i + 1 < sg.w) {
-        int ox[2], oy[2];
-        if (succ_local(g, kind, rx, ry, gcode, ox, oy) != 1) { atomicOr(a.status, ST_INVARIANT); break; }
-        rx = ox[0]; ry = oy[0];
+        const uint32_t nc = c.nextc[edge_id(g, rx, ry)];
+        if (nc == HOP_END) { atomicOr(a.status, ST_INVARIANT); break; }
+        rx = (int)(nc & 0xffff); ry = (int)(nc >> 16);
       }
     }
   }
@@ -584,42 +586,28 @@ __global__ void k_zip_blocks(DiscArgs a, ChainArgs c) {
   }
 }
 
-// one warp per block: out[base + P + q] = cell of level t_b + q / a of the
-// (q % a)-th alive chain
-__global__ void __launch_bounds__(256) k_zip(DiscArgs a, ChainArgs c, long long nch, const uint32_t *off, uint32_t *out) {
-  __shared__ uint32_t src[8][KMAX];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long k = w0; k < nch; k += nw) {
-    const uint4 b = c.blocks[k];
-    if (!b.z || b.y < b.x) continue;
-    const uint32_t s = c.csaddle[k], cb = c.cbase[s];
-    const uint32_t na = (uint32_t)__popc(b.z), levels = b.y - b.x + 1;
-    const unsigned long long n64 = (unsigned long long)levels * na;
-    const uint32_t base = off[s] + c.mc[s] + b.w, end = off[s + 1];
-    if ((unsigned long long)base + n64 > end) { if (lane == 0) atomicOr(a.status, ST_INVARIANT); continue; }
-    const uint32_t n = (uint32_t)n64;  // within one disc, whose length fits 32 bits
-    // lane r < na: start in tmp of the r-th alive chain at level t_b
-    if (lane < (int)na) {
-      uint32_t m = b.z;
-      for (int z = 0; z < lane; ++z) m &= m - 1;
-      src[wib][lane] = c.cofs[cb + (uint32_t)__ffs(m) - 1] + b.x - 1;
-    }
-    __syncwarp();
-    uint32_t *o = out + base;
-    if (na == 1) {
-      const uint32_t *p = c.tmp + src[wib][0];
-      for (uint32_t q = lane; q < n; q += 32) o[q] = p[q];
-    } else if (na == 2) {
-      for (uint32_t q = lane; q < n; q += 32) o[q] = c.tmp[src[wib][q & 1] + (q >> 1)];
-    } else {
-      for (uint32_t q = lane; q < n; q += 32) {
-        const uint32_t t = q / na;
-        o[q] = c.tmp[src[wib][q - t * na] + t];
+// one thread per chain: its cells, read in order from tmp, go to their
+// interleaved places block by block (the chains of one saddle are adjacent
+// threads, so their stores fill the same stretch of the disc together)
+__global__ void k_zip(DiscArgs a, ChainArgs c, long long nch, const uint32_t *off, uint32_t *out) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nch; k += (long long)gridDim.x * blockDim.x) {
+    const uint32_t s = c.csaddle[k], cb = c.cbase[s], j = (uint32_t)k - cb, L = c.clen[k];
+    const uint32_t base = off[s] + c.mc[s], end = off[s + 1];
+    const uint32_t *src = c.tmp + c.cofs[k];
+    uint32_t t = 1, bi = cb;
+    const uint32_t be = cb + c.kc[s];
+    while (t <= L && bi < be) {
+      const uint4 b = c.blocks[bi++];
+      if (!((b.z >> j) & 1u)) break;  // blocks end with the chain's last level
+      const uint32_t na = (uint32_t)__popc(b.z), r = (uint32_t)__popc(b.z & ((1u << j) - 1u));
+      const uint32_t te = b.y < L ? b.y : L;
+      if ((unsigned long long)base + b.w + (unsigned long long)(te - b.x) * na + r >= end) {
+        atomicOr(a.status, ST_INVARIANT);
+        break;
       }
+      for (; t <= te; ++t) out[base + b.w + (t - b.x) * na + r] = src[t - 1];
     }
-    __syncwarp();
+    if (t <= L) atomicOr(a.status, ST_INVARIANT);
   }
 }
 
@@ -681,9 +669,9 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   const long long nF = (long long)((g.rx1 - g.rx0) / 2) * ((g.ry1 - g.ry0) / 2);
   const long long nmax = std::max(std::max(nV, nF), std::max(io.nasc, io.ndes)) + 1;
   const long long nE = 2ll * g.vnx * g.vny;  // edge ids of the ext window
-  // words: 7 ncp + 8 | 4 nmax | 2 (nV + nF) | 3 ncp + 1 (kc, mc, cbase) | ncp / 4 (big) | 2.5 nE (hops)
+  // words: 7 ncp + 8 | 4 nmax | 2 (nV + nF) | 3 ncp + 1 (kc, mc, cbase) | ncp / 4 (big) | 3.5 nE (hops)
   size_t words = (size_t)ncp * 7 + 8 + (size_t)nmax * 4 + (size_t)(nV + nF) * 2 + (size_t)ncp * 3 + 1 +
-                 (size_t)ncp / 4 + 1 + 2 * (size_t)nE + (size_t)nE / 2 + 64;
+                 (size_t)ncp / 4 + 1 + 3 * (size_t)nE + (size_t)nE / 2 + 64;
   uint32_t *buf = nullptr;
   cudaError_t e = hops_attr();
   if (e != cudaSuccess) return e;
@@ -695,8 +683,8 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   uint32_t *gkey[2] = {vt + nmax, vt + nmax + nV}, *gval[2] = {vt + nmax + nV + nF, vt + nmax + 2 * nV + nF};
   uint32_t *kc = gval[1] + nF, *mc = kc + ncp, *cbase = mc + ncp;  // cbase: ncp+1
   uint8_t *big = (uint8_t *)(cbase + ncp + 1);
-  uint32_t *hop_to = cbase + ncp + 1 + ncp / 4 + 1, *j64 = hop_to + nE;
-  uint16_t *hop_len = (uint16_t *)(j64 + nE);
+  uint32_t *hop_to = cbase + ncp + 1 + ncp / 4 + 1, *j64 = hop_to + nE, *nextc = j64 + nE;
+  uint16_t *hop_len = (uint16_t *)(nextc + nE);
   const long long gn[2] = {nV, nF};
   auto L = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
   uint32_t *chain_buf = nullptr, *tmp = nullptr;
@@ -714,7 +702,8 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     k_redir_saddles<<<nb(ncp), 256, 0, st>>>(a, redir);
     DMSC_LAUNCHED(2);
   }
-  k_disc_hops<<<dim3(g.ntx, g.nty), HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, hop_to, hop_len, j64, io.status);
+  k_disc_hops<<<dim3(g.ntx, g.nty), HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, hop_to, hop_len, j64, nextc,
+                                                                        io.status);
   DMSC_LAUNCHED(1);
   L(cudaMemsetAsync(acnt, 0, sizeof(uint32_t) * ncp * 2, st));
   // extremum discs: vertices -> minima (asc_disc), faces -> maxima (des_disc),
@@ -753,7 +742,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     }
     SeedRuns sr{val, sstart, scount};
     ChainArgs c{};
-    c.hop_to = hop_to; c.hop_len = hop_len; c.j64 = j64;
+    c.hop_to = hop_to; c.hop_len = hop_len; c.j64 = j64; c.nextc = nextc;
     c.kc = kc; c.mc = mc; c.big = big; c.cbase = cbase; c.limit = io.limit;
     k_chain_count<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c);
     DMSC_LAUNCHED(1);
@@ -796,7 +785,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
       DMSC_LAUNCHED(1);
     }
     if (tot[1]) {
-      k_seg_write<<<nb(tot[1]), 128, 0, st>>>(a, kind, c, tot[1]);
+      k_seg_write<<<nb(tot[1]), 128, 0, st>>>(a, c, tot[1]);
       DMSC_LAUNCHED(1);
     }
     k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c);
@@ -804,7 +793,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);
     DMSC_LAUNCHED(3);
     if (nch) {
-      k_zip<<<nb(32ll * nch), 256, 0, st>>>(a, c, nch, offs, ob->p);
+      k_zip<<<nb(nch), 128, 0, st>>>(a, c, nch, offs, ob->p);
       DMSC_LAUNCHED(1);
     }
     long long n = gn[kind];
