@@ -44,17 +44,19 @@ SIMPLIFY_TRESH = 0.01
 # heap pushes + pops of the reference's simplification of this field at 1%,
 # counted by the oracle (2.956808816e9 pushes, 2.954259461e9 pops)
 SIMPLIFY_HEAP_OPS = 2956808816 + 2954259461
-# Algorithmic bytes of each stage: (per vertex, per critical point, per arc, per disc cell).
-STAGE_BYTES = {
-    "gradient": (8.0, 0, 0, 0),        # 4 B height read + 4 B gradient codes written
-    "labels_arcs": (20.0, 12, 8, 0),   # 4 B codes read + 16 B owner labels written; cp records and arcs
-    "connectivity": (0, 24, 16, 0),    # cp records read/written, arcs sorted into CSR (read + write)
-    "discs": (20.0, 8, 0, 4),          # codes + owner labels read, 4 B per disc cell written
+# Algorithmic bytes of the single-kernel stages: (per vertex, per critical point, per arc, per disc cell).
+KERNEL_BYTES = {
+    "gradient": (8.0, 0, 0, 0),        # k_gradient: 4 B height read + 4 B gradient codes written
+    "labels_arcs": (20.0, 12, 8, 0),   # k_labels: 4 B codes read + 16 B owner labels written; cp records, arcs
+    "disc_hops": (32.0, 0, 0, 0),      # k_disc_hops: 4 B codes read; per edge (2 a vertex) 14 B of hop data written
 }
+KERNEL_NAMES = {"gradient": "k_gradient", "labels_arcs": "k_labels", "disc_hops": "k_disc_hops"}
+# The whole step: 24 B/vertex (height, gradient, owner labels) + 12 B/cp + 8 B/arc + 4 B per disc cell written.
+PIPE_BYTES = (24.0, 12, 8, 4)
 
 
 def stage_bytes(stage, nverts, ncp, narcs, ndisc):
-    v, c, a, d = STAGE_BYTES.get(stage, (0, 0, 0, 0))
+    v, c, a, d = KERNEL_BYTES.get(stage, (0, 0, 0, 0)) if stage != "pipeline" else PIPE_BYTES
     return v * nverts + c * ncp + a * narcs + d * ndisc
 
 
@@ -423,16 +425,13 @@ def main():
     torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
 
-    disc_ev = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)]
     held = {}  # one complex per loop, overwritten in place every step
 
     def step(slot="dev"):
         ds.init(dev, stream=sh)
         ds.work(stream=sh)
         m = held[slot] = ds.writeout_connectivity(held.get(slot), stream=sh)
-        disc_ev[0].record(stream)
         ds.post_merge_fill_discs(m, stream=sh)
-        disc_ev[1].record(stream)
         return m
 
     for _ in range(max(3, args.warmup)):
@@ -446,7 +445,7 @@ def main():
     barrier()
     torch.cuda.synchronize()
     launches0 = kernel_launches()
-    times, stages = [], {k: [] for k in M.GridDataset.STAGES + ("discs",)}
+    times, stages = [], {k: [] for k in M.GridDataset.STAGES}
     for _ in range(args.steps):
         flush.fill_(1.0)  # evict L2 between steps (outside the timed interval)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -455,9 +454,8 @@ def main():
         e1.record(stream)
         e1.synchronize()
         times.append(e0.elapsed_time(e1))
-        for k, v in ds.stage_times().items():
+        for k, v in ds.stage_times(with_discs=True).items():
             stages[k].append(v)
-        stages["discs"].append(disc_ev[0].elapsed_time(disc_ev[1]))
     torch.cuda.synchronize()
     launches = kernel_launches() - launches0
     barrier()
@@ -471,15 +469,15 @@ def main():
 
     # roofline of the dominant kernel (median stage time, live CUDA events)
     med = {k: statistics.median(v) for k, v in stages.items()}
-    dom = max(STAGE_BYTES, key=lambda k: med[k])
+    dom = max(KERNEL_BYTES, key=lambda k: med[k])
     alg_bytes = stage_bytes(dom, nverts, ncp, nasc + ndes, nadisc + nddisc)
     peak, peak_kind = peaks()
     achieved = alg_bytes / (med[dom] / 1e3) / 1e9
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
-        traffic = json.load(open(tp)).get(f"{dom}:bumps4096q")
-    pipe_bytes = sum(stage_bytes(k, nverts, ncp, nasc + ndes, nadisc + nddisc) for k in STAGE_BYTES)
+        traffic = json.load(open(tp)).get(f"{KERNEL_NAMES[dom]}:bumps4096q")
+    pipe_bytes = stage_bytes("pipeline", nverts, ncp, nasc + ndes, nadisc + nddisc)
 
     # ---- persistence cancellation at 1%: device replay rate under an operation budget ----
     simp = simplify_rate(M, ds, stream, sh, torch)
@@ -526,7 +524,7 @@ def main():
                        "l2": "flushed between steps (256 MB write)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "stages_ms": {k: round(v, 4) for k, v in med.items()},
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": round(achieved, 1), "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "alg_bytes_per_launch": int(alg_bytes), "traffic": traffic},
             "pipeline_roofline": {"alg_bytes": int(pipe_bytes),

@@ -257,7 +257,8 @@ int dmsc_sort_pairs(dmsc_ctx *ctx, uint32_t *d_dst_key, uint32_t *d_dst_val, con
 int dmsc_set_timing(dmsc_ctx *ctx, int enable);
 /* Stage times in ms of the dataset's last work + writeout_connectivity:
  * [0] gradient, [1] collation scan, [2] border resolve, [3] owner labels and
- * arcs, [4] connectivity CSR.  Writes min(n, 5) floats. */
+ * arcs, [4] connectivity CSR; and of its last fill_discs: [5] the hop kernel,
+ * [6] the whole pass.  Writes min(n, 7) floats. */
 int dmsc_dataset_stage_times(dmsc_dataset *ds, float *ms, int n);
 /* Kernels launched by this library so far in this process. */
 int dmsc_kernel_launches(uint64_t *count);

@@ -146,13 +146,13 @@ int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float 
     B->tile0[g + 1] = B->tile0[g] + (long long)G.ntx * G.nty;
   }
   const long long NV = B->vbase[ngrids], NR = B->rbase[ngrids], NS = B->sbase[ngrids], NT = B->tile0[ngrids];
-  if (B->codes.ensure(NV) || B->terms.ensure(NV) || B->labels.ensure(NV) || B->rowcnt.ensure(NR) ||
-      B->offsets.ensure(NR + 1) || B->table.ensure(NS) || B->scal.ensure(4) || B->grids.ensure(ngrids) ||
-      B->cpb_dev.ensure(ngrids + 1) || B->bases_dev.ensure(2 * (ngrids + 1) + 2 * ngrids + 2))
+  if (B->codes.ensure(NV, st) || B->terms.ensure(NV, st) || B->labels.ensure(NV, st) || B->rowcnt.ensure(NR, st) ||
+      B->offsets.ensure(NR + 1, st) || B->table.ensure(NS, st) || B->scal.ensure(4, st) || B->grids.ensure(ngrids, st) ||
+      B->cpb_dev.ensure(ngrids + 1, st) || B->bases_dev.ensure(2 * (ngrids + 1) + 2 * ngrids + 2, st))
     return fail(berr(DMSC_ERR_OOM, "batch buffers"));
   const float *hgt = heights;
   if (!on_device) {
-    if (B->hgt.ensure(NV)) return fail(berr(DMSC_ERR_OOM, "batch heights"));
+    if (B->hgt.ensure(NV, st)) return fail(berr(DMSC_ERR_OOM, "batch heights"));
     if (cudaMemcpyAsync(B->hgt.p, heights, sizeof(float) * NV, cudaMemcpyHostToDevice, st) != cudaSuccess)
       return fail(berr(DMSC_ERR_CUDA, "heights copy"));
     hgt = B->hgt.p;
@@ -194,10 +194,10 @@ int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float 
   const long long ncp = B->cpb[ngrids];
   B->ncp = ncp;
   const size_t n = (size_t)ncp;
-  if (B->cp_cellid.ensure(n + 1) || B->cp_fn.ensure(n + 1) || B->cp_flags.ensure(n + 1) || B->cp_pair_cell.ensure(n + 1) ||
-      B->cp_des2.ensure(2 * n + 2) || B->cp_asc2.ensure(2 * n + 2) || B->cp_acnt.ensure(n + 1) ||
-      B->cp_dcnt.ensure(n + 1) || B->pair_idx.ensure(n + 1) || B->flags.ensure(n + 1) || B->aoff.ensure(n + 1) ||
-      B->doff.ensure(n + 1) || B->asc.ensure(4 * n + 1) || B->des.ensure(4 * n + 1))
+  if (B->cp_cellid.ensure(n + 1, st) || B->cp_fn.ensure(n + 1, st) || B->cp_flags.ensure(n + 1, st) || B->cp_pair_cell.ensure(n + 1, st) ||
+      B->cp_des2.ensure(2 * n + 2, st) || B->cp_asc2.ensure(2 * n + 2, st) || B->cp_acnt.ensure(n + 1, st) ||
+      B->cp_dcnt.ensure(n + 1, st) || B->pair_idx.ensure(n + 1, st) || B->flags.ensure(n + 1, st) || B->aoff.ensure(n + 1, st) ||
+      B->doff.ensure(n + 1, st) || B->asc.ensure(4 * n + 1, st) || B->des.ensure(4 * n + 1, st))
     return fail(berr(DMSC_ERR_OOM, "batch critical points"));
   CpOut cp{B->cp_cellid.p, B->cp_fn.p, B->cp_flags.p, B->cp_pair_cell.p, B->cp_des2.p, B->cp_asc2.p,
            B->cp_acnt.p, B->cp_dcnt.p, ncp};
@@ -282,7 +282,7 @@ int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float 
       }
     }
     if (rc == DMSC_OK) {
-      if (B->asc.ensure((size_t)io.nasc_out + 1) || B->des.ensure((size_t)io.ndes_out + 1) ||
+      if (B->asc.ensure((size_t)io.nasc_out + 1, st) || B->des.ensure((size_t)io.ndes_out + 1, st) ||
           simplify_batch_emit(io, B->asc.p, B->des.p, st))
         rc = berr(DMSC_ERR_CUDA, "batch simplify output");
     }

@@ -702,9 +702,11 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     k_redir_saddles<<<nb(ncp), 256, 0, st>>>(a, redir);
     DMSC_LAUNCHED(2);
   }
+  if (io.ev_hops[0]) L(cudaEventRecord(io.ev_hops[0], st));
   k_disc_hops<<<dim3(g.ntx, g.nty), HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, hop_to, hop_len, j64, nextc,
                                                                         io.status);
   DMSC_LAUNCHED(1);
+  if (io.ev_hops[1]) L(cudaEventRecord(io.ev_hops[1], st));
   L(cudaMemsetAsync(acnt, 0, sizeof(uint32_t) * ncp * 2, st));
   // extremum discs: vertices -> minima (asc_disc), faces -> maxima (des_disc),
   // grouped by owner with a stable sort (row-major order is the append order)

@@ -325,8 +325,9 @@ int dmsc_dataset_stage_times(dmsc_dataset *d, float *ms, int n) {
   if (!d || !ms) return fail(DMSC_ERR_BAD_ARG, "null argument");
   if (!d->ev_ready) return fail(DMSC_ERR_STATE, "timing was not enabled for the last run");
   CK(cudaSetDevice(d->ctx->device));
-  const int pairs[5][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 4}, {5, 6}};
-  for (int i = 0; i < n && i < 5; ++i) {
+  // gradient, collate_scan, border_resolve, labels_arcs, connectivity, disc_hops, discs
+  const int pairs[7][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 4}, {5, 6}, {7, 8}, {7, 9}};
+  for (int i = 0; i < n && i < 7; ++i) {
     CK(cudaEventSynchronize(d->ev[pairs[i][1]]));
     float t = 0;
     if (cudaEventElapsedTime(&t, d->ev[pairs[i][0]], d->ev[pairs[i][1]]) != cudaSuccess) { cudaGetLastError(); t = -1; }
@@ -394,8 +395,15 @@ int dmsc_dataset_fill_discs(dmsc_dataset *d, dmsc_msc *m, void *stream) {
   io.status = d->scal.p;
   // a gradient path visits each cell at most once: bounds every chain of a disc
   io.limit = (unsigned long long)(d->g.cx + 1) * (d->g.cy + 1) + 16;
+  const bool tm = d->ctx->timing && d->ev_ready;
+  if (tm) {
+    io.ev_hops[0] = d->ev[7];
+    io.ev_hops[1] = d->ev[8];
+    CK(cudaEventRecord(d->ev[7], st));
+  }
   CK(cudaMemsetAsync(d->scal.p, 0, sizeof(uint32_t), st));
   CK(fill_discs(io, st));
+  if (tm) CK(cudaEventRecord(d->ev[9], st));
   uint32_t stw = 0;
   CK(cudaMemcpyAsync(&stw, d->scal.p, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));

@@ -135,6 +135,7 @@ struct DiscIO {
   DevBuf<uint32_t> *adisc = nullptr, *ddisc = nullptr;
   uint32_t *status = nullptr;
   unsigned long long limit = 1ull << 31;  // bound on one gradient chain (cells of the window)
+  cudaEvent_t ev_hops[2] = {nullptr, nullptr};  // recorded around the hop kernel when set
   long long nadisc = 0, nddisc = 0;
 };
 cudaError_t fill_discs(DiscIO &io, cudaStream_t st);

@@ -6,11 +6,17 @@
 #include "dmsc.h"
 #include "dmsc_common.cuh"
 
-// Grow-only device buffer.
+// Grow-only device buffer.  ensure(count) uses cudaMalloc / cudaFree (which
+// synchronise the device); ensure(count, stream) uses the stream-ordered pool,
+// so growing a buffer never waits for work on other streams.  A buffer that
+// came from the pool is returned to it on release (ordered on the legacy
+// stream: every use of it has completed by then, each call that fills one
+// synchronises its own stream before returning).
 template <typename T>
 struct DevBuf {
   T *p = nullptr;
   size_t n = 0;
+  bool pooled = false;
   DevBuf() = default;
   DevBuf(const DevBuf &) = delete;
   DevBuf &operator=(const DevBuf &) = delete;
@@ -24,10 +30,29 @@ struct DevBuf {
     n = count;
     return cudaSuccess;
   }
-  void release() {
-    if (p) cudaFree(p);
+  cudaError_t ensure(size_t count, cudaStream_t st) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) {
+      if (pooled) cudaFreeAsync(p, st);
+      else cudaFree(p);
+    }
     p = nullptr;
     n = 0;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMallocAsync((void **)&p, sizeof(T) * count, st);
+    if (e != cudaSuccess) { p = nullptr; return e; }
+    n = count;
+    pooled = true;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) {
+      if (pooled) cudaFreeAsync(p, 0);
+      else cudaFree(p);
+    }
+    p = nullptr;
+    n = 0;
+    pooled = false;
   }
 };
 
@@ -52,7 +77,7 @@ struct dmsc_dataset {
   DevBuf<uint32_t> cp_cellid, cp_pair_cell, cp_des2, cp_asc2, cp_acnt, cp_dcnt, cp_pair_idx;
   DevBuf<float> cp_fn;
   DevBuf<uint8_t> cp_flags;
-  cudaEvent_t ev[8] = {};     // stage events (only when the context has timing enabled)
+  cudaEvent_t ev[10] = {};    // stage events (only when the context has timing enabled)
   bool ev_ready = false;
 
   long long nslots() const { return (long long)g.ntx * g.nty * dmsc::SLOTS_PER_TILE; }

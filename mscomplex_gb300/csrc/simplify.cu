@@ -48,7 +48,6 @@ struct SimpArgs {
   HeapEnt *heap;
   unsigned long long heap_cap;
   uint2 *resub;       // resubmit list (capacity heap_cap)
-  uint2 *pend;        // new edges of one cancellation (capacity heap_cap; warp replay only)
   uint2 *canc;        // cancellation list (capacity ncp)
   int rx0, ry0, rx1, ry1;  // m_rect of the complex (cell coordinates)
   double tresh;
@@ -191,242 +190,13 @@ struct Simp {
   }
 };
 
-// The same replay by a whole warp: lane 0 runs the graph logic while the
-// heap's sift paths are walked cooperatively -- a pop loads the 30 nodes of
-// the next 4 levels below the hole at once and chooses the path with
-// shuffles, a sift-up loads all ancestors at once and finds where the value
-// stops with a ballot -- so a heap operation costs a few dependent memory
-// round trips instead of one per level.  Every heap array write is the one
-// the single-thread replay makes, so the heap evolves identically.
-struct SimpW {
-  SimpArgs A;
-  unsigned long long nheap = 0;
-  static constexpr unsigned FULL = 0xffffffffu;
-
-  __device__ __forceinline__ static bool comp(float a, float b) { return a > b; }  // comp(x, y) on persistences
-
-  // sift-up of val from `hole` towards the root (__push_heap with topIndex 0)
-  __device__ void push_at(unsigned long long hole, HeapEnt val, int lane) {
-    HeapEnt *v = A.heap;
-    // lane i holds ancestor i + 1 of the hole
-    unsigned long long anc = hole;
-    for (int i = 0; i <= lane && anc > 0; ++i) anc = (anc - 1) / 2;
-    int depth = 0;  // ancestors of the hole: floor(log2(hole + 1))
-    for (unsigned long long h = hole + 1; h > 1; h >>= 1) ++depth;
-    const bool has = lane < depth;
-    HeapEnt mine = has ? v[anc] : HeapEnt{0.f, 0u, 0u};
-    const unsigned moves = __ballot_sync(FULL, has && comp(mine.d, val.d));
-    const int k = __ffs(~moves) - 1;  // consecutive moving ancestors from the parent up
-    // ancestor i + 1 (lane i < k) moves down into ancestor i (ancestor 0 = the hole)
-    if (lane < k) {
-      unsigned long long below = hole;
-      for (int i = 0; i < lane; ++i) below = (below - 1) / 2;
-      v[below] = mine;
-    }
-    if (lane == 0) {
-      unsigned long long dst = hole;
-      for (int i = 0; i < k; ++i) dst = (dst - 1) / 2;
-      v[dst] = val;
-    }
-    __syncwarp();
-  }
-  __device__ bool push(uint32_t a, uint32_t b, float d, int lane) {
-    if (nheap >= A.heap_cap) return false;
-    const HeapEnt x{d, a, b};
-    push_at(nheap, x, lane);
-    ++nheap;
-    return true;
-  }
-  __device__ HeapEnt pop(int lane) {
-    HeapEnt *v = A.heap;
-    const HeapEnt top = v[0];
-    if (nheap > 1) {
-      const unsigned long long len = nheap - 1;
-      const HeapEnt val = v[len];
-      unsigned long long hole = 0;
-      // lane l < 30 holds node l of the 4 levels below the hole (2, 4, 8, 16 nodes)
-      const int lvl = lane < 2 ? 1 : lane < 6 ? 2 : lane < 14 ? 3 : 4;
-      const int off = lane + 2 - (1 << lvl);
-      while (hole < (len - 1) / 2) {
-        const unsigned long long first = (hole + 1) * (1ull << lvl) - 1;
-        const unsigned long long idx = first + off;
-        const bool has = lane < 30 && idx < len;
-        HeapEnt mine = has ? v[idx] : HeapEnt{0.f, 0u, 0u};
-        unsigned long long cur = hole;
-        int steps = 0, path_lane[4];
-        for (int st = 0; st < 4 && cur < (len - 1) / 2; ++st) {
-          // children of cur at level st + 1 below the chunk's hole
-          const unsigned long long right = 2 * (cur + 1), left = right - 1;
-          const unsigned long long base = (hole + 1) * (1ull << (st + 1)) - 1;
-          const int lr = (1 << (st + 1)) - 2 + (int)(right - base), ll = lr - 1;
-          const float dr = __shfl_sync(FULL, mine.d, lr), dl = __shfl_sync(FULL, mine.d, ll);
-          const bool take_left = comp(dr, dl);
-          cur = take_left ? left : right;
-          path_lane[st] = take_left ? ll : lr;
-          ++steps;
-        }
-        // moves: node of path step st goes up to its parent (the hole for st = 0)
-        unsigned long long parent = hole;
-        for (int st = 0; st < steps; ++st) {
-          const int pl = path_lane[st];
-          if (lane == pl) v[parent] = mine;
-          const unsigned long long node = (hole + 1) * (1ull << (st + 1)) - 1 + (pl - ((1 << (st + 1)) - 2));
-          parent = node;
-        }
-        hole = cur;
-      }
-      if ((len & 1) == 0 && hole == (len - 2) / 2) {
-        const unsigned long long child = 2 * (hole + 1) - 1;
-        const HeapEnt c = v[child];
-        if (lane == 0) v[hole] = c;
-        hole = child;
-      }
-      __syncwarp();
-      push_at(hole, val, lane);
-    }
-    --nheap;
-    return top;
-  }
-
-  __device__ void run() {
-    const int lane = threadIdx.x & 31;
-    Graph &G = A.G;
-    const uint32_t n = G.ncp;
-    float max_val = 1.17549435e-38f;  // std::numeric_limits<float>::min(), as in the reference (:399)
-    float min_val = 3.40282347e+38f;
-    unsigned long long pushes = 0, pops = 0, nres = 0, ncanc = 0;
-    int fail = 0;
-    // strangulation pre-mark, value range, and every (cp, des) pair pushed in index order
-    for (uint32_t i = 0; i < n && !fail; ++i) {
-      if (lane == 0 && G.dim(i) == 1) {
-        for (int j = 0; j < 2; ++j) {
-          const uint32_t l = 2 * i + j;
-          if (G.L.total[l] == 2 && G.runs(l)[0].y == 2) G.flags[i] |= F_STRANG;  // both elements equal
-        }
-      }
-      const float f = A.fn[i];
-      max_val = (max_val < f) ? f : max_val;  // std::max
-      min_val = (f < min_val) ? f : min_val;  // std::min
-      const uint32_t ld = 2 * i + 1;
-      const uint32_t nr = G.L.nrun[ld];
-      for (uint32_t k = 0; k < nr && !fail; ++k) {
-        const uint2 r = G.runs(ld)[k];
-        const float d = fabsf(fsub_rn(A.fn[r.x], f));
-        for (uint32_t c = 0; c < r.y && !fail; ++c) {
-          if (!push(i, r.x, d, lane)) fail = 1;
-          else ++pushes;
-        }
-      }
-    }
-    __syncwarp();
-    const float max_persistence = fsub_rn(max_val, min_val);
-    while (nheap != 0 && !fail) {
-      if (lane == 0 && !G.tick()) fail = 1;
-      fail = __shfl_sync(FULL, fail, 0);
-      if (fail) break;
-      const HeapEnt e = pop(lane);
-      ++pops;
-      if ((double)e.d / (double)max_persistence > A.tresh) break;
-      // lane 0: checks and the cancellation; action 0 skip, 1 resubmitted, 2 cancelled (npend new edges)
-      int action = 0;
-      unsigned long long npend = 0;
-      if (lane == 0) {
-        uint32_t v1 = e.a, v2 = e.b;
-        if (G.dim(v2) == 1) { uint32_t t = v1; v1 = v2; v2 = t; }
-        const int cp2_dim = G.dim(v2);
-        bool skip = (G.flags[v1] & F_CANCELLED) || (G.flags[v2] & F_CANCELLED);
-        bool b1 = false, b2 = false;
-        if (!skip) {
-          b1 = on_boundary(v1); b2 = on_boundary(v2);
-          skip = b1 != b2;
-        }
-        const bool strang = !skip && (G.flags[v1] & F_STRANG);
-        if (!skip && strang && G.L.total[2 * v2 + cp2_dim / 2] != 1) {
-          if (nres >= A.heap_cap) fail = 1;
-          else { A.resub[nres++] = make_uint2(e.a, e.b); action = 1; }
-        } else if (!skip && !(strang && b1)) {
-          uint32_t cp0 = v1, cp1 = v2;
-          const bool connected = G.cancel_pairs(cp0, cp1);
-          if (G.fail) fail = 1;
-          if (!fail) {
-            G.flags[v1] |= F_BCANCEL;
-            G.flags[v2] |= F_BCANCEL;
-            G.pair_idx[v1] = v2;
-            G.pair_idx[v2] = v1;
-            if (ncanc >= n) fail = 1;
-            else A.canc[ncanc++] = make_uint2(e.a, e.b);
-          }
-          if (!fail && connected) {  // new edges (d, a) in the reference's order
-            const uint32_t la0 = 2 * cp0, ld1 = 2 * cp1 + 1;
-            for (uint32_t i = 0; i < G.L.nrun[la0] && !fail; ++i) {
-              const uint2 ra = G.runs(la0)[i];
-              if (ra.x == cp1) continue;
-              for (uint32_t ca = 0; ca < ra.y && !fail; ++ca)
-                for (uint32_t j = 0; j < G.L.nrun[ld1] && !fail; ++j) {
-                  const uint2 rd = G.runs(ld1)[j];
-                  if (rd.x == cp0) continue;
-                  for (uint32_t cd = 0; cd < rd.y && !fail; ++cd) {
-                    if (npend >= A.heap_cap) fail = 1;
-                    else A.pend[npend++] = make_uint2(rd.x, ra.x);
-                  }
-                }
-            }
-          }
-          action = 2;
-        }
-      }
-      __syncwarp();
-      fail = __shfl_sync(FULL, fail, 0);
-      action = __shfl_sync(FULL, action, 0);
-      if (fail) break;
-      if (action != 2) continue;
-      npend = __shfl_sync(FULL, npend, 0);
-      nres = __shfl_sync(FULL, nres, 0);
-      for (unsigned long long q = 0; q < npend && !fail; ++q) {
-        const uint2 p = A.pend[q];
-        if (!push(p.x, p.y, fabsf(fsub_rn(A.fn[p.y], A.fn[p.x])), lane)) fail = 1;
-        else ++pushes;
-      }
-      for (unsigned long long q = 0; q < nres && !fail; ++q) {
-        const uint2 p = A.resub[q];
-        if (!push(p.x, p.y, fabsf(fsub_rn(A.fn[p.y], A.fn[p.x])), lane)) fail = 1;
-        else ++pushes;
-      }
-      nres = 0;
-    }
-    ncanc = __shfl_sync(FULL, ncanc, 0);
-    if (lane == 0) {
-      if (fail) G.fail = true;
-      A.stats[0] = pushes;
-      A.stats[1] = pops;
-      A.stats[2] = ncanc;
-      if (!G.fail) {
-        for (unsigned long long k = ncanc; k-- > 0;) {
-          const uint2 c = A.canc[k];
-          if (!G.uncancel_pairs(c.x, c.y)) { A.stats[4] |= ST_INVARIANT; break; }
-          if (G.fail) break;
-        }
-      }
-      A.stats[3] = G.ops;
-      if (G.fail) A.stats[4] |= ST_SIMPLIFY_LIMIT;
-    }
-  }
-
-  __device__ __forceinline__ bool on_boundary(uint32_t k) const {  // m_rect.isOnBoundry
-    const uint32_t c = A.G.cellid[k];
-    const int x = (int16_t)(c & 0xffff), y = (int16_t)(c >> 16);
-    const bool contains = x >= A.rx0 && y >= A.ry0 && x <= A.rx1 && y <= A.ry1;
-    const bool interior = x > A.rx0 && y > A.ry0 && x < A.rx1 && y < A.ry1;
-    return contains && !interior;
-  }
-};
-
-// one warp replays the simplification (SimpW); launched with 32 threads
-__global__ void __launch_bounds__(32) k_simplify(SimpArgs a) {
-  if (blockIdx.x != 0) return;
-  SimpW s;
+__global__ void k_simplify(SimpArgs a) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  Simp s;
   s.A = a;
   s.run();
+  a.stats[3] = s.A.G.ops;
+  if (s.A.G.fail) a.stats[4] |= ST_SIMPLIFY_LIMIT;
 }
 
 // CSR (expanded, ascending) -> run-length lists.  Capacity of a list is its
@@ -490,8 +260,7 @@ cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st) {
   size_t sizes[] = {sizeof(uint32_t) * 2 * ncp, sizeof(uint32_t) * 2 * ncp, sizeof(uint32_t) * 2 * ncp,
                     sizeof(uint32_t) * 2 * ncp, sizeof(uint2) * pool_cap, sizeof(uint2) * tmp_cap, sizeof(HeapEnt) * heap_cap,
                     sizeof(uint2) * heap_cap, sizeof(uint2) * (ncp + 1), sizeof(unsigned long long) * 8,
-                    sizeof(uint8_t) * (ncp + 1), sizeof(uint32_t) * (ncp + 1), sizeof(uint32_t) * (ncp + 1),
-                    sizeof(uint2) * heap_cap};
+                    sizeof(uint8_t) * (ncp + 1), sizeof(uint32_t) * (ncp + 1), sizeof(uint32_t) * (ncp + 1)};
   size_t bytes = 0;
   for (size_t z : sizes) bytes += rnd(z);
   SimplifyWork *w = new SimplifyWork;
@@ -523,7 +292,6 @@ cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st) {
   G.flags = (uint8_t *)take();
   G.pair_idx = (uint32_t *)take();
   w->lens = (uint32_t *)take();
-  a.pend = (uint2 *)take();
   w->flags_in = io.flags;
   w->pair_in = io.pair_idx;
   a.rx0 = io.rect[0]; a.ry0 = io.rect[1]; a.rx1 = io.rect[2]; a.ry1 = io.rect[3];
@@ -586,11 +354,13 @@ void simplify_release(SimplifyIO &io, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 // batches: one block per complex to simplify, all in one launch
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(32) k_simplify_batch(SimpArgs *args, int n) {
-  if (blockIdx.x >= (unsigned)n) return;
-  SimpW s;
+__global__ void k_simplify_batch(SimpArgs *args, int n) {
+  if (threadIdx.x != 0 || blockIdx.x >= (unsigned)n) return;
+  Simp s;
   s.A = args[blockIdx.x];
   s.run();
+  s.A.stats[3] = s.A.G.ops;
+  if (s.A.G.fail) s.A.stats[4] |= ST_SIMPLIFY_LIMIT;
 }
 
 struct BatchSimplifyWork {
@@ -632,7 +402,7 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
   const size_t sizes[] = {4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * (ncp + 1),
                           sizeof(uint2) * pool_cap, sizeof(uint2) * tmp, sizeof(HeapEnt) * heap, sizeof(uint2) * heap,
                           sizeof(uint2) * canc, sizeof(unsigned long long) * 8 * (size_t)(ns + 1),
-                          sizeof(SimpArgs) * (size_t)(ns + 1), sizeof(uint2) * heap};
+                          sizeof(SimpArgs) * (size_t)(ns + 1)};
   size_t bytes = 0;
   for (size_t z : sizes) bytes += rnd(z);
   BatchSimplifyWork *w = new BatchSimplifyWork;
@@ -651,7 +421,6 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
   uint2 *dcanc = (uint2 *)take();
   w->dstats = (unsigned long long *)take();
   w->dargs = (SimpArgs *)take();
-  uint2 *dpend = (uint2 *)take();
   w->nsimp = ns;
   if (ncp) {
     k_lists_from_csr<<<blocks_for(ncp), 256, 0, st>>>(ncp, io.aoff, io.asc, io.doff, io.des, des_base, w->off, w->nrun,
@@ -686,7 +455,6 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
     a.fn = io.fn + c0;
     a.heap = dheap + ho;
     a.resub = dres + ho;
-    a.pend = dpend + ho;
     a.heap_cap = heap_of(nd);
     ho += a.heap_cap;
     a.canc = dcanc + co;

@@ -130,11 +130,14 @@ class GridDataset:
             check(self.lib.dmsc_dataset_export_critical(self.h, _ptr(out), None))
         return out
 
-    STAGES = ("gradient", "collate_scan", "border_resolve", "labels_arcs", "connectivity")
+    STAGES = ("gradient", "collate_scan", "border_resolve", "labels_arcs", "connectivity", "disc_hops", "discs")
 
-    def stage_times(self) -> dict:
-        ms = np.zeros(5, np.float32)
-        check(self.lib.dmsc_dataset_stage_times(self.h, _ptr(ms), 5))
+    def stage_times(self, with_discs: bool = False) -> dict:
+        """Device times (ms) of the last work / writeout_connectivity (and, with
+        with_discs, post_merge_fill_discs: its hop kernel and the whole pass)."""
+        n = 7 if with_discs else 5
+        ms = np.zeros(n, np.float32)
+        check(self.lib.dmsc_dataset_stage_times(self.h, _ptr(ms), n))
         return dict(zip(self.STAGES, (float(v) for v in ms)))
 
     def post_merge_fill_discs(self, msc: "GridMSComplex", stream=None) -> "GridMSComplex":
