@@ -310,6 +310,8 @@ __device__ __forceinline__ int chain_kind(uint32_t code, int rx, int ry) {
 }
 
 constexpr int HOP_THREADS = 512;
+// successor of an edge along its chain as a cell offset (dx + 2) + 5 (dy + 2), |dx|, |dy| <= 2
+constexpr uint8_t SUCC_NONE = 0xFF;
 constexpr int SEG_MAX = 64;  // cells of a write piece: the jump pointer distance (2^6)
 
 struct HopSmem {
@@ -324,7 +326,7 @@ struct HopSmem {
 // same run, HOP_END if the run is shorter).  One block per tile.
 __global__ void __launch_bounds__(HOP_THREADS, 3)
 k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict__ to, uint16_t *__restrict__ len,
-            uint32_t *__restrict__ j64, uint32_t *__restrict__ nextc, uint32_t *status) {
+            uint32_t *__restrict__ j64, uint8_t *__restrict__ nextd, uint32_t *status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   HopSmem &S = *reinterpret_cast<HopSmem *>(smem_raw);
   const int tx0 = blockIdx.x * TX, ty0 = blockIdx.y * TY;
@@ -356,17 +358,17 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict
     uint32_t nx = SLOT_NIL;
     if (slot_cell(sl, rx, ry)) {
       const int kind = chain_kind(code(rx, ry), rx, ry);
-      uint32_t succ = HOP_END;
+      uint8_t succ = SUCC_NONE;
       if (kind >= 0) {
         const int n = succ_local(g, kind, rx, ry, code, ox, oy);
         if (n < 0) st |= ST_INVARIANT;
-        if (n == 1) succ = (uint32_t)ox[0] | ((uint32_t)oy[0] << 16);
+        if (n == 1) succ = (uint8_t)((ox[0] - rx + 2) + 5 * (oy[0] - ry + 2));
         if (n == 1 && in_tile(ox[0], oy[0])) {
           nx = (uint32_t)((((oy[0] >> 1) - ty0) * TX + ((ox[0] >> 1) - tx0)) << 1) | (uint32_t)(oy[0] & 1);
           active = 1;
         }
       }
-      nextc[edge_id(g, rx, ry)] = succ;
+      nextd[edge_id(g, rx, ry)] = succ;
     }
     S.nv[sl] = (nx << 16) | 1u;
     S.tail[sl] = (uint16_t)sl;
@@ -437,7 +439,7 @@ struct ChainArgs {
   const uint32_t *hop_to;
   const uint16_t *hop_len;
   const uint32_t *j64;
-  const uint32_t *nextc;  // per edge: its chain successor (ext-local x | y << 16), HOP_END if none
+  const uint8_t *nextd;   // per edge: its chain successor as a cell offset (SUCC_NONE if none)
   uint32_t *kc;         // per cp: chains of a saddle handled here (0 otherwise)
   uint32_t *mc;         // per cp: level-0 items
   uint8_t *big;         // per cp: surviving saddle with more than KMAX chains
@@ -555,9 +557,10 @@ __global__ void k_seg_write(DiscArgs a, ChainArgs c, long long nsegs) {
     for (uint32_t i = 0; i < sg.w; ++i) {
       dst[i] = pack_cellid(g.ex0 + rx, g.ey0 + ry);
       if (i + 1 < sg.w) {
-        const uint32_t nc = c.nextc[edge_id(g, rx, ry)];
-        if (nc == HOP_END) { atomicOr(a.status, ST_INVARIANT); break; }
-        rx = (int)(nc & 0xffff); ry = (int)(nc >> 16);
+        const uint32_t d = c.nextd[edge_id(g, rx, ry)];
+        if (d == SUCC_NONE) { atomicOr(a.status, ST_INVARIANT); break; }
+        rx += (int)(d % 5) - 2;
+        ry += (int)(d / 5) - 2;
       }
     }
   }
@@ -586,28 +589,46 @@ __global__ void k_zip_blocks(DiscArgs a, ChainArgs c) {
   }
 }
 
-// one thread per chain: its cells, read in order from tmp, go to their
-// interleaved places block by block (the chains of one saddle are adjacent
-// threads, so their stores fill the same stretch of the disc together)
-__global__ void k_zip(DiscArgs a, ChainArgs c, long long nch, const uint32_t *off, uint32_t *out) {
-  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nch; k += (long long)gridDim.x * blockDim.x) {
-    const uint32_t s = c.csaddle[k], cb = c.cbase[s], j = (uint32_t)k - cb, L = c.clen[k];
-    const uint32_t base = off[s] + c.mc[s], end = off[s + 1];
-    const uint32_t *src = c.tmp + c.cofs[k];
-    uint32_t t = 1, bi = cb;
-    const uint32_t be = cb + c.kc[s];
-    while (t <= L && bi < be) {
-      const uint4 b = c.blocks[bi++];
-      if (!((b.z >> j) & 1u)) break;  // blocks end with the chain's last level
-      const uint32_t na = (uint32_t)__popc(b.z), r = (uint32_t)__popc(b.z & ((1u << j) - 1u));
-      const uint32_t te = b.y < L ? b.y : L;
-      if ((unsigned long long)base + b.w + (unsigned long long)(te - b.x) * na + r >= end) {
-        atomicOr(a.status, ST_INVARIANT);
-        break;
+// one warp per saddle: each of its blocks is a regular interleave of the
+// alive chains, written in order -- out[base + P + q] = the cell of level
+// t_b + q / a of the (q % a)-th alive chain
+__global__ void __launch_bounds__(256) k_zip(DiscArgs a, ChainArgs c, const uint32_t *off, uint32_t *out) {
+  __shared__ uint32_t src[8][KMAX];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long s = w0; s < a.ncp; s += nw) {
+    const uint32_t K = c.kc[s];
+    if (!K) continue;
+    const uint32_t cb = c.cbase[s], base = off[s] + c.mc[s], end = off[s + 1];
+    for (uint32_t bi = cb; bi < cb + K; ++bi) {
+      const uint4 b = c.blocks[bi];
+      if (!b.z || b.y < b.x) break;
+      const uint32_t na = (uint32_t)__popc(b.z), levels = b.y - b.x + 1;
+      const unsigned long long n64 = (unsigned long long)levels * na;
+      if ((unsigned long long)base + b.w + n64 > end) { if (lane == 0) atomicOr(a.status, ST_INVARIANT); break; }
+      const uint32_t n = (uint32_t)n64;  // within one disc, whose length fits 32 bits
+      // lane r < na: start in tmp of the r-th alive chain at level t_b
+      __syncwarp();
+      if (lane < (int)na) {
+        uint32_t m = b.z;
+        for (int z = 0; z < lane; ++z) m &= m - 1;
+        src[wib][lane] = c.cofs[cb + (uint32_t)__ffs(m) - 1] + b.x - 1;
       }
-      for (; t <= te; ++t) out[base + b.w + (t - b.x) * na + r] = src[t - 1];
+      __syncwarp();
+      uint32_t *o = out + base + b.w;
+      if (na == 1) {
+        const uint32_t *p = c.tmp + src[wib][0];
+        for (uint32_t q = lane; q < n; q += 32) o[q] = p[q];
+      } else if (na == 2) {
+        for (uint32_t q = lane; q < n; q += 32) o[q] = c.tmp[src[wib][q & 1] + (q >> 1)];
+      } else {
+        for (uint32_t q = lane; q < n; q += 32) {
+          const uint32_t t = q / na;
+          o[q] = c.tmp[src[wib][q - t * na] + t];
+        }
+      }
     }
-    if (t <= L) atomicOr(a.status, ST_INVARIANT);
   }
 }
 
@@ -669,9 +690,9 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   const long long nF = (long long)((g.rx1 - g.rx0) / 2) * ((g.ry1 - g.ry0) / 2);
   const long long nmax = std::max(std::max(nV, nF), std::max(io.nasc, io.ndes)) + 1;
   const long long nE = 2ll * g.vnx * g.vny;  // edge ids of the ext window
-  // words: 7 ncp + 8 | 4 nmax | 2 (nV + nF) | 3 ncp + 1 (kc, mc, cbase) | ncp / 4 (big) | 3.5 nE (hops)
+  // words: 7 ncp + 8 | 4 nmax | 2 (nV + nF) | 3 ncp + 1 (kc, mc, cbase) | ncp / 4 (big) | 2.75 nE (hops)
   size_t words = (size_t)ncp * 7 + 8 + (size_t)nmax * 4 + (size_t)(nV + nF) * 2 + (size_t)ncp * 3 + 1 +
-                 (size_t)ncp / 4 + 1 + 3 * (size_t)nE + (size_t)nE / 2 + 64;
+                 (size_t)ncp / 4 + 1 + 2 * (size_t)nE + (size_t)nE / 2 + (size_t)nE / 4 + 64;
   uint32_t *buf = nullptr;
   cudaError_t e = hops_attr();
   if (e != cudaSuccess) return e;
@@ -683,8 +704,9 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   uint32_t *gkey[2] = {vt + nmax, vt + nmax + nV}, *gval[2] = {vt + nmax + nV + nF, vt + nmax + 2 * nV + nF};
   uint32_t *kc = gval[1] + nF, *mc = kc + ncp, *cbase = mc + ncp;  // cbase: ncp+1
   uint8_t *big = (uint8_t *)(cbase + ncp + 1);
-  uint32_t *hop_to = cbase + ncp + 1 + ncp / 4 + 1, *j64 = hop_to + nE, *nextc = j64 + nE;
-  uint16_t *hop_len = (uint16_t *)(nextc + nE);
+  uint32_t *hop_to = cbase + ncp + 1 + ncp / 4 + 1, *j64 = hop_to + nE;
+  uint16_t *hop_len = (uint16_t *)(j64 + nE);
+  uint8_t *nextd = (uint8_t *)(hop_len + nE);
   const long long gn[2] = {nV, nF};
   auto L = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
   uint32_t *chain_buf = nullptr, *tmp = nullptr;
@@ -703,7 +725,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     DMSC_LAUNCHED(2);
   }
   if (io.ev_hops[0]) L(cudaEventRecord(io.ev_hops[0], st));
-  k_disc_hops<<<dim3(g.ntx, g.nty), HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, hop_to, hop_len, j64, nextc,
+  k_disc_hops<<<dim3(g.ntx, g.nty), HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, hop_to, hop_len, j64, nextd,
                                                                         io.status);
   DMSC_LAUNCHED(1);
   if (io.ev_hops[1]) L(cudaEventRecord(io.ev_hops[1], st));
@@ -744,7 +766,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     }
     SeedRuns sr{val, sstart, scount};
     ChainArgs c{};
-    c.hop_to = hop_to; c.hop_len = hop_len; c.j64 = j64; c.nextc = nextc;
+    c.hop_to = hop_to; c.hop_len = hop_len; c.j64 = j64; c.nextd = nextd;
     c.kc = kc; c.mc = mc; c.big = big; c.cbase = cbase; c.limit = io.limit;
     k_chain_count<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c);
     DMSC_LAUNCHED(1);
@@ -795,7 +817,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);
     DMSC_LAUNCHED(3);
     if (nch) {
-      k_zip<<<nb(nch), 128, 0, st>>>(a, c, nch, offs, ob->p);
+      k_zip<<<nb(32ll * ncp), 256, 0, st>>>(a, c, offs, ob->p);
       DMSC_LAUNCHED(1);
     }
     long long n = gn[kind];
