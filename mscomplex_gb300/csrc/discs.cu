@@ -543,26 +543,46 @@ __global__ void k_level0(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, const u
   }
 }
 
-// one thread per piece (at most SEG_MAX cells of one chain): follow the
-// successor cells into the chain's span of tmp
-__global__ void k_seg_write(DiscArgs a, ChainArgs c, long long nsegs) {
+// Pieces of at most SEG_MAX cells of one chain.  Each lane of a warp follows
+// the 1-byte successor offsets of one piece into shared memory, then the
+// warp copies the 32 pieces out one after another with coalesced stores into
+// their chains' spans of tmp (a lane's own stores would each touch a
+// different sector).
+constexpr int SEG_WARPS = 4;
+__global__ void __launch_bounds__(SEG_WARPS * 32) k_seg_write(DiscArgs a, ChainArgs c, long long nsegs) {
+  __shared__ uint32_t buf[SEG_WARPS][32][SEG_MAX + 1];  // +1: lanes' rows fall in different banks
   const GridGeom &g = a.g;
-  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nsegs; k += (long long)gridDim.x * blockDim.x) {
-    const uint4 sg = c.segs[k];
-    const uint32_t ch = sg.x;
-    if (sg.z - 1 + sg.w > c.clen[ch]) { atomicOr(a.status, ST_INVARIANT); continue; }
-    uint32_t *dst = c.tmp + c.cofs[ch] + (sg.z - 1);
-    int rx, ry;
-    edge_cell(g, sg.y, rx, ry);
-    for (uint32_t i = 0; i < sg.w; ++i) {
-      dst[i] = pack_cellid(g.ex0 + rx, g.ey0 + ry);
-      if (i + 1 < sg.w) {
-        const uint32_t d = c.nextd[edge_id(g, rx, ry)];
-        if (d == SUCC_NONE) { atomicOr(a.status, ST_INVARIANT); break; }
-        rx += (int)(d % 5) - 2;
-        ry += (int)(d / 5) - 2;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long gw = ((long long)blockIdx.x * SEG_WARPS + w), nwarps = (long long)gridDim.x * SEG_WARPS;
+  for (long long k0 = gw * 32; k0 < nsegs; k0 += nwarps * 32) {
+    const long long k = k0 + lane;
+    uint32_t len = 0, dst = 0;
+    if (k < nsegs) {
+      const uint4 sg = c.segs[k];
+      const uint32_t ch = sg.x;
+      if (sg.z - 1 + sg.w > c.clen[ch]) atomicOr(a.status, ST_INVARIANT);
+      else {
+        dst = c.cofs[ch] + (sg.z - 1);
+        int rx, ry;
+        edge_cell(g, sg.y, rx, ry);
+        for (uint32_t i = 0; i < sg.w; ++i) {
+          buf[w][lane][i] = pack_cellid(g.ex0 + rx, g.ey0 + ry);
+          ++len;
+          if (i + 1 < sg.w) {
+            const uint32_t d = c.nextd[edge_id(g, rx, ry)];
+            if (d == SUCC_NONE) { atomicOr(a.status, ST_INVARIANT); break; }
+            rx += (int)(d % 5) - 2;
+            ry += (int)(d / 5) - 2;
+          }
+        }
       }
     }
+    __syncwarp();
+    for (int p = 0; p < 32; ++p) {
+      const uint32_t n = __shfl_sync(0xffffffffu, len, p), o = __shfl_sync(0xffffffffu, dst, p);
+      for (uint32_t i = lane; i < n; i += 32) c.tmp[o + i] = buf[w][p][i];
+    }
+    __syncwarp();
   }
 }
 
@@ -589,43 +609,59 @@ __global__ void k_zip_blocks(DiscArgs a, ChainArgs c) {
   }
 }
 
-// one warp per saddle: each of its blocks is a regular interleave of the
-// alive chains, written in order -- out[base + P + q] = the cell of level
-// t_b + q / a of the (q % a)-th alive chain
+// One warp per 32 consecutive saddles: lane i loads the header of saddle i;
+// then, saddle by saddle, lane j < K loads block j and the tmp start of chain
+// j at once, and the warp writes each block -- a regular interleave of its
+// alive chains: out[base + P + q] = the cell of level t_b + q / a of the
+// (q % a)-th alive chain -- with coalesced stores.
 __global__ void __launch_bounds__(256) k_zip(DiscArgs a, ChainArgs c, const uint32_t *off, uint32_t *out) {
-  __shared__ uint32_t src[8][KMAX];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
   const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long s = w0; s < a.ncp; s += nw) {
-    const uint32_t K = c.kc[s];
-    if (!K) continue;
-    const uint32_t cb = c.cbase[s], base = off[s] + c.mc[s], end = off[s + 1];
-    for (uint32_t bi = cb; bi < cb + K; ++bi) {
-      const uint4 b = c.blocks[bi];
-      if (!b.z || b.y < b.x) break;
-      const uint32_t na = (uint32_t)__popc(b.z), levels = b.y - b.x + 1;
-      const unsigned long long n64 = (unsigned long long)levels * na;
-      if ((unsigned long long)base + b.w + n64 > end) { if (lane == 0) atomicOr(a.status, ST_INVARIANT); break; }
-      const uint32_t n = (uint32_t)n64;  // within one disc, whose length fits 32 bits
-      // lane r < na: start in tmp of the r-th alive chain at level t_b
-      __syncwarp();
-      if (lane < (int)na) {
-        uint32_t m = b.z;
-        for (int z = 0; z < lane; ++z) m &= m - 1;
-        src[wib][lane] = c.cofs[cb + (uint32_t)__ffs(m) - 1] + b.x - 1;
-      }
-      __syncwarp();
-      uint32_t *o = out + base + b.w;
-      if (na == 1) {
-        const uint32_t *p = c.tmp + src[wib][0];
-        for (uint32_t q = lane; q < n; q += 32) o[q] = p[q];
-      } else if (na == 2) {
-        for (uint32_t q = lane; q < n; q += 32) o[q] = c.tmp[src[wib][q & 1] + (q >> 1)];
-      } else {
-        for (uint32_t q = lane; q < n; q += 32) {
-          const uint32_t t = q / na;
-          o[q] = c.tmp[src[wib][q - t * na] + t];
+  for (long long s0 = w0 * 32; s0 < a.ncp; s0 += nw * 32) {
+    const long long sl = s0 + lane;
+    uint32_t K = 0, cb = 0, base = 0, end = 0;
+    if (sl < a.ncp) {
+      K = c.kc[sl];
+      if (K) { cb = c.cbase[sl]; base = off[sl] + c.mc[sl]; end = off[sl + 1]; }
+    }
+    unsigned todo = __ballot_sync(FULL, K != 0);
+    while (todo) {
+      const int p = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const uint32_t Kp = __shfl_sync(FULL, K, p), cbp = __shfl_sync(FULL, cb, p);
+      const uint32_t bp = __shfl_sync(FULL, base, p), ep = __shfl_sync(FULL, end, p);
+      uint4 blk = make_uint4(1, 0, 0, 0);
+      uint32_t cof = 0;
+      if ((uint32_t)lane < Kp) { blk = c.blocks[cbp + lane]; cof = c.cofs[cbp + lane]; }
+      for (uint32_t bi = 0; bi < Kp; ++bi) {
+        const uint32_t tb = __shfl_sync(FULL, blk.x, bi), te = __shfl_sync(FULL, blk.y, bi);
+        const uint32_t mask = __shfl_sync(FULL, blk.z, bi), P = __shfl_sync(FULL, blk.w, bi);
+        if (!mask || te < tb) break;
+        const uint32_t na = (uint32_t)__popc(mask), levels = te - tb + 1;
+        const unsigned long long n64 = (unsigned long long)levels * na;
+        if ((unsigned long long)bp + P + n64 > ep) { if (lane == 0) atomicOr(a.status, ST_INVARIANT); break; }
+        const uint32_t n = (uint32_t)n64;  // within one disc, whose length fits 32 bits
+        // start in tmp (at level tb) of the r-th alive chain, for r = lane < na
+        uint32_t m = mask;
+        for (int z = 0; z < lane && m; ++z) m &= m - 1;
+        const int jr = m ? __ffs(m) - 1 : 0;
+        const uint32_t my_src = __shfl_sync(FULL, cof, jr) + tb - 1;
+        uint32_t *o = out + bp + P;
+        if (na == 1) {
+          const uint32_t *q0 = c.tmp + __shfl_sync(FULL, my_src, 0);
+          for (uint32_t q = lane; q < n; q += 32) o[q] = q0[q];
+        } else if (na == 2) {
+          const uint32_t s0x = __shfl_sync(FULL, my_src, 0), s1x = __shfl_sync(FULL, my_src, 1);
+          for (uint32_t q = lane; q < n; q += 32) o[q] = c.tmp[((q & 1) ? s1x : s0x) + (q >> 1)];
+        } else {
+          for (uint32_t q0 = 0; q0 < n; q0 += 32) {
+            const uint32_t q = q0 + lane;
+            const uint32_t t = q / na, r = q - t * na;
+            const uint32_t sr = __shfl_sync(FULL, my_src, (int)(r & 31));
+            if (q < n) o[q] = c.tmp[sr + t];
+          }
         }
       }
     }
@@ -809,7 +845,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
       DMSC_LAUNCHED(1);
     }
     if (tot[1]) {
-      k_seg_write<<<nb(tot[1]), 128, 0, st>>>(a, c, tot[1]);
+      k_seg_write<<<nb((tot[1] + 31) / 32 * 32), SEG_WARPS * 32, 0, st>>>(a, c, tot[1]);
       DMSC_LAUNCHED(1);
     }
     k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c);
@@ -817,7 +853,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);
     DMSC_LAUNCHED(3);
     if (nch) {
-      k_zip<<<nb(32ll * ncp), 256, 0, st>>>(a, c, offs, ob->p);
+      k_zip<<<nb(ncp), 256, 0, st>>>(a, c, offs, ob->p);
       DMSC_LAUNCHED(1);
     }
     long long n = gn[kind];
