@@ -448,7 +448,7 @@ struct ChainArgs {
   uint4 *segs;          // (chain, first edge, first level, cells)
   uint32_t *cofs;       // exclusive scan of clen: each chain's cells in tmp
   uint32_t *tmp;        // chain-major cells
-  uint4 *blocks;        // per chain slot of a saddle: (first level, last level, alive mask, offset)
+  uint4 *blocks;        // per chain slot of a saddle, 2 uint4: an interleave record (k_zip_blocks)
   unsigned long long limit;
 };
 
@@ -588,81 +588,67 @@ __global__ void __launch_bounds__(SEG_WARPS * 32) k_seg_write(DiscArgs a, ChainA
 
 // Per saddle: the level ranges over which the set of alive chains is
 // constant.  Between consecutive distinct chain lengths the disc is a
-// regular interleave of the alive chains.
-__global__ void k_zip_blocks(DiscArgs a, ChainArgs c) {
+// regular interleave of the alive chains.  Each range becomes a record of
+// two uint4: (first output position, cells, alive chains, alive mask) and
+// (tmp start of the first and second alive chain at the range's first level,
+// the saddle's first chain slot, the first level).
+__global__ void k_zip_blocks(DiscArgs a, ChainArgs c, const uint32_t *off) {
   for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < a.ncp; s += gridDim.x * blockDim.x) {
     const uint32_t K = c.kc[s], cb = c.cbase[s];
     if (!K) continue;
     uint32_t L[KMAX];
     for (uint32_t q = 0; q < K; ++q) L[q] = c.clen[cb + q];
+    const uint32_t base = off[s] + c.mc[s];
     uint32_t prev = 0, P = 0, nb = 0;
     for (;;) {
       uint32_t u = 0xFFFFFFFFu, mask = 0;
       for (uint32_t q = 0; q < K; ++q)
         if (L[q] > prev) { mask |= 1u << q; u = L[q] < u ? L[q] : u; }
       if (!mask) break;
-      c.blocks[cb + nb++] = make_uint4(prev + 1, u, mask, P);
-      P += (u - prev) * (uint32_t)__popc(mask);
+      const uint32_t na = (uint32_t)__popc(mask), n = (u - prev) * na;
+      const uint32_t j0 = (uint32_t)__ffs(mask) - 1, m1 = mask & (mask - 1);
+      const uint32_t j1 = m1 ? (uint32_t)__ffs(m1) - 1 : j0;
+      c.blocks[2 * (cb + nb)] = make_uint4(base + P, n, na, mask);
+      c.blocks[2 * (cb + nb) + 1] = make_uint4(c.cofs[cb + j0] + prev, c.cofs[cb + j1] + prev, cb, prev + 1);
+      ++nb;
+      P += n;
       prev = u;
     }
-    for (; nb < K; ++nb) c.blocks[cb + nb] = make_uint4(1, 0, 0, 0);
+    for (; nb < K; ++nb) c.blocks[2 * (cb + nb)] = make_uint4(0, 0, 0, 0);
   }
 }
 
-// One warp per 32 consecutive saddles: lane i loads the header of saddle i;
-// then, saddle by saddle, lane j < K loads block j and the tmp start of chain
-// j at once, and the warp writes each block -- a regular interleave of its
-// alive chains: out[base + P + q] = the cell of level t_b + q / a of the
-// (q % a)-th alive chain -- with coalesced stores.
-__global__ void __launch_bounds__(256) k_zip(DiscArgs a, ChainArgs c, const uint32_t *off, uint32_t *out) {
-  const unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
+// One warp per record: out[start + q] = the cell of level t_b + q / a of the
+// (q % a)-th alive chain, coalesced stores.
+__global__ void __launch_bounds__(256) k_zip(DiscArgs a, ChainArgs c, long long nch, uint32_t *out,
+                                             unsigned long long out_len) {
+  __shared__ uint32_t src[8][KMAX];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long s0 = w0 * 32; s0 < a.ncp; s0 += nw * 32) {
-    const long long sl = s0 + lane;
-    uint32_t K = 0, cb = 0, base = 0, end = 0;
-    if (sl < a.ncp) {
-      K = c.kc[sl];
-      if (K) { cb = c.cbase[sl]; base = off[sl] + c.mc[sl]; end = off[sl + 1]; }
-    }
-    unsigned todo = __ballot_sync(FULL, K != 0);
-    while (todo) {
-      const int p = __ffs(todo) - 1;
-      todo &= todo - 1;
-      const uint32_t Kp = __shfl_sync(FULL, K, p), cbp = __shfl_sync(FULL, cb, p);
-      const uint32_t bp = __shfl_sync(FULL, base, p), ep = __shfl_sync(FULL, end, p);
-      uint4 blk = make_uint4(1, 0, 0, 0);
-      uint32_t cof = 0;
-      if ((uint32_t)lane < Kp) { blk = c.blocks[cbp + lane]; cof = c.cofs[cbp + lane]; }
-      for (uint32_t bi = 0; bi < Kp; ++bi) {
-        const uint32_t tb = __shfl_sync(FULL, blk.x, bi), te = __shfl_sync(FULL, blk.y, bi);
-        const uint32_t mask = __shfl_sync(FULL, blk.z, bi), P = __shfl_sync(FULL, blk.w, bi);
-        if (!mask || te < tb) break;
-        const uint32_t na = (uint32_t)__popc(mask), levels = te - tb + 1;
-        const unsigned long long n64 = (unsigned long long)levels * na;
-        if ((unsigned long long)bp + P + n64 > ep) { if (lane == 0) atomicOr(a.status, ST_INVARIANT); break; }
-        const uint32_t n = (uint32_t)n64;  // within one disc, whose length fits 32 bits
-        // start in tmp (at level tb) of the r-th alive chain, for r = lane < na
-        uint32_t m = mask;
-        for (int z = 0; z < lane && m; ++z) m &= m - 1;
-        const int jr = m ? __ffs(m) - 1 : 0;
-        const uint32_t my_src = __shfl_sync(FULL, cof, jr) + tb - 1;
-        uint32_t *o = out + bp + P;
-        if (na == 1) {
-          const uint32_t *q0 = c.tmp + __shfl_sync(FULL, my_src, 0);
-          for (uint32_t q = lane; q < n; q += 32) o[q] = q0[q];
-        } else if (na == 2) {
-          const uint32_t s0x = __shfl_sync(FULL, my_src, 0), s1x = __shfl_sync(FULL, my_src, 1);
-          for (uint32_t q = lane; q < n; q += 32) o[q] = c.tmp[((q & 1) ? s1x : s0x) + (q >> 1)];
-        } else {
-          for (uint32_t q0 = 0; q0 < n; q0 += 32) {
-            const uint32_t q = q0 + lane;
-            const uint32_t t = q / na, r = q - t * na;
-            const uint32_t sr = __shfl_sync(FULL, my_src, (int)(r & 31));
-            if (q < n) o[q] = c.tmp[sr + t];
-          }
-        }
+  for (long long k = w0; k < nch; k += nw) {
+    const uint4 r0 = c.blocks[2 * k];
+    if (!r0.y) continue;
+    const uint4 r1 = c.blocks[2 * k + 1];
+    const uint32_t n = r0.y, na = r0.z;
+    if ((unsigned long long)r0.x + n > out_len) { if (lane == 0) atomicOr(a.status, ST_INVARIANT); continue; }
+    uint32_t *o = out + r0.x;
+    if (na == 1) {
+      const uint32_t *p = c.tmp + r1.x;
+      for (uint32_t q = lane; q < n; q += 32) o[q] = p[q];
+    } else if (na == 2) {
+      for (uint32_t q = lane; q < n; q += 32) o[q] = c.tmp[((q & 1) ? r1.y : r1.x) + (q >> 1)];
+    } else {
+      __syncwarp();
+      if (lane < (int)na) {  // lane r: tmp start of the r-th alive chain
+        uint32_t m = r0.w;
+        for (int z = 0; z < lane; ++z) m &= m - 1;
+        src[wib][lane] = c.cofs[r1.z + (uint32_t)__ffs(m) - 1] + r1.w - 1;
+      }
+      __syncwarp();
+      for (uint32_t q = lane; q < n; q += 32) {
+        const uint32_t t = q / na;
+        o[q] = c.tmp[src[wib][q - t * na] + t];
       }
     }
   }
@@ -813,7 +799,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     if (e != cudaSuccess) break;
     // per chain: cstart csaddle clen cnseg | csegoff cofs (nch + 1 each)
     L(cudaMallocAsync((void **)&chain_buf, sizeof(uint32_t) * (6ull * nch + 8), st));
-    L(cudaMallocAsync((void **)&blocks, sizeof(uint4) * ((size_t)nch + 1), st));
+    L(cudaMallocAsync((void **)&blocks, sizeof(uint4) * (2 * (size_t)nch + 2), st));
     if (e != cudaSuccess) break;
     c.cstart = chain_buf; c.csaddle = chain_buf + nch; c.clen = chain_buf + 2 * nch; c.cnseg = chain_buf + 3 * nch;
     c.csegoff = chain_buf + 4 * nch;      // nch + 1
@@ -848,12 +834,12 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
       k_seg_write<<<nb((tot[1] + 31) / 32 * 32), SEG_WARPS * 32, 0, st>>>(a, c, tot[1]);
       DMSC_LAUNCHED(1);
     }
-    k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c);
+    k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c, offs);
     k_level0<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, offs, ob->p);
     k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);
     DMSC_LAUNCHED(3);
     if (nch) {
-      k_zip<<<nb(ncp), 256, 0, st>>>(a, c, offs, ob->p);
+      k_zip<<<nb(32ll * nch), 256, 0, st>>>(a, c, nch, ob->p, (unsigned long long)tot[0]);
       DMSC_LAUNCHED(1);
     }
     long long n = gn[kind];
