@@ -82,32 +82,54 @@ __global__ void k_redir_saddles(DiscArgs a, uint32_t *redir) {
   }
 }
 
-// 2. owner keys of the rect vertices (kind 0) or faces (kind 1), row-major
-__global__ void k_disc_keys(DiscArgs a, const uint32_t *redir, int kind, uint32_t *key, uint32_t *val) {
-  const GridGeom &g = a.g;
-  int x0 = g.rx0 + kind, y0 = g.ry0 + kind;
-  int nx = (g.rx1 - g.rx0) / 2 + 1 - kind, ny = (g.ry1 - g.ry0) / 2 + 1 - kind;
-  long long n = (long long)nx * ny;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    int jj = (int)(t / nx), ii = (int)(t - (long long)jj * nx);
-    int rx = x0 + 2 * ii, ry = y0 + 2 * jj;
-    uint4 L = a.labels[(long long)(ry >> 1) * g.vnx + (rx >> 1)];
-    uint32_t m = kind ? L.w : L.x, o = LABEL_NONE;
-    if (m != LABEL_NONE) {
-      if (m >= a.ncp_ds || m >= a.ncp) { atomicOr(a.status, ST_INVARIANT); m = LABEL_NONE; }
-      else {
-        uint32_t mc = a.cellid[m];
-        o = rect_has(g, cx(mc), cy(mc)) ? redir[m] : m;
-        // the owner must be a surviving extremum of the right dimension
-        if (o >= a.ncp || (a.flags[o] & F_BCANCEL) || cdim(a.cellid[o]) != 2 * kind) {
-          atomicOr(a.status, ST_INVARIANT);
-          o = LABEL_NONE;
-        }
-      }
+// 2a. the disc owner of every critical point used as a label: one level of
+// redirection (:1142-1187).  fo = owner | grid << 30 (grid 0: a minimum, for
+// vertices; 1: a maximum, for faces); FO_BAD where a label would break the
+// reference's invariants (the owner must be a surviving extremum of the
+// label's dimension).
+constexpr uint32_t FO_BAD = 0xFFFFFFFFu;
+__global__ void k_owner_final(DiscArgs a, const uint32_t *redir, uint32_t *fo) {
+  const uint32_t n = a.ncp_ds < a.ncp ? a.ncp_ds : a.ncp;
+  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+    const uint32_t mc = a.cellid[m];
+    const int d = cdim(mc);
+    uint32_t o = FO_BAD;
+    if (d != 1) {
+      const uint32_t r = rect_has(a.g, cx(mc), cy(mc)) ? redir[m] : m;
+      if (r < a.ncp && !(a.flags[r] & F_BCANCEL) && cdim(a.cellid[r]) == d) o = r | ((uint32_t)(d >> 1) << 30);
     }
-    key[t] = o == LABEL_NONE ? a.ncp : o;
-    val[t] = pack_cellid(g.ex0 + rx, g.ey0 + ry);
+    fo[m] = o;
   }
+}
+
+// 2b. owner keys of the rect vertices (vertex grid) and faces (face grid),
+// row-major, from one read of the labels
+__global__ void k_disc_keys(DiscArgs a, const uint32_t *fo, uint32_t *key0, uint32_t *val0, uint32_t *key1,
+                            uint32_t *val1) {
+  const GridGeom &g = a.g;
+  const int nx = (g.rx1 - g.rx0) / 2 + 1, ny = (g.ry1 - g.ry0) / 2 + 1;
+  const uint32_t n_ok = a.ncp_ds < a.ncp ? a.ncp_ds : a.ncp;
+  const long long n = (long long)nx * ny;
+  uint32_t bad = 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int jj = (int)(t / nx), ii = (int)(t - (long long)jj * nx);
+    const int rx = g.rx0 + 2 * ii, ry = g.ry0 + 2 * jj;
+    const uint4 L = a.labels[(long long)(ry >> 1) * g.vnx + (rx >> 1)];
+    for (int kind = 0; kind < 2; ++kind) {
+      if (kind && (ii == nx - 1 || jj == ny - 1)) continue;
+      const uint32_t m = kind ? L.w : L.x;
+      uint32_t o = a.ncp;
+      if (m != LABEL_NONE) {
+        const uint32_t v = m < n_ok ? fo[m] : FO_BAD;
+        if (v == FO_BAD || (v >> 30) != (uint32_t)kind) bad = 1;
+        else o = v & 0x3FFFFFFFu;
+      }
+      const long long fi = kind ? (long long)jj * (nx - 1) + ii : t;
+      (kind ? key1 : key0)[fi] = o;
+      (kind ? val1 : val0)[fi] = pack_cellid(g.ex0 + rx + kind, g.ey0 + ry + kind);
+    }
+  }
+  if (bad) atomicOr(a.status, ST_INVARIANT);
 }
 
 // 3. seeds from cancelled extrema: counts, then (saddle, pusher) items in pusher order
@@ -255,9 +277,9 @@ __global__ void k_saddle_disc_write(DiscArgs a, int kind, SeedRuns sr, const uin
 //     m + sum_j' min(L_j', t - 1) + #{ j' < j : L_j' >= t }
 // where L_j is the length of chain j.  Chains are followed in "hops": per
 // 64x64 vertex tile, list ranking in shared memory gives every edge the
-// number of cells to its tile exit, the edge after it and the edge 64 cells
-// ahead, so a chain's length costs one step per tile crossed and its cells
-// are written by one thread per piece of at most 64 cells, into a
+// number of cells to its tile exit, the edge after it and the edge SEG_MAX
+// cells ahead, so a chain's length costs one step per tile crossed and its
+// cells are written by one thread per piece of at most SEG_MAX cells, into a
 // chain-major buffer that a last pass interleaves.
 // ---------------------------------------------------------------------------
 constexpr int KMAX = 32;                 // saddles with more chains take the serial pass
@@ -312,21 +334,23 @@ __device__ __forceinline__ int chain_kind(uint32_t code, int rx, int ry) {
 constexpr int HOP_THREADS = 512;
 // successor of an edge along its chain as a cell offset (dx + 2) + 5 (dy + 2), |dx|, |dy| <= 2
 constexpr uint8_t SUCC_NONE = 0xFF;
-constexpr int SEG_MAX = 64;  // cells of a write piece: the jump pointer distance (2^6)
+constexpr int SEG_LOG = 5, SEG_MAX = 1 << SEG_LOG;  // cells of a write piece: the jump pointer distance
 
+constexpr uint8_t SUCC_TWO = 0xFE;  // a cell with two successors (it ends no chain)
 struct HopSmem {
   uint32_t code[(TX + 2) * (TY + 2)];
   uint32_t nv[HOP_SLOTS];     // next slot << 16 | cells counted so far
   uint16_t tail[HOP_SLOTS];
+  uint8_t sd[HOP_SLOTS];      // successor offset code of every slot (SUCC_NONE / SUCC_TWO)
 };
 
 // Per edge, for the chains of its own kind: hop_to (the edge after its
 // in-tile run, HOP_END if the chain ends in the tile), hop_len (cells of the
-// run, 0 for a branching cell) and j64 (the edge SEG_MAX cells ahead in the
+// run, 0 for a branching cell) and jseg (the edge SEG_MAX cells ahead in the
 // same run, HOP_END if the run is shorter).  One block per tile.
 __global__ void __launch_bounds__(HOP_THREADS, 3)
 k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict__ to, uint16_t *__restrict__ len,
-            uint32_t *__restrict__ j64, uint8_t *__restrict__ nextd, uint32_t *status) {
+            uint32_t *__restrict__ jseg, uint8_t *__restrict__ nextd, uint32_t *status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   HopSmem &S = *reinterpret_cast<HopSmem *>(smem_raw);
   const int tx0 = blockIdx.x * TX, ty0 = blockIdx.y * TY;
@@ -358,23 +382,27 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict
     uint32_t nx = SLOT_NIL;
     if (slot_cell(sl, rx, ry)) {
       const int kind = chain_kind(code(rx, ry), rx, ry);
-      uint8_t succ = SUCC_NONE;
+      uint8_t succ = SUCC_NONE, sd = SUCC_NONE;
       if (kind >= 0) {
         const int n = succ_local(g, kind, rx, ry, code, ox, oy);
         if (n < 0) st |= ST_INVARIANT;
-        if (n == 1) succ = (uint8_t)((ox[0] - rx + 2) + 5 * (oy[0] - ry + 2));
+        if (n == 1) sd = succ = (uint8_t)((ox[0] - rx + 2) + 5 * (oy[0] - ry + 2));
+        if (n == 2) sd = SUCC_TWO;
         if (n == 1 && in_tile(ox[0], oy[0])) {
           nx = (uint32_t)((((oy[0] >> 1) - ty0) * TX + ((ox[0] >> 1) - tx0)) << 1) | (uint32_t)(oy[0] & 1);
           active = 1;
         }
       }
       nextd[edge_id(g, rx, ry)] = succ;
+      S.sd[sl] = sd;
+    } else {
+      S.sd[sl] = SUCC_NONE;
     }
     S.nv[sl] = (nx << 16) | 1u;
     S.tail[sl] = (uint16_t)sl;
   }
-  // list ranking: at most 13 rounds (2^13 = HOP_SLOTS cells); after round 6
-  // every pointer still inside the tile is exactly SEG_MAX cells ahead
+  // list ranking: at most 13 rounds (2^13 = HOP_SLOTS cells); after round
+  // SEG_LOG every pointer still inside the tile is exactly SEG_MAX cells ahead
   constexpr int PER = HOP_SLOTS / HOP_THREADS;
   int rounds = 0;
   for (int round = 0; round < 14 && __syncthreads_or(active); ++round) {
@@ -400,13 +428,13 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict
     for (int q = 0; q < PER; ++q) {
       const int sl = threadIdx.x + q * HOP_THREADS;
       S.nv[sl] = nn[q]; S.tail[sl] = nt[q];
-      if (round == 5) {  // pointers now SEG_MAX cells ahead (or none)
+      if (round == SEG_LOG - 1) {  // pointers now SEG_MAX cells ahead (or none)
         int rx, ry, jx, jy;
         if (slot_cell(sl, rx, ry)) {
           const uint32_t js = nn[q] >> 16;
           uint32_t jv = HOP_END;
           if (js != SLOT_NIL) { slot_cell((int)js, jx, jy); jv = edge_id(g, jx, jy); }
-          j64[edge_id(g, rx, ry)] = jv;
+          jseg[edge_id(g, rx, ry)] = jv;
         }
       }
     }
@@ -418,19 +446,20 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict
     const uint32_t e = edge_id(g, rx, ry);
     const uint32_t v = S.nv[sl];
     if ((v >> 16) != SLOT_NIL) { st |= ST_CYCLE; to[e] = HOP_END; len[e] = 0; continue; }
-    int tx, ty;
-    slot_cell(S.tail[sl], tx, ty);
-    const int kind = chain_kind(code(tx, ty), tx, ty);
+    const int tl = S.tail[sl];
+    const uint8_t sd = S.sd[tl];
     uint32_t dst = HOP_END;
-    int n = 0;
-    if (kind >= 0) {
-      n = succ_local(g, kind, tx, ty, code, ox, oy);
-      if (n == 1 && !in_tile(ox[0], oy[0])) dst = edge_id(g, ox[0], oy[0]);
+    if (sd < SUCC_TWO) {  // the run leaves the tile after its tail
+      int tx, ty;
+      slot_cell(tl, tx, ty);
+      ox[0] = tx + (int)(sd % 5) - 2;
+      oy[0] = ty + (int)(sd / 5) - 2;
+      dst = edge_id(g, ox[0], oy[0]);
     }
     to[e] = dst;
     // a cell with two successors ends no chain: length 0 marks it for the walkers
-    len[e] = n == 2 ? 0 : (uint16_t)(v & 0xFFFFu);
-    if (rounds < 6) j64[e] = HOP_END;  // every run in the tile is shorter than SEG_MAX + 1 cells
+    len[e] = sd == SUCC_TWO ? 0 : (uint16_t)(v & 0xFFFFu);
+    if (rounds < SEG_LOG) jseg[e] = HOP_END;  // every run in the tile is shorter than SEG_MAX + 1 cells
   }
   if (st) atomicOr(status, st);
 }
@@ -438,7 +467,7 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict
 struct ChainArgs {
   const uint32_t *hop_to;
   const uint16_t *hop_len;
-  const uint32_t *j64;
+  const uint32_t *jseg;
   const uint8_t *nextd;   // per edge: its chain successor as a cell offset (SUCC_NONE if none)
   uint32_t *kc;         // per cp: chains of a saddle handled here (0 otherwise)
   uint32_t *mc;         // per cp: level-0 items
@@ -524,7 +553,7 @@ __global__ void k_chain_segs(long long nchains, ChainArgs c) {
       for (uint32_t done = 0; done < l && o < end && x != HOP_END; done += SEG_MAX) {
         const uint32_t w = l - done < (uint32_t)SEG_MAX ? l - done : (uint32_t)SEG_MAX;
         c.segs[o++] = make_uint4((uint32_t)k, x, T + done, w);
-        if (done + SEG_MAX < l) x = c.j64[x];
+        if (done + SEG_MAX < l) x = c.jseg[x];
       }
       T += l;
     }
@@ -726,8 +755,8 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   uint32_t *gkey[2] = {vt + nmax, vt + nmax + nV}, *gval[2] = {vt + nmax + nV + nF, vt + nmax + 2 * nV + nF};
   uint32_t *kc = gval[1] + nF, *mc = kc + ncp, *cbase = mc + ncp;  // cbase: ncp+1
   uint8_t *big = (uint8_t *)(cbase + ncp + 1);
-  uint32_t *hop_to = cbase + ncp + 1 + ncp / 4 + 1, *j64 = hop_to + nE;
-  uint16_t *hop_len = (uint16_t *)(j64 + nE);
+  uint32_t *hop_to = cbase + ncp + 1 + ncp / 4 + 1, *jseg = hop_to + nE;
+  uint16_t *hop_len = (uint16_t *)(jseg + nE);
   uint8_t *nextd = (uint8_t *)(hop_len + nE);
   const long long gn[2] = {nV, nF};
   auto L = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
@@ -747,19 +776,22 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     DMSC_LAUNCHED(2);
   }
   if (io.ev_hops[0]) L(cudaEventRecord(io.ev_hops[0], st));
-  k_disc_hops<<<dim3(g.ntx, g.nty), HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, hop_to, hop_len, j64, nextd,
+  k_disc_hops<<<dim3(g.ntx, g.nty), HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, hop_to, hop_len, jseg, nextd,
                                                                         io.status);
   DMSC_LAUNCHED(1);
   if (io.ev_hops[1]) L(cudaEventRecord(io.ev_hops[1], st));
   L(cudaMemsetAsync(acnt, 0, sizeof(uint32_t) * ncp * 2, st));
   // extremum discs: vertices -> minima (asc_disc), faces -> maxima (des_disc),
   // grouped by owner with a stable sort (row-major order is the append order)
+  if (ncp) {
+    k_owner_final<<<nb(ncp), 256, 0, st>>>(a, redir, scount);  // scount is free until the saddle passes
+    k_disc_keys<<<nb(nV), 256, 0, st>>>(a, scount, gkey[0], gval[0], gkey[1], gval[1]);
+    DMSC_LAUNCHED(2);
+  }
   for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind) {
     long long n = gn[kind];
     if (n <= 0) continue;
-    k_disc_keys<<<nb(n), 256, 0, st>>>(a, redir, kind, gkey[kind], gval[kind]);
-    DMSC_LAUNCHED(1);
-    L(radix_sort_pairs(gkey[kind], gval[kind], kt, vt, n, nbits_for(ncp), st));
+    L(radix_sort_pairs(gkey[kind], gval[kind], kt, vt, n, nbits_for(ncp + 1), st));
     k_seed_runs<<<nb(n), 256, 0, st>>>(n, (uint32_t)ncp, gkey[kind], sstart);
     k_run_len<<<nb(n), 256, 0, st>>>(n, (uint32_t)ncp, gkey[kind], sstart, kind ? dcnt : acnt, 1);
     DMSC_LAUNCHED(2);
@@ -788,7 +820,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     }
     SeedRuns sr{val, sstart, scount};
     ChainArgs c{};
-    c.hop_to = hop_to; c.hop_len = hop_len; c.j64 = j64; c.nextd = nextd;
+    c.hop_to = hop_to; c.hop_len = hop_len; c.jseg = jseg; c.nextd = nextd;
     c.kc = kc; c.mc = mc; c.big = big; c.cbase = cbase; c.limit = io.limit;
     k_chain_count<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c);
     DMSC_LAUNCHED(1);

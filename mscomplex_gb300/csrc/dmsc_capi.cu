@@ -381,6 +381,7 @@ int dmsc_dataset_fill_discs(dmsc_dataset *d, dmsc_msc *m, void *stream) {
   if (!d || !m) return fail(DMSC_ERR_BAD_ARG, "null argument");
   if (!d->worked) return fail(DMSC_ERR_STATE, "dataset_work has not run");
   if (m->ncp < d->ncp) return fail(DMSC_ERR_BAD_ARG, "complex does not hold the dataset's critical points");
+  if (m->ncp >= (1ll << 30)) return fail(DMSC_ERR_BAD_ARG, "disc collection supports fewer than 2^30 critical points");
   CK(cudaSetDevice(d->ctx->device));
   cudaStream_t st = pick(d->ctx, stream);
   const size_t n = (size_t)m->ncp;
