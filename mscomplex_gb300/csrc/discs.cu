@@ -104,8 +104,7 @@ __global__ void k_owner_final(DiscArgs a, const uint32_t *redir, uint32_t *fo) {
 
 // 2b. owner keys of the rect vertices (vertex grid) and faces (face grid),
 // row-major, from one read of the labels
-__global__ void k_disc_keys(DiscArgs a, const uint32_t *fo, uint32_t *key0, uint32_t *val0, uint32_t *key1,
-                            uint32_t *val1) {
+__global__ void k_disc_keys(DiscArgs a, const uint32_t *fo, uint32_t *key0, uint32_t *key1) {
   const GridGeom &g = a.g;
   const int nx = (g.rx1 - g.rx0) / 2 + 1, ny = (g.ry1 - g.ry0) / 2 + 1;
   const uint32_t n_ok = a.ncp_ds < a.ncp ? a.ncp_ds : a.ncp;
@@ -126,7 +125,6 @@ __global__ void k_disc_keys(DiscArgs a, const uint32_t *fo, uint32_t *key0, uint
       }
       const long long fi = kind ? (long long)jj * (nx - 1) + ii : t;
       (kind ? key1 : key0)[fi] = o;
-      (kind ? val1 : val0)[fi] = pack_cellid(g.ex0 + rx + kind, g.ey0 + ry + kind);
     }
   }
   if (bad) atomicOr(a.status, ST_INVARIANT);
@@ -705,12 +703,70 @@ __global__ void k_seed_runs(long long n, uint32_t ncp, const uint32_t *key, uint
     if (k < ncp && (p == 0 || key[p - 1] != k)) start[k] = (uint32_t)p;
   }
 }
-__global__ void k_group_scatter(long long n, uint32_t ncp, const uint32_t *key, const uint32_t *val,
-                                const uint32_t *start, const uint32_t *off, uint32_t *out) {
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
-    uint32_t k = key[p];
-    if (k < ncp) out[off[k] + (uint32_t)p - start[k]] = val[p];
+
+// ---- extremum discs from runs: a row of the vertex (face) grid splits into
+// runs of one owner; the disc of an owner is its runs in row-major order, so
+// a stable sort of the runs (far fewer than the cells) by owner gives every
+// cell's place.
+__device__ __forceinline__ bool run_start(const uint32_t *key, long long t, int w) {
+  return (t % w) == 0 || key[t] != key[t - 1];
+}
+__device__ __forceinline__ bool run_end(const uint32_t *key, long long t, long long n, int w) {
+  return (t % w) == w - 1 || t + 1 == n || key[t + 1] != key[t];
+}
+__global__ void k_run_flags(const uint32_t *key, long long n, int w, uint32_t *flag) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+    flag[t] = run_start(key, t, w) ? 1u : 0u;
+}
+// rid: exclusive scan of the start flags (the run of a start cell)
+__global__ void k_run_records(const uint32_t *key, long long n, int w, const uint32_t *rid, uint32_t *rkey,
+                              uint32_t *rstart, uint32_t *rend) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const bool s = run_start(key, t, w);
+    const uint32_t r = s ? rid[t] : rid[t] - 1u;  // the run holding t
+    if (s) { rkey[r] = key[t]; rstart[r] = (uint32_t)t; }
+    if (run_end(key, t, n, w)) rend[r] = (uint32_t)t + 1;
   }
+}
+__global__ void k_runs_sorted_len(long long R, uint32_t ncp, const uint32_t *rkey_s, const uint32_t *ridx,
+                                  const uint32_t *rstart, const uint32_t *rend, uint32_t *len_s) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < R; i += (long long)gridDim.x * blockDim.x)
+    len_s[i] = rkey_s[i] < ncp ? rend[ridx[i]] - rstart[ridx[i]] : 0u;
+}
+// the first sorted position of each owner's runs (gbase), then each run's place
+// in its owner's disc and the owner's count
+__global__ void k_runs_group_base(long long R, uint32_t ncp, const uint32_t *rkey_s, const uint32_t *spos, uint32_t *gbase) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < R; i += (long long)gridDim.x * blockDim.x) {
+    const uint32_t k = rkey_s[i];
+    if (k < ncp && (i == 0 || rkey_s[i - 1] != k)) gbase[k] = spos[i];
+  }
+}
+__global__ void k_runs_place(long long R, uint32_t ncp, const uint32_t *rkey_s, const uint32_t *ridx, const uint32_t *spos,
+                             const uint32_t *len_s, const uint32_t *gbase, uint32_t *rpos, uint32_t *cnt) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < R; i += (long long)gridDim.x * blockDim.x) {
+    const uint32_t k = rkey_s[i];
+    if (k >= ncp) continue;
+    rpos[ridx[i]] = spos[i] - gbase[k];
+    if (i + 1 == R || rkey_s[i + 1] != k) cnt[k] += spos[i] + len_s[i] - gbase[k];
+  }
+}
+// every owned cell to its owner's disc: off[owner] + its run's place + offset in the run
+__global__ void k_runs_scatter(const GridGeom g, int kind, const uint32_t *key, long long n, int w, uint32_t ncp,
+                               const uint32_t *rid, const uint32_t *rpos, const uint32_t *rstart, const uint32_t *off,
+                               uint32_t *out) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const uint32_t k = key[t];
+    if (k >= ncp) continue;
+    const bool s = run_start(key, t, w);
+    const uint32_t r = s ? rid[t] : rid[t] - 1u;
+    const long long jj = t / w, ii = t - jj * w;
+    out[off[k] + rpos[r] + ((uint32_t)t - rstart[r])] =
+        pack_cellid(g.ex0 + g.rx0 + kind + 2 * (int)ii, g.ey0 + g.ry0 + kind + 2 * (int)jj);
+  }
+}
+__global__ void k_iota_u32(long long n, uint32_t *a) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a[i] = (uint32_t)i;
 }
 
 static unsigned nb(long long n) {
@@ -785,16 +841,46 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   // grouped by owner with a stable sort (row-major order is the append order)
   if (ncp) {
     k_owner_final<<<nb(ncp), 256, 0, st>>>(a, redir, scount);  // scount is free until the saddle passes
-    k_disc_keys<<<nb(nV), 256, 0, st>>>(a, scount, gkey[0], gval[0], gkey[1], gval[1]);
+    k_disc_keys<<<nb(nV), 256, 0, st>>>(a, scount, gkey[0], gkey[1]);
     DMSC_LAUNCHED(2);
   }
+  // runs of one owner along the rows, numbered row-major (gval holds the run ids)
+  const int gw[2] = {(g.rx1 - g.rx0) / 2 + 1, (g.rx1 - g.rx0) / 2};
+  uint32_t nrun[2] = {0, 0};
   for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind) {
-    long long n = gn[kind];
-    if (n <= 0) continue;
-    L(radix_sort_pairs(gkey[kind], gval[kind], kt, vt, n, nbits_for(ncp + 1), st));
-    k_seed_runs<<<nb(n), 256, 0, st>>>(n, (uint32_t)ncp, gkey[kind], sstart);
-    k_run_len<<<nb(n), 256, 0, st>>>(n, (uint32_t)ncp, gkey[kind], sstart, kind ? dcnt : acnt, 1);
+    const long long n = gn[kind];
+    if (n <= 0 || !ncp) continue;
+    k_run_flags<<<nb(n), 256, 0, st>>>(gkey[kind], n, gw[kind], gval[kind]);
+    DMSC_LAUNCHED(1);
+    L(scan_exclusive_u32(gval[kind], n, gval[kind], soff, st));
+    L(cudaMemcpyAsync(&nrun[kind], soff, 4, cudaMemcpyDeviceToHost, st));
+  }
+  L(cudaStreamSynchronize(st));
+  uint32_t *runbuf = nullptr, *rpos[2] = {nullptr, nullptr}, *rstart_k[2] = {nullptr, nullptr};
+  {
+    const size_t R0 = nrun[0], R1 = nrun[1];
+    // per kind: rkey ridx rstart rend len_s spos rpos + sort scratch (2 R); gbase (ncp)
+    L(cudaMallocAsync((void **)&runbuf, sizeof(uint32_t) * (9 * (R0 + R1) + (size_t)ncp + 16), st));
+  }
+  for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind) {
+    const long long n = gn[kind], R = nrun[kind];
+    if (n <= 0 || R == 0) continue;
+    uint32_t *base = runbuf + (kind ? 9 * (size_t)nrun[0] : 0);
+    uint32_t *rkey = base, *ridx = base + R, *rstart = base + 2 * R, *rend = base + 3 * R, *len_s = base + 4 * R;
+    uint32_t *spos = base + 5 * R, *rp = base + 6 * R, *tk = base + 7 * R, *tv = base + 8 * R;
+    uint32_t *gbase = runbuf + 9 * ((size_t)nrun[0] + nrun[1]);
+    k_run_records<<<nb(n), 256, 0, st>>>(gkey[kind], n, gw[kind], gval[kind], rkey, rstart, rend);
+    k_iota_u32<<<nb(R), 256, 0, st>>>(R, ridx);
     DMSC_LAUNCHED(2);
+    L(radix_sort_pairs(rkey, ridx, tk, tv, R, nbits_for(ncp + 1), st));  // stable: runs stay row-major
+    k_runs_sorted_len<<<nb(R), 256, 0, st>>>(R, (uint32_t)ncp, rkey, ridx, rstart, rend, len_s);
+    DMSC_LAUNCHED(1);
+    L(scan_exclusive_u32(len_s, R, spos, nullptr, st));
+    k_runs_group_base<<<nb(R), 256, 0, st>>>(R, (uint32_t)ncp, rkey, spos, gbase);
+    k_runs_place<<<nb(R), 256, 0, st>>>(R, (uint32_t)ncp, rkey, ridx, spos, len_s, gbase, rp, kind ? dcnt : acnt);
+    DMSC_LAUNCHED(2);
+    rpos[kind] = rp;
+    rstart_k[kind] = rstart;
   }
   // saddle discs
   for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind) {
@@ -874,17 +960,17 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
       k_zip<<<nb(32ll * nch), 256, 0, st>>>(a, c, nch, ob->p, (unsigned long long)tot[0]);
       DMSC_LAUNCHED(1);
     }
-    long long n = gn[kind];
-    if (n > 0) {  // extremum groups of this kind
-      k_seed_runs<<<nb(n), 256, 0, st>>>(n, (uint32_t)ncp, gkey[kind], sstart);
-      DMSC_LAUNCHED(1);
-      k_group_scatter<<<nb(n), 256, 0, st>>>(n, (uint32_t)ncp, gkey[kind], gval[kind], sstart, offs, ob->p);
+    const long long n = gn[kind];
+    if (n > 0 && nrun[kind]) {  // extremum discs of this kind
+      k_runs_scatter<<<nb(n), 256, 0, st>>>(g, kind, gkey[kind], n, gw[kind], (uint32_t)ncp, gval[kind], rpos[kind],
+                                            rstart_k[kind], offs, ob->p);
       DMSC_LAUNCHED(1);
     }
     (kind ? io.nddisc : io.nadisc) = tot[0];
     release();
   }
   release();
+  if (runbuf) cudaFreeAsync(runbuf, st);
   cudaFreeAsync(buf, st);
   if (e == cudaSuccess) e = cudaGetLastError();
   return e;
