@@ -473,6 +473,8 @@ struct ChainArgs {
   uint32_t *cbase;      // exclusive scan of kc
   uint32_t *cstart, *csaddle, *clen, *cnseg, *csegoff;  // per chain
   uint4 *segs;          // (chain, first edge, first level, cells)
+  uint32_t *cofs;       // exclusive scan of clen: each chain's cells in tmp
+  uint32_t *tmp;        // chain-major cells
   uint4 *blocks;        // per chain slot of a saddle, 2 uint4: an interleave record (k_zip_blocks)
   unsigned long long limit;
 };
@@ -569,29 +571,25 @@ __global__ void k_level0(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, const u
 }
 
 // Pieces of at most SEG_MAX cells of one chain.  Each lane of a warp follows
-// the 1-byte successor offsets of one piece into shared memory; then the warp
-// places the 32 pieces one after another: the cell of level t of chain j
-// goes to its level range's record -- out[start + (t - t_b) na + rank of j
-// among the alive chains] -- so the chains of one saddle interleave in the
-// disc directly (their pieces are neighbours in the piece order, so their
-// stores meet in the same sectors close in time).
+// the 1-byte successor offsets of one piece into shared memory, then the
+// warp copies the 32 pieces out one after another with coalesced stores into
+// their chains' spans of tmp (a lane's own stores would each touch a
+// different sector).
 constexpr int SEG_WARPS = 4;
-__global__ void __launch_bounds__(SEG_WARPS * 32) k_seg_write(DiscArgs a, ChainArgs c, long long nsegs, uint32_t *out,
-                                                              unsigned long long out_len) {
+__global__ void __launch_bounds__(SEG_WARPS * 32) k_seg_write(DiscArgs a, ChainArgs c, long long nsegs) {
   __shared__ uint32_t buf[SEG_WARPS][32][SEG_MAX + 1];  // +1: lanes' rows fall in different banks
-  const unsigned FULL = 0xffffffffu;
   const GridGeom &g = a.g;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const long long gw = ((long long)blockIdx.x * SEG_WARPS + w), nwarps = (long long)gridDim.x * SEG_WARPS;
   for (long long k0 = gw * 32; k0 < nsegs; k0 += nwarps * 32) {
     const long long k = k0 + lane;
-    uint32_t len = 0, ch = 0, T = 0;
+    uint32_t len = 0, dst = 0;
     if (k < nsegs) {
       const uint4 sg = c.segs[k];
-      ch = sg.x;
-      T = sg.z;
+      const uint32_t ch = sg.x;
       if (sg.z - 1 + sg.w > c.clen[ch]) atomicOr(a.status, ST_INVARIANT);
       else {
+        dst = c.cofs[ch] + (sg.z - 1);
         int rx, ry;
         edge_cell(g, sg.y, rx, ry);
         for (uint32_t i = 0; i < sg.w; ++i) {
@@ -608,31 +606,8 @@ __global__ void __launch_bounds__(SEG_WARPS * 32) k_seg_write(DiscArgs a, ChainA
     }
     __syncwarp();
     for (int p = 0; p < 32; ++p) {
-      const uint32_t n = __shfl_sync(FULL, len, p);
-      if (!n) continue;
-      const uint32_t chp = __shfl_sync(FULL, ch, p), Tp = __shfl_sync(FULL, T, p);
-      const uint32_t s = c.csaddle[chp], cb = c.cbase[s], K = c.kc[s], j = chp - cb;
-      // lane b < K holds level range b of the saddle
-      uint4 r0 = make_uint4(0, 0, 0, 0);
-      uint32_t tb = 0;
-      if ((uint32_t)lane < K) { r0 = c.blocks[2 * (cb + lane)]; tb = c.blocks[2 * (cb + lane) + 1].w; }
-      for (uint32_t i0 = 0; i0 < n; i0 += 32) {
-        const uint32_t i = i0 + (uint32_t)lane, t = Tp + i;
-        unsigned long long pos = ~0ull;
-        for (uint32_t b = 0; b < K; ++b) {
-          const uint32_t st0 = __shfl_sync(FULL, r0.x, b), nn = __shfl_sync(FULL, r0.y, b);
-          const uint32_t na = __shfl_sync(FULL, r0.z, b), mask = __shfl_sync(FULL, r0.w, b);
-          const uint32_t tbb = __shfl_sync(FULL, tb, b);
-          if (!na) break;
-          const uint32_t te = tbb + nn / na - 1;
-          if (pos == ~0ull && t >= tbb && t <= te && ((mask >> j) & 1u))
-            pos = (unsigned long long)st0 + (unsigned long long)(t - tbb) * na + (uint32_t)__popc(mask & ((1u << j) - 1u));
-        }
-        if (i < n) {
-          if (pos < out_len) out[pos] = buf[w][p][i];
-          else atomicOr(a.status, ST_INVARIANT);
-        }
-      }
+      const uint32_t n = __shfl_sync(0xffffffffu, len, p), o = __shfl_sync(0xffffffffu, dst, p);
+      for (uint32_t i = lane; i < n; i += 32) c.tmp[o + i] = buf[w][p][i];
     }
     __syncwarp();
   }
@@ -642,7 +617,8 @@ __global__ void __launch_bounds__(SEG_WARPS * 32) k_seg_write(DiscArgs a, ChainA
 // constant.  Between consecutive distinct chain lengths the disc is a
 // regular interleave of the alive chains.  Each range becomes a record of
 // two uint4: (first output position, cells, alive chains, alive mask) and
-// (0, 0, the saddle's first chain slot, the first level).
+// (tmp start of the first and second alive chain at the range's first level,
+// the saddle's first chain slot, the first level).
 __global__ void k_zip_blocks(DiscArgs a, ChainArgs c, const uint32_t *off) {
   for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < a.ncp; s += gridDim.x * blockDim.x) {
     const uint32_t K = c.kc[s], cb = c.cbase[s];
@@ -657,8 +633,10 @@ __global__ void k_zip_blocks(DiscArgs a, ChainArgs c, const uint32_t *off) {
         if (L[q] > prev) { mask |= 1u << q; u = L[q] < u ? L[q] : u; }
       if (!mask) break;
       const uint32_t na = (uint32_t)__popc(mask), n = (u - prev) * na;
+      const uint32_t j0 = (uint32_t)__ffs(mask) - 1, m1 = mask & (mask - 1);
+      const uint32_t j1 = m1 ? (uint32_t)__ffs(m1) - 1 : j0;
       c.blocks[2 * (cb + nb)] = make_uint4(base + P, n, na, mask);
-      c.blocks[2 * (cb + nb) + 1] = make_uint4(0, 0, cb, prev + 1);
+      c.blocks[2 * (cb + nb) + 1] = make_uint4(c.cofs[cb + j0] + prev, c.cofs[cb + j1] + prev, cb, prev + 1);
       ++nb;
       P += n;
       prev = u;
@@ -667,6 +645,41 @@ __global__ void k_zip_blocks(DiscArgs a, ChainArgs c, const uint32_t *off) {
   }
 }
 
+// One warp per record: out[start + q] = the cell of level t_b + q / a of the
+// (q % a)-th alive chain, coalesced stores.
+__global__ void __launch_bounds__(256) k_zip(DiscArgs a, ChainArgs c, long long nch, uint32_t *out,
+                                             unsigned long long out_len) {
+  __shared__ uint32_t src[8][KMAX];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long k = w0; k < nch; k += nw) {
+    const uint4 r0 = c.blocks[2 * k];
+    if (!r0.y) continue;
+    const uint4 r1 = c.blocks[2 * k + 1];
+    const uint32_t n = r0.y, na = r0.z;
+    if ((unsigned long long)r0.x + n > out_len) { if (lane == 0) atomicOr(a.status, ST_INVARIANT); continue; }
+    uint32_t *o = out + r0.x;
+    if (na == 1) {
+      const uint32_t *p = c.tmp + r1.x;
+      for (uint32_t q = lane; q < n; q += 32) o[q] = p[q];
+    } else if (na == 2) {
+      for (uint32_t q = lane; q < n; q += 32) o[q] = c.tmp[((q & 1) ? r1.y : r1.x) + (q >> 1)];
+    } else {
+      __syncwarp();
+      if (lane < (int)na) {  // lane r: tmp start of the r-th alive chain
+        uint32_t m = r0.w;
+        for (int z = 0; z < lane; ++z) m &= m - 1;
+        src[wib][lane] = c.cofs[r1.z + (uint32_t)__ffs(m) - 1] + r1.w - 1;
+      }
+      __syncwarp();
+      for (uint32_t q = lane; q < n; q += 32) {
+        const uint32_t t = q / na;
+        o[q] = c.tmp[src[wib][q - t * na] + t];
+      }
+    }
+  }
+}
 
 // 5. runs of equal sorted keys: the last element of each run writes (or adds)
 // its length, after k_seed_runs has recorded the run starts
@@ -803,13 +816,14 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   uint8_t *nextd = (uint8_t *)(hop_len + nE);
   const long long gn[2] = {nV, nF};
   auto L = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-  uint32_t *chain_buf = nullptr;
+  uint32_t *chain_buf = nullptr, *tmp = nullptr;
   uint4 *segs = nullptr, *blocks = nullptr;
   auto release = [&]() {
     if (segs) cudaFreeAsync(segs, st);
+    if (tmp) cudaFreeAsync(tmp, st);
     if (blocks) cudaFreeAsync(blocks, st);
     if (chain_buf) cudaFreeAsync(chain_buf, st);
-    segs = nullptr; blocks = nullptr; chain_buf = nullptr;
+    segs = nullptr; tmp = nullptr; blocks = nullptr; chain_buf = nullptr;
   };
 
   if (ncp) {
@@ -901,12 +915,13 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     L(cudaMemcpyAsync(&nch, cbase + ncp, 4, cudaMemcpyDeviceToHost, st));
     L(cudaStreamSynchronize(st));
     if (e != cudaSuccess) break;
-    // per chain: cstart csaddle clen cnseg | csegoff (nch + 1)
+    // per chain: cstart csaddle clen cnseg | csegoff cofs (nch + 1 each)
     L(cudaMallocAsync((void **)&chain_buf, sizeof(uint32_t) * (6ull * nch + 8), st));
     L(cudaMallocAsync((void **)&blocks, sizeof(uint4) * (2 * (size_t)nch + 2), st));
     if (e != cudaSuccess) break;
     c.cstart = chain_buf; c.csaddle = chain_buf + nch; c.clen = chain_buf + 2 * nch; c.cnseg = chain_buf + 3 * nch;
     c.csegoff = chain_buf + 4 * nch;      // nch + 1
+    c.cofs = chain_buf + 5 * nch + 1;     // nch + 1
     c.blocks = blocks;
     k_chain_len<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, slen);
     k_saddle_disc_count<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, slen, io.limit);
@@ -915,30 +930,36 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     uint32_t *offs = kind ? io.ddoff : io.adoff;
     L(scan_exclusive_u32(kind ? dcnt : acnt, ncp, offs, offs + ncp, st));
     L(scan_exclusive_u32(c.cnseg, nch, c.csegoff, c.csegoff + nch, st));
+    L(scan_exclusive_u32(c.clen, nch, c.cofs, c.cofs + nch, st));
     uint32_t tot[3] = {0, 0, 0};
     L(cudaMemcpyAsync(&tot[0], offs + ncp, 4, cudaMemcpyDeviceToHost, st));
     L(cudaMemcpyAsync(&tot[1], c.csegoff + nch, 4, cudaMemcpyDeviceToHost, st));
+    L(cudaMemcpyAsync(&tot[2], c.cofs + nch, 4, cudaMemcpyDeviceToHost, st));
     L(cudaStreamSynchronize(st));
     if (e != cudaSuccess) break;
     DevBuf<uint32_t> *ob = kind ? io.ddisc : io.adisc;
     L(ob->ensure((size_t)tot[0] + 1));
     L(cudaMallocAsync((void **)&segs, sizeof(uint4) * ((size_t)tot[1] + 1), st));
+    L(cudaMallocAsync((void **)&tmp, sizeof(uint32_t) * ((size_t)tot[2] + 1), st));
     if (e != cudaSuccess) break;
     c.segs = segs;
+    c.tmp = tmp;
     if (nch) {
       k_chain_segs<<<nb(nch), 128, 0, st>>>(nch, c);
       DMSC_LAUNCHED(1);
     }
-    k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c, offs);
-    DMSC_LAUNCHED(1);
     if (tot[1]) {
-      k_seg_write<<<nb((tot[1] + 31) / 32 * 32), SEG_WARPS * 32, 0, st>>>(a, c, tot[1], ob->p,
-                                                                        (unsigned long long)tot[0]);
+      k_seg_write<<<nb((tot[1] + 31) / 32 * 32), SEG_WARPS * 32, 0, st>>>(a, c, tot[1]);
       DMSC_LAUNCHED(1);
     }
+    k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c, offs);
     k_level0<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, offs, ob->p);
     k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);
-    DMSC_LAUNCHED(2);
+    DMSC_LAUNCHED(3);
+    if (nch) {
+      k_zip<<<nb(32ll * nch), 256, 0, st>>>(a, c, nch, ob->p, (unsigned long long)tot[0]);
+      DMSC_LAUNCHED(1);
+    }
     const long long n = gn[kind];
     if (n > 0 && nrun[kind]) {  // extremum discs of this kind
       k_runs_scatter<<<nb(n), 256, 0, st>>>(g, kind, gkey[kind], n, gw[kind], (uint32_t)ncp, gval[kind], rpos[kind],
