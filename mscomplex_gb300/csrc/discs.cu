@@ -476,6 +476,7 @@ struct ChainArgs {
   uint32_t *cofs;       // exclusive scan of clen: each chain's cells in tmp
   uint32_t *tmp;        // chain-major cells
   uint4 *blocks;        // per chain slot of a saddle, 2 uint4: an interleave record (k_zip_blocks)
+  uint32_t cap;         // chain slots allocated
   unsigned long long limit;
 };
 
@@ -529,7 +530,8 @@ __global__ void k_chain_len(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, uint
           nseg += (l + SEG_MAX - 1) / SEG_MAX;
           if (L > c.limit) { bad = true; break; }
         }
-        c.cstart[j] = ch[b]; c.csaddle[j] = s; c.clen[j] = (uint32_t)L; c.cnseg[j] = nseg;
+        if (j < c.cap) { c.cstart[j] = ch[b]; c.csaddle[j] = s; c.clen[j] = (uint32_t)L; c.cnseg[j] = nseg; }
+        else atomicOr(a.status, ST_CAPACITY);
         ++j;
         total += L;
       }
@@ -623,6 +625,7 @@ __global__ void k_zip_blocks(DiscArgs a, ChainArgs c, const uint32_t *off) {
   for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < a.ncp; s += gridDim.x * blockDim.x) {
     const uint32_t K = c.kc[s], cb = c.cbase[s];
     if (!K) continue;
+    if (cb + K > c.cap) { atomicOr(a.status, ST_CAPACITY); continue; }
     uint32_t L[KMAX];
     for (uint32_t q = 0; q < K; ++q) L[q] = c.clen[cb + q];
     const uint32_t base = off[s] + c.mc[s];
@@ -828,8 +831,11 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
 
   if (ncp) {
     k_redir_init<<<nb(ncp), 256, 0, st>>>((uint32_t)ncp, redir);
-    k_redir_saddles<<<nb(ncp), 256, 0, st>>>(a, redir);
-    DMSC_LAUNCHED(2);
+    DMSC_LAUNCHED(1);
+    if (!io.no_cancel) {
+      k_redir_saddles<<<nb(ncp), 256, 0, st>>>(a, redir);
+      DMSC_LAUNCHED(1);
+    }
   }
   if (io.ev_hops[0]) L(cudaEventRecord(io.ev_hops[0], st));
   k_disc_hops<<<dim3(g.ntx, g.nty), HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, hop_to, hop_len, jseg, nextd,
@@ -884,13 +890,16 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   }
   // saddle discs
   for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind) {
-    // seeds pushed by cancelled extrema: asc from maxima (via des), des from minima (via asc)
-    k_seed_count<<<nb(ncp), 256, 0, st>>>(a, kind, slen);
-    DMSC_LAUNCHED(1);
-    L(scan_exclusive_u32(slen, ncp, soff, soff + ncp, st));
+    // seeds pushed by cancelled extrema: asc from maxima (via des), des from minima (via asc);
+    // a complex without boundary-cancelable points has none
     uint32_t ns = 0;
-    L(cudaMemcpyAsync(&ns, soff + ncp, 4, cudaMemcpyDeviceToHost, st));
-    L(cudaStreamSynchronize(st));
+    if (!io.no_cancel) {
+      k_seed_count<<<nb(ncp), 256, 0, st>>>(a, kind, slen);
+      DMSC_LAUNCHED(1);
+      L(scan_exclusive_u32(slen, ncp, soff, soff + ncp, st));
+      L(cudaMemcpyAsync(&ns, soff + ncp, 4, cudaMemcpyDeviceToHost, st));
+      L(cudaStreamSynchronize(st));
+    }
     if (e != cudaSuccess) break;
     if ((long long)ns > nmax) { e = cudaErrorInvalidValue; break; }
     if (ns) {
@@ -911,14 +920,26 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     k_chain_count<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c);
     DMSC_LAUNCHED(1);
     L(scan_exclusive_u32(kc, ncp, cbase, cbase + ncp, st));
+    // chain slots: the exact count, or without seeds from cancelled extrema the
+    // bound of two chains per saddle (two own seeds, one successor each), with
+    // the unused slots zeroed -- saving a synchronisation
     uint32_t nch = 0;
-    L(cudaMemcpyAsync(&nch, cbase + ncp, 4, cudaMemcpyDeviceToHost, st));
-    L(cudaStreamSynchronize(st));
+    if (ns || !io.no_cancel) {
+      L(cudaMemcpyAsync(&nch, cbase + ncp, 4, cudaMemcpyDeviceToHost, st));
+      L(cudaStreamSynchronize(st));
+    } else {
+      nch = (uint32_t)std::min<long long>(2 * ncp, 0xFFFFFFF0ll);
+    }
     if (e != cudaSuccess) break;
+    c.cap = nch;
     // per chain: cstart csaddle clen cnseg | csegoff cofs (nch + 1 each)
     L(cudaMallocAsync((void **)&chain_buf, sizeof(uint32_t) * (6ull * nch + 8), st));
     L(cudaMallocAsync((void **)&blocks, sizeof(uint4) * (2 * (size_t)nch + 2), st));
     if (e != cudaSuccess) break;
+    if (!ns && io.no_cancel) {
+      L(cudaMemsetAsync(chain_buf, 0, sizeof(uint32_t) * 4ull * nch, st));
+      L(cudaMemsetAsync(blocks, 0, sizeof(uint4) * 2ull * nch, st));
+    }
     c.cstart = chain_buf; c.csaddle = chain_buf + nch; c.clen = chain_buf + 2 * nch; c.cnseg = chain_buf + 3 * nch;
     c.csegoff = chain_buf + 4 * nch;      // nch + 1
     c.cofs = chain_buf + 5 * nch + 1;     // nch + 1

@@ -362,7 +362,11 @@ int dmsc_msc_simplify_un_simplify(dmsc_msc *m, double tresh, int64_t max_ops, vo
     if (e == cudaSuccess) e = simplify_emit(io, m->asc.p, m->des.p, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) rc = cuda_fail(e, "simplify_emit");
-    else { m->nasc = io.nasc_out; m->ndes = io.ndes_out; }
+    else {
+      m->nasc = io.nasc_out;
+      m->ndes = io.ndes_out;
+      if (hs[2]) m->any_bcancel = true;  // cancelled pairs are left boundary-cancelable
+    }
   }
   for (int i = 0; i < 5; ++i) m->simp_stats[i] = hs[i];
   simplify_release(io, st);
@@ -396,6 +400,7 @@ int dmsc_dataset_fill_discs(dmsc_dataset *d, dmsc_msc *m, void *stream) {
   io.status = d->scal.p;
   // a gradient path visits each cell at most once: bounds every chain of a disc
   io.limit = (unsigned long long)(d->g.cx + 1) * (d->g.cy + 1) + 16;
+  io.no_cancel = !m->any_bcancel;
   const bool tm = d->ctx->timing && d->ev_ready;
   if (tm) {
     io.ev_hops[0] = d->ev[7];
@@ -516,6 +521,7 @@ dmsc_dataset::~dmsc_dataset() {
 
 int dmsc_msc::writeout_from(const dmsc_dataset &d, cudaStream_t st) {
   ncp = d.ncp;
+  any_bcancel = !d.rect_is_ext();  // only pieces hold paired critical cells
   size_t n = (size_t)ncp;
   CK(cellid.ensure(n + 1));
   CK(fn.ensure(n + 1));

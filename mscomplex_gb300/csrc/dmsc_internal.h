@@ -136,6 +136,7 @@ struct DiscIO {
   uint32_t *status = nullptr;
   unsigned long long limit = 1ull << 31;  // bound on one gradient chain (cells of the window)
   cudaEvent_t ev_hops[2] = {nullptr, nullptr};  // recorded around the hop kernel when set
+  bool no_cancel = false;  // the complex has no boundary-cancelable critical point
   long long nadisc = 0, nddisc = 0;
 };
 cudaError_t fill_discs(DiscIO &io, cudaStream_t st);

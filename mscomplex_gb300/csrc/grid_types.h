@@ -105,6 +105,7 @@ struct dmsc_msc {
   DevBuf<float> fn;
   DevBuf<uint8_t> flags;  // bit0 isCancelled, bit1 isOnStrangulationPath, bit2 isBoundryCancelable
   unsigned long long simp_stats[5] = {0, 0, 0, 0, 0};
+  bool any_bcancel = true;  // false only when known to hold no boundary-cancelable point
 
   int writeout_from(const dmsc_dataset &d, cudaStream_t st);
 };

@@ -397,6 +397,7 @@ void mgraph_set_rects(MGraphHost &h, const int rect[4], const int ext[4]) {
 cudaError_t mgraph_to_csr(const MGraphHost &h, dmsc_msc &out, cudaStream_t st) {
   const MGraph &m = *reinterpret_cast<const MGraph *>(h.raw);
   uint32_t n = m.G.ncp;
+  out.any_bcancel = true;  // merged complexes carry the pieces' boundary pairs
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = out.cellid.ensure(n + 1);
   if (e == cudaSuccess) e = out.fn.ensure(n + 1);
