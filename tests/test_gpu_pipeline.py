@@ -90,3 +90,23 @@ def test_pipeline_bad_args(gpu_lib):
         gpu_lib.GridDataManager(f, levels=-1)
     with pytest.raises(gpu_lib.DmscError):
         gpu_lib.GridDataManager(f[:1], levels=0)
+
+
+def test_cli_matches_oracle_discs(gpu_lib, oracle, tmp_path):
+    from mscomplex_gb300.__main__ import main
+    from mscomplex_gb300 import synth
+    f = synth.bumps256()
+    raw = tmp_path / "f.raw"
+    f.tofile(raw)
+    out = tmp_path / "out"
+    assert main(["-gf", str(raw), "-d", "256", "256", "-l", "2", "--simp-tresh", "0.05", "--outdir", str(out)]) == 0
+    want = oracle.Pipeline(f, levels=2, tresh=0.05, split2d=False).disc_files()
+    files = {}
+    for p in out.iterdir():
+        name = p.name[len("dp__disc_"):]
+        kind = 0 if name.startswith("asc_") else 1
+        x, y = (int(v) for v in name[5:-1].split(","))
+        files[(kind, x, y)] = np.fromfile(p, np.int16).reshape(-1, 2)
+    assert set(files) == set(want)
+    for k in want:
+        assert np.array_equal(files[k], want[k]), k
