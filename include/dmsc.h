@@ -43,7 +43,8 @@ enum {
   DMSC_ERR_DEVICE_TIMEOUT = 5, /* a bounded device loop ran out of iterations */
   DMSC_ERR_INVARIANT = 6,      /* a reference std::logic_error condition */
   DMSC_ERR_INPUT = 7,          /* input outside the supported domain (NaN heights) */
-  DMSC_ERR_STATE = 8           /* call out of order (e.g. export before work) */
+  DMSC_ERR_STATE = 8,          /* call out of order (e.g. export before work) */
+  DMSC_ERR_PARTIAL = 9         /* a batch ran but some of its grids failed (dmsc_batch_grid_status) */
 };
 
 /* Message of the calling thread's last error ("" if none). */
@@ -156,6 +157,10 @@ int dmsc_pipeline_write_discs(dmsc_pipeline *p, const char *prefix);
 /* Host wall time (ms) of the last run's stages: pieces, merge up, simplify,
  * merge down, discs. */
 int dmsc_pipeline_stage_times(dmsc_pipeline *p, double ms[5]);
+/* Tree levels whose largest merge involves at least min_cps critical points
+ * (default 2048) run the parallel merges; smaller levels run every merge on
+ * one thread (one block per merge).  Both give the same complexes. */
+int dmsc_set_merge_parallel_min(dmsc_ctx *ctx, int64_t min_cps);
 
 /* ---- batches of whole grids ----
  * No counterpart in the reference, which builds one GridDataset at a time
@@ -166,7 +171,11 @@ int dmsc_pipeline_stage_times(dmsc_pipeline *p, double ms[5]);
  * simplify_un_simplify(tresh[g]) (skipped where tresh[g] == 0) in shared
  * launches.  Every grid's complex is identical to the one-grid path.
  * *out == NULL: a new batch; otherwise that batch is rerun in place (buffers
- * reused).  max_ops bounds each grid's simplification (<= 0: 20,000,000). */
+ * reused).  max_ops bounds each grid's simplification (<= 0: 20,000,000).
+ * A grid whose simplification exhausts max_ops (or breaks an invariant) fails
+ * alone: the run returns DMSC_ERR_PARTIAL, the batch is still *out, the
+ * other grids export as usual, and dmsc_batch_export of a failed grid returns
+ * its own error (dmsc_batch_export_all refuses a batch with failed grids). */
 typedef struct dmsc_batch dmsc_batch;
 int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float *heights, int on_device,
                    const double *tresh, int64_t max_ops, dmsc_batch **out, void *stream);
@@ -174,6 +183,8 @@ int dmsc_batch_destroy(dmsc_batch *b);
 int dmsc_batch_num_grids(dmsc_batch *b, int64_t *n);
 /* [0] critical points, [1] asc entries, [2] des entries of grid i */
 int dmsc_batch_sizes(dmsc_batch *b, int64_t i, int64_t sizes[3]);
+/* grid i's own status (DMSC_OK or its error) and message (may be NULL) */
+int dmsc_batch_grid_status(dmsc_batch *b, int64_t i, int *status, char *error, int error_len);
 /* simplification counters of grid i, as dmsc_msc_simplify_stats */
 int dmsc_batch_simplify_stats(dmsc_batch *b, int64_t i, uint64_t stats[5]);
 /* grid i's complex in the layout of dmsc_msc_export (no discs) */

@@ -17,8 +17,9 @@ _lib = None
 DMSC_OK = 0
 ERRORS = {
     1: "BAD_ARG", 2: "OOM", 3: "CUDA", 4: "INT16_OVERFLOW", 5: "DEVICE_TIMEOUT",
-    6: "INVARIANT", 7: "INPUT", 8: "STATE",
+    6: "INVARIANT", 7: "INPUT", 8: "STATE", 9: "PARTIAL",
 }
+DMSC_ERR_PARTIAL = 9
 
 # Every extern "C" entry point declared in include/dmsc.h, with its argument types.
 _vp, _i64, _i32, _f64 = C.c_void_p, C.c_int64, C.c_int, C.c_double
@@ -57,6 +58,8 @@ SIGNATURES = {
     "dmsc_batch_simplify_stats": ([_vp, _i64, _vp], _i32),
     "dmsc_batch_export": ([_vp, _i64] + [_vp] * 9 + [_vp], _i32),
     "dmsc_batch_totals": ([_vp, _vp], _i32),
+    "dmsc_set_merge_parallel_min": ([_vp, _i64], _i32),
+    "dmsc_batch_grid_status": ([_vp, _i64, _vp, C.c_char_p, _i32], _i32),
     "dmsc_batch_export_all": ([_vp] + [_vp] * 11 + [_vp], _i32),
     "dmsc_server_create": ([_vp, _i64, _i32, _i32, _i64, _vp], _i32),
     "dmsc_server_submit": ([_vp, _vp, _i32, _i32, C.c_double, _vp], _i32),

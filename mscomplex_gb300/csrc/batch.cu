@@ -42,6 +42,9 @@ struct dmsc_batch {
   DevBuf<uint8_t> flags;
   std::vector<uint32_t> cpb, abase, dbase;            // ngrids + 1 each
   std::vector<unsigned long long> stats;              // 5 per grid
+  std::vector<int> gstat;                             // per grid: DMSC_OK or the grid's own error
+  std::vector<std::string> gerr;                      // its message
+  int ndead = 0;
 };
 
 namespace {
@@ -117,6 +120,9 @@ int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float 
   if (!fresh && B->ctx != ctx) return berr(DMSC_ERR_BAD_ARG, "batch belongs to another context");
   B->ctx = ctx;
   B->ngrids = ngrids;
+  B->gstat.assign(ngrids, DMSC_OK);
+  B->gerr.assign(ngrids, std::string());
+  B->ndead = 0;
   auto fail = [&](int rc) {
     if (fresh) delete B;
     else { B->ncp = 0; B->cpb.clear(); B->abase.clear(); B->dbase.clear(); }
@@ -253,9 +259,12 @@ int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float 
     io.max_ops = max_ops > 0 ? (unsigned long long)max_ops : 20000000ull;
     io.host_stats = B->stats.data();
     int rc = DMSC_OK;
+    std::vector<int> dead;
     // a grid that ran out of list pool, heap or scratch (not of its operation
     // budget) makes the whole simplification rerun with larger capacities;
-    // whole grids start with no flags and no pairs, so the rerun starts clean
+    // whole grids start with no flags and no pairs, so the rerun starts clean.
+    // A grid that exhausts its operation budget or breaks an invariant fails
+    // alone: its lists are emptied and the other grids complete.
     for (int attempt = 0;; ++attempt) {
       cudaError_t e = simplify_batch_run(io, st);
       if (e != cudaSuccess) {
@@ -264,16 +273,25 @@ int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float 
         break;
       }
       bool capacity = false;
-      for (int g = 0; g < ngrids && rc == DMSC_OK; ++g) {
+      dead.clear();
+      for (int g = 0; g < ngrids; ++g) {
         const unsigned long long s = B->stats[5 * g + 4];
         if (!s) continue;
-        if (s == ST_SIMPLIFY_LIMIT && B->stats[5 * g + 3] <= io.max_ops && attempt < 3) capacity = true;
-        else if (s & ST_SIMPLIFY_LIMIT)
-          rc = berr(DMSC_ERR_DEVICE_TIMEOUT, "grid " + std::to_string(g) + ": simplification ran out of its operation budget");
-        else
-          rc = berr(DMSC_ERR_INVARIANT, "grid " + std::to_string(g) + ": simplification status " + std::to_string(s));
+        if (s == ST_SIMPLIFY_LIMIT && B->stats[5 * g + 3] <= io.max_ops && attempt < 3) { capacity = true; continue; }
+        dead.push_back(g);
+        if (s == ST_SIMPLIFY_LIMIT && B->stats[5 * g + 3] <= io.max_ops) {
+          B->gstat[g] = DMSC_ERR_DEVICE_TIMEOUT;
+          B->gerr[g] = "grid " + std::to_string(g) + ": simplification ran out of list pool after retries";
+        } else if (s & ST_SIMPLIFY_LIMIT) {
+          B->gstat[g] = DMSC_ERR_DEVICE_TIMEOUT;
+          B->gerr[g] = "grid " + std::to_string(g) + ": simplification ran out of its operation budget";
+        } else {
+          B->gstat[g] = DMSC_ERR_INVARIANT;
+          B->gerr[g] = "grid " + std::to_string(g) + ": simplification status " + std::to_string(s);
+        }
       }
-      if (rc != DMSC_OK || !capacity) break;
+      if (!capacity) break;
+      for (int g : dead) { B->gstat[g] = DMSC_OK; B->gerr[g].clear(); }
       simplify_batch_release(io, st);
       io.scale *= 4;
       if (cudaMemsetAsync(B->flags.p, 0, n, st) || cudaMemsetAsync(B->pair_idx.p, 0xFF, 4 * n, st)) {
@@ -281,11 +299,14 @@ int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float 
         break;
       }
     }
+    if (rc == DMSC_OK && simplify_batch_offsets(io, dead, st) != cudaSuccess)
+      rc = berr(DMSC_ERR_CUDA, "batch simplify offsets");
     if (rc == DMSC_OK) {
       if (B->asc.ensure((size_t)io.nasc_out + 1, st) || B->des.ensure((size_t)io.ndes_out + 1, st) ||
           simplify_batch_emit(io, B->asc.p, B->des.p, st))
         rc = berr(DMSC_ERR_CUDA, "batch simplify output");
     }
+    B->ndead = (int)dead.size();
     simplify_batch_release(io, st);
     if (rc) return fail(rc);
     B->nasc = io.nasc_out;
@@ -298,6 +319,11 @@ int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float 
       return fail(berr(DMSC_ERR_CUDA, "batch list bases"));
   }
   *out = B;
+  if (B->ndead) {
+    for (int g = 0; g < ngrids; ++g)
+      if (B->gstat[g] != DMSC_OK)
+        return berr(DMSC_ERR_PARTIAL, std::to_string(B->ndead) + " grid(s) failed; first: " + B->gerr[g]);
+  }
   return DMSC_OK;
 }
 
@@ -324,6 +350,17 @@ int dmsc_batch_sizes(dmsc_batch *b, int64_t i, int64_t sizes[3]) {
   return DMSC_OK;
 }
 
+int dmsc_batch_grid_status(dmsc_batch *b, int64_t i, int *status, char *error, int error_len) {
+  if (!b || !status || i < 0 || i >= b->ngrids || b->gstat.size() != (size_t)b->ngrids)
+    return berr(DMSC_ERR_BAD_ARG, "no such grid");
+  *status = b->gstat[i];
+  if (error && error_len > 0) {
+    std::strncpy(error, b->gerr[i].c_str(), (size_t)error_len - 1);
+    error[error_len - 1] = 0;
+  }
+  return DMSC_OK;
+}
+
 int dmsc_batch_simplify_stats(dmsc_batch *b, int64_t i, uint64_t stats[5]) {
   if (!b || !stats || i < 0 || i >= b->ngrids || b->stats.size() != 5 * (size_t)b->ngrids)
     return berr(DMSC_ERR_BAD_ARG, "no such grid");
@@ -335,6 +372,7 @@ int dmsc_batch_export(dmsc_batch *b, int64_t i, int16_t rect_ext[8], int16_t *ce
                       uint8_t *flags, uint32_t *asc_off, uint32_t *asc, uint32_t *des_off, uint32_t *des, void *stream) {
   if (!b || i < 0 || i >= b->ngrids) return berr(DMSC_ERR_BAD_ARG, "no such grid");
   if (b->cpb.size() != (size_t)b->ngrids + 1) return berr(DMSC_ERR_STATE, "batch has not run");
+  if (b->gstat[i] != DMSC_OK) return berr(b->gstat[i], b->gerr[i]);
   BCK(cudaSetDevice(b->ctx->device));
   cudaStream_t st = stream ? (cudaStream_t)stream : b->ctx->stream;
   const size_t c0 = b->cpb[i], n = b->cpb[i + 1] - c0;
@@ -371,6 +409,7 @@ int dmsc_batch_export_all(dmsc_batch *b, uint32_t *cp_base, uint32_t *asc_base, 
                           uint32_t *des_off, uint32_t *des, void *stream) {
   if (!b) return berr(DMSC_ERR_BAD_ARG, "batch is null");
   if (b->cpb.size() != (size_t)b->ngrids + 1) return berr(DMSC_ERR_STATE, "batch has not run");
+  if (b->ndead) return berr(DMSC_ERR_STATE, "batch has failed grids; export the others one by one");
   BCK(cudaSetDevice(b->ctx->device));
   cudaStream_t st = stream ? (cudaStream_t)stream : b->ctx->stream;
   const size_t n = (size_t)b->ncp, g1 = (size_t)b->ngrids + 1;

@@ -321,6 +321,12 @@ int dmsc_set_timing(dmsc_ctx *ctx, int enable) {
   return DMSC_OK;
 }
 
+int dmsc_set_merge_parallel_min(dmsc_ctx *ctx, int64_t min_cps) {
+  if (!ctx || min_cps < 0) return fail(DMSC_ERR_BAD_ARG, "ctx is null or min_cps negative");
+  ctx->merge_parallel_min = min_cps;
+  return DMSC_OK;
+}
+
 int dmsc_dataset_stage_times(dmsc_dataset *d, float *ms, int n) {
   if (!d || !ms) return fail(DMSC_ERR_BAD_ARG, "null argument");
   if (!d->ev_ready) return fail(DMSC_ERR_STATE, "timing was not enabled for the last run");

@@ -36,6 +36,7 @@ enum : uint32_t {
   ST_SIMPLIFY_LIMIT = 1u << 5, // simplification pool / iteration bound exceeded
   ST_INVARIANT = 1u << 6,      // a reference logic_error condition (merge / disc invariants)
   ST_CAPACITY = 1u << 7,       // critical-point arrays too small (host grows them and reruns)
+  ST_FALLBACK = 1u << 8,       // a parallel merge met a case only the one-thread restatement reproduces
 };
 
 constexpr uint32_t LABEL_NONE = 0xFFFFFFFFu;

@@ -2,6 +2,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <vector>
 #include "dmsc_common.cuh"
 
 namespace dmsc {
@@ -115,6 +116,7 @@ struct BatchSimplifyIO {
   void *work = nullptr;
 };
 cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st);
+cudaError_t simplify_batch_offsets(BatchSimplifyIO &io, const std::vector<int> &dead, cudaStream_t st);
 cudaError_t simplify_batch_emit(BatchSimplifyIO &io, uint32_t *asc, uint32_t *des, cudaStream_t st);
 void simplify_batch_release(BatchSimplifyIO &io, cudaStream_t st);
 
@@ -162,4 +164,17 @@ cudaError_t mgraph_to_csr(const MGraphHost &h, dmsc_msc &out, cudaStream_t st);
 // merge down: parent a into children b and c; ixn4: the shared 1-manifold (l,b,r,t).
 cudaError_t merge_level(bool up, MGraphHost *hosts, int ngraphs, const int *jobs3, const int *ixn4, int njobs,
                         uint32_t *status, cudaStream_t st);
+// Parallel merges of one tree level (merge_par.cu): up builds each parent
+// from its children a, b; down pushes each parent into its children.  The
+// shared 1-manifold is ixn (l, b, r, t).  grow scales the list pools; *stw
+// is the OR of the device status words (ST_FALLBACK: rerun the level with
+// merge_level; ST_SIMPLIFY_LIMIT: rerun with a larger grow).
+struct MergeJob {
+  dmsc_msc *a, *b, *parent;
+  int ixn[4];
+};
+cudaError_t merge_up_level_par(const std::vector<MergeJob> &jobs, unsigned long long grow, uint32_t *status,
+                               uint32_t *stw, cudaStream_t st);
+cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned long long grow, uint32_t *status,
+                                 uint32_t *stw, cudaStream_t st);
 }  // namespace dmsc

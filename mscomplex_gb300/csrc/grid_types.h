@@ -94,6 +94,7 @@ struct dmsc_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool timing = false;
+  long long merge_parallel_min = 2048;  // pipeline levels with merges this large take the parallel merges
 };
 
 struct dmsc_msc {

@@ -1,0 +1,729 @@
+// merge_par.cu -- the piece merges of one tree level with the bulk of their
+// work spread over the GPU: GridMSComplex::merge_up and merge_down
+// (dmsc/src/grid_mscomplex.cpp:24-322) for complexes of millions of critical
+// points, where one thread per merge (merge.cu) would walk every critical
+// point and every arc in sequence.
+//
+// merge_up (:24-156) splits into
+//   * the union of the critical points (:56-75): A's uncancelled points keep
+//     their order, then B's uncancelled points whose cell A does not hold --
+//     a scan over each input gives every point its index in the result;
+//   * the boundary pairs (:84-92): each input's uncancelled boundary-cancelable
+//     point takes its partner's index (B's assignment after A's, as the
+//     reference's loop order leaves it);
+//   * the connectivity (:77-122): the result's list of a point is the
+//     multiset union of A's list and B's list (B's without arcs inside the
+//     shared boundary when the point itself lies on it), restricted to
+//     uncancelled points -- counts, a scan, a scatter, and a sort of each list
+//     by index (the ascending order in which a std::multiset iterates);
+//   * the cancellations along the shared boundary (:124-153), row-major and
+//     order dependent: one thread per merge, on the mutable graph
+//     (merge_up_cancel in merge_graph.cuh), all merges of the level in one
+//     launch.
+// merge_down (:158-322) splits into
+//   * the uncancellations along the shared boundary (:172-201) and the
+//     parent's boundary-cancelable points pushed into each child (:207-281):
+//     one thread per parent and per child (merge_down_boundary /
+//     merge_down_loop1), the latter visiting only the parent's
+//     boundary-cancelable points, which a parallel pass lists in index order
+//     after checking that no parent point is cancelled;
+//   * every other parent point the child holds takes the parent's lists,
+//     restricted to points the child holds (:283-320): independent per point,
+//     so counts, a scan, a scatter and a sort per list, written straight into
+//     the child's CSR arrays.
+// A step whose outcome only the one-thread restatement reproduces (a partner
+// missing from the union, where the reference's std::map::operator[] would
+// insert index 0) reports ST_FALLBACK and the caller reruns the level with
+// the one-thread merges.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dmsc_common.cuh"
+#include "dmsc_internal.h"
+#include "grid_types.h"
+#include "merge_graph.cuh"
+
+namespace dmsc {
+
+namespace {
+
+unsigned nblk(long long n) {
+  long long b = (n + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+#define GRID_LOOP(i, n) for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (long long)(n); i += (long long)gridDim.x * blockDim.x)
+
+// Open-addressing map from cell id to critical-point index (the hash
+// function of MGraph).  Inserts and lookups run in separate launches.
+struct CidHash {
+  uint32_t *key, *val;
+  uint32_t mask;
+  __device__ uint32_t find(uint32_t cid) const {
+    uint32_t h = MGraph::hash(cid) & mask;
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+      const uint32_t k = key[h];
+      if (k == cid) return val[h];
+      if (k == HASH_EMPTY) return NO_CP;
+      h = (h + 1) & mask;
+    }
+    return NO_CP;
+  }
+  __device__ bool insert(uint32_t cid, uint32_t v) {
+    uint32_t h = MGraph::hash(cid) & mask;
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+      const uint32_t prev = atomicCAS(key + h, HASH_EMPTY, cid);
+      if (prev == HASH_EMPTY || prev == cid) { val[h] = v; return true; }
+      h = (h + 1) & mask;
+    }
+    return false;
+  }
+};
+
+uint32_t hash_capacity(long long n) {
+  uint32_t c = 1024;
+  while ((long long)c < 2 * n + 16) c <<= 1;
+  return c;
+}
+
+__device__ __forceinline__ bool cancelled(const uint8_t *fl, uint32_t i) { return fl[i] & F_CANCELLED; }
+
+// ---------------------------------------------------------------------------
+// sorting every list of a CSR array by value
+// ---------------------------------------------------------------------------
+constexpr uint32_t SS_THREAD = 32, SS_BLOCK = 8192;
+
+// Segments of up to SS_THREAD values: insertion sort by one thread; longer
+// ones are queued (up to SS_BLOCK for one block each, beyond for the radix
+// sort).  `need` (may be null) marks the segments that can be out of order.
+__global__ void k_ss_small(long long nseg, const uint32_t *__restrict__ off, const uint8_t *__restrict__ need,
+                           uint32_t *__restrict__ vals, uint32_t *__restrict__ q_block, uint32_t *__restrict__ n_block,
+                           uint32_t *__restrict__ q_huge, uint32_t *__restrict__ n_huge) {
+  GRID_LOOP(s, nseg) {
+    if (need && !need[s]) continue;
+    const uint32_t b = off[s], n = off[s + 1] - b;
+    if (n <= 1) continue;
+    if (n > SS_THREAD) {
+      if (n > SS_BLOCK) q_huge[atomicAdd(n_huge, 1u)] = (uint32_t)s;
+      else q_block[atomicAdd(n_block, 1u)] = (uint32_t)s;
+      continue;
+    }
+    uint32_t v[SS_THREAD];
+    for (uint32_t i = 0; i < n; ++i) v[i] = vals[b + i];
+    for (uint32_t i = 1; i < n; ++i) {
+      const uint32_t x = v[i];
+      uint32_t j = i;
+      while (j > 0 && v[j - 1] > x) { v[j] = v[j - 1]; --j; }
+      v[j] = x;
+    }
+    for (uint32_t i = 0; i < n; ++i) vals[b + i] = v[i];
+  }
+}
+
+// queued segments of up to SS_BLOCK values: one block each, bitonic sort in shared memory
+__global__ void __launch_bounds__(512) k_ss_block(const uint32_t *__restrict__ off, uint32_t *__restrict__ vals,
+                                                  const uint32_t *__restrict__ q, const uint32_t *__restrict__ nq) {
+  __shared__ uint32_t sh[SS_BLOCK];
+  const uint32_t count = *nq;
+  for (uint32_t k = blockIdx.x; k < count; k += gridDim.x) {
+    const uint32_t s = q[k], b = off[s], n = off[s + 1] - b;
+    uint32_t p2 = 1;
+    while (p2 < n) p2 <<= 1;
+    for (uint32_t i = threadIdx.x; i < p2; i += blockDim.x) sh[i] = i < n ? vals[b + i] : 0xFFFFFFFFu;
+    __syncthreads();
+    for (uint32_t size = 2; size <= p2; size <<= 1)
+      for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+        for (uint32_t i = threadIdx.x; i < p2; i += blockDim.x) {
+          const uint32_t j = i ^ stride;
+          if (j > i) {
+            const bool up = (i & size) == 0;
+            const uint32_t x = sh[i], y = sh[j];
+            if ((x > y) == up) { sh[i] = y; sh[j] = x; }
+          }
+        }
+        __syncthreads();
+      }
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) vals[b + i] = sh[i];
+    __syncthreads();
+  }
+}
+
+// Sorts segments [off[s], off[s+1]) of vals for s < nseg where need[s] (all
+// when need is null).  `off` is on the device; synchronises `st` once.
+cudaError_t sort_segments(long long nseg, const uint32_t *off, uint32_t *vals, const uint8_t *need, cudaStream_t st) {
+  if (nseg <= 0) return cudaSuccess;
+  uint32_t *buf = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&buf, 4ull * (2 * nseg + 4), st);
+  if (e != cudaSuccess) return e;
+  uint32_t *q_block = buf, *q_huge = buf + nseg, *cnt = buf + 2 * nseg;
+  e = cudaMemsetAsync(cnt, 0, 16, st);
+  if (e == cudaSuccess) {
+    k_ss_small<<<nblk(nseg), 256, 0, st>>>(nseg, off, need, vals, q_block, cnt, q_huge, cnt + 1);
+    k_ss_block<<<152 * 2, 512, 0, st>>>(off, vals, q_block, cnt);
+    DMSC_LAUNCHED(2);
+    e = cudaGetLastError();
+  }
+  uint32_t nh = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&nh, cnt + 1, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess && nh) {  // rare: lists longer than SS_BLOCK, one radix sort each
+    std::vector<uint32_t> segs(nh), o0(nh), o1(nh);
+    e = cudaMemcpy(segs.data(), q_huge, 4ull * nh, cudaMemcpyDeviceToHost);
+    for (uint32_t k = 0; k < nh && e == cudaSuccess; ++k) {
+      e = cudaMemcpy(&o0[k], off + segs[k], 4, cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess) e = cudaMemcpy(&o1[k], off + segs[k] + 1, 4, cudaMemcpyDeviceToHost);
+    }
+    for (uint32_t k = 0; k < nh && e == cudaSuccess; ++k) {
+      const long long n = (long long)o1[k] - o0[k];
+      uint32_t *tmp = nullptr;
+      e = cudaMallocAsync((void **)&tmp, 12ull * n, st);
+      if (e != cudaSuccess) break;
+      e = cudaMemsetAsync(tmp, 0, 4ull * n, st);
+      if (e == cudaSuccess) e = radix_sort_pairs(vals + o0[k], tmp, tmp + n, tmp + 2 * n, n, 32, st);
+      cudaFreeAsync(tmp, st);
+    }
+  }
+  cudaFreeAsync(buf, st);
+  return e;
+}
+
+// ---------------------------------------------------------------------------
+// merge_up: union, boundary pairs, connectivity
+// ---------------------------------------------------------------------------
+struct CsrIn {  // a complex being read (device arrays)
+  long long n;
+  const uint32_t *cellid, *pair, *aoff, *asc, *doff, *des;
+  const float *fn;
+  const uint8_t *flags;
+};
+struct CsrOut {
+  uint32_t *cellid, *pair, *aoff, *asc, *doff, *des;
+  float *fn;
+  uint8_t *flags;
+};
+
+CsrIn csr_in(const dmsc_msc &m) {
+  return CsrIn{m.ncp, m.cellid.p, m.pair_idx.p, m.aoff.p, m.asc.p, m.doff.p, m.des.p, m.fn.p, m.flags.p};
+}
+
+__global__ void k_keep(CsrIn a, uint32_t *keep) {
+  GRID_LOOP(j, a.n) keep[j] = cancelled(a.flags, (uint32_t)j) ? 0u : 1u;
+}
+
+// shallow_replicate_cp (grid_mscomplex.cpp:7-22): flags copied, partner unset
+__device__ __forceinline__ void put_cp(const CsrIn &a, long long j, uint32_t d, CsrOut &o) {
+  o.cellid[d] = a.cellid[j];
+  o.fn[d] = a.fn[j];
+  o.flags[d] = a.flags[j] & (F_CANCELLED | F_STRANG | F_BCANCEL);
+  o.pair[d] = NO_CP;
+}
+
+// A's uncancelled points: index = scan of the keep flags
+__global__ void k_up_a(CsrIn a, const uint32_t *idx, CidHash H, CsrOut o, uint32_t *status) {
+  GRID_LOOP(j, a.n) {
+    if (cancelled(a.flags, (uint32_t)j)) continue;
+    if (!H.insert(a.cellid[j], idx[j])) { atomicOr(status, ST_SIMPLIFY_LIMIT); continue; }
+    put_cp(a, j, idx[j], o);
+  }
+}
+
+// B's uncancelled points: the index of A's copy, or new (counted by isnew)
+__global__ void k_up_b_classify(CsrIn b, CidHash H, uint32_t *idx, uint32_t *isnew) {
+  GRID_LOOP(j, b.n) {
+    uint32_t d = NO_CP, nw = 0;
+    if (!cancelled(b.flags, (uint32_t)j)) {
+      d = H.find(b.cellid[j]);
+      nw = d == NO_CP;
+    }
+    idx[j] = d;
+    isnew[j] = nw;
+  }
+}
+
+__global__ void k_up_b_new(CsrIn b, const uint32_t *isnew, const uint32_t *pos, const uint32_t *na, CidHash H, uint32_t *idx,
+                           CsrOut o, uint32_t *status) {
+  const uint32_t base = *na;
+  GRID_LOOP(j, b.n) {
+    if (!isnew[j]) continue;
+    const uint32_t d = base + pos[j];
+    idx[j] = d;
+    if (!H.insert(b.cellid[j], d)) { atomicOr(status, ST_SIMPLIFY_LIMIT); continue; }
+    put_cp(b, j, d, o);
+  }
+}
+
+// boundary pairs (:84-92) of one input; idx = the result index of each point
+__global__ void k_up_pairs(CsrIn a, const uint32_t *idx, CidHash H, uint32_t *opair, uint32_t *status) {
+  GRID_LOOP(j, a.n) {
+    const uint8_t fl = a.flags[j];
+    if ((fl & F_CANCELLED) || !(fl & F_BCANCEL)) continue;
+    const uint32_t p = a.pair[j];
+    if (p >= (uint32_t)a.n) { atomicOr(status, ST_INVARIANT); continue; }
+    const uint32_t t = H.find(a.cellid[p]);
+    if (t == NO_CP) { atomicOr(status, ST_FALLBACK); continue; }
+    opair[idx[j]] = t;
+  }
+}
+
+// list lengths: A's stored, B's added (each result point has at most one
+// source point in each input); mix marks the lists that B contributed to
+__global__ void k_up_count(CsrIn a, const uint32_t *idx, bool second, CRect ixn, uint32_t *tot_a, uint32_t *tot_d,
+                           uint8_t *mix, uint32_t *status) {
+  GRID_LOOP(j, a.n) {
+    if (cancelled(a.flags, (uint32_t)j)) continue;
+    const uint32_t d = idx[j], cid = a.cellid[j];
+    const bool cmn = second && ixn.contains(px_(cid), py_(cid));
+    uint32_t c[2] = {0, 0};
+    for (int w = 0; w < 2; ++w) {
+      const uint32_t *o = w ? a.doff : a.aoff, *l = w ? a.des : a.asc;
+      for (uint32_t q = o[j]; q < o[j + 1]; ++q) {
+        const uint32_t r = l[q];
+        if (r >= (uint32_t)a.n) { atomicOr(status, ST_INVARIANT); continue; }
+        if (cancelled(a.flags, r)) continue;
+        if (cmn && ixn.contains(px_(a.cellid[r]), py_(a.cellid[r]))) continue;
+        ++c[w];
+      }
+    }
+    if (second) {
+      tot_a[d] += c[0];
+      tot_d[d] += c[1];
+      if (c[0] + c[1]) mix[d] = 1;
+    } else {
+      tot_a[d] = c[0];
+      tot_d[d] = c[1];
+    }
+  }
+}
+
+// entries: A's from the front of each list (in order), B's from the back
+__global__ void k_up_write(CsrIn a, const uint32_t *idx, bool second, CRect ixn, CsrOut o) {
+  GRID_LOOP(j, a.n) {
+    if (cancelled(a.flags, (uint32_t)j)) continue;
+    const uint32_t d = idx[j], cid = a.cellid[j];
+    const bool cmn = second && ixn.contains(px_(cid), py_(cid));
+    for (int w = 0; w < 2; ++w) {
+      const uint32_t *io = w ? a.doff : a.aoff, *l = w ? a.des : a.asc;
+      uint32_t *oo = w ? o.doff : o.aoff, *ol = w ? o.des : o.asc;
+      const uint32_t lo = oo[d], hi = oo[d + 1];
+      uint32_t p = second ? hi : lo;
+      for (uint32_t q = io[j]; q < io[j + 1]; ++q) {
+        const uint32_t r = l[q];
+        if (r >= (uint32_t)a.n || cancelled(a.flags, r)) continue;
+        if (cmn && ixn.contains(px_(a.cellid[r]), py_(a.cellid[r]))) continue;
+        if (second) { if (p > lo) ol[--p] = idx[r]; }
+        else if (p < hi) ol[p++] = idx[r];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// merge_down: parent checks, its boundary-cancelable list, the child rewrite
+// ---------------------------------------------------------------------------
+// "all cps ought to be uncancelled" (:209) and the boundary-cancelable flags
+__global__ void k_down_check(MGraph P, uint32_t *bflag, uint32_t *status) {
+  GRID_LOOP(j, P.G.ncp) {
+    const uint8_t fl = P.G.flags[j];
+    if (fl & F_CANCELLED) atomicOr(status, ST_INVARIANT);
+    bflag[j] = (fl & F_BCANCEL) ? 1u : 0u;
+  }
+}
+
+// the boundary-cancelable points in index order, and a bound on the points
+// they can add to a child (themselves, their partners, their list entries)
+__global__ void k_down_list(MGraph P, const uint32_t *bflag, const uint32_t *pos, uint32_t *jb,
+                            unsigned long long *adds) {
+  unsigned long long mine = 0;
+  GRID_LOOP(j, P.G.ncp) {
+    if (!bflag[j]) continue;
+    jb[pos[j]] = (uint32_t)j;
+    mine += 2ull + P.G.L.nrun[2 * j] + P.G.L.nrun[2 * j + 1];
+  }
+  if (mine) atomicAdd(adds, mine);
+}
+
+// the parent point (not boundary-cancelable) whose lists replace each child point's
+__global__ void k_down_repl(MGraph P, MGraph C, uint32_t *repl) {
+  GRID_LOOP(j, P.G.ncp) {
+    if (P.G.flags[j] & F_BCANCEL) continue;
+    const uint32_t d = C.find(P.G.cellid[j]);
+    if (d != NO_CP && d < C.G.ncp) repl[d] = (uint32_t)j;
+  }
+}
+
+__global__ void k_down_count(MGraph P, MGraph C, const uint32_t *repl, uint32_t *tot_a, uint32_t *tot_d, uint8_t *need) {
+  GRID_LOOP(d, C.G.ncp) {
+    const uint32_t j = repl[d];
+    for (int w = 0; w < 2; ++w) {
+      uint32_t c = 0;
+      if (j == NO_CP) {
+        c = C.G.L.total[2 * d + w];
+      } else {
+        const uint2 *r = P.G.runs(2 * j + w);
+        for (uint32_t q = 0; q < P.G.L.nrun[2 * j + w]; ++q)
+          if (C.find(P.G.cellid[r[q].x]) != NO_CP) c += r[q].y;
+      }
+      (w ? tot_d : tot_a)[d] = c;
+    }
+    need[d] = j != NO_CP;
+  }
+}
+
+__global__ void k_down_write(MGraph P, MGraph C, const uint32_t *repl, CsrOut o) {
+  GRID_LOOP(d, C.G.ncp) {
+    o.cellid[d] = C.G.cellid[d];
+    o.fn[d] = C.fn[d];
+    o.flags[d] = C.G.flags[d];
+    o.pair[d] = C.G.pair_idx[d];
+    const uint32_t j = repl[d];
+    for (int w = 0; w < 2; ++w) {
+      const uint32_t *oo = w ? o.doff : o.aoff;
+      uint32_t p = oo[d];
+      const uint32_t end = oo[d + 1];
+      uint32_t *ol = w ? o.des : o.asc;
+      if (j == NO_CP) {
+        const uint2 *r = C.G.runs(2 * d + w);
+        for (uint32_t q = 0; q < C.G.L.nrun[2 * d + w]; ++q)
+          for (uint32_t c = 0; c < r[q].y && p < end; ++c) ol[p++] = r[q].x;
+      } else {
+        const uint2 *r = P.G.runs(2 * j + w);
+        for (uint32_t q = 0; q < P.G.L.nrun[2 * j + w]; ++q) {
+          const uint32_t ci = C.find(P.G.cellid[r[q].x]);
+          if (ci == NO_CP) continue;
+          for (uint32_t c = 0; c < r[q].y && p < end; ++c) ol[p++] = ci;
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// the one-thread steps of a level, one block per job
+// ---------------------------------------------------------------------------
+enum SeqKind : int { SEQ_UP_CANCEL = 0, SEQ_DOWN_BOUNDARY = 1, SEQ_DOWN_LOOP1 = 2 };
+struct SeqJob {
+  int kind, g0, g1;
+  CRect ixn;
+  const uint32_t *only;   // SEQ_DOWN_LOOP1: the parent's boundary-cancelable points
+  const uint32_t *nonly;  // and their number (device)
+};
+
+__global__ void k_merge_seq(MGraph *graphs, const SeqJob *jobs, int njobs, uint32_t *status) {
+  const int b = blockIdx.x;
+  if (b >= njobs || threadIdx.x != 0) return;
+  const SeqJob jb = jobs[b];
+  if (jb.kind == SEQ_UP_CANCEL) {
+    merge_up_cancel(graphs[jb.g0], jb.ixn, status);
+    if (graphs[jb.g0].G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+  } else if (jb.kind == SEQ_DOWN_BOUNDARY) {
+    merge_down_boundary(graphs[jb.g0], jb.ixn, status);
+    if (graphs[jb.g0].G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+  } else {
+    merge_down_loop1(graphs[jb.g0], graphs[jb.g1], jb.only, *jb.nonly, status);
+    if (graphs[jb.g1].G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+  }
+}
+
+MGraph &mg(MGraphHost &h) { return *reinterpret_cast<MGraph *>(h.raw); }
+
+// Runs the jobs (one block each) and brings the graphs' counters back.
+cudaError_t run_seq(std::vector<MGraphHost *> &graphs, const std::vector<SeqJob> &jobs, uint32_t *status,
+                    cudaStream_t st) {
+  if (jobs.empty()) return cudaSuccess;
+  const size_t ng = graphs.size();
+  char *buf = nullptr;
+  const size_t gb = sizeof(MGraph) * ng, jbytes = sizeof(SeqJob) * jobs.size();
+  cudaError_t e = cudaMallocAsync((void **)&buf, gb + jbytes + 64, st);
+  if (e != cudaSuccess) return e;
+  MGraph *dg = (MGraph *)buf;
+  SeqJob *dj = (SeqJob *)(buf + ((gb + 15) / 16) * 16);
+  std::vector<MGraph> hg(ng);
+  for (size_t i = 0; i < ng; ++i) hg[i] = mg(*graphs[i]);
+  e = cudaMemcpyAsync(dg, hg.data(), gb, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dj, jobs.data(), jbytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    k_merge_seq<<<(unsigned)jobs.size(), 32, 0, st>>>(dg, dj, (int)jobs.size(), status);
+    DMSC_LAUNCHED(1);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hg.data(), dg, gb, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess)
+    for (size_t i = 0; i < ng; ++i) mg(*graphs[i]) = hg[i];
+  cudaFreeAsync(buf, st);
+  return e;
+}
+
+struct Scratch {  // one device allocation carved into arrays
+  char *buf = nullptr;
+  std::vector<size_t> sz;
+  std::vector<void *> ptr;
+  cudaError_t alloc(cudaStream_t st) {
+    size_t tot = 0;
+    for (size_t s : sz) tot += (s + 255) / 256 * 256;
+    cudaError_t e = cudaMallocAsync((void **)&buf, tot + 256, st);
+    if (e != cudaSuccess) { buf = nullptr; return e; }
+    char *p = buf;
+    for (size_t s : sz) { ptr.push_back(p); p += (s + 255) / 256 * 256; }
+    return cudaSuccess;
+  }
+  void free(cudaStream_t st) {
+    if (buf) cudaFreeAsync(buf, st);
+    buf = nullptr;
+  }
+};
+
+CsrOut csr_out(dmsc_msc &m) {
+  return CsrOut{m.cellid.p, m.pair_idx.p, m.aoff.p, m.asc.p, m.doff.p, m.des.p, m.fn.p, m.flags.p};
+}
+
+// merge_up of one pair into o's CSR arrays (before the boundary cancellations)
+cudaError_t union_one(const dmsc_msc &A, const dmsc_msc &B, dmsc_msc &O, CRect ixn, uint32_t *status, cudaStream_t st) {
+  const long long nA = A.ncp, nB = B.ncp, bound = nA + nB;
+  if (bound >= (1ll << 30) || A.nasc + B.nasc >= (1ll << 32) - 1 || A.ndes + B.ndes >= (1ll << 32) - 1)
+    return cudaErrorInvalidValue;  // 32-bit indices and offsets
+  const uint32_t hcap = hash_capacity(bound);
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = O.cellid.ensure(bound + 1, st);
+  if (e == cudaSuccess) e = O.fn.ensure(bound + 1, st);
+  if (e == cudaSuccess) e = O.pair_idx.ensure(bound + 1, st);
+  if (e == cudaSuccess) e = O.flags.ensure(bound + 1, st);
+  if (e == cudaSuccess) e = O.aoff.ensure(bound + 1, st);
+  if (e == cudaSuccess) e = O.doff.ensure(bound + 1, st);
+  if (e == cudaSuccess) e = O.asc.ensure(A.nasc + B.nasc + 1, st);
+  if (e == cudaSuccess) e = O.des.ensure(A.ndes + B.ndes + 1, st);
+  if (e != cudaSuccess) return e;
+  Scratch s;
+  // keepA, idxA, idxB, isnew, posB, hash keys, hash values, tot_a, tot_d, mix, counters
+  s.sz = {4ull * (nA + 1), 4ull * (nA + 1), 4ull * (nB + 1), 4ull * (nB + 1), 4ull * (nB + 1), 4ull * hcap,
+          4ull * hcap, 4ull * (bound + 1), 4ull * (bound + 1), (size_t)bound + 1, 64};
+  if ((e = s.alloc(st)) != cudaSuccess) return e;
+  uint32_t *keep = (uint32_t *)s.ptr[0], *idxA = (uint32_t *)s.ptr[1], *idxB = (uint32_t *)s.ptr[2];
+  uint32_t *isnew = (uint32_t *)s.ptr[3], *posB = (uint32_t *)s.ptr[4];
+  CidHash H{(uint32_t *)s.ptr[5], (uint32_t *)s.ptr[6], hcap - 1};
+  uint32_t *tot_a = (uint32_t *)s.ptr[7], *tot_d = (uint32_t *)s.ptr[8];
+  uint8_t *mix = (uint8_t *)s.ptr[9];
+  uint32_t *cnt = (uint32_t *)s.ptr[10];  // [0] kept of A, [1] new of B
+  const CsrIn a = csr_in(A), b = csr_in(B);
+  CsrOut o = csr_out(O);
+  e = cudaMemsetAsync(H.key, 0xFF, 4ull * hcap, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(tot_a, 0, 4ull * (bound + 1), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(tot_d, 0, 4ull * (bound + 1), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(mix, 0, bound + 1, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, 64, st);
+  // union (:56-75)
+  if (e == cudaSuccess && nA) {
+    k_keep<<<nblk(nA), 256, 0, st>>>(a, keep);
+    DMSC_LAUNCHED(1);
+    e = scan_exclusive_u32(keep, nA, idxA, cnt, st);
+    if (e == cudaSuccess) {
+      k_up_a<<<nblk(nA), 256, 0, st>>>(a, idxA, H, o, status);
+      DMSC_LAUNCHED(1);
+    }
+  }
+  if (e == cudaSuccess && nB) {
+    k_up_b_classify<<<nblk(nB), 256, 0, st>>>(b, H, idxB, isnew);
+    DMSC_LAUNCHED(1);
+    e = scan_exclusive_u32(isnew, nB, posB, cnt + 1, st);
+    if (e == cudaSuccess) {
+      k_up_b_new<<<nblk(nB), 256, 0, st>>>(b, isnew, posB, cnt, H, idxB, o, status);
+      DMSC_LAUNCHED(1);
+    }
+  }
+  // boundary pairs (:84-92), A's then B's
+  if (e == cudaSuccess && nA) { k_up_pairs<<<nblk(nA), 256, 0, st>>>(a, idxA, H, o.pair, status); DMSC_LAUNCHED(1); }
+  if (e == cudaSuccess && nB) { k_up_pairs<<<nblk(nB), 256, 0, st>>>(b, idxB, H, o.pair, status); DMSC_LAUNCHED(1); }
+  // connectivity (:94-121)
+  if (e == cudaSuccess && nA) {
+    k_up_count<<<nblk(nA), 256, 0, st>>>(a, idxA, false, ixn, tot_a, tot_d, mix, status);
+    DMSC_LAUNCHED(1);
+  }
+  if (e == cudaSuccess && nB) {
+    k_up_count<<<nblk(nB), 256, 0, st>>>(b, idxB, true, ixn, tot_a, tot_d, mix, status);
+    DMSC_LAUNCHED(1);
+  }
+  if (e == cudaSuccess) e = scan_exclusive_u32(tot_a, bound, o.aoff, o.aoff + bound, st);
+  if (e == cudaSuccess) e = scan_exclusive_u32(tot_d, bound, o.doff, o.doff + bound, st);
+  if (e == cudaSuccess && nA) { k_up_write<<<nblk(nA), 256, 0, st>>>(a, idxA, false, ixn, o); DMSC_LAUNCHED(1); }
+  if (e == cudaSuccess && nB) { k_up_write<<<nblk(nB), 256, 0, st>>>(b, idxB, true, ixn, o); DMSC_LAUNCHED(1); }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = sort_segments(bound, o.aoff, o.asc, mix, st);
+  if (e == cudaSuccess) e = sort_segments(bound, o.doff, o.des, mix, st);
+  uint32_t h[4] = {0, 0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, cnt, 8, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h + 2, o.aoff + bound, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h + 3, o.doff + bound, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  s.free(st);
+  if (e != cudaSuccess) return e;
+  O.ncp = (long long)h[0] + h[1];
+  O.nasc = h[2];
+  O.ndes = h[3];
+  O.any_bcancel = true;
+  return cudaSuccess;
+}
+
+// the child's final CSR: merge_down's second loop (:283-320) and the writeout
+cudaError_t down_child_out(MGraphHost &hp, MGraphHost &hc, dmsc_msc &C, cudaStream_t st) {
+  MGraph &P = mg(hp), &Cg = mg(hc);
+  const long long n = Cg.G.ncp;
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = C.cellid.ensure(n + 1, st);
+  if (e == cudaSuccess) e = C.fn.ensure(n + 1, st);
+  if (e == cudaSuccess) e = C.pair_idx.ensure(n + 1, st);
+  if (e == cudaSuccess) e = C.flags.ensure(n + 1, st);
+  if (e == cudaSuccess) e = C.aoff.ensure(n + 1, st);
+  if (e == cudaSuccess) e = C.doff.ensure(n + 1, st);
+  if (e != cudaSuccess) return e;
+  Scratch s;
+  s.sz = {4ull * (n + 1), 4ull * (n + 1), 4ull * (n + 1), (size_t)n + 1};
+  if ((e = s.alloc(st)) != cudaSuccess) return e;
+  uint32_t *repl = (uint32_t *)s.ptr[0], *tot_a = (uint32_t *)s.ptr[1], *tot_d = (uint32_t *)s.ptr[2];
+  uint8_t *need = (uint8_t *)s.ptr[3];
+  e = cudaMemsetAsync(repl, 0xFF, 4ull * (n + 1), st);
+  if (e == cudaSuccess && P.G.ncp) {
+    k_down_repl<<<nblk(P.G.ncp), 256, 0, st>>>(P, Cg, repl);
+    DMSC_LAUNCHED(1);
+  }
+  if (e == cudaSuccess && n) {
+    k_down_count<<<nblk(n), 256, 0, st>>>(P, Cg, repl, tot_a, tot_d, need);
+    DMSC_LAUNCHED(1);
+  }
+  if (e == cudaSuccess) e = scan_exclusive_u32(tot_a, n, C.aoff.p, C.aoff.p + n, st);
+  if (e == cudaSuccess) e = scan_exclusive_u32(tot_d, n, C.doff.p, C.doff.p + n, st);
+  uint32_t tot[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&tot[0], C.aoff.p + n, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&tot[1], C.doff.p + n, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = C.asc.ensure((size_t)tot[0] + 1, st);
+  if (e == cudaSuccess) e = C.des.ensure((size_t)tot[1] + 1, st);
+  if (e == cudaSuccess && n) {
+    k_down_write<<<nblk(n), 256, 0, st>>>(P, Cg, repl, csr_out(C));
+    DMSC_LAUNCHED(1);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = sort_segments(n, C.aoff.p, C.asc.p, need, st);
+  if (e == cudaSuccess) e = sort_segments(n, C.doff.p, C.des.p, need, st);
+  s.free(st);
+  if (e != cudaSuccess) return e;
+  C.ncp = n;
+  C.nasc = tot[0];
+  C.ndes = tot[1];
+  C.any_bcancel = true;
+  return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t merge_up_level_par(const std::vector<MergeJob> &jobs, unsigned long long grow, uint32_t *status,
+                               uint32_t *stw, cudaStream_t st) {
+  *stw = 0;
+  cudaError_t e = cudaMemsetAsync(status, 0, 4, st);
+  // union and connectivity, merge by merge
+  for (size_t k = 0; k < jobs.size() && e == cudaSuccess; ++k) {
+    const MergeJob &J = jobs[k];
+    e = union_one(*J.a, *J.b, *J.parent, CRect{J.ixn[0], J.ixn[1], J.ixn[2], J.ixn[3]}, status, st);
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess || *stw) return e;
+  // the boundary cancellations, one thread per merge, on mutable graphs
+  std::vector<MGraphHost> g(jobs.size());
+  std::vector<MGraphHost *> gp;
+  std::vector<SeqJob> seq;
+  for (size_t k = 0; k < jobs.size() && e == cudaSuccess; ++k) {
+    const dmsc_msc &O = *jobs[k].parent;
+    const unsigned long long po = O.nasc + O.ndes + 8ull * O.ncp;
+    e = mgraph_alloc(g[k], O, (uint32_t)O.ncp, grow * 2 * po + 4096, st);
+    gp.push_back(&g[k]);
+    const int *x = jobs[k].ixn;
+    seq.push_back(SeqJob{SEQ_UP_CANCEL, (int)k, -1, CRect{x[0], x[1], x[2], x[3]}, nullptr, nullptr});
+  }
+  if (e == cudaSuccess) e = run_seq(gp, seq, status, st);
+  if (e == cudaSuccess) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
+  for (size_t k = 0; k < jobs.size() && e == cudaSuccess && !*stw; ++k) e = mgraph_to_csr(g[k], *jobs[k].parent, st);
+  for (auto &h : g) mgraph_free(h, st);
+  return e;
+}
+
+cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned long long grow, uint32_t *status,
+                                 uint32_t *stw, cudaStream_t st) {
+  *stw = 0;
+  const size_t nj = jobs.size();
+  cudaError_t e = cudaMemsetAsync(status, 0, 4, st);
+  // graphs: 3 per job (parent, child a, child b)
+  std::vector<MGraphHost> g(3 * nj);
+  std::vector<MGraphHost *> gp;
+  for (auto &h : g) gp.push_back(&h);
+  std::vector<SeqJob> seq;
+  for (size_t k = 0; k < nj && e == cudaSuccess; ++k) {
+    const dmsc_msc &P = *jobs[k].parent;
+    const unsigned long long pp = P.nasc + P.ndes + 8ull * P.ncp;
+    e = mgraph_alloc(g[3 * k], P, (uint32_t)P.ncp, grow * 2 * pp + 4096, st);
+    const int *x = jobs[k].ixn;
+    seq.push_back(SeqJob{SEQ_DOWN_BOUNDARY, (int)(3 * k), -1, CRect{x[0], x[1], x[2], x[3]}, nullptr, nullptr});
+  }
+  // the uncancellations along each shared boundary (:172-201)
+  if (e == cudaSuccess) e = run_seq(gp, seq, status, st);
+  // checks, the boundary-cancelable lists and the bounds of the children's growth
+  Scratch s;
+  for (size_t k = 0; k < nj; ++k) {
+    const long long n = jobs[k].parent->ncp;
+    for (int q = 0; q < 3; ++q) s.sz.push_back(4ull * (n + 1));  // flags, positions, the list
+  }
+  s.sz.push_back(16ull * (nj + 1));  // per job: count, adds
+  if (e == cudaSuccess) e = s.alloc(st);
+  unsigned long long *ctr = e == cudaSuccess ? (unsigned long long *)s.ptr[3 * nj] : nullptr;
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, 16ull * (nj + 1), st);
+  for (size_t k = 0; k < nj && e == cudaSuccess; ++k) {
+    MGraph &P = mg(g[3 * k]);
+    uint32_t *bflag = (uint32_t *)s.ptr[3 * k], *pos = (uint32_t *)s.ptr[3 * k + 1], *jb = (uint32_t *)s.ptr[3 * k + 2];
+    uint32_t *njb = (uint32_t *)(ctr + 2 * k);
+    if (!P.G.ncp) continue;
+    k_down_check<<<nblk(P.G.ncp), 256, 0, st>>>(P, bflag, status);
+    DMSC_LAUNCHED(1);
+    e = scan_exclusive_u32(bflag, P.G.ncp, pos, njb, st);
+    if (e == cudaSuccess) {
+      k_down_list<<<nblk(P.G.ncp), 256, 0, st>>>(P, bflag, pos, jb, ctr + 2 * k + 1);
+      DMSC_LAUNCHED(1);
+    }
+  }
+  std::vector<unsigned long long> hc(2 * (nj + 1), 0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hc.data(), ctr, 16ull * nj, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
+  // the children's graphs, with room for what the parent's boundary points add
+  seq.clear();
+  for (size_t k = 0; k < nj && e == cudaSuccess && !*stw; ++k) {
+    const unsigned long long adds = hc[2 * k + 1];
+    const uint32_t *jb = (const uint32_t *)s.ptr[3 * k + 2];
+    const uint32_t *njb = (const uint32_t *)(ctr + 2 * k);
+    for (int c = 0; c < 2 && e == cudaSuccess; ++c) {
+      const dmsc_msc &C = *(c ? jobs[k].b : jobs[k].a);
+      const unsigned long long pc = C.nasc + C.ndes + 8ull * C.ncp;
+      const unsigned long long cap = (unsigned long long)C.ncp + adds + 16;
+      if (cap > 0xffffffffull) { e = cudaErrorInvalidValue; break; }
+      e = mgraph_alloc(g[3 * k + 1 + c], C, (uint32_t)cap, grow * (2 * pc + 2 * adds) + 4096, st);
+      if (e == cudaSuccess && hc[2 * k])
+        seq.push_back(SeqJob{SEQ_DOWN_LOOP1, (int)(3 * k), (int)(3 * k + 1 + c), CRect{0, 0, 0, 0}, jb, njb});
+    }
+  }
+  // the parent's boundary-cancelable points into each child (:207-281)
+  if (e == cudaSuccess && !*stw) e = run_seq(gp, seq, status, st);
+  if (e == cudaSuccess && !*stw) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
+  // every other point the child holds (:283-320), straight into the child's
+  // CSR arrays; then the parent's own write-back
+  for (size_t k = 0; k < nj && e == cudaSuccess && !*stw; ++k) {
+    e = down_child_out(g[3 * k], g[3 * k + 1], *jobs[k].a, st);
+    if (e == cudaSuccess) e = down_child_out(g[3 * k], g[3 * k + 2], *jobs[k].b, st);
+    if (e == cudaSuccess) e = mgraph_to_csr(g[3 * k], *jobs[k].parent, st);
+  }
+  s.free(st);
+  for (auto &h : g) mgraph_free(h, st);
+  cudaStreamSynchronize(st);
+  return e;
+}
+
+}  // namespace dmsc

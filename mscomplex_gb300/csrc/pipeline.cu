@@ -95,11 +95,68 @@ static dmsc_msc *new_msc(dmsc_ctx *c, const R4 &r, const R4 &e) {
   return m;
 }
 
+// The shared 1-manifold of the children of `node` (rect_t::intersection,
+// rectangle_complex.h); false when they do not share one.
+static bool shared_edge(dmsc_pipeline *P, int node, int ixn[4]) {
+  const int N = (int)P->pieces.size(), k = node - N;
+  const dmsc_msc *ma = P->msc[2 * k], *mb = P->msc[2 * k + 1];
+  const int x0 = std::max(ma->rect[0], mb->rect[0]), y0 = std::max(ma->rect[1], mb->rect[1]);
+  const int x1 = std::min(ma->rect[2], mb->rect[2]), y1 = std::min(ma->rect[3], mb->rect[3]);
+  ixn[0] = x0; ixn[1] = y0; ixn[2] = x1; ixn[3] = y1;
+  return !(x0 > x1 || y0 > y1 || (x0 != x1 && y0 != y1) || (x0 == x1 && y0 == y1));
+}
+
+constexpr int LEVEL_FALLBACK = -1;
+
+// One tree level through the parallel merges (merge_par.cu), with the same
+// retries as below; LEVEL_FALLBACK when a merge needs the one-thread path.
+static int run_level_par(dmsc_pipeline *P, bool up, const std::vector<int> &nodes, cudaStream_t st) {
+  const int N = (int)P->pieces.size();
+  std::vector<MergeJob> jobs;
+  for (int node : nodes) {
+    MergeJob J;
+    const int k = node - N;
+    J.a = P->msc[2 * k]; J.b = P->msc[2 * k + 1]; J.parent = P->msc[node];
+    if (!shared_edge(P, node, J.ixn)) return perr(DMSC_ERR_INVARIANT, "pieces must share a 1-manifold");
+    jobs.push_back(J);
+  }
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    const unsigned long long grow = 1ull << (2 * attempt);
+    uint32_t stw = 0;
+    cudaError_t e = up ? merge_up_level_par(jobs, grow, P->status.p, &stw, st)
+                       : merge_down_level_par(jobs, grow, P->status.p, &stw, st);
+    if (e != cudaSuccess)
+      return perr(e == cudaErrorMemoryAllocation ? DMSC_ERR_OOM : DMSC_ERR_CUDA,
+                  std::string("parallel merge level: ") + cudaGetErrorString(e));
+    if (stw & ST_FALLBACK) {
+      for (auto &J : jobs) J.parent->ncp = J.parent->nasc = J.parent->ndes = 0;  // the one-thread merge_up starts empty
+      return LEVEL_FALLBACK;
+    }
+    if (stw == ST_SIMPLIFY_LIMIT && attempt + 1 < 4) continue;
+    if (stw & ST_SIMPLIFY_LIMIT) return perr(DMSC_ERR_DEVICE_TIMEOUT, "a merge ran out of list pool or table room");
+    if (stw) return perr(DMSC_ERR_INVARIANT, "merge invariant violated (status " + std::to_string(stw) + ")");
+    return DMSC_OK;
+  }
+  return perr(DMSC_ERR_DEVICE_TIMEOUT, "merge pools still too small after retries");
+}
+
 // One tree level of merges, with retries: a level that runs out of list pool
 // is rerun from its unchanged inputs with larger pools.  Up: node N+k is built
 // from nodes 2k and 2k+1.  Down: node N+k pushes into nodes 2k and 2k+1.
+// Levels whose largest merge involves at least the context's
+// merge_parallel_min critical points take the parallel merges.
 static int run_level(dmsc_pipeline *P, bool up, const std::vector<int> &nodes, cudaStream_t st) {
   const int N = (int)P->pieces.size();
+  long long biggest = 0;
+  for (int node : nodes) {
+    const int k = node - N;
+    long long n = P->msc[2 * k]->ncp + P->msc[2 * k + 1]->ncp + (up ? 0 : P->msc[node]->ncp);
+    biggest = std::max(biggest, n);
+  }
+  if (biggest >= P->ctx->merge_parallel_min) {
+    const int rc = run_level_par(P, up, nodes, st);
+    if (rc != LEVEL_FALLBACK) return rc;
+  }
   for (int attempt = 0; attempt < 4; ++attempt) {
     const unsigned long long grow = 1ull << (2 * attempt);
     std::vector<MGraphHost> g(3 * nodes.size());
@@ -108,11 +165,9 @@ static int run_level(dmsc_pipeline *P, bool up, const std::vector<int> &nodes, c
     for (size_t j = 0; j < nodes.size() && rc == DMSC_OK; ++j) {
       const int node = nodes[j], k = node - N, a = 2 * k, b = 2 * k + 1;
       dmsc_msc *ma = P->msc[a], *mb = P->msc[b], *mp = P->msc[node];
-      // rect_t::intersection of the children (rectangle_complex.h), a 1-manifold
-      const int x0 = std::max(ma->rect[0], mb->rect[0]), y0 = std::max(ma->rect[1], mb->rect[1]);
-      const int x1 = std::min(ma->rect[2], mb->rect[2]), y1 = std::min(ma->rect[3], mb->rect[3]);
-      if (x0 > x1 || y0 > y1 || (x0 != x1 && y0 != y1) || (x0 == x1 && y0 == y1))
-        return perr(DMSC_ERR_INVARIANT, "pieces must share a 1-manifold");
+      int x[4];
+      if (!shared_edge(P, node, x)) return perr(DMSC_ERR_INVARIANT, "pieces must share a 1-manifold");
+      const int x0 = x[0], y0 = x[1], x1 = x[2], y1 = x[3];
       const int ia = 3 * (int)j, ib = ia + 1, ip = ia + 2;
       gnode[ia] = a; gnode[ib] = b; gnode[ip] = node;
       const unsigned long long pa = ma->nasc + ma->ndes + 8ull * ma->ncp;

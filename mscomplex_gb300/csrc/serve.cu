@@ -17,7 +17,10 @@
 // batch completes with its slowest grid.  So requests with tresh > 0 whose
 // heights have more than 1% equal neighbour pairs are "heavy" and queue for
 // lane 0 alone (when there are two or more lanes); the other lanes never wait
-// behind them.
+// behind them.  A request whose simplification exhausts the operation budget
+// fails alone (DMSC_ERR_PARTIAL from the batch); its batch mates complete.
+// Only a batch that fails as a whole (NaN heights, an allocation) is rerun
+// one grid at a time.
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -155,7 +158,8 @@ void dmsc_server::lane(int k) {
         o += r->heights.size();
       }
       rc = dmsc_batch_run(ctx, (int)take.size(), sizes.data(), staging, 0, tr.data(), max_ops, &batch, st);
-      if (rc) err = dmsc_last_error();
+      if (rc == DMSC_ERR_PARTIAL) rc = DMSC_OK;  // a failed grid's export returns its own error
+      else if (rc) err = dmsc_last_error();
     }
     // a failed batch of several grids is rerun one grid at a time, so that
     // one bad request (NaN heights, an exhausted budget) fails alone
@@ -170,6 +174,11 @@ void dmsc_server::lane(int k) {
         if (solo[i] == DMSC_OK) solo[i] = 1000;  // done alone: export below, then mark
         else {
           r.error = dmsc_last_error();
+          if (solo[i] == DMSC_ERR_PARTIAL) {  // the grid's own status and message
+            char msg[512] = {0};
+            dmsc_batch_grid_status(batch, 0, &solo[i], msg, (int)sizeof(msg));
+            r.error = msg;
+          }
           r.t_start = t_start;
           r.t_done = now_ms();
           std::lock_guard<std::mutex> lk(mu);

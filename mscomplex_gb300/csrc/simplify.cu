@@ -219,14 +219,16 @@ __global__ void k_lists_from_csr(uint32_t ncp, const uint32_t *aoff, const uint3
   }
 }
 
-// run-length lists -> expanded CSR (offsets from a scan of the totals)
+// run-length lists -> expanded CSR (offsets from a scan of the totals; a
+// list never writes past the next list's offset)
 __global__ void k_csr_from_lists(uint32_t ncp, const uint32_t *off, const uint32_t *nrun, const uint2 *pool, int which,
                                  const uint32_t *outoff, uint32_t *out) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ncp; i += gridDim.x * blockDim.x) {
     uint32_t l = 2 * i + which, o = outoff[i];
+    const uint32_t end = outoff[i + 1];
     const uint2 *p = pool + off[l];
     for (uint32_t k = 0; k < nrun[l]; ++k)
-      for (uint32_t c = 0; c < p[k].y; ++c) out[o++] = p[k].x;
+      for (uint32_t c = 0; c < p[k].y && o < end; ++c) out[o++] = p[k].x;
   }
 }
 __global__ void k_pick_len(uint32_t ncp, const uint32_t *len, int which, uint32_t *out) {
@@ -475,12 +477,24 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   for (int g = 0; g < io.ngrids; ++g)
     for (int q = 0; q < 5; ++q) io.host_stats[5 * g + q] = 0;
-  bool bad = false;
-  for (int k = 0; k < ns; ++k) {
+  for (int k = 0; k < ns; ++k)
     for (int q = 0; q < 5; ++q) io.host_stats[5 * which[k] + q] = hs[8 * k + q];
-    bad |= hs[8 * k + 4] != 0;
+  return cudaSuccess;  // the caller reads the per-grid status
+}
+
+// List offsets of the simplified batch; the grids in `dead` (whose
+// simplification failed) keep their critical points but get empty lists.
+cudaError_t simplify_batch_offsets(BatchSimplifyIO &io, const std::vector<int> &dead, cudaStream_t st) {
+  BatchSimplifyWork *w = (BatchSimplifyWork *)io.work;
+  const uint32_t ncp = (uint32_t)io.ncp;
+  io.nasc_out = io.ndes_out = 0;
+  if (!w || !ncp) return cudaSuccess;
+  cudaError_t e = cudaSuccess;
+  for (int g : dead) {  // no runs and no total: the emit writes nothing for them
+    const unsigned long long c0 = io.cpb[g], n = io.cpb[g + 1] - c0;
+    if (n && e == cudaSuccess) e = cudaMemsetAsync(w->total + 2 * c0, 0, 8ull * n, st);
+    if (n && e == cudaSuccess) e = cudaMemsetAsync(w->nrun + 2 * c0, 0, 8ull * n, st);
   }
-  if (bad || !ncp) return cudaSuccess;  // the caller reads the per-grid status
   for (int wch = 0; wch < 2 && e == cudaSuccess; ++wch) {
     uint32_t *offs = wch ? io.doff : io.aoff;
     k_pick_len<<<blocks_for(ncp), 256, 0, st>>>(ncp, w->total, wch, w->lens);

@@ -14,7 +14,7 @@ import threading
 
 import numpy as np
 
-from ._native import check, load
+from ._native import DMSC_ERR_PARTIAL, check, load
 
 _ctx_lock = threading.Lock()
 _ctx = {}
@@ -36,6 +36,11 @@ class Context:
 
     def set_timing(self, enable: bool = True):
         check(self.lib.dmsc_set_timing(self.h, int(enable)))
+
+    def set_merge_parallel_min(self, min_cps: int):
+        """Pipeline tree levels whose largest merge involves at least min_cps
+        critical points take the parallel merges (default 2048)."""
+        check(self.lib.dmsc_set_merge_parallel_min(self.h, int(min_cps)))
 
     def close(self):
         if self.h:
@@ -311,7 +316,11 @@ class GridBatch:
         packed = np.concatenate([np.ascontiguousarray(f, np.float32).reshape(-1) for f in fields])
         return packed, sizes
 
-    def run(self, fields=None, tresh=0.0, *, packed=None, sizes=None, max_ops: int = 0, stream=None):
+    def run(self, fields=None, tresh=0.0, *, packed=None, sizes=None, max_ops: int = 0, stream=None,
+            partial_ok: bool = False):
+        """Runs the batch.  A grid whose simplification fails (its operation
+        budget, an invariant) fails alone; with partial_ok the batch is kept
+        and grid_status(i) names the failed grids, otherwise DmscError."""
         if fields is not None:
             packed, sizes = self.pack(fields)
         sizes = np.ascontiguousarray(sizes, np.int32).reshape(-1)
@@ -329,8 +338,10 @@ class GridBatch:
             packed = np.ascontiguousarray(packed, np.float32)
             self._keep = packed
             ptr, on_dev = _ptr(packed), 0
-        check(self.lib.dmsc_batch_run(self.ctx.h, n, _ptr(sizes), ptr, on_dev, _ptr(t), int(max_ops),
-                                      C.byref(self.h), stream))
+        rc = self.lib.dmsc_batch_run(self.ctx.h, n, _ptr(sizes), ptr, on_dev, _ptr(t), int(max_ops),
+                                     C.byref(self.h), stream)
+        if not (partial_ok and rc == DMSC_ERR_PARTIAL):
+            check(rc)
         self.n = n
         self._sizes = sizes
         return self
@@ -339,6 +350,13 @@ class GridBatch:
         s = np.zeros(3, np.int64)
         check(self.lib.dmsc_batch_sizes(self.h, int(i), _ptr(s)))
         return [int(v) for v in s]
+
+    def grid_status(self, i: int):
+        """(status code, message) of grid i: DMSC_OK (0) or its own error."""
+        code = C.c_int(0)
+        msg = C.create_string_buffer(512)
+        check(self.lib.dmsc_batch_grid_status(self.h, int(i), C.byref(code), msg, 512))
+        return int(code.value), msg.value.decode()
 
     def simplify_stats(self, i: int) -> dict:
         a = np.zeros(5, np.uint64)

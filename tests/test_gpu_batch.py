@@ -91,3 +91,35 @@ def test_batch_bad_input(gpu_lib):
     f[3, 4] = np.nan
     with pytest.raises(gpu_lib.DmscError):
         gpu_lib.GridBatch().run([smooth_field(10, 10, 0), f])
+
+
+def budget_case(M):
+    """Three grids whose middle one (exact ties everywhere) needs more
+    simplification operations than the other two; the budget is the largest
+    of the other two's counts."""
+    fields = [smooth_field(60, 60, 0), tie_field(40, 50, 5, 1), smooth_field(50, 70, 2)]
+    tresh = [0.05, 0.3, 0.05]
+    full = M.GridBatch().run(fields, tresh)
+    ops = [full.simplify_stats(i)["ops"] for i in range(3)]
+    assert ops[1] > max(ops[0], ops[2]), ops
+    return fields, tresh, max(ops[0], ops[2])
+
+
+def test_batch_budget_failure_is_per_grid(gpu_lib, oracle):
+    fields, tresh, budget = budget_case(gpu_lib)
+    with pytest.raises(gpu_lib.DmscError) as ei:
+        gpu_lib.GridBatch().run(fields, tresh, max_ops=budget)
+    assert ei.value.code == 9  # DMSC_ERR_PARTIAL
+    b = gpu_lib.GridBatch().run(fields, tresh, max_ops=budget, partial_ok=True)
+    code, msg = b.grid_status(1)
+    assert code == 5 and "budget" in msg  # DMSC_ERR_DEVICE_TIMEOUT
+    for i in (0, 2):
+        assert b.grid_status(i) == (0, "")
+        r = full_rect(fields[i])
+        want = oracle.Dataset(fields[i], r, r, tresh=tresh[i]).msc()
+        assert_same_complex(b.export(i), want, f"budget batch grid {i}", keys=KEYS)
+    with pytest.raises(gpu_lib.DmscError) as ei:
+        b.export(1)
+    assert ei.value.code == 5
+    with pytest.raises(gpu_lib.DmscError):
+        b.export_all()

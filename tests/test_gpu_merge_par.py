@@ -1,0 +1,92 @@
+"""GPU parity of the parallel piece merges (merge_up / merge_down of
+dmsc/src/grid_mscomplex.cpp:24-322 with the union, the connectivity and the
+child rewrite spread over the GPU): every tree level forced onto them,
+against the oracle's pipeline, node by node, and against the one-thread
+merges on larger fields."""
+import numpy as np
+import pytest
+
+from helpers import assert_same_complex, smooth_field, tie_field
+
+pytestmark = pytest.mark.gpu
+
+GRAPH_KEYS = ("rect_ext", "cellid", "fn", "pair_idx", "flags", "asc_off", "asc", "des_off", "des")
+
+
+@pytest.fixture(scope="module")
+def par_ctx(gpu_lib):
+    ctx = gpu_lib.Context()
+    ctx.set_merge_parallel_min(0)
+    yield ctx
+    ctx.close()
+
+
+@pytest.fixture(scope="module")
+def seq_ctx(gpu_lib):
+    ctx = gpu_lib.Context()
+    ctx.set_merge_parallel_min(1 << 62)
+    yield ctx
+    ctx.close()
+
+
+def compare(got, want, what, leaves_full=True):
+    N = got.num_pieces
+    for i in range(2 * N - 1):
+        g = got.piece(i).export()
+        w = want.piece(i) if not hasattr(want, "num_pieces") else want.piece(i).export()
+        if i < N and leaves_full:
+            assert_same_complex(g, w, f"{what} leaf {i}")
+        else:
+            assert_same_complex(g, w, f"{what} node {i}", keys=GRAPH_KEYS)
+
+
+def check(M, oracle, ctx, f, levels, tresh, split2d, what):
+    want = oracle.Pipeline(f, levels=levels, tresh=tresh, split2d=split2d)
+    got = M.GridDataManager(f, levels=levels, tresh=tresh, split2d=split2d, ctx=ctx)
+    assert got.num_pieces == want.nleaves
+    compare(got, want, what)
+
+
+@pytest.mark.parametrize("levels", [1, 2, 3])
+@pytest.mark.parametrize("split2d", [False, True])
+@pytest.mark.parametrize("tresh", [0.0, 0.05])
+def test_par_smooth(gpu_lib, oracle, par_ctx, levels, split2d, tresh):
+    check(gpu_lib, oracle, par_ctx, smooth_field(70, 90, 5), levels, tresh, split2d,
+          f"par smooth L{levels} 2d={split2d} t={tresh}")
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_par_ties(gpu_lib, oracle, par_ctx, seed):
+    f = tie_field(40 + 7 * seed, 50 + 5 * seed, 5, seed)
+    check(gpu_lib, oracle, par_ctx, f, 2 + seed % 2, 0.05, seed % 2 == 1, f"par ties seed={seed}")
+
+
+def test_par_bumps256(gpu_lib, oracle, par_ctx):
+    from mscomplex_gb300 import synth
+    check(gpu_lib, oracle, par_ctx, synth.bumps256(), 3, 0.05, True, "par bumps256 L3")
+
+
+def test_par_quantized(gpu_lib, oracle, par_ctx):
+    from mscomplex_gb300 import synth
+    check(gpu_lib, oracle, par_ctx, synth.bumps4096q(n=256), 2, 0.01, False, "par bumps256q L2")
+
+
+@pytest.mark.parametrize("n,levels", [(64, 2), (128, 4), (256, 4)])
+def test_par_noise(gpu_lib, oracle, par_ctx, n, levels):
+    from mscomplex_gb300 import synth
+    check(gpu_lib, oracle, par_ctx, synth.noise(n, seed=2), levels, 0.0, True, f"par noise{n} L{levels}")
+
+
+def test_par_noise_simplified(gpu_lib, oracle, par_ctx):
+    from mscomplex_gb300 import synth
+    check(gpu_lib, oracle, par_ctx, synth.noise(96, seed=5), 3, 0.02, False, "par noise96 L3 t=0.02")
+
+
+@pytest.mark.parametrize("n,levels,split2d", [(512, 3, True), (384, 2, False)])
+def test_par_equals_sequential(gpu_lib, par_ctx, seq_ctx, n, levels, split2d):
+    """Larger noise fields: the parallel merges against the one-thread merges."""
+    from mscomplex_gb300 import synth
+    f = synth.noise(n, seed=9)
+    a = gpu_lib.GridDataManager(f, levels=levels, tresh=0.0, split2d=split2d, ctx=par_ctx)
+    b = gpu_lib.GridDataManager(f, levels=levels, tresh=0.0, split2d=split2d, ctx=seq_ctx)
+    compare(a, b, f"noise{n} par vs seq")

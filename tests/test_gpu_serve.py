@@ -80,3 +80,24 @@ def test_server_bad_request(gpu_lib):
     with pytest.raises(gpu_lib.DmscError):
         srv.result(rid)
     srv.close()
+
+
+def test_server_budget_failure_fails_alone(gpu_lib):
+    """A request that exhausts the simplification budget fails with its own
+    error; the requests batched with it complete unchanged."""
+    fields = [smooth_field(60, 60, 0), tie_field(40, 50, 5, 1), smooth_field(50, 70, 2), tie_field(20, 24, 5, 3)]
+    tresh = [0.05, 0.3, 0.05, 0.3]
+    full = gpu_lib.GridBatch().run(fields, tresh)
+    ops = [full.simplify_stats(i)["ops"] for i in range(4)]
+    budget = max(ops[0], ops[2], ops[3])
+    assert ops[1] > budget, ops
+    srv = gpu_lib.GridServer(arena_bytes=1 << 30, lanes=2, max_batch=8, max_ops=budget)
+    ids = [srv.submit(f, t) for f, t in zip(fields, tresh)]
+    for i, (rid, f, t) in enumerate(zip(ids, fields, tresh)):
+        if i == 1:
+            with pytest.raises(gpu_lib.DmscError) as ei:
+                srv.result(rid)
+            assert ei.value.code == 5
+        else:
+            assert_same_complex(srv.result(rid), alone(gpu_lib, f, t), f"request {i}", keys=KEYS)
+    srv.close()
