@@ -154,7 +154,8 @@ struct MGraphHost {
 
 struct dmsc_msc;
 namespace dmsc {
-cudaError_t mgraph_alloc(MGraphHost &h, const dmsc_msc &src, uint32_t cap, unsigned long long pool, cudaStream_t st);
+cudaError_t mgraph_alloc(MGraphHost &h, const dmsc_msc &src, uint32_t cap, unsigned long long pool, cudaStream_t st,
+                         uint32_t slack = 4);
 void mgraph_free(MGraphHost &h, cudaStream_t st);
 void mgraph_set_rects(MGraphHost &h, const int rect[4], const int ext[4]);
 uint32_t mgraph_ncp(const MGraphHost &h);
@@ -173,8 +174,9 @@ struct MergeJob {
   dmsc_msc *a, *b, *parent;
   int ixn[4];
 };
+// seq_ms accumulates the host wall time of the one-thread steps.
 cudaError_t merge_up_level_par(const std::vector<MergeJob> &jobs, unsigned long long grow, uint32_t *status,
-                               uint32_t *stw, cudaStream_t st);
+                               uint32_t *stw, cudaStream_t st, double *seq_ms);
 cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned long long grow, uint32_t *status,
-                                 uint32_t *stw, cudaStream_t st);
+                                 uint32_t *stw, cudaStream_t st, double *seq_ms);
 }  // namespace dmsc

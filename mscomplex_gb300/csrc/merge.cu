@@ -13,27 +13,34 @@
 
 namespace dmsc {
 
-// One block per merge of a tree level; thread 0 works.
+// One block per merge of a tree level; thread 0 works, on local copies of
+// the graph descriptors (kept in registers rather than reloaded from global
+// memory after every store through a list pointer).
 __global__ void k_merge_up(MGraph *graphs, const int3 *jobs, const CRect *ixns, int njobs, uint32_t *status) {
   int b = blockIdx.x;
   if (b >= njobs || threadIdx.x != 0) return;
   int3 jb = jobs[b];  // (left child, right child, output)
-  MGraph *in[2] = {&graphs[jb.x], &graphs[jb.y]};
-  merge_up_one(in, graphs[jb.z], ixns[b], status);
-  if (graphs[jb.z].G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+  MGraph ga = graphs[jb.x], gb = graphs[jb.y], go = graphs[jb.z];
+  MGraph *in[2] = {&ga, &gb};
+  merge_up_one(in, go, ixns[b], status);
+  if (go.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+  graphs[jb.z] = go;
 }
 
 __global__ void k_merge_down(MGraph *graphs, const int3 *jobs, const CRect *ixns, int njobs, uint32_t *status) {
   int b = blockIdx.x;
   if (b >= njobs || threadIdx.x != 0) return;
   int3 jb = jobs[b];  // (parent, child 1, child 2)
-  MGraph &P = graphs[jb.x];
+  MGraph P = graphs[jb.x], C1 = graphs[jb.y], C2 = graphs[jb.z];
   merge_down_boundary(P, ixns[b], status);
-  if (P.G.fail) { set_status(status, ST_SIMPLIFY_LIMIT); return; }
-  merge_down_child(P, graphs[jb.y], status);
-  if (graphs[jb.y].G.fail) { set_status(status, ST_SIMPLIFY_LIMIT); return; }
-  merge_down_child(P, graphs[jb.z], status);
-  if (graphs[jb.z].G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+  if (P.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+  if (!P.G.fail) merge_down_child(P, C1, status);
+  if (C1.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+  if (!P.G.fail && !C1.G.fail) merge_down_child(P, C2, status);
+  if (C2.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+  graphs[jb.x] = P;
+  graphs[jb.y] = C1;
+  graphs[jb.z] = C2;
 }
 
 // ---------------------------------------------------------------------------
@@ -41,7 +48,7 @@ __global__ void k_merge_down(MGraph *graphs, const int3 *jobs, const CRect *ixns
 // ---------------------------------------------------------------------------
 __global__ void k_mg_from_csr(MGraph m, uint32_t n, const uint32_t *cellid, const float *fn, const uint8_t *flags,
                               const uint32_t *pair_idx, const uint32_t *aoff, const uint32_t *asc, const uint32_t *doff,
-                              const uint32_t *des) {
+                              const uint32_t *des, uint32_t slack) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     m.G.cellid[i] = cellid[i];
     m.fn[i] = fn[i];
@@ -50,14 +57,15 @@ __global__ void k_mg_from_csr(MGraph m, uint32_t n, const uint32_t *cellid, cons
     for (int w = 0; w < 2; ++w) {
       const uint32_t *o = w ? doff : aoff, *src = w ? des : asc;
       uint32_t b = o[i], e = o[i + 1];
-      // initial lists: asc runs at aoff[i] + i*4, des runs after all asc runs
-      unsigned long long base = w ? (unsigned long long)aoff[n] + 4ull * n + doff[i] + 4ull * i : aoff[i] + 4ull * i;
+      // initial lists: asc runs at aoff[i] + i*slack, des runs after all asc runs
+      unsigned long long base = w ? (unsigned long long)aoff[n] + (unsigned long long)slack * n + doff[i] + (unsigned long long)slack * i
+                                  : aoff[i] + (unsigned long long)slack * i;
       uint32_t r = 0;
       for (uint32_t k = b; k < e; ++k) {
         if (r > 0 && m.G.L.pool[base + r - 1].x == src[k]) m.G.L.pool[base + r - 1].y += 1;
         else m.G.L.pool[base + r++] = make_uint2(src[k], 1u);
       }
-      m.G.L.off[2 * i + w] = (uint32_t)base; m.G.L.nrun[2 * i + w] = r; m.G.L.cap[2 * i + w] = (e - b) + 4;
+      m.G.L.off[2 * i + w] = (uint32_t)base; m.G.L.nrun[2 * i + w] = r; m.G.L.cap[2 * i + w] = (e - b) + slack;
       m.G.L.total[2 * i + w] = e - b;
     }
     // hash insert (keys are unique within a complex)
@@ -90,13 +98,16 @@ static unsigned nblk(long long n) {
 }
 
 // Allocates an MGraph with room for `cap` critical points and a list pool of
-// `pool` runs, and fills it from a CSR complex (n critical points, may be 0).
-cudaError_t mgraph_alloc(MGraphHost &h, const dmsc_msc &src, uint32_t cap, unsigned long long pool, cudaStream_t st) {
+// `pool` runs, and fills it from a CSR complex (n critical points, may be 0);
+// each list starts with room for `slack` more runs than it holds.
+cudaError_t mgraph_alloc(MGraphHost &h, const dmsc_msc &src, uint32_t cap, unsigned long long pool, cudaStream_t st,
+                         uint32_t slack) {
   uint32_t n = (uint32_t)src.ncp;
   if (cap < n) cap = n;
+  if (cap >= (1u << 30)) return cudaErrorInvalidValue;
   uint32_t hcap = 1;
   while (hcap < 2 * cap + 16) hcap <<= 1;
-  unsigned long long base = (unsigned long long)src.nasc + src.ndes + 8ull * n;
+  unsigned long long base = (unsigned long long)src.nasc + src.ndes + 2ull * slack * n;
   if (pool < base + 1024) pool = base + 1024;
   if (pool > 0xffffffffull) return cudaErrorInvalidValue;
   unsigned long long tmpc = 1ull << 20;
@@ -133,7 +144,7 @@ cudaError_t mgraph_alloc(MGraphHost &h, const dmsc_msc &src, uint32_t cap, unsig
   e = cudaMemsetAsync(m.hkey, 0xFF, sizeof(uint32_t) * hcap, st);
   if (e == cudaSuccess && n) {
     k_mg_from_csr<<<nblk(n), 256, 0, st>>>(m, n, src.cellid.p, src.fn.p, src.flags.p, src.pair_idx.p, src.aoff.p,
-                                          src.asc.p, src.doff.p, src.des.p);
+                                          src.asc.p, src.doff.p, src.des.p, slack);
     DMSC_LAUNCHED(1);
     e = cudaGetLastError();
   }

@@ -36,6 +36,7 @@
 // insert index 0) reports ST_FALLBACK and the caller reruns the level with
 // the one-thread merges.
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -411,28 +412,113 @@ struct SeqJob {
   const uint32_t *nonly;  // and their number (device)
 };
 
+// Loads, across the GPU, what the one-thread step of a job will read -- the
+// boundary points, their partners, their lists and their neighbours' list
+// descriptors -- so that the step finds it in L2 instead of DRAM.  Reads
+// only; the sum is stored only under a condition that never holds, so the
+// loads are kept.
+__device__ __forceinline__ uint32_t touch_cp(const MGraph &M, uint32_t c) {
+  if (c >= M.G.ncp) return 0;
+  uint32_t acc = M.G.flags[c] ^ M.G.pair_idx[c] ^ M.G.cellid[c];
+  for (int w = 0; w < 2; ++w) {
+    const uint32_t l = 2 * c + w, n = M.G.L.nrun[l];
+    const uint2 *r = M.G.L.pool + M.G.L.off[l];
+    acc ^= M.G.L.cap[l] ^ M.G.L.total[l];
+    for (uint32_t q = 0; q < n && q < 64; ++q) {
+      const uint32_t v = r[q].x;
+      if (v >= M.G.ncp) continue;
+      acc ^= M.G.flags[v] ^ M.G.pair_idx[v] ^ M.G.cellid[v];
+      for (int u = 0; u < 2; ++u) {
+        const uint32_t lv = 2 * v + u;
+        acc ^= M.G.L.nrun[lv] ^ M.G.L.cap[lv] ^ M.G.L.total[lv];
+        if (M.G.L.nrun[lv]) acc ^= M.G.L.pool[M.G.L.off[lv]].x;
+      }
+    }
+  }
+  return acc;
+}
+
+__global__ void k_seq_prefetch(const MGraph *graphs, const SeqJob *jobs, uint32_t *sink) {
+  const SeqJob jb = jobs[blockIdx.y];
+  const MGraph &M = graphs[jb.g0];
+  uint32_t acc = 0;
+  if (jb.kind != SEQ_DOWN_LOOP1) {
+    const long long w = jb.ixn.r - jb.ixn.l + 1, h = jb.ixn.t - jb.ixn.b + 1;
+    GRID_LOOP(t, w * h) {
+      const uint32_t si = M.find(pack_cellid(jb.ixn.l + (int)(t % w), jb.ixn.b + (int)(t / w)));
+      if (si == NO_CP || si >= M.G.ncp) continue;
+      acc ^= touch_cp(M, si) ^ touch_cp(M, M.G.pair_idx[si]);
+    }
+  } else {
+    const MGraph &C = graphs[jb.g1];
+    const uint32_t n = *jb.nonly;
+    GRID_LOOP(q, n) {
+      const uint32_t j = jb.only[q];
+      if (j >= M.G.ncp) continue;
+      acc ^= touch_cp(M, j);
+      const uint32_t sp = M.G.pair_idx[j];
+      acc ^= C.find(M.G.cellid[j]);
+      if (sp < M.G.ncp) acc ^= C.find(M.G.cellid[sp]);
+      for (int w = 0; w < 2; ++w) {
+        const uint32_t l = 2 * j + w;
+        const uint2 *r = M.G.L.pool + M.G.L.off[l];
+        for (uint32_t k = 0; k < M.G.L.nrun[l] && k < 64; ++k)
+          if (r[k].x < M.G.ncp) acc ^= C.find(M.G.cellid[r[k].x]);
+      }
+    }
+  }
+  if (acc == 0x9E3779B9u && sink) *sink = acc;
+}
+
+// The graphs are worked on as local copies of their descriptors: the
+// pointers and counters stay in registers instead of being reloaded from
+// global memory after every store through a list pointer.
 __global__ void k_merge_seq(MGraph *graphs, const SeqJob *jobs, int njobs, uint32_t *status) {
   const int b = blockIdx.x;
   if (b >= njobs || threadIdx.x != 0) return;
   const SeqJob jb = jobs[b];
+  MGraph g0 = graphs[jb.g0];
   if (jb.kind == SEQ_UP_CANCEL) {
-    merge_up_cancel(graphs[jb.g0], jb.ixn, status);
-    if (graphs[jb.g0].G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+    merge_up_cancel(g0, jb.ixn, status);
+    if (g0.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+    graphs[jb.g0] = g0;
   } else if (jb.kind == SEQ_DOWN_BOUNDARY) {
-    merge_down_boundary(graphs[jb.g0], jb.ixn, status);
-    if (graphs[jb.g0].G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+    merge_down_boundary(g0, jb.ixn, status);
+    if (g0.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+    graphs[jb.g0] = g0;
   } else {
-    merge_down_loop1(graphs[jb.g0], graphs[jb.g1], jb.only, *jb.nonly, status);
-    if (graphs[jb.g1].G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+    MGraph g1 = graphs[jb.g1];
+    merge_down_loop1(g0, g1, jb.only, *jb.nonly, status);
+    if (g1.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+    graphs[jb.g1] = g1;
   }
 }
 
 MGraph &mg(MGraphHost &h) { return *reinterpret_cast<MGraph *>(h.raw); }
 
-// Runs the jobs (one block each) and brings the graphs' counters back.
+// List pool (runs) beyond the lists themselves for the one-thread steps
+// along a shared boundary: lists there relocate to the pool top as they
+// grow (the graphs start without slack); retries multiply it.
+unsigned long long boundary_room(const int ixn[4]) {
+  const unsigned long long cells = (unsigned long long)(ixn[2] - ixn[0] + 1) * (ixn[3] - ixn[1] + 1);
+  return (1ull << 20) + 256ull * cells;
+}
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Runs the jobs (one block each) and brings the graphs' counters back; adds
+// its wall time to *ms.
 cudaError_t run_seq(std::vector<MGraphHost *> &graphs, const std::vector<SeqJob> &jobs, uint32_t *status,
-                    cudaStream_t st) {
+                    cudaStream_t st, double *ms) {
   if (jobs.empty()) return cudaSuccess;
+  cudaStreamSynchronize(st);
+  const double t0 = now_ms();
+  struct Acc {
+    double *ms, t0;
+    ~Acc() { if (ms) *ms += now_ms() - t0; }
+  } acc{ms, t0};
   const size_t ng = graphs.size();
   char *buf = nullptr;
   const size_t gb = sizeof(MGraph) * ng, jbytes = sizeof(SeqJob) * jobs.size();
@@ -445,8 +531,9 @@ cudaError_t run_seq(std::vector<MGraphHost *> &graphs, const std::vector<SeqJob>
   e = cudaMemcpyAsync(dg, hg.data(), gb, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dj, jobs.data(), jbytes, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
+    k_seq_prefetch<<<dim3(64, (unsigned)jobs.size()), 256, 0, st>>>(dg, dj, nullptr);
     k_merge_seq<<<(unsigned)jobs.size(), 32, 0, st>>>(dg, dj, (int)jobs.size(), status);
-    DMSC_LAUNCHED(1);
+    DMSC_LAUNCHED(2);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(hg.data(), dg, gb, cudaMemcpyDeviceToHost, st);
@@ -619,7 +706,7 @@ cudaError_t down_child_out(MGraphHost &hp, MGraphHost &hc, dmsc_msc &C, cudaStre
 }  // namespace
 
 cudaError_t merge_up_level_par(const std::vector<MergeJob> &jobs, unsigned long long grow, uint32_t *status,
-                               uint32_t *stw, cudaStream_t st) {
+                               uint32_t *stw, cudaStream_t st, double *seq_ms) {
   *stw = 0;
   cudaError_t e = cudaMemsetAsync(status, 0, 4, st);
   // union and connectivity, merge by merge
@@ -635,13 +722,12 @@ cudaError_t merge_up_level_par(const std::vector<MergeJob> &jobs, unsigned long 
   std::vector<SeqJob> seq;
   for (size_t k = 0; k < jobs.size() && e == cudaSuccess; ++k) {
     const dmsc_msc &O = *jobs[k].parent;
-    const unsigned long long po = O.nasc + O.ndes + 8ull * O.ncp;
-    e = mgraph_alloc(g[k], O, (uint32_t)O.ncp, grow * 2 * po + 4096, st);
-    gp.push_back(&g[k]);
     const int *x = jobs[k].ixn;
+    e = mgraph_alloc(g[k], O, (uint32_t)O.ncp, O.nasc + O.ndes + grow * boundary_room(x), st, 0);
+    gp.push_back(&g[k]);
     seq.push_back(SeqJob{SEQ_UP_CANCEL, (int)k, -1, CRect{x[0], x[1], x[2], x[3]}, nullptr, nullptr});
   }
-  if (e == cudaSuccess) e = run_seq(gp, seq, status, st);
+  if (e == cudaSuccess) e = run_seq(gp, seq, status, st, seq_ms);
   if (e == cudaSuccess) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
   for (size_t k = 0; k < jobs.size() && e == cudaSuccess && !*stw; ++k) e = mgraph_to_csr(g[k], *jobs[k].parent, st);
   for (auto &h : g) mgraph_free(h, st);
@@ -649,7 +735,7 @@ cudaError_t merge_up_level_par(const std::vector<MergeJob> &jobs, unsigned long 
 }
 
 cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned long long grow, uint32_t *status,
-                                 uint32_t *stw, cudaStream_t st) {
+                                 uint32_t *stw, cudaStream_t st, double *seq_ms) {
   *stw = 0;
   const size_t nj = jobs.size();
   cudaError_t e = cudaMemsetAsync(status, 0, 4, st);
@@ -660,13 +746,12 @@ cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned lon
   std::vector<SeqJob> seq;
   for (size_t k = 0; k < nj && e == cudaSuccess; ++k) {
     const dmsc_msc &P = *jobs[k].parent;
-    const unsigned long long pp = P.nasc + P.ndes + 8ull * P.ncp;
-    e = mgraph_alloc(g[3 * k], P, (uint32_t)P.ncp, grow * 2 * pp + 4096, st);
     const int *x = jobs[k].ixn;
+    e = mgraph_alloc(g[3 * k], P, (uint32_t)P.ncp, P.nasc + P.ndes + grow * boundary_room(x), st, 0);
     seq.push_back(SeqJob{SEQ_DOWN_BOUNDARY, (int)(3 * k), -1, CRect{x[0], x[1], x[2], x[3]}, nullptr, nullptr});
   }
   // the uncancellations along each shared boundary (:172-201)
-  if (e == cudaSuccess) e = run_seq(gp, seq, status, st);
+  if (e == cudaSuccess) e = run_seq(gp, seq, status, st, seq_ms);
   // checks, the boundary-cancelable lists and the bounds of the children's growth
   Scratch s;
   for (size_t k = 0; k < nj; ++k) {
@@ -702,16 +787,15 @@ cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned lon
     const uint32_t *njb = (const uint32_t *)(ctr + 2 * k);
     for (int c = 0; c < 2 && e == cudaSuccess; ++c) {
       const dmsc_msc &C = *(c ? jobs[k].b : jobs[k].a);
-      const unsigned long long pc = C.nasc + C.ndes + 8ull * C.ncp;
       const unsigned long long cap = (unsigned long long)C.ncp + adds + 16;
       if (cap > 0xffffffffull) { e = cudaErrorInvalidValue; break; }
-      e = mgraph_alloc(g[3 * k + 1 + c], C, (uint32_t)cap, grow * (2 * pc + 2 * adds) + 4096, st);
+      e = mgraph_alloc(g[3 * k + 1 + c], C, (uint32_t)cap, C.nasc + C.ndes + grow * (4 * adds + (1ull << 20)), st, 0);
       if (e == cudaSuccess && hc[2 * k])
         seq.push_back(SeqJob{SEQ_DOWN_LOOP1, (int)(3 * k), (int)(3 * k + 1 + c), CRect{0, 0, 0, 0}, jb, njb});
     }
   }
   // the parent's boundary-cancelable points into each child (:207-281)
-  if (e == cudaSuccess && !*stw) e = run_seq(gp, seq, status, st);
+  if (e == cudaSuccess && !*stw) e = run_seq(gp, seq, status, st, seq_ms);
   if (e == cudaSuccess && !*stw) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
   // every other point the child holds (:283-320), straight into the child's
   // CSR arrays; then the parent's own write-back

@@ -66,6 +66,7 @@ struct dmsc_pipeline {
   DevBuf<float> field;                    // device copy when the input was on the host
   DevBuf<uint32_t> status;
   double ms[5] = {0, 0, 0, 0, 0};
+  double seq_ms[2] = {0, 0};  // one-thread steps of the parallel merges: up, down
   unsigned long long simp[5] = {0, 0, 0, 0, 0};
   ~dmsc_pipeline() {
     for (auto *d : ds) dmsc_dataset_destroy(d);
@@ -123,8 +124,8 @@ static int run_level_par(dmsc_pipeline *P, bool up, const std::vector<int> &node
   for (int attempt = 0; attempt < 4; ++attempt) {
     const unsigned long long grow = 1ull << (2 * attempt);
     uint32_t stw = 0;
-    cudaError_t e = up ? merge_up_level_par(jobs, grow, P->status.p, &stw, st)
-                       : merge_down_level_par(jobs, grow, P->status.p, &stw, st);
+    cudaError_t e = up ? merge_up_level_par(jobs, grow, P->status.p, &stw, st, &P->seq_ms[0])
+                       : merge_down_level_par(jobs, grow, P->status.p, &stw, st, &P->seq_ms[1]);
     if (e != cudaSuccess)
       return perr(e == cudaErrorMemoryAllocation ? DMSC_ERR_OOM : DMSC_ERR_CUDA,
                   std::string("parallel merge level: ") + cudaGetErrorString(e));
@@ -344,6 +345,12 @@ int dmsc_pipeline_write_discs(dmsc_pipeline *p, const char *prefix) {
 int dmsc_pipeline_stage_times(dmsc_pipeline *p, double ms[5]) {
   if (!p || !ms) return perr(DMSC_ERR_BAD_ARG, "null argument");
   std::memcpy(ms, p->ms, sizeof(p->ms));
+  return DMSC_OK;
+}
+
+int dmsc_pipeline_merge_times(dmsc_pipeline *p, double ms[2]) {
+  if (!p || !ms) return perr(DMSC_ERR_BAD_ARG, "null argument");
+  std::memcpy(ms, p->seq_ms, sizeof(p->seq_ms));
   return DMSC_OK;
 }
 

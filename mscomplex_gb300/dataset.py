@@ -288,6 +288,12 @@ class GridDataManager:
         check(self.lib.dmsc_pipeline_stage_times(self.h, _ptr(ms)))
         return dict(zip(self.STAGES, (float(v) for v in ms)))
 
+    def merge_seq_times(self) -> dict:
+        """Of merge up / down, the ms spent in the one-thread boundary steps."""
+        ms = np.zeros(2, np.float64)
+        check(self.lib.dmsc_pipeline_merge_times(self.h, _ptr(ms)))
+        return {"merge_up": float(ms[0]), "merge_down": float(ms[1])}
+
 
 class GridBatch:
     """Many whole grids through work + writeout_connectivity +
