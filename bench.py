@@ -331,6 +331,47 @@ def bench_served(M, torch, count=300, rates=(None, 200.0), max_ops=2_000_000):
     return out
 
 
+PIPE_WORKLOAD = ("noise16384: 16384x16384 float32 i.i.d. U[0,1), seed 2; 8 levels of binary splits alternating y and x "
+                 "(256 blocks of 1024x1024 with a one-vertex halo); one complex per block, merge up to the root, "
+                 "tresh 0, merge down, manifold discs of every block")
+
+
+def bench_pipeline(M, torch, n=16384, levels=8, runs=2, cpu_side=1024):
+    """The whole piece pipeline on the white-noise field (heights resident in
+    HBM), wall clock per run; stage times from the library."""
+    from mscomplex_gb300 import synth
+    f = torch.from_numpy(synth.noise(n, seed=2)).cuda()
+    torch.cuda.synchronize()
+    walls, last = [], None
+    for r in range(runs + 1):  # the first run is warm-up
+        t0 = time.perf_counter()
+        p = M.GridDataManager(f, levels=levels, tresh=0.0, split2d=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if r:
+            walls.append(dt)
+        last = (p.stage_times(), p.merge_seq_times(), p.piece(2 * p.num_pieces - 2).sizes())
+        del p
+    wall = statistics.median(walls)
+    stages, seq, root = last
+    out = {"workload": PIPE_WORKLOAD, "Mvert_per_s": round(n * n / wall / 1e6, 2), "s_per_run": round(wall, 3),
+           "runs": runs, "stages_ms": {k: round(v, 1) for k, v in stages.items()},
+           "one_thread_boundary_steps_ms": {k: round(v, 1) for k, v in seq.items()},
+           "root_complex": {"critical_points": root[0], "asc": root[1], "des": root[2]}}
+    if cpu_side:
+        # the oracle's whole pipeline (one thread) on a smaller field of the same kind, 2 levels of splits
+        from oracle import oracle as O
+        O.build()
+        g = synth.noise(cpu_side, seed=2)
+        t0 = time.perf_counter()
+        O.Pipeline(g, levels=2, tresh=0.0, split2d=True)
+        secs = time.perf_counter() - t0
+        out["cpu_oracle"] = {"value": round(g.size / secs / 1e6, 3), "unit": "Mvert/s", "cores": 1, "kind": "port",
+                             "sample": f"{cpu_side}x{cpu_side} white noise (seed 2), 4 blocks of {cpu_side // 2}^2, "
+                                       f"the oracle's whole pipeline in {secs:.1f} s"}
+    return out
+
+
 def run_reference(args):
     """--impl reference: the oracle on the host cores (all threads via processes)."""
     rank, world, _ = dist_env()
@@ -390,6 +431,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="leave out the mixed-size batch measurement")
+    ap.add_argument("--no-pipeline", action="store_true", help="leave out the 16384^2 piece-pipeline measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -540,6 +582,8 @@ def main():
         if world == 1 and not args.no_batch:
             line["batched"] = bench_batched(M, torch, stream, sh)
             line["served"] = bench_served(M, torch)
+        if world == 1 and not args.no_pipeline:
+            line["pipeline"] = bench_pipeline(M, torch, cpu_side=0 if args.no_cpu_baseline else 1024)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -959,7 +959,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
     L(cudaStreamSynchronize(st));
     if (e != cudaSuccess) break;
     DevBuf<uint32_t> *ob = kind ? io.ddisc : io.adisc;
-    L(ob->ensure((size_t)tot[0] + 1));
+    L(ob->ensure((size_t)tot[0] + 1, st));
     L(cudaMallocAsync((void **)&segs, sizeof(uint4) * ((size_t)tot[1] + 1), st));
     L(cudaMallocAsync((void **)&tmp, sizeof(uint32_t) * ((size_t)tot[2] + 1), st));
     if (e != cudaSuccess) break;

@@ -7,6 +7,7 @@
 // here is a CUDA kernel launch.
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -134,7 +135,7 @@ int dmsc_dataset_init(dmsc_dataset *d, const float *heights, int64_t pitch, int 
     d->hgt = heights;
     g.pitch = pitch;
   } else {
-    CK(d->hown.ensure((size_t)g.vnx * g.vny));
+    CK(d->hown.ensure((size_t)g.vnx * g.vny, st));
     CK(cudaMemcpy2DAsync(d->hown.p, sizeof(float) * g.vnx, heights, sizeof(float) * pitch, sizeof(float) * g.vnx,
                          g.vny, cudaMemcpyHostToDevice, st));
     d->hgt = d->hown.p;
@@ -151,7 +152,7 @@ int dmsc_dataset_work(dmsc_dataset *d, void *stream) {
   if (!d->hgt) return fail(DMSC_ERR_STATE, "dataset has no heights (call dmsc_dataset_init first)");
   CK(cudaSetDevice(d->ctx->device));
   cudaStream_t st = pick(d->ctx, stream);
-  int rc = d->alloc_cells();
+  int rc = d->alloc_cells(st);
   if (rc) return rc;
   const GridGeom &g = d->g;
   const bool tm = d->ctx->timing;
@@ -169,7 +170,7 @@ int dmsc_dataset_work(dmsc_dataset *d, void *stream) {
   if (tm) CK(cudaEventRecord(d->ev[3], st));
   if (d->cap <= 0) d->cap = (long long)g.vnx * g.vny / 16 + 4096;
   for (int attempt = 0; attempt < 2; ++attempt) {
-    rc = d->alloc_cps(d->cap);
+    rc = d->alloc_cps(d->cap, st);
     if (rc) return rc;
     CK(cudaMemsetAsync(d->cp_acnt.p, 0, sizeof(uint32_t) * d->cap, st));
     CK(cudaMemsetAsync(d->cp_dcnt.p, 0, sizeof(uint32_t) * d->cap, st));
@@ -190,7 +191,7 @@ int dmsc_dataset_work(dmsc_dataset *d, void *stream) {
   rc = status_to_error(d->host_scal[0]);
   if (rc) return rc;
   // pair_idx of critical cells that keep a pair (boundary rule; only with rect != ext)
-  CK(d->cp_pair_idx.ensure(d->cap));
+  CK(d->cp_pair_idx.ensure(d->cap, st));
   if (d->rect_is_ext()) {
     if (d->ncp) CK(cudaMemsetAsync(d->cp_pair_idx.p, 0xFF, sizeof(uint32_t) * d->ncp, st));
   } else {
@@ -220,9 +221,9 @@ int dmsc_dataset_export_cells(dmsc_dataset *d, int8_t *flags, int16_t *pairs, in
   size_t n = (size_t)(g.cx + 1) * (g.cy + 1);
   DevBuf<int8_t> f;
   DevBuf<int16_t> p, o;
-  if (flags) CK(f.ensure(n));
-  if (pairs) CK(p.ensure(2 * n));
-  if (own) CK(o.ensure(2 * n));
+  if (flags) CK(f.ensure(n, st));
+  if (pairs) CK(p.ensure(2 * n, st));
+  if (own) CK(o.ensure(2 * n, st));
   CK(launch_export_cells(g, d->codes.p, d->labels.p, d->cp_cellid.p, d->ncp, f.p, p.p, o.p, st));
   if (flags) CK(cudaMemcpyAsync(flags, f.p, n, cudaMemcpyDeviceToHost, st));
   if (pairs) CK(cudaMemcpyAsync(pairs, p.p, 4 * n, cudaMemcpyDeviceToHost, st));
@@ -363,8 +364,8 @@ int dmsc_msc_simplify_un_simplify(dmsc_msc *m, double tresh, int64_t max_ops, vo
   else if (hs[4] != 0) rc = status_to_error((uint32_t)hs[4]);
   if (rc == DMSC_OK) {
     // grow the CSR arrays if needed, then write the new lists
-    if ((size_t)io.nasc_out + 1 > m->asc.n) e = m->asc.ensure(io.nasc_out + io.nasc_out / 4 + 16);
-    if (e == cudaSuccess && (size_t)io.ndes_out + 1 > m->des.n) e = m->des.ensure(io.ndes_out + io.ndes_out / 4 + 16);
+    if ((size_t)io.nasc_out + 1 > m->asc.n) e = m->asc.ensure(io.nasc_out + io.nasc_out / 4 + 16, st);
+    if (e == cudaSuccess && (size_t)io.ndes_out + 1 > m->des.n) e = m->des.ensure(io.ndes_out + io.ndes_out / 4 + 16, st);
     if (e == cudaSuccess) e = simplify_emit(io, m->asc.p, m->des.p, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) rc = cuda_fail(e, "simplify_emit");
@@ -395,8 +396,8 @@ int dmsc_dataset_fill_discs(dmsc_dataset *d, dmsc_msc *m, void *stream) {
   CK(cudaSetDevice(d->ctx->device));
   cudaStream_t st = pick(d->ctx, stream);
   const size_t n = (size_t)m->ncp;
-  CK(m->adoff.ensure(n + 1));
-  CK(m->ddoff.ensure(n + 1));
+  CK(m->adoff.ensure(n + 1, st));
+  CK(m->ddoff.ensure(n + 1, st));
   DiscIO io;
   io.g = d->g; io.codes = d->codes.p; io.labels = d->labels.p; io.ncp_ds = d->ncp;
   io.ncp = m->ncp; io.nasc = m->nasc; io.ndes = m->ndes;
@@ -494,33 +495,64 @@ int dmsc_kernel_launches(uint64_t *count) {
 // ---------------------------------------------------------------------------
 // member functions of the handle types
 // ---------------------------------------------------------------------------
-int dmsc_dataset::alloc_cells() {
+// Pinned 16-byte slots for the status read-back of datasets, carved from
+// pinned blocks that live as long as the process (pinning a small buffer per
+// dataset would serialise on the driver when many pieces start at once).
+namespace {
+std::mutex &pin_mu() {
+  static std::mutex *m = new std::mutex;
+  return *m;
+}
+std::vector<uint32_t *> &pin_free() {
+  static std::vector<uint32_t *> *v = new std::vector<uint32_t *>;
+  return *v;
+}
+uint32_t *pin_take() {
+  std::lock_guard<std::mutex> lk(pin_mu());
+  auto &f = pin_free();
+  if (f.empty()) {
+    constexpr int SLOTS = 1024;
+    uint32_t *blk = nullptr;
+    if (cudaMallocHost((void **)&blk, sizeof(uint32_t) * 4 * SLOTS) != cudaSuccess) return nullptr;
+    for (int i = SLOTS - 1; i >= 0; --i) f.push_back(blk + 4 * i);
+  }
+  uint32_t *p = f.back();
+  f.pop_back();
+  return p;
+}
+void pin_give(uint32_t *p) {
+  std::lock_guard<std::mutex> lk(pin_mu());
+  pin_free().push_back(p);
+}
+}  // namespace
+
+int dmsc_dataset::alloc_cells(cudaStream_t st) {
   size_t nv = (size_t)g.vnx * g.vny;
-  CK(codes.ensure(nv));
-  CK(terms.ensure(nv));
-  CK(labels.ensure(nv));
-  CK(rowcnt.ensure((size_t)(g.cy + 1) * g.ntx));
-  CK(offsets.ensure((size_t)(g.cy + 1) * g.ntx));
-  CK(table.ensure((size_t)nslots()));
-  CK(scal.ensure(4));
-  if (!host_scal) CK(cudaMallocHost((void **)&host_scal, sizeof(uint32_t) * 4));
+  CK(codes.ensure(nv, st));
+  CK(terms.ensure(nv, st));
+  CK(labels.ensure(nv, st));
+  CK(rowcnt.ensure((size_t)(g.cy + 1) * g.ntx, st));
+  CK(offsets.ensure((size_t)(g.cy + 1) * g.ntx, st));
+  CK(table.ensure((size_t)nslots(), st));
+  CK(scal.ensure(4, st));
+  if (!host_scal && !(host_scal = pin_take())) return fail(DMSC_ERR_OOM, "pinned status slot");
   return DMSC_OK;
 }
 
-int dmsc_dataset::alloc_cps(long long n) {
-  CK(cp_cellid.ensure(n));
-  CK(cp_fn.ensure(n));
-  CK(cp_flags.ensure(n));
-  CK(cp_pair_cell.ensure(n));
-  CK(cp_des2.ensure(2 * n));
-  CK(cp_asc2.ensure(2 * n));
-  CK(cp_acnt.ensure(n));
-  CK(cp_dcnt.ensure(n));
+int dmsc_dataset::alloc_cps(long long n, cudaStream_t st) {
+  CK(cp_cellid.ensure(n, st));
+  CK(cp_fn.ensure(n, st));
+  CK(cp_flags.ensure(n, st));
+  CK(cp_pair_cell.ensure(n, st));
+  CK(cp_des2.ensure(2 * n, st));
+  CK(cp_asc2.ensure(2 * n, st));
+  CK(cp_acnt.ensure(n, st));
+  CK(cp_dcnt.ensure(n, st));
   return DMSC_OK;
 }
 
 dmsc_dataset::~dmsc_dataset() {
-  if (host_scal) cudaFreeHost(host_scal);
+  if (host_scal) pin_give(host_scal);
   if (ev_ready)
     for (auto &e : ev) cudaEventDestroy(e);
 }
@@ -529,14 +561,14 @@ int dmsc_msc::writeout_from(const dmsc_dataset &d, cudaStream_t st) {
   ncp = d.ncp;
   any_bcancel = !d.rect_is_ext();  // only pieces hold paired critical cells
   size_t n = (size_t)ncp;
-  CK(cellid.ensure(n + 1));
-  CK(fn.ensure(n + 1));
-  CK(pair_idx.ensure(n + 1));
-  CK(flags.ensure(n + 1));
-  CK(aoff.ensure(n + 1));
-  CK(doff.ensure(n + 1));
-  CK(asc.ensure(4 * n + 1));
-  CK(des.ensure(4 * n + 1));
+  CK(cellid.ensure(n + 1, st));
+  CK(fn.ensure(n + 1, st));
+  CK(pair_idx.ensure(n + 1, st));
+  CK(flags.ensure(n + 1, st));
+  CK(aoff.ensure(n + 1, st));
+  CK(doff.ensure(n + 1, st));
+  CK(asc.ensure(4 * n + 1, st));
+  CK(des.ensure(4 * n + 1, st));
   if (n) {
     CK(cudaMemcpyAsync(cellid.p, d.cp_cellid.p, 4 * n, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(fn.p, d.cp_fn.p, 4 * n, cudaMemcpyDeviceToDevice, st));

@@ -84,8 +84,8 @@ struct dmsc_dataset {
   bool rect_is_ext() const {
     return rect[0] == ext[0] && rect[1] == ext[1] && rect[2] == ext[2] && rect[3] == ext[3];
   }
-  int alloc_cells();
-  int alloc_cps(long long n);
+  int alloc_cells(cudaStream_t st);
+  int alloc_cps(long long n, cudaStream_t st);
   ~dmsc_dataset();
 };
 

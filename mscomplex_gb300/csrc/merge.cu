@@ -206,12 +206,12 @@ cudaError_t mgraph_to_csr(const MGraphHost &h, dmsc_msc &out, cudaStream_t st) {
   uint32_t n = m.G.ncp;
   out.any_bcancel = true;  // merged complexes carry the pieces' boundary pairs
   cudaError_t e = cudaSuccess;
-  if (e == cudaSuccess) e = out.cellid.ensure(n + 1);
-  if (e == cudaSuccess) e = out.fn.ensure(n + 1);
-  if (e == cudaSuccess) e = out.pair_idx.ensure(n + 1);
-  if (e == cudaSuccess) e = out.flags.ensure(n + 1);
-  if (e == cudaSuccess) e = out.aoff.ensure(n + 1);
-  if (e == cudaSuccess) e = out.doff.ensure(n + 1);
+  if (e == cudaSuccess) e = out.cellid.ensure(n + 1, st);
+  if (e == cudaSuccess) e = out.fn.ensure(n + 1, st);
+  if (e == cudaSuccess) e = out.pair_idx.ensure(n + 1, st);
+  if (e == cudaSuccess) e = out.flags.ensure(n + 1, st);
+  if (e == cudaSuccess) e = out.aoff.ensure(n + 1, st);
+  if (e == cudaSuccess) e = out.doff.ensure(n + 1, st);
   if (e != cudaSuccess) return e;
   out.ncp = n;
   if (n) {
@@ -234,7 +234,7 @@ cudaError_t mgraph_to_csr(const MGraphHost &h, dmsc_msc &out, cudaStream_t st) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(&total, off + n, 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     DevBuf<uint32_t> &lb = w ? out.des : out.asc;
-    if (e == cudaSuccess) e = lb.ensure((size_t)total + 1);
+    if (e == cudaSuccess) e = lb.ensure((size_t)total + 1, st);
     if (e == cudaSuccess && n) {
       k_mg_to_csr<<<nblk(n), 256, 0, st>>>(m, w, off, lb.p);
       DMSC_LAUNCHED(1);

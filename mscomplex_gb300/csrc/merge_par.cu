@@ -44,6 +44,7 @@
 #include "dmsc_common.cuh"
 #include "dmsc_internal.h"
 #include "grid_types.h"
+#include "host_pool.h"
 #include "merge_graph.cuh"
 
 namespace dmsc {
@@ -705,105 +706,139 @@ cudaError_t down_child_out(MGraphHost &hp, MGraphHost &hc, dmsc_msc &C, cudaStre
 
 }  // namespace
 
+namespace {
+constexpr int MERGE_WORKERS = 8;
+
+cudaError_t as_cuda(int rc) {
+  return rc == 0 ? cudaSuccess : rc < 0 ? cudaErrorUnknown : (cudaError_t)rc;
+}
+int current_device() {
+  int d = 0;
+  cudaGetDevice(&d);
+  return d;
+}
+}  // namespace
+
+// The merges of a level run side by side on their own streams (several host
+// threads); the one-thread steps of all of them run in one launch on `st`.
 cudaError_t merge_up_level_par(const std::vector<MergeJob> &jobs, unsigned long long grow, uint32_t *status,
                                uint32_t *stw, cudaStream_t st, double *seq_ms) {
   *stw = 0;
+  const int nj = (int)jobs.size(), dev = current_device();
   cudaError_t e = cudaMemsetAsync(status, 0, 4, st);
-  // union and connectivity, merge by merge
-  for (size_t k = 0; k < jobs.size() && e == cudaSuccess; ++k) {
-    const MergeJob &J = jobs[k];
-    e = union_one(*J.a, *J.b, *J.parent, CRect{J.ixn[0], J.ixn[1], J.ixn[2], J.ixn[3]}, status, st);
-  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  // union and connectivity
+  if (e == cudaSuccess)
+    e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS, [&](int k, cudaStream_t s) {
+      const MergeJob &J = jobs[k];
+      return (int)union_one(*J.a, *J.b, *J.parent, CRect{J.ixn[0], J.ixn[1], J.ixn[2], J.ixn[3]}, status, s);
+    }));
   if (e == cudaSuccess) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess || *stw) return e;
   // the boundary cancellations, one thread per merge, on mutable graphs
-  std::vector<MGraphHost> g(jobs.size());
+  std::vector<MGraphHost> g(nj);
   std::vector<MGraphHost *> gp;
   std::vector<SeqJob> seq;
-  for (size_t k = 0; k < jobs.size() && e == cudaSuccess; ++k) {
-    const dmsc_msc &O = *jobs[k].parent;
+  for (int k = 0; k < nj; ++k) {
     const int *x = jobs[k].ixn;
-    e = mgraph_alloc(g[k], O, (uint32_t)O.ncp, O.nasc + O.ndes + grow * boundary_room(x), st, 0);
     gp.push_back(&g[k]);
-    seq.push_back(SeqJob{SEQ_UP_CANCEL, (int)k, -1, CRect{x[0], x[1], x[2], x[3]}, nullptr, nullptr});
+    seq.push_back(SeqJob{SEQ_UP_CANCEL, k, -1, CRect{x[0], x[1], x[2], x[3]}, nullptr, nullptr});
   }
+  e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS, [&](int k, cudaStream_t s) {
+    const dmsc_msc &O = *jobs[k].parent;
+    return (int)mgraph_alloc(g[k], O, (uint32_t)O.ncp, O.nasc + O.ndes + grow * boundary_room(jobs[k].ixn), s, 0);
+  }));
   if (e == cudaSuccess) e = run_seq(gp, seq, status, st, seq_ms);
   if (e == cudaSuccess) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
-  for (size_t k = 0; k < jobs.size() && e == cudaSuccess && !*stw; ++k) e = mgraph_to_csr(g[k], *jobs[k].parent, st);
+  if (e == cudaSuccess && !*stw)
+    e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS,
+                                    [&](int k, cudaStream_t s) { return (int)mgraph_to_csr(g[k], *jobs[k].parent, s); }));
   for (auto &h : g) mgraph_free(h, st);
+  cudaStreamSynchronize(st);
   return e;
 }
 
 cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned long long grow, uint32_t *status,
                                  uint32_t *stw, cudaStream_t st, double *seq_ms) {
   *stw = 0;
-  const size_t nj = jobs.size();
+  const int nj = (int)jobs.size(), dev = current_device();
   cudaError_t e = cudaMemsetAsync(status, 0, 4, st);
   // graphs: 3 per job (parent, child a, child b)
   std::vector<MGraphHost> g(3 * nj);
   std::vector<MGraphHost *> gp;
   for (auto &h : g) gp.push_back(&h);
   std::vector<SeqJob> seq;
-  for (size_t k = 0; k < nj && e == cudaSuccess; ++k) {
-    const dmsc_msc &P = *jobs[k].parent;
+  for (int k = 0; k < nj; ++k) {
     const int *x = jobs[k].ixn;
-    e = mgraph_alloc(g[3 * k], P, (uint32_t)P.ncp, P.nasc + P.ndes + grow * boundary_room(x), st, 0);
-    seq.push_back(SeqJob{SEQ_DOWN_BOUNDARY, (int)(3 * k), -1, CRect{x[0], x[1], x[2], x[3]}, nullptr, nullptr});
+    seq.push_back(SeqJob{SEQ_DOWN_BOUNDARY, 3 * k, -1, CRect{x[0], x[1], x[2], x[3]}, nullptr, nullptr});
   }
-  // the uncancellations along each shared boundary (:172-201)
-  if (e == cudaSuccess) e = run_seq(gp, seq, status, st, seq_ms);
-  // checks, the boundary-cancelable lists and the bounds of the children's growth
+  // scratch: per job the boundary-cancelable flags, positions and list; counters
   Scratch s;
-  for (size_t k = 0; k < nj; ++k) {
+  for (int k = 0; k < nj; ++k) {
     const long long n = jobs[k].parent->ncp;
-    for (int q = 0; q < 3; ++q) s.sz.push_back(4ull * (n + 1));  // flags, positions, the list
+    for (int q = 0; q < 3; ++q) s.sz.push_back(4ull * (n + 1));
   }
   s.sz.push_back(16ull * (nj + 1));  // per job: count, adds
   if (e == cudaSuccess) e = s.alloc(st);
   unsigned long long *ctr = e == cudaSuccess ? (unsigned long long *)s.ptr[3 * nj] : nullptr;
   if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, 16ull * (nj + 1), st);
-  for (size_t k = 0; k < nj && e == cudaSuccess; ++k) {
-    MGraph &P = mg(g[3 * k]);
-    uint32_t *bflag = (uint32_t *)s.ptr[3 * k], *pos = (uint32_t *)s.ptr[3 * k + 1], *jb = (uint32_t *)s.ptr[3 * k + 2];
-    uint32_t *njb = (uint32_t *)(ctr + 2 * k);
-    if (!P.G.ncp) continue;
-    k_down_check<<<nblk(P.G.ncp), 256, 0, st>>>(P, bflag, status);
-    DMSC_LAUNCHED(1);
-    e = scan_exclusive_u32(bflag, P.G.ncp, pos, njb, st);
-    if (e == cudaSuccess) {
-      k_down_list<<<nblk(P.G.ncp), 256, 0, st>>>(P, bflag, pos, jb, ctr + 2 * k + 1);
-      DMSC_LAUNCHED(1);
-    }
-  }
-  std::vector<unsigned long long> hc(2 * (nj + 1), 0);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(hc.data(), ctr, 16ull * nj, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess)
+    e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS, [&](int k, cudaStream_t q) {
+      const dmsc_msc &P = *jobs[k].parent;
+      return (int)mgraph_alloc(g[3 * k], P, (uint32_t)P.ncp, P.nasc + P.ndes + grow * boundary_room(jobs[k].ixn), q, 0);
+    }));
+  // the uncancellations along each shared boundary (:172-201)
+  if (e == cudaSuccess) e = run_seq(gp, seq, status, st, seq_ms);
+  // checks, the boundary-cancelable lists and the bounds of the children's growth
+  if (e == cudaSuccess)
+    e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS, [&](int k, cudaStream_t q) {
+      MGraph &P = mg(g[3 * k]);
+      uint32_t *bflag = (uint32_t *)s.ptr[3 * k], *pos = (uint32_t *)s.ptr[3 * k + 1], *jb = (uint32_t *)s.ptr[3 * k + 2];
+      uint32_t *njb = (uint32_t *)(ctr + 2 * k);
+      if (!P.G.ncp) return 0;
+      k_down_check<<<nblk(P.G.ncp), 256, 0, q>>>(P, bflag, status);
+      DMSC_LAUNCHED(1);
+      cudaError_t r = scan_exclusive_u32(bflag, P.G.ncp, pos, njb, q);
+      if (r == cudaSuccess) {
+        k_down_list<<<nblk(P.G.ncp), 256, 0, q>>>(P, bflag, pos, jb, ctr + 2 * k + 1);
+        DMSC_LAUNCHED(1);
+        r = cudaGetLastError();
+      }
+      return (int)r;
+    }));
+  std::vector<unsigned long long> hc(2 * (nj + 1), 0);
+  if (e == cudaSuccess) e = cudaMemcpy(hc.data(), ctr, 16ull * nj, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
   // the children's graphs, with room for what the parent's boundary points add
   seq.clear();
-  for (size_t k = 0; k < nj && e == cudaSuccess && !*stw; ++k) {
-    const unsigned long long adds = hc[2 * k + 1];
-    const uint32_t *jb = (const uint32_t *)s.ptr[3 * k + 2];
-    const uint32_t *njb = (const uint32_t *)(ctr + 2 * k);
-    for (int c = 0; c < 2 && e == cudaSuccess; ++c) {
+  for (int k = 0; k < nj; ++k)
+    if (hc[2 * k])
+      for (int c = 0; c < 2; ++c)
+        seq.push_back(SeqJob{SEQ_DOWN_LOOP1, 3 * k, 3 * k + 1 + c, CRect{0, 0, 0, 0}, (const uint32_t *)s.ptr[3 * k + 2],
+                             (const uint32_t *)(ctr + 2 * k)});
+  if (e == cudaSuccess && !*stw)
+    e = as_cuda(for_each_on_streams(dev, 2 * nj, MERGE_WORKERS, [&](int kc, cudaStream_t q) {
+      const int k = kc / 2, c = kc % 2;
+      const unsigned long long adds = hc[2 * k + 1];
       const dmsc_msc &C = *(c ? jobs[k].b : jobs[k].a);
       const unsigned long long cap = (unsigned long long)C.ncp + adds + 16;
-      if (cap > 0xffffffffull) { e = cudaErrorInvalidValue; break; }
-      e = mgraph_alloc(g[3 * k + 1 + c], C, (uint32_t)cap, C.nasc + C.ndes + grow * (4 * adds + (1ull << 20)), st, 0);
-      if (e == cudaSuccess && hc[2 * k])
-        seq.push_back(SeqJob{SEQ_DOWN_LOOP1, (int)(3 * k), (int)(3 * k + 1 + c), CRect{0, 0, 0, 0}, jb, njb});
-    }
-  }
+      if (cap > 0xffffffffull) return (int)cudaErrorInvalidValue;
+      return (int)mgraph_alloc(g[3 * k + 1 + c], C, (uint32_t)cap, C.nasc + C.ndes + grow * (4 * adds + (1ull << 20)),
+                               q, 0);
+    }));
   // the parent's boundary-cancelable points into each child (:207-281)
   if (e == cudaSuccess && !*stw) e = run_seq(gp, seq, status, st, seq_ms);
   if (e == cudaSuccess && !*stw) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
   // every other point the child holds (:283-320), straight into the child's
   // CSR arrays; then the parent's own write-back
-  for (size_t k = 0; k < nj && e == cudaSuccess && !*stw; ++k) {
-    e = down_child_out(g[3 * k], g[3 * k + 1], *jobs[k].a, st);
-    if (e == cudaSuccess) e = down_child_out(g[3 * k], g[3 * k + 2], *jobs[k].b, st);
-    if (e == cudaSuccess) e = mgraph_to_csr(g[3 * k], *jobs[k].parent, st);
-  }
+  if (e == cudaSuccess && !*stw)
+    e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS, [&](int k, cudaStream_t q) {
+      cudaError_t r = down_child_out(g[3 * k], g[3 * k + 1], *jobs[k].a, q);
+      if (r == cudaSuccess) r = down_child_out(g[3 * k], g[3 * k + 2], *jobs[k].b, q);
+      if (r == cudaSuccess) r = mgraph_to_csr(g[3 * k], *jobs[k].parent, q);
+      return (int)r;
+    }));
   s.free(st);
   for (auto &h : g) mgraph_free(h, st);
   cudaStreamSynchronize(st);

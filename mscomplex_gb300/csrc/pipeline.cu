@@ -8,14 +8,18 @@
 // alternates y and x splits per level to produce square blocks (merge_up and
 // merge_down accept any shared 1-manifold, grid_mscomplex.cpp:35-39).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "dmsc.h"
 #include "dmsc_internal.h"
 #include "grid_types.h"
+#include "host_pool.h"
 
 using namespace dmsc;
 
@@ -53,6 +57,8 @@ void pmax(int ax, int ay, int bx, int by, int &ox, int &oy) {
 double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
+
+constexpr int PIECE_WORKERS = 8;
 }  // namespace
 
 struct dmsc_pipeline {
@@ -246,19 +252,24 @@ int dmsc_pipeline_run(dmsc_ctx *ctx, const float *heights, int64_t pitch, int on
   const int N = (int)P->pieces.size();
   P->msc.assign(2 * N - 1, nullptr);
   double t0 = now_ms();
-  // computeSubdomainMsgraphs (:493-528): every leaf independently
-  for (int i = 0; i < N; ++i) {
-    const R4 &r = P->pieces[i].first, &e = P->pieces[i].second;
-    int16_t rr[4] = {(int16_t)r.l, (int16_t)r.b, (int16_t)r.r, (int16_t)r.t};
-    int16_t ee[4] = {(int16_t)e.l, (int16_t)e.b, (int16_t)e.r, (int16_t)e.t};
-    dmsc_dataset *d = nullptr;
-    int rc = dmsc_dataset_create(ctx, rr, ee, &d);
-    if (rc) return fail(rc);
-    P->ds.push_back(d);
-    rc = dmsc_dataset_init(d, dev + (long long)(e.b / 2) * pitch + e.l / 2, pitch, 1, st);
-    if (!rc) rc = dmsc_dataset_work(d, st);
-    if (!rc) rc = dmsc_dataset_writeout_connectivity(d, &P->msc[i], st);
-    if (rc) return fail(rc);
+  // computeSubdomainMsgraphs (:493-528): every leaf independently, several at a time
+  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(perr(DMSC_ERR_CUDA, "field copy"));
+  P->ds.assign(N, nullptr);
+  {
+    std::string msg;
+    std::mutex mu;
+    const int rc = for_each_on_streams(ctx->device, N, PIECE_WORKERS, [&](int i, cudaStream_t s) {
+      const R4 &r = P->pieces[i].first, &e = P->pieces[i].second;
+      int16_t rr[4] = {(int16_t)r.l, (int16_t)r.b, (int16_t)r.r, (int16_t)r.t};
+      int16_t ee[4] = {(int16_t)e.l, (int16_t)e.b, (int16_t)e.r, (int16_t)e.t};
+      int q = dmsc_dataset_create(ctx, rr, ee, &P->ds[i]);
+      if (!q) q = dmsc_dataset_init(P->ds[i], dev + (long long)(e.b / 2) * pitch + e.l / 2, pitch, 1, s);
+      if (!q) q = dmsc_dataset_work(P->ds[i], s);
+      if (!q) q = dmsc_dataset_writeout_connectivity(P->ds[i], &P->msc[i], s);
+      if (q) { std::lock_guard<std::mutex> lk(mu); msg = dmsc_last_error(); }
+      return q;
+    });
+    if (rc) return fail(perr(rc < 0 ? DMSC_ERR_CUDA : rc, rc < 0 ? "worker stream" : msg));
   }
   double t1 = now_ms();
   // mergePiecesUp (:258-306), one level at a time
@@ -306,10 +317,17 @@ int dmsc_pipeline_run(dmsc_ctx *ctx, const float *heights, int64_t pitch, int on
     }
   }
   double t4 = now_ms();
-  // collectSubdomainManifolds (:454-490): discs of every leaf
-  for (int i = 0; i < N; ++i) {
-    int rc = dmsc_dataset_fill_discs(P->ds[i], P->msc[i], st);
-    if (rc) return fail(rc);
+  // collectSubdomainManifolds (:454-490): discs of every leaf, several at a time
+  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(perr(DMSC_ERR_CUDA, "merge down"));
+  {
+    std::string msg;
+    std::mutex mu;
+    const int rc = for_each_on_streams(ctx->device, N, PIECE_WORKERS, [&](int i, cudaStream_t s) {
+      const int q = dmsc_dataset_fill_discs(P->ds[i], P->msc[i], s);
+      if (q) { std::lock_guard<std::mutex> lk(mu); msg = dmsc_last_error(); }
+      return q;
+    });
+    if (rc) return fail(perr(rc < 0 ? DMSC_ERR_CUDA : rc, rc < 0 ? "worker stream" : msg));
   }
   double t5 = now_ms();
   P->ms[0] = t1 - t0; P->ms[1] = t2 - t1; P->ms[2] = t3 - t2; P->ms[3] = t4 - t3; P->ms[4] = t5 - t4;
