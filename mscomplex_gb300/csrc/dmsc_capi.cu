@@ -255,6 +255,7 @@ int dmsc_dataset_writeout_connectivity(dmsc_dataset *d, dmsc_msc **out, void *st
   m->ctx = d->ctx;
   std::memcpy(m->rect, d->rect, 8);
   std::memcpy(m->ext, d->ext, 8);
+  for (int i = 0; i < 4; ++i) m->bbox[i] = d->ext[i];
   m->nadisc = m->nddisc = 0;
   for (auto &v : m->simp_stats) v = 0;
   if (d->ctx->timing && d->ev_ready) CK(cudaEventRecord(d->ev[5], st));

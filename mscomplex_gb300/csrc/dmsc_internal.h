@@ -147,6 +147,8 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st);
 // MGraph (a complex as a mutable graph with its cell-id hash).
 struct MGraphHost {
   uint32_t *buf = nullptr;
+  uint32_t *tab = nullptr;     // its cell table (owned)
+  uint32_t *status = nullptr;  // device status word for the fill (ST_INVARIANT: a cell outside the box)
   alignas(16) unsigned char raw[320];
 };
 
@@ -155,7 +157,9 @@ struct MGraphHost {
 struct dmsc_msc;
 namespace dmsc {
 cudaError_t mgraph_alloc(MGraphHost &h, const dmsc_msc &src, uint32_t cap, unsigned long long pool, cudaStream_t st,
-                         uint32_t slack = 4);
+                         uint32_t slack = 4, uint32_t *tab = nullptr, const int *box = nullptr);
+// Sets m.bbox to the box of its critical cells (synchronises st).
+cudaError_t cell_box(dmsc_msc &m, cudaStream_t st);
 void mgraph_free(MGraphHost &h, cudaStream_t st);
 void mgraph_set_rects(MGraphHost &h, const int rect[4], const int ext[4]);
 uint32_t mgraph_ncp(const MGraphHost &h);

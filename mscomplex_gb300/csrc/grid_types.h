@@ -100,6 +100,7 @@ struct dmsc_ctx {
 struct dmsc_msc {
   dmsc_ctx *ctx = nullptr;
   int16_t rect[4], ext[4];
+  int bbox[4] = {0, 0, -1, -1};  // a box (l, b, r, t) of cell coordinates holding every critical cell
   long long ncp = 0, nasc = 0, ndes = 0, nadisc = 0, nddisc = 0;
   DevBuf<uint32_t> cellid, pair_idx, aoff, asc, doff, des, adoff, ddoff;
   DevBuf<uint32_t> adisc, ddisc;  // packed cell ids

@@ -48,7 +48,7 @@ __global__ void k_merge_down(MGraph *graphs, const int3 *jobs, const CRect *ixns
 // ---------------------------------------------------------------------------
 __global__ void k_mg_from_csr(MGraph m, uint32_t n, const uint32_t *cellid, const float *fn, const uint8_t *flags,
                               const uint32_t *pair_idx, const uint32_t *aoff, const uint32_t *asc, const uint32_t *doff,
-                              const uint32_t *des, uint32_t slack) {
+                              const uint32_t *des, uint32_t slack, bool fill_tab, uint32_t *status) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     m.G.cellid[i] = cellid[i];
     m.fn[i] = fn[i];
@@ -68,12 +68,11 @@ __global__ void k_mg_from_csr(MGraph m, uint32_t n, const uint32_t *cellid, cons
       m.G.L.off[2 * i + w] = (uint32_t)base; m.G.L.nrun[2 * i + w] = r; m.G.L.cap[2 * i + w] = (e - b) + slack;
       m.G.L.total[2 * i + w] = e - b;
     }
-    // hash insert (keys are unique within a complex)
-    uint32_t cid = cellid[i], h = MGraph::hash(cid) & m.hmask;
-    for (uint32_t probe = 0; probe <= m.hmask; ++probe) {
-      uint32_t prev = atomicCAS(m.hkey + h, HASH_EMPTY, cid);
-      if (prev == HASH_EMPTY || prev == cid) { m.hval[h] = i; break; }
-      h = (h + 1) & m.hmask;
+    // the cell -> index table (cell ids are unique within a complex)
+    if (fill_tab) {
+      const long long sl = m.slot(cellid[i]);
+      if (sl >= 0) m.tab[sl] = i;
+      else if (status) atomicOr(status, ST_INVARIANT);  // a critical cell outside the complex's box
     }
   }
 }
@@ -99,21 +98,33 @@ static unsigned nblk(long long n) {
 
 // Allocates an MGraph with room for `cap` critical points and a list pool of
 // `pool` runs, and fills it from a CSR complex (n critical points, may be 0);
-// each list starts with room for `slack` more runs than it holds.
+// each list starts with room for `slack` more runs than it holds.  The cell
+// table covers src.bbox; `tab` (may be null) is a table over that box that
+// already maps src's cells, which the graph then takes over; `box` (may be
+// null) replaces src.bbox as the table's box.
 cudaError_t mgraph_alloc(MGraphHost &h, const dmsc_msc &src, uint32_t cap, unsigned long long pool, cudaStream_t st,
-                         uint32_t slack) {
+                         uint32_t slack, uint32_t *tab, const int *box) {
   uint32_t n = (uint32_t)src.ncp;
   if (cap < n) cap = n;
   if (cap >= (1u << 30)) return cudaErrorInvalidValue;
-  uint32_t hcap = 1;
-  while (hcap < 2 * cap + 16) hcap <<= 1;
+  if (!box) box = src.bbox;
+  const int tx0 = box[0], ty0 = box[1], tw = box[2] - box[0] + 1, th = box[3] - box[1] + 1;
+  if (tw <= 0 || th <= 0) return cudaErrorInvalidValue;
   unsigned long long base = (unsigned long long)src.nasc + src.ndes + 2ull * slack * n;
   if (pool < base + 1024) pool = base + 1024;
   if (pool > 0xffffffffull) return cudaErrorInvalidValue;
   unsigned long long tmpc = 1ull << 20;
-  size_t words = 4ull * cap + 8ull * cap + 2ull * hcap + 2 * pool + 2 * tmpc + 64;
+  size_t words = 4ull * cap + 8ull * cap + 2 * pool + 2 * tmpc + 64;
   cudaError_t e = cudaMallocAsync((void **)&h.buf, sizeof(uint32_t) * words, st);
   if (e != cudaSuccess) return e;
+  const size_t tcells = (size_t)tw * th;
+  const bool fill_tab = tab == nullptr;
+  if (fill_tab) {
+    e = cudaMallocAsync((void **)&tab, sizeof(uint32_t) * tcells, st);
+    if (e != cudaSuccess) { cudaFreeAsync(h.buf, st); h.buf = nullptr; return e; }
+    e = cudaMemsetAsync(tab, 0xFF, sizeof(uint32_t) * tcells, st);
+  }
+  h.tab = tab;
   uint32_t *p = h.buf;
   MGraph &m = *reinterpret_cast<MGraph *>(h.raw);
   static_assert(sizeof(MGraph) <= sizeof(h.raw), "MGraphHost storage");
@@ -126,8 +137,6 @@ cudaError_t mgraph_alloc(MGraphHost &h, const dmsc_msc &src, uint32_t cap, unsig
   m.G.L.nrun = p; p += 2ull * cap;
   m.G.L.cap = p; p += 2ull * cap;
   m.G.L.total = p; p += 2ull * cap;
-  m.hkey = p; p += hcap;
-  m.hval = p; p += hcap;
   m.G.L.pool = (uint2 *)p; p += 2 * pool;
   m.G.tmp = (uint2 *)p; p += 2 * tmpc;
   m.G.tmp_cap = tmpc;
@@ -138,22 +147,63 @@ cudaError_t mgraph_alloc(MGraphHost &h, const dmsc_msc &src, uint32_t cap, unsig
   m.G.ops = 0;
   m.G.fail = false;
   m.cap = cap;
-  m.hmask = hcap - 1;
+  m.tab = tab;
+  m.tx0 = tx0; m.ty0 = ty0; m.tw = tw; m.th = th;
   m.rect = CRect{src.rect[0], src.rect[1], src.rect[2], src.rect[3]};
   m.ext = CRect{src.ext[0], src.ext[1], src.ext[2], src.ext[3]};
-  e = cudaMemsetAsync(m.hkey, 0xFF, sizeof(uint32_t) * hcap, st);
   if (e == cudaSuccess && n) {
     k_mg_from_csr<<<nblk(n), 256, 0, st>>>(m, n, src.cellid.p, src.fn.p, src.flags.p, src.pair_idx.p, src.aoff.p,
-                                          src.asc.p, src.doff.p, src.des.p, slack);
+                                          src.asc.p, src.doff.p, src.des.p, slack, fill_tab, h.status);
     DMSC_LAUNCHED(1);
     e = cudaGetLastError();
   }
   return e;
 }
 
+__global__ void k_cell_box(long long n, const uint32_t *cellid, int *box) {
+  int b[4] = {1 << 30, 1 << 30, -1, -1};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(cellid[i] & 0xffffu), y = (int)(cellid[i] >> 16);
+    b[0] = min(b[0], x); b[1] = min(b[1], y); b[2] = max(b[2], x); b[3] = max(b[3], y);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    b[0] = min(b[0], __shfl_xor_sync(0xffffffffu, b[0], o)); b[1] = min(b[1], __shfl_xor_sync(0xffffffffu, b[1], o));
+    b[2] = max(b[2], __shfl_xor_sync(0xffffffffu, b[2], o)); b[3] = max(b[3], __shfl_xor_sync(0xffffffffu, b[3], o));
+  }
+  if ((threadIdx.x & 31) == 0 && b[2] >= 0) {
+    atomicMin(box, b[0]); atomicMin(box + 1, b[1]); atomicMax(box + 2, b[2]); atomicMax(box + 3, b[3]);
+  }
+}
+
+// The box of a complex's critical cells (its ext rect when it has none).
+cudaError_t cell_box(dmsc_msc &m, cudaStream_t st) {
+  if (m.ncp <= 0) {
+    for (int i = 0; i < 4; ++i) m.bbox[i] = m.ext[i];
+    return cudaSuccess;
+  }
+  int *d = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&d, 16, st);
+  if (e != cudaSuccess) return e;
+  const int init[4] = {1 << 30, 1 << 30, -1, -1};
+  int hb[4];
+  e = cudaMemcpyAsync(d, init, 16, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    k_cell_box<<<nblk(m.ncp), 256, 0, st>>>(m.ncp, m.cellid.p, d);
+    DMSC_LAUNCHED(1);
+    e = cudaMemcpyAsync(hb, d, 16, cudaMemcpyDeviceToHost, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFreeAsync(d, st);
+  if (e == cudaSuccess)
+    for (int i = 0; i < 4; ++i) m.bbox[i] = hb[i];
+  return e;
+}
+
 void mgraph_free(MGraphHost &h, cudaStream_t st) {
   if (h.buf) cudaFreeAsync(h.buf, st);
+  if (h.tab) cudaFreeAsync(h.tab, st);
   h.buf = nullptr;
+  h.tab = nullptr;
 }
 
 // Runs one tree level of merges; graphs[] is a device array of MGraph.

@@ -13,7 +13,6 @@
 
 namespace dmsc {
 
-constexpr uint32_t HASH_EMPTY = 0xFFFFFFFFu;
 constexpr uint32_t NO_CP = 0xFFFFFFFFu;
 
 struct CRect {  // rect_t (dmsc/include/rectangle_complex.h:108-308), global cell coordinates
@@ -27,32 +26,26 @@ struct MGraph {
   Graph G;           // G.ncp is the current number of critical points
   float *fn;
   uint32_t cap;      // capacity of the per-cp arrays
-  uint32_t *hkey, *hval;
-  uint32_t hmask;    // hash capacity - 1 (power of two)
+  // m_id_cp_map: critical-point index of every cell of the box
+  // [tx0, tx0 + tw) x [ty0, ty0 + th) (cell coordinates), NO_CP where none
+  uint32_t *tab;
+  int tx0, ty0, tw, th;
   CRect rect, ext;
 
-  __host__ __device__ static uint32_t hash(uint32_t k) {
-    k ^= k >> 16; k *= 0x7feb352du; k ^= k >> 15; k *= 0x846ca68bu; k ^= k >> 16;
-    return k;
+  __host__ __device__ long long slot(uint32_t cid) const {
+    const int x = (int)(cid & 0xffffu) - tx0, y = (int)(cid >> 16) - ty0;
+    if (x < 0 || y < 0 || x >= tw || y >= th) return -1;
+    return (long long)y * tw + x;
   }
   __host__ __device__ uint32_t find(uint32_t cid) const {
-    uint32_t h = hash(cid) & hmask;
-    for (uint32_t probe = 0; probe <= hmask; ++probe) {
-      uint32_t k = hkey[h];
-      if (k == cid) return hval[h];
-      if (k == HASH_EMPTY) return NO_CP;
-      h = (h + 1) & hmask;
-    }
-    return NO_CP;
+    const long long s = slot(cid);
+    return s < 0 ? NO_CP : tab[s];
   }
   __host__ __device__ bool put(uint32_t cid, uint32_t idx) {
-    uint32_t h = hash(cid) & hmask;
-    for (uint32_t probe = 0; probe <= hmask; ++probe) {
-      if (hkey[h] == HASH_EMPTY || hkey[h] == cid) { hkey[h] = cid; hval[h] = idx; return true; }
-      h = (h + 1) & hmask;
-    }
-    G.fail = true;
-    return false;
+    const long long s = slot(cid);
+    if (s < 0) { G.fail = true; return false; }  // outside the box the complex was given
+    tab[s] = idx;
+    return true;
   }
   // std::map::operator[]: inserts index 0 for a missing key
   __host__ __device__ uint32_t at(uint32_t cid) {

@@ -59,37 +59,28 @@ unsigned nblk(long long n) {
 
 #define GRID_LOOP(i, n) for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (long long)(n); i += (long long)gridDim.x * blockDim.x)
 
-// Open-addressing map from cell id to critical-point index (the hash
-// function of MGraph).  Inserts and lookups run in separate launches.
-struct CidHash {
-  uint32_t *key, *val;
-  uint32_t mask;
+// Cell id -> critical-point index over a box of cell coordinates (the same
+// table a merged graph keeps).  Entries are written and read in separate
+// launches; each cell is written once.
+struct CellTab {
+  uint32_t *tab;
+  int x0, y0, w, h;
+  __device__ long long slot(uint32_t cid) const {
+    const int x = (int)(cid & 0xffffu) - x0, y = (int)(cid >> 16) - y0;
+    if (x < 0 || y < 0 || x >= w || y >= h) return -1;
+    return (long long)y * w + x;
+  }
   __device__ uint32_t find(uint32_t cid) const {
-    uint32_t h = MGraph::hash(cid) & mask;
-    for (uint32_t probe = 0; probe <= mask; ++probe) {
-      const uint32_t k = key[h];
-      if (k == cid) return val[h];
-      if (k == HASH_EMPTY) return NO_CP;
-      h = (h + 1) & mask;
-    }
-    return NO_CP;
+    const long long s = slot(cid);
+    return s < 0 ? NO_CP : tab[s];
   }
   __device__ bool insert(uint32_t cid, uint32_t v) {
-    uint32_t h = MGraph::hash(cid) & mask;
-    for (uint32_t probe = 0; probe <= mask; ++probe) {
-      const uint32_t prev = atomicCAS(key + h, HASH_EMPTY, cid);
-      if (prev == HASH_EMPTY || prev == cid) { val[h] = v; return true; }
-      h = (h + 1) & mask;
-    }
-    return false;
+    const long long s = slot(cid);
+    if (s < 0) return false;
+    tab[s] = v;
+    return true;
   }
 };
-
-uint32_t hash_capacity(long long n) {
-  uint32_t c = 1024;
-  while ((long long)c < 2 * n + 16) c <<= 1;
-  return c;
-}
 
 __device__ __forceinline__ bool cancelled(const uint8_t *fl, uint32_t i) { return fl[i] & F_CANCELLED; }
 
@@ -224,7 +215,7 @@ __device__ __forceinline__ void put_cp(const CsrIn &a, long long j, uint32_t d, 
 }
 
 // A's uncancelled points: index = scan of the keep flags
-__global__ void k_up_a(CsrIn a, const uint32_t *idx, CidHash H, CsrOut o, uint32_t *status) {
+__global__ void k_up_a(CsrIn a, const uint32_t *idx, CellTab H, CsrOut o, uint32_t *status) {
   GRID_LOOP(j, a.n) {
     if (cancelled(a.flags, (uint32_t)j)) continue;
     if (!H.insert(a.cellid[j], idx[j])) { atomicOr(status, ST_SIMPLIFY_LIMIT); continue; }
@@ -233,7 +224,7 @@ __global__ void k_up_a(CsrIn a, const uint32_t *idx, CidHash H, CsrOut o, uint32
 }
 
 // B's uncancelled points: the index of A's copy, or new (counted by isnew)
-__global__ void k_up_b_classify(CsrIn b, CidHash H, uint32_t *idx, uint32_t *isnew) {
+__global__ void k_up_b_classify(CsrIn b, CellTab H, uint32_t *idx, uint32_t *isnew) {
   GRID_LOOP(j, b.n) {
     uint32_t d = NO_CP, nw = 0;
     if (!cancelled(b.flags, (uint32_t)j)) {
@@ -245,7 +236,7 @@ __global__ void k_up_b_classify(CsrIn b, CidHash H, uint32_t *idx, uint32_t *isn
   }
 }
 
-__global__ void k_up_b_new(CsrIn b, const uint32_t *isnew, const uint32_t *pos, const uint32_t *na, CidHash H, uint32_t *idx,
+__global__ void k_up_b_new(CsrIn b, const uint32_t *isnew, const uint32_t *pos, const uint32_t *na, CellTab H, uint32_t *idx,
                            CsrOut o, uint32_t *status) {
   const uint32_t base = *na;
   GRID_LOOP(j, b.n) {
@@ -258,7 +249,7 @@ __global__ void k_up_b_new(CsrIn b, const uint32_t *isnew, const uint32_t *pos, 
 }
 
 // boundary pairs (:84-92) of one input; idx = the result index of each point
-__global__ void k_up_pairs(CsrIn a, const uint32_t *idx, CidHash H, uint32_t *opair, uint32_t *status) {
+__global__ void k_up_pairs(CsrIn a, const uint32_t *idx, CellTab H, uint32_t *opair, uint32_t *status) {
   GRID_LOOP(j, a.n) {
     const uint8_t fl = a.flags[j];
     if ((fl & F_CANCELLED) || !(fl & F_BCANCEL)) continue;
@@ -334,17 +325,34 @@ __global__ void k_down_check(MGraph P, uint32_t *bflag, uint32_t *status) {
   }
 }
 
-// the boundary-cancelable points in index order, and a bound on the points
-// they can add to a child (themselves, their partners, their list entries)
+// the boundary-cancelable points in index order, a bound on the points they
+// can add to a child (themselves, their partners, their list entries) and
+// the box of those points' cells (box: l, b, r, t)
+__device__ __forceinline__ void box_add(int b[4], uint32_t cid) {
+  const int x = (int)(cid & 0xffffu), y = (int)(cid >> 16);
+  b[0] = min(b[0], x); b[1] = min(b[1], y); b[2] = max(b[2], x); b[3] = max(b[3], y);
+}
 __global__ void k_down_list(MGraph P, const uint32_t *bflag, const uint32_t *pos, uint32_t *jb,
-                            unsigned long long *adds) {
+                            unsigned long long *adds, int *box) {
   unsigned long long mine = 0;
+  int b[4] = {1 << 30, 1 << 30, -1, -1};
   GRID_LOOP(j, P.G.ncp) {
     if (!bflag[j]) continue;
     jb[pos[j]] = (uint32_t)j;
     mine += 2ull + P.G.L.nrun[2 * j] + P.G.L.nrun[2 * j + 1];
+    box_add(b, P.G.cellid[j]);
+    const uint32_t sp = P.G.pair_idx[j];
+    if (sp < P.G.ncp) box_add(b, P.G.cellid[sp]);
+    for (int w = 0; w < 2; ++w) {
+      const uint2 *r = P.G.runs(2 * j + w);
+      for (uint32_t q = 0; q < P.G.L.nrun[2 * j + w]; ++q)
+        if (r[q].x < P.G.ncp) box_add(b, P.G.cellid[r[q].x]);
+    }
   }
   if (mine) atomicAdd(adds, mine);
+  if (b[2] >= 0) {
+    atomicMin(box, b[0]); atomicMin(box + 1, b[1]); atomicMax(box + 2, b[2]); atomicMax(box + 3, b[3]);
+  }
 }
 
 // the parent point (not boundary-cancelable) whose lists replace each child point's
@@ -568,13 +576,19 @@ CsrOut csr_out(dmsc_msc &m) {
   return CsrOut{m.cellid.p, m.pair_idx.p, m.aoff.p, m.asc.p, m.doff.p, m.des.p, m.fn.p, m.flags.p};
 }
 
-// merge_up of one pair into o's CSR arrays (before the boundary cancellations)
-cudaError_t union_one(const dmsc_msc &A, const dmsc_msc &B, dmsc_msc &O, CRect ixn, uint32_t *status, cudaStream_t st) {
+// merge_up of one pair into o's CSR arrays (before the boundary cancellations);
+// *tab receives the cell table of the result over O.bbox (the caller owns it).
+cudaError_t union_one(const dmsc_msc &A, const dmsc_msc &B, dmsc_msc &O, CRect ixn, uint32_t *status, uint32_t **tab,
+                      cudaStream_t st) {
   const long long nA = A.ncp, nB = B.ncp, bound = nA + nB;
   if (bound >= (1ll << 30) || A.nasc + B.nasc >= (1ll << 32) - 1 || A.ndes + B.ndes >= (1ll << 32) - 1)
     return cudaErrorInvalidValue;  // 32-bit indices and offsets
-  const uint32_t hcap = hash_capacity(bound);
-  cudaError_t e = cudaSuccess;
+  const int tw = O.bbox[2] - O.bbox[0] + 1, th = O.bbox[3] - O.bbox[1] + 1;
+  if (tw <= 0 || th <= 0) return cudaErrorInvalidValue;
+  const size_t tcells = (size_t)tw * th;
+  cudaError_t e = cudaMallocAsync((void **)tab, sizeof(uint32_t) * tcells, st);
+  if (e != cudaSuccess) { *tab = nullptr; return e; }
+  e = cudaMemsetAsync(*tab, 0xFF, sizeof(uint32_t) * tcells, st);
   if (e == cudaSuccess) e = O.cellid.ensure(bound + 1, st);
   if (e == cudaSuccess) e = O.fn.ensure(bound + 1, st);
   if (e == cudaSuccess) e = O.pair_idx.ensure(bound + 1, st);
@@ -585,19 +599,19 @@ cudaError_t union_one(const dmsc_msc &A, const dmsc_msc &B, dmsc_msc &O, CRect i
   if (e == cudaSuccess) e = O.des.ensure(A.ndes + B.ndes + 1, st);
   if (e != cudaSuccess) return e;
   Scratch s;
-  // keepA, idxA, idxB, isnew, posB, hash keys, hash values, tot_a, tot_d, mix, counters
-  s.sz = {4ull * (nA + 1), 4ull * (nA + 1), 4ull * (nB + 1), 4ull * (nB + 1), 4ull * (nB + 1), 4ull * hcap,
-          4ull * hcap, 4ull * (bound + 1), 4ull * (bound + 1), (size_t)bound + 1, 64};
-  if ((e = s.alloc(st)) != cudaSuccess) return e;
+  // keepA, idxA, idxB, isnew, posB, tot_a, tot_d, mix, counters
+  s.sz = {4ull * (nA + 1), 4ull * (nA + 1), 4ull * (nB + 1), 4ull * (nB + 1), 4ull * (nB + 1),
+          4ull * (bound + 1), 4ull * (bound + 1), (size_t)bound + 1, 64};
+  if (e == cudaSuccess) e = s.alloc(st);
+  if (e != cudaSuccess) return e;
   uint32_t *keep = (uint32_t *)s.ptr[0], *idxA = (uint32_t *)s.ptr[1], *idxB = (uint32_t *)s.ptr[2];
   uint32_t *isnew = (uint32_t *)s.ptr[3], *posB = (uint32_t *)s.ptr[4];
-  CidHash H{(uint32_t *)s.ptr[5], (uint32_t *)s.ptr[6], hcap - 1};
-  uint32_t *tot_a = (uint32_t *)s.ptr[7], *tot_d = (uint32_t *)s.ptr[8];
-  uint8_t *mix = (uint8_t *)s.ptr[9];
-  uint32_t *cnt = (uint32_t *)s.ptr[10];  // [0] kept of A, [1] new of B
+  CellTab H{*tab, O.bbox[0], O.bbox[1], tw, th};
+  uint32_t *tot_a = (uint32_t *)s.ptr[5], *tot_d = (uint32_t *)s.ptr[6];
+  uint8_t *mix = (uint8_t *)s.ptr[7];
+  uint32_t *cnt = (uint32_t *)s.ptr[8];  // [0] kept of A, [1] new of B
   const CsrIn a = csr_in(A), b = csr_in(B);
   CsrOut o = csr_out(O);
-  e = cudaMemsetAsync(H.key, 0xFF, 4ull * hcap, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(tot_a, 0, 4ull * (bound + 1), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(tot_d, 0, 4ull * (bound + 1), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(mix, 0, bound + 1, st);
@@ -727,16 +741,22 @@ cudaError_t merge_up_level_par(const std::vector<MergeJob> &jobs, unsigned long 
   const int nj = (int)jobs.size(), dev = current_device();
   cudaError_t e = cudaMemsetAsync(status, 0, 4, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  // union and connectivity
+  // union and connectivity; each result's cell table passes to its graph
+  std::vector<MGraphHost> g(nj);
+  std::vector<uint32_t *> tabs(nj, nullptr);
   if (e == cudaSuccess)
     e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS, [&](int k, cudaStream_t s) {
       const MergeJob &J = jobs[k];
-      return (int)union_one(*J.a, *J.b, *J.parent, CRect{J.ixn[0], J.ixn[1], J.ixn[2], J.ixn[3]}, status, s);
+      return (int)union_one(*J.a, *J.b, *J.parent, CRect{J.ixn[0], J.ixn[1], J.ixn[2], J.ixn[3]}, status, &tabs[k], s);
     }));
   if (e == cudaSuccess) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess || *stw) return e;
+  if (e != cudaSuccess || *stw) {
+    for (uint32_t *t : tabs)
+      if (t) cudaFreeAsync(t, st);
+    cudaStreamSynchronize(st);
+    return e;
+  }
   // the boundary cancellations, one thread per merge, on mutable graphs
-  std::vector<MGraphHost> g(nj);
   std::vector<MGraphHost *> gp;
   std::vector<SeqJob> seq;
   for (int k = 0; k < nj; ++k) {
@@ -746,8 +766,14 @@ cudaError_t merge_up_level_par(const std::vector<MergeJob> &jobs, unsigned long 
   }
   e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS, [&](int k, cudaStream_t s) {
     const dmsc_msc &O = *jobs[k].parent;
-    return (int)mgraph_alloc(g[k], O, (uint32_t)O.ncp, O.nasc + O.ndes + grow * boundary_room(jobs[k].ixn), s, 0);
+    g[k].status = status;
+    const cudaError_t r =
+        mgraph_alloc(g[k], O, (uint32_t)O.ncp, O.nasc + O.ndes + grow * boundary_room(jobs[k].ixn), s, 0, tabs[k]);
+    if (g[k].tab) tabs[k] = nullptr;  // the graph owns it now
+    return (int)r;
   }));
+  for (uint32_t *t : tabs)
+    if (t) cudaFreeAsync(t, st);
   if (e == cudaSuccess) e = run_seq(gp, seq, status, st, seq_ms);
   if (e == cudaSuccess) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && !*stw)
@@ -779,13 +805,22 @@ cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned lon
     for (int q = 0; q < 3; ++q) s.sz.push_back(4ull * (n + 1));
   }
   s.sz.push_back(16ull * (nj + 1));  // per job: count, adds
+  s.sz.push_back(16ull * (nj + 1));  // per job: the box of the cells its boundary points can add
   if (e == cudaSuccess) e = s.alloc(st);
   unsigned long long *ctr = e == cudaSuccess ? (unsigned long long *)s.ptr[3 * nj] : nullptr;
+  int *boxes = e == cudaSuccess ? (int *)s.ptr[3 * nj + 1] : nullptr;
+  std::vector<int> hbox(4 * (nj + 1));
+  for (int k = 0; k <= nj; ++k) {
+    hbox[4 * k] = hbox[4 * k + 1] = 1 << 30;
+    hbox[4 * k + 2] = hbox[4 * k + 3] = -1;
+  }
   if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, 16ull * (nj + 1), st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(boxes, hbox.data(), 16ull * (nj + 1), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e == cudaSuccess)
     e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS, [&](int k, cudaStream_t q) {
       const dmsc_msc &P = *jobs[k].parent;
+      g[3 * k].status = status;
       return (int)mgraph_alloc(g[3 * k], P, (uint32_t)P.ncp, P.nasc + P.ndes + grow * boundary_room(jobs[k].ixn), q, 0);
     }));
   // the uncancellations along each shared boundary (:172-201)
@@ -801,7 +836,7 @@ cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned lon
       DMSC_LAUNCHED(1);
       cudaError_t r = scan_exclusive_u32(bflag, P.G.ncp, pos, njb, q);
       if (r == cudaSuccess) {
-        k_down_list<<<nblk(P.G.ncp), 256, 0, q>>>(P, bflag, pos, jb, ctr + 2 * k + 1);
+        k_down_list<<<nblk(P.G.ncp), 256, 0, q>>>(P, bflag, pos, jb, ctr + 2 * k + 1, boxes + 4 * k);
         DMSC_LAUNCHED(1);
         r = cudaGetLastError();
       }
@@ -809,6 +844,20 @@ cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned lon
     }));
   std::vector<unsigned long long> hc(2 * (nj + 1), 0);
   if (e == cudaSuccess) e = cudaMemcpy(hc.data(), ctr, 16ull * nj, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(hbox.data(), boxes, 16ull * nj, cudaMemcpyDeviceToHost);
+  // each child's table covers its own cells and the cells its parent's boundary points can add
+  std::vector<int> cbox(8 * nj);
+  for (int k = 0; k < nj; ++k)
+    for (int c = 0; c < 2; ++c) {
+      const dmsc_msc &C = *(c ? jobs[k].b : jobs[k].a);
+      int *o = &cbox[8 * k + 4 * c];
+      const int *t = &hbox[4 * k];
+      for (int i = 0; i < 4; ++i) o[i] = C.bbox[i];
+      if (t[2] >= 0) {
+        o[0] = std::min(o[0], t[0]); o[1] = std::min(o[1], t[1]);
+        o[2] = std::max(o[2], t[2]); o[3] = std::max(o[3], t[3]);
+      }
+    }
   if (e == cudaSuccess) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
   // the children's graphs, with room for what the parent's boundary points add
   seq.clear();
@@ -824,8 +873,9 @@ cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned lon
       const dmsc_msc &C = *(c ? jobs[k].b : jobs[k].a);
       const unsigned long long cap = (unsigned long long)C.ncp + adds + 16;
       if (cap > 0xffffffffull) return (int)cudaErrorInvalidValue;
+      g[3 * k + 1 + c].status = status;
       return (int)mgraph_alloc(g[3 * k + 1 + c], C, (uint32_t)cap, C.nasc + C.ndes + grow * (4 * adds + (1ull << 20)),
-                               q, 0);
+                               q, 0, nullptr, &cbox[8 * k + 4 * c]);
     }));
   // the parent's boundary-cancelable points into each child (:207-281)
   if (e == cudaSuccess && !*stw) e = run_seq(gp, seq, status, st, seq_ms);
@@ -837,6 +887,11 @@ cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned lon
       cudaError_t r = down_child_out(g[3 * k], g[3 * k + 1], *jobs[k].a, q);
       if (r == cudaSuccess) r = down_child_out(g[3 * k], g[3 * k + 2], *jobs[k].b, q);
       if (r == cudaSuccess) r = mgraph_to_csr(g[3 * k], *jobs[k].parent, q);
+      if (r == cudaSuccess)
+        for (int c = 0; c < 2; ++c) {
+          dmsc_msc &C = *(c ? jobs[k].b : jobs[k].a);
+          for (int i = 0; i < 4; ++i) C.bbox[i] = cbox[8 * k + 4 * c + i];
+        }
       return (int)r;
     }));
   s.free(st);

@@ -115,6 +115,12 @@ static bool shared_edge(dmsc_pipeline *P, int node, int ixn[4]) {
 
 constexpr int LEVEL_FALLBACK = -1;
 
+static void box_join(int *o, const int *a) {
+  if (o[2] < o[0]) { for (int i = 0; i < 4; ++i) o[i] = a[i]; return; }
+  o[0] = std::min(o[0], a[0]); o[1] = std::min(o[1], a[1]);
+  o[2] = std::max(o[2], a[2]); o[3] = std::max(o[3], a[3]);
+}
+
 // One tree level through the parallel merges (merge_par.cu), with the same
 // retries as below; LEVEL_FALLBACK when a merge needs the one-thread path.
 static int run_level_par(dmsc_pipeline *P, bool up, const std::vector<int> &nodes, cudaStream_t st) {
@@ -154,6 +160,13 @@ static int run_level_par(dmsc_pipeline *P, bool up, const std::vector<int> &node
 // merge_parallel_min critical points take the parallel merges.
 static int run_level(dmsc_pipeline *P, bool up, const std::vector<int> &nodes, cudaStream_t st) {
   const int N = (int)P->pieces.size();
+  // the box of cell coordinates holding a merged complex's critical cells:
+  // its children's (a child's box after merge_down is measured afterwards)
+  for (int node : nodes) {
+    const int k = node - N;
+    dmsc_msc *ma = P->msc[2 * k], *mb = P->msc[2 * k + 1], *mp = P->msc[node];
+    if (up) { box_join(mp->bbox, ma->bbox); box_join(mp->bbox, mb->bbox); }
+  }
   long long biggest = 0;
   for (int node : nodes) {
     const int k = node - N;
@@ -169,6 +182,8 @@ static int run_level(dmsc_pipeline *P, bool up, const std::vector<int> &nodes, c
     std::vector<MGraphHost> g(3 * nodes.size());
     std::vector<int> jobs, ixn, gnode(3 * nodes.size(), -1);
     int rc = DMSC_OK;
+    if (cudaMemsetAsync(P->status.p, 0, 4, st) != cudaSuccess) return perr(DMSC_ERR_CUDA, "merge status");
+    for (auto &h : g) h.status = P->status.p;
     for (size_t j = 0; j < nodes.size() && rc == DMSC_OK; ++j) {
       const int node = nodes[j], k = node - N, a = 2 * k, b = 2 * k + 1;
       dmsc_msc *ma = P->msc[a], *mb = P->msc[b], *mp = P->msc[node];
@@ -187,12 +202,18 @@ static int run_level(dmsc_pipeline *P, bool up, const std::vector<int> &nodes, c
         if (e == cudaSuccess)
           e = mgraph_alloc(g[ip], *mp, (uint32_t)(ma->ncp + mb->ncp + 16), grow * 2 * (pa + pb) + 4096, st);
         jobs.insert(jobs.end(), {ia, ib, ip});
-      } else {  // parent uncancels its boundary, children take the parent's cps
+      } else {  // parent uncancels its boundary, children take the parent's cps (tables over both boxes)
+        int boxa[4], boxb[4];
+        for (int i = 0; i < 4; ++i) { boxa[i] = ma->bbox[i]; boxb[i] = mb->bbox[i]; }
+        box_join(boxa, mp->bbox);
+        box_join(boxb, mp->bbox);
         e = mgraph_alloc(g[ip], *mp, (uint32_t)mp->ncp, grow * 2 * pp + 4096, st);
         if (e == cudaSuccess)
-          e = mgraph_alloc(g[ia], *ma, (uint32_t)(ma->ncp + mp->ncp + 16), grow * 2 * (pa + pp) + 4096, st);
+          e = mgraph_alloc(g[ia], *ma, (uint32_t)(ma->ncp + mp->ncp + 16), grow * 2 * (pa + pp) + 4096, st, 4, nullptr,
+                           boxa);
         if (e == cudaSuccess)
-          e = mgraph_alloc(g[ib], *mb, (uint32_t)(mb->ncp + mp->ncp + 16), grow * 2 * (pb + pp) + 4096, st);
+          e = mgraph_alloc(g[ib], *mb, (uint32_t)(mb->ncp + mp->ncp + 16), grow * 2 * (pb + pp) + 4096, st, 4, nullptr,
+                           boxb);
         jobs.insert(jobs.end(), {ip, ia, ib});
       }
       ixn.insert(ixn.end(), {x0, y0, x1, y1});
@@ -200,9 +221,8 @@ static int run_level(dmsc_pipeline *P, bool up, const std::vector<int> &nodes, c
     }
     uint32_t stw = 0;
     if (rc == DMSC_OK) {
-      cudaError_t e = cudaMemsetAsync(P->status.p, 0, 4, st);
-      if (e == cudaSuccess)
-        e = merge_level(up, g.data(), (int)g.size(), jobs.data(), ixn.data(), (int)nodes.size(), P->status.p, st);
+      cudaError_t e =
+          merge_level(up, g.data(), (int)g.size(), jobs.data(), ixn.data(), (int)nodes.size(), P->status.p, st);
       if (e == cudaSuccess) e = cudaMemcpy(&stw, P->status.p, 4, cudaMemcpyDeviceToHost);
       if (e != cudaSuccess) rc = perr(DMSC_ERR_CUDA, std::string("merge level: ") + cudaGetErrorString(e));
     }
@@ -214,6 +234,7 @@ static int run_level(dmsc_pipeline *P, bool up, const std::vector<int> &nodes, c
       for (size_t i = 0; i < g.size() && rc == DMSC_OK; ++i) {
         if (up && (i % 3) != 2) continue;
         cudaError_t e = mgraph_to_csr(g[i], *P->msc[gnode[i]], st);
+        if (e == cudaSuccess && !up && (i % 3) != 2) e = cell_box(*P->msc[gnode[i]], st);  // a child
         if (e != cudaSuccess) rc = perr(DMSC_ERR_CUDA, std::string("merge writeback: ") + cudaGetErrorString(e));
       }
     }
