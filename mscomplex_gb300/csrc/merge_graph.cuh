@@ -143,13 +143,10 @@ inline __host__ __device__ void merge_up_cancel(MGraph &out, CRect ixn, uint32_t
 
 // merge_down (grid_mscomplex.cpp:158-322) of parent P into one child C; the
 // boundary uncancellation on P is done once by the caller.
-// The cancelable critical points of the parent (:207-281), in index order;
-// with `only` the caller has listed them (n of them, ascending).
-inline __host__ __device__ void merge_down_loop1(MGraph &P, MGraph &C, const uint32_t *only, uint32_t n, uint32_t *status) {
+// The cancelable critical points of the parent (:207-281), in index order.
+inline __host__ __device__ void merge_down_loop1(MGraph &P, MGraph &C, uint32_t *status) {
   Graph &G = C.G;
-  const uint32_t count = only ? n : P.G.ncp;
-  for (uint32_t q = 0; q < count && !G.fail; ++q) {
-    const uint32_t j = only ? only[q] : q;
+  for (uint32_t j = 0; j < P.G.ncp && !G.fail; ++j) {
     if (P.G.flags[j] & F_CANCELLED) { set_status(status, ST_INVARIANT); return; }  // "all cps ought to be uncancelled"
     if (!(P.G.flags[j] & F_BCANCEL)) continue;
     uint32_t sp = P.G.pair_idx[j];
@@ -184,7 +181,7 @@ inline __host__ __device__ void merge_down_loop1(MGraph &P, MGraph &C, const uin
 }
 
 inline __host__ __device__ void merge_down_child(MGraph &P, MGraph &C, uint32_t *status) {
-  merge_down_loop1(P, C, nullptr, 0, status);
+  merge_down_loop1(P, C, status);
   Graph &G = C.G;
   // the other critical points the child holds (:283-320)
   for (uint32_t j = 0; j < P.G.ncp && !G.fail; ++j) {

@@ -21,20 +21,19 @@
 //     (merge_up_cancel in merge_graph.cuh), all merges of the level in one
 //     launch.
 // merge_down (:158-322) splits into
-//   * the uncancellations along the shared boundary (:172-201) and the
-//     parent's boundary-cancelable points pushed into each child (:207-281):
-//     one thread per parent and per child (merge_down_boundary /
-//     merge_down_loop1), the latter visiting only the parent's
-//     boundary-cancelable points, which a parallel pass lists in index order
-//     after checking that no parent point is cancelled;
-//   * every other parent point the child holds takes the parent's lists,
-//     restricted to points the child holds (:283-320): independent per point,
-//     so counts, a scan, a scatter and a sort per list, written straight into
-//     the child's CSR arrays.
+//   * the uncancellations along the shared boundary (:172-201): one thread
+//     per parent (merge_down_boundary), all merges of the level in one launch;
+//   * the parent's boundary-cancelable points pushed into each child
+//     (:207-281): the points it adds to the child are numbered by a scan over
+//     the sequence of additions the reference's loop makes (down_child);
+//   * every child point whose cell the parent holds takes the parent's
+//     lists, restricted to points the child holds (:283-320): counts, a scan,
+//     a scatter and a sort per list into the child's new CSR arrays.
 // A step whose outcome only the one-thread restatement reproduces (a partner
 // missing from the union, where the reference's std::map::operator[] would
-// insert index 0) reports ST_FALLBACK and the caller reruns the level with
-// the one-thread merges.
+// insert index 0; a boundary-cancelable point whose partner does not point
+// back) reports ST_FALLBACK and the caller reruns the level with the
+// one-thread merges.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -355,26 +354,169 @@ __global__ void k_down_list(MGraph P, const uint32_t *bflag, const uint32_t *pos
   }
 }
 
-// the parent point (not boundary-cancelable) whose lists replace each child point's
-__global__ void k_down_repl(MGraph P, MGraph C, uint32_t *repl) {
-  GRID_LOOP(j, P.G.ncp) {
-    if (P.G.flags[j] & F_BCANCEL) continue;
-    const uint32_t d = C.find(P.G.cellid[j]);
-    if (d != NO_CP && d < C.G.ncp) repl[d] = (uint32_t)j;
+// ---------------------------------------------------------------------------
+// merge_down into one child (:207-320) without a mutable graph of the child.
+// The parent's boundary-cancelable points j (in index order, the list jb)
+// come in pairs (j, sp).  A pair whose two cells the child lacks is skipped;
+// when it holds exactly one, the first of the pair (lower index) adds the
+// other; the pair is then marked boundary-cancelable and paired in the child
+// unless both cells were already there with the mark.  The first of each
+// non-skipped point's list entries that the child lacks adds it, in the
+// order the reference's loop meets them: so every addition is an event in
+// one sequence (per point: its partner, then its asc, then its des entries),
+// and a scan over that sequence numbers the added points.  Finally every
+// child point whose cell the parent holds takes the parent's lists,
+// restricted to the points the child holds (for boundary-cancelable points
+// the child holds them all by then); the others keep their own.
+// ---------------------------------------------------------------------------
+enum : uint8_t { DC_SKIP = 1, DC_ADD = 2, DC_FIRST = 4, DC_S0 = 8, DC_P0 = 16 };
+
+struct DcArgs {
+  MGraph P;                 // the parent after its boundary uncancellations
+  const uint32_t *jb;       // its boundary-cancelable points, ascending
+  uint32_t njb;
+  CsrIn c;                  // the child before the merge
+  CellTab tab;              // child cell -> index (initial points, then the added ones)
+  CellTab first;            // missing cell -> position of its first list event
+  uint32_t *cnt, *base, *addsrc;
+  uint8_t *kind;            // per boundary point
+  uint32_t *addf, *rank;    // per event
+  CsrOut o;                 // the child's point arrays after the merge
+  uint32_t ncp0;
+  uint32_t *status;
+};
+
+__global__ void k_dc_table(CsrIn c, CellTab tab, uint32_t *status) {
+  GRID_LOOP(i, c.n) {
+    if (!tab.insert(c.cellid[i], (uint32_t)i)) atomicOr(status, ST_INVARIANT);
   }
 }
 
-__global__ void k_down_count(MGraph P, MGraph C, const uint32_t *repl, uint32_t *tot_a, uint32_t *tot_d, uint8_t *need) {
-  GRID_LOOP(d, C.G.ncp) {
-    const uint32_t j = repl[d];
+__global__ void k_dc_classify(DcArgs a) {
+  GRID_LOOP(q, a.njb) {
+    const uint32_t j = a.jb[q], sp = a.P.G.pair_idx[j];
+    uint8_t kd = 0;
+    uint32_t n = 0;
+    if (sp >= a.P.G.ncp || sp == j || a.P.G.pair_idx[sp] != j || !(a.P.G.flags[sp] & F_BCANCEL)) {
+      atomicOr(a.status, ST_FALLBACK);  // not a plain pair: the one-thread merge handles it
+      kd = DC_SKIP;
+    } else {
+      const bool s0 = a.tab.find(a.P.G.cellid[j]) != NO_CP, p0 = a.tab.find(a.P.G.cellid[sp]) != NO_CP;
+      if (s0) kd |= DC_S0;
+      if (p0) kd |= DC_P0;
+      if (j < sp) kd |= DC_FIRST;
+      if (!s0 && !p0) kd |= DC_SKIP;
+      else {
+        if (j < sp && s0 != p0) { kd |= DC_ADD; a.addsrc[q] = s0 ? sp : j; ++n; }
+        n += a.P.G.L.nrun[2 * j] + a.P.G.L.nrun[2 * j + 1];
+      }
+    }
+    a.kind[q] = kd;
+    a.cnt[q] = n;
+  }
+}
+
+// the first list event of every cell the child lacks
+__global__ void k_dc_first(DcArgs a) {
+  GRID_LOOP(q, a.njb) {
+    const uint8_t kd = a.kind[q];
+    if (kd & DC_SKIP) continue;
+    const uint32_t j = a.jb[q];
+    uint32_t pos = a.base[q] + ((kd & DC_ADD) ? 1 : 0);
+    for (int w = 0; w < 2; ++w) {
+      const uint2 *r = a.P.G.runs(2 * j + w);
+      for (uint32_t k = 0; k < a.P.G.L.nrun[2 * j + w]; ++k, ++pos) {
+        const uint32_t x = r[k].x;
+        if (x >= a.P.G.ncp || (a.P.G.flags[x] & F_BCANCEL)) { atomicOr(a.status, ST_INVARIANT); continue; }
+        const uint32_t cc = a.P.G.cellid[x];
+        if (a.tab.find(cc) != NO_CP) continue;
+        const long long sl = a.first.slot(cc);
+        if (sl < 0) atomicOr(a.status, ST_INVARIANT);
+        else atomicMin(a.first.tab + sl, pos);
+      }
+    }
+  }
+}
+
+__global__ void k_dc_addflags(DcArgs a) {
+  GRID_LOOP(q, a.njb) {
+    const uint8_t kd = a.kind[q];
+    if (kd & DC_SKIP) continue;
+    const uint32_t j = a.jb[q];
+    uint32_t pos = a.base[q];
+    if (kd & DC_ADD) a.addf[pos++] = 1;
+    for (int w = 0; w < 2; ++w) {
+      const uint2 *r = a.P.G.runs(2 * j + w);
+      for (uint32_t k = 0; k < a.P.G.L.nrun[2 * j + w]; ++k, ++pos) {
+        const uint32_t x = r[k].x;
+        if (x >= a.P.G.ncp) continue;
+        const uint32_t cc = a.P.G.cellid[x];
+        const long long sl = a.first.slot(cc);
+        a.addf[pos] = (a.tab.find(cc) == NO_CP && sl >= 0 && a.first.tab[sl] == pos) ? 1u : 0u;
+      }
+    }
+  }
+}
+
+// shallow_replicate_cp of parent point x as child point d
+__device__ __forceinline__ void dc_put(DcArgs &a, uint32_t x, uint32_t d) {
+  const uint32_t cid = a.P.G.cellid[x];
+  a.o.cellid[d] = cid;
+  a.o.fn[d] = a.P.fn[x];
+  a.o.flags[d] = a.P.G.flags[x] & (F_CANCELLED | F_STRANG | F_BCANCEL);
+  a.o.pair[d] = NO_CP;
+  if (!a.tab.insert(cid, d)) atomicOr(a.status, ST_INVARIANT);
+}
+
+__global__ void k_dc_add(DcArgs a) {
+  GRID_LOOP(q, a.njb) {
+    const uint8_t kd = a.kind[q];
+    if (kd & DC_SKIP) continue;
+    const uint32_t j = a.jb[q];
+    uint32_t pos = a.base[q];
+    if (kd & DC_ADD) { dc_put(a, a.addsrc[q], a.ncp0 + a.rank[pos]); ++pos; }
+    for (int w = 0; w < 2; ++w) {
+      const uint2 *r = a.P.G.runs(2 * j + w);
+      for (uint32_t k = 0; k < a.P.G.L.nrun[2 * j + w]; ++k, ++pos)
+        if (a.addf[pos]) dc_put(a, r[k].x, a.ncp0 + a.rank[pos]);
+    }
+  }
+}
+
+// the pairing of each non-skipped pair, once (by its first point)
+__global__ void k_dc_pairing(DcArgs a) {
+  GRID_LOOP(q, a.njb) {
+    const uint8_t kd = a.kind[q];
+    if ((kd & DC_SKIP) || !(kd & DC_FIRST)) continue;
+    const uint32_t j = a.jb[q], sp = a.P.G.pair_idx[j];
+    const uint32_t d1 = a.tab.find(a.P.G.cellid[j]), d2 = a.tab.find(a.P.G.cellid[sp]);
+    if (d1 == NO_CP || d2 == NO_CP) { atomicOr(a.status, ST_INVARIANT); continue; }
+    const bool set = (kd & DC_ADD) || !(a.o.flags[d1] & F_BCANCEL) || !(a.o.flags[d2] & F_BCANCEL);
+    if (!set) continue;
+    a.o.flags[d1] |= F_BCANCEL;
+    a.o.flags[d2] |= F_BCANCEL;
+    a.o.pair[d1] = d2;
+    a.o.pair[d2] = d1;
+  }
+}
+
+// the parent point (if any) whose lists each child point takes
+__global__ void k_dc_src(DcArgs a, uint32_t n, uint32_t *src) {
+  GRID_LOOP(d, n) src[d] = a.P.find(a.o.cellid[d]);
+}
+
+__global__ void k_dc_count(DcArgs a, uint32_t n, const uint32_t *src, uint32_t *tot_a, uint32_t *tot_d, uint8_t *need) {
+  GRID_LOOP(d, n) {
+    const uint32_t j = src[d];
     for (int w = 0; w < 2; ++w) {
       uint32_t c = 0;
       if (j == NO_CP) {
-        c = C.G.L.total[2 * d + w];
+        const uint32_t *off = w ? a.c.doff : a.c.aoff;
+        if (d < a.ncp0) c = off[d + 1] - off[d];
       } else {
-        const uint2 *r = P.G.runs(2 * j + w);
-        for (uint32_t q = 0; q < P.G.L.nrun[2 * j + w]; ++q)
-          if (C.find(P.G.cellid[r[q].x]) != NO_CP) c += r[q].y;
+        const uint2 *r = a.P.G.runs(2 * j + w);
+        for (uint32_t k = 0; k < a.P.G.L.nrun[2 * j + w]; ++k)
+          if (r[k].x < a.P.G.ncp && a.tab.find(a.P.G.cellid[r[k].x]) != NO_CP) c += r[k].y;
       }
       (w ? tot_d : tot_a)[d] = c;
     }
@@ -382,28 +524,25 @@ __global__ void k_down_count(MGraph P, MGraph C, const uint32_t *repl, uint32_t 
   }
 }
 
-__global__ void k_down_write(MGraph P, MGraph C, const uint32_t *repl, CsrOut o) {
-  GRID_LOOP(d, C.G.ncp) {
-    o.cellid[d] = C.G.cellid[d];
-    o.fn[d] = C.fn[d];
-    o.flags[d] = C.G.flags[d];
-    o.pair[d] = C.G.pair_idx[d];
-    const uint32_t j = repl[d];
+__global__ void k_dc_write(DcArgs a, uint32_t n, const uint32_t *src) {
+  GRID_LOOP(d, n) {
+    const uint32_t j = src[d];
     for (int w = 0; w < 2; ++w) {
-      const uint32_t *oo = w ? o.doff : o.aoff;
+      const uint32_t *oo = w ? a.o.doff : a.o.aoff;
       uint32_t p = oo[d];
       const uint32_t end = oo[d + 1];
-      uint32_t *ol = w ? o.des : o.asc;
+      uint32_t *ol = w ? a.o.des : a.o.asc;
       if (j == NO_CP) {
-        const uint2 *r = C.G.runs(2 * d + w);
-        for (uint32_t q = 0; q < C.G.L.nrun[2 * d + w]; ++q)
-          for (uint32_t c = 0; c < r[q].y && p < end; ++c) ol[p++] = r[q].x;
+        if (d >= a.ncp0) continue;
+        const uint32_t *off = w ? a.c.doff : a.c.aoff, *l = w ? a.c.des : a.c.asc;
+        for (uint32_t q = off[d]; q < off[d + 1] && p < end; ++q) ol[p++] = l[q];
       } else {
-        const uint2 *r = P.G.runs(2 * j + w);
-        for (uint32_t q = 0; q < P.G.L.nrun[2 * j + w]; ++q) {
-          const uint32_t ci = C.find(P.G.cellid[r[q].x]);
+        const uint2 *r = a.P.G.runs(2 * j + w);
+        for (uint32_t k = 0; k < a.P.G.L.nrun[2 * j + w]; ++k) {
+          if (r[k].x >= a.P.G.ncp) continue;
+          const uint32_t ci = a.tab.find(a.P.G.cellid[r[k].x]);
           if (ci == NO_CP) continue;
-          for (uint32_t c = 0; c < r[q].y && p < end; ++c) ol[p++] = ci;
+          for (uint32_t c = 0; c < r[k].y && p < end; ++c) ol[p++] = ci;
         }
       }
     }
@@ -413,12 +552,10 @@ __global__ void k_down_write(MGraph P, MGraph C, const uint32_t *repl, CsrOut o)
 // ---------------------------------------------------------------------------
 // the one-thread steps of a level, one block per job
 // ---------------------------------------------------------------------------
-enum SeqKind : int { SEQ_UP_CANCEL = 0, SEQ_DOWN_BOUNDARY = 1, SEQ_DOWN_LOOP1 = 2 };
+enum SeqKind : int { SEQ_UP_CANCEL = 0, SEQ_DOWN_BOUNDARY = 1 };
 struct SeqJob {
-  int kind, g0, g1;
+  int kind, g0;
   CRect ixn;
-  const uint32_t *only;   // SEQ_DOWN_LOOP1: the parent's boundary-cancelable points
-  const uint32_t *nonly;  // and their number (device)
 };
 
 // Loads, across the GPU, what the one-thread step of a job will read -- the
@@ -451,30 +588,11 @@ __global__ void k_seq_prefetch(const MGraph *graphs, const SeqJob *jobs, uint32_
   const SeqJob jb = jobs[blockIdx.y];
   const MGraph &M = graphs[jb.g0];
   uint32_t acc = 0;
-  if (jb.kind != SEQ_DOWN_LOOP1) {
-    const long long w = jb.ixn.r - jb.ixn.l + 1, h = jb.ixn.t - jb.ixn.b + 1;
-    GRID_LOOP(t, w * h) {
-      const uint32_t si = M.find(pack_cellid(jb.ixn.l + (int)(t % w), jb.ixn.b + (int)(t / w)));
-      if (si == NO_CP || si >= M.G.ncp) continue;
-      acc ^= touch_cp(M, si) ^ touch_cp(M, M.G.pair_idx[si]);
-    }
-  } else {
-    const MGraph &C = graphs[jb.g1];
-    const uint32_t n = *jb.nonly;
-    GRID_LOOP(q, n) {
-      const uint32_t j = jb.only[q];
-      if (j >= M.G.ncp) continue;
-      acc ^= touch_cp(M, j);
-      const uint32_t sp = M.G.pair_idx[j];
-      acc ^= C.find(M.G.cellid[j]);
-      if (sp < M.G.ncp) acc ^= C.find(M.G.cellid[sp]);
-      for (int w = 0; w < 2; ++w) {
-        const uint32_t l = 2 * j + w;
-        const uint2 *r = M.G.L.pool + M.G.L.off[l];
-        for (uint32_t k = 0; k < M.G.L.nrun[l] && k < 64; ++k)
-          if (r[k].x < M.G.ncp) acc ^= C.find(M.G.cellid[r[k].x]);
-      }
-    }
+  const long long w = jb.ixn.r - jb.ixn.l + 1, h = jb.ixn.t - jb.ixn.b + 1;
+  GRID_LOOP(t, w * h) {
+    const uint32_t si = M.find(pack_cellid(jb.ixn.l + (int)(t % w), jb.ixn.b + (int)(t / w)));
+    if (si == NO_CP || si >= M.G.ncp) continue;
+    acc ^= touch_cp(M, si) ^ touch_cp(M, M.G.pair_idx[si]);
   }
   if (acc == 0x9E3779B9u && sink) *sink = acc;
 }
@@ -487,20 +605,10 @@ __global__ void k_merge_seq(MGraph *graphs, const SeqJob *jobs, int njobs, uint3
   if (b >= njobs || threadIdx.x != 0) return;
   const SeqJob jb = jobs[b];
   MGraph g0 = graphs[jb.g0];
-  if (jb.kind == SEQ_UP_CANCEL) {
-    merge_up_cancel(g0, jb.ixn, status);
-    if (g0.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
-    graphs[jb.g0] = g0;
-  } else if (jb.kind == SEQ_DOWN_BOUNDARY) {
-    merge_down_boundary(g0, jb.ixn, status);
-    if (g0.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
-    graphs[jb.g0] = g0;
-  } else {
-    MGraph g1 = graphs[jb.g1];
-    merge_down_loop1(g0, g1, jb.only, *jb.nonly, status);
-    if (g1.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
-    graphs[jb.g1] = g1;
-  }
+  if (jb.kind == SEQ_UP_CANCEL) merge_up_cancel(g0, jb.ixn, status);
+  else merge_down_boundary(g0, jb.ixn, status);
+  if (g0.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+  graphs[jb.g0] = g0;
 }
 
 MGraph &mg(MGraphHost &h) { return *reinterpret_cast<MGraph *>(h.raw); }
@@ -668,53 +776,135 @@ cudaError_t union_one(const dmsc_msc &A, const dmsc_msc &B, dmsc_msc &O, CRect i
   return cudaSuccess;
 }
 
-// the child's final CSR: merge_down's second loop (:283-320) and the writeout
-cudaError_t down_child_out(MGraphHost &hp, MGraphHost &hc, dmsc_msc &C, cudaStream_t st) {
-  MGraph &P = mg(hp), &Cg = mg(hc);
-  const long long n = Cg.G.ncp;
+// A child's complex after merge_down, computed beside it (the child itself
+// is replaced only once every merge of the level has succeeded).
+struct ChildOut {
+  DevBuf<uint32_t> cellid, pair_idx, aoff, asc, doff, des;
+  DevBuf<float> fn;
+  DevBuf<uint8_t> flags;
+  long long ncp = 0, nasc = 0, ndes = 0;
+};
+
+template <typename T> void swap_buf(DevBuf<T> &a, DevBuf<T> &b) {
+  std::swap(a.p, b.p);
+  std::swap(a.n, b.n);
+  std::swap(a.pooled, b.pooled);
+}
+
+void child_take(dmsc_msc &C, ChildOut &o, const int box[4]) {
+  swap_buf(C.cellid, o.cellid); swap_buf(C.pair_idx, o.pair_idx); swap_buf(C.aoff, o.aoff); swap_buf(C.asc, o.asc);
+  swap_buf(C.doff, o.doff); swap_buf(C.des, o.des); swap_buf(C.fn, o.fn); swap_buf(C.flags, o.flags);
+  C.ncp = o.ncp; C.nasc = o.nasc; C.ndes = o.ndes;
+  C.any_bcancel = true;
+  for (int i = 0; i < 4; ++i) C.bbox[i] = box[i];
+}
+
+// merge_down of parent graph hp into child C (:207-320), into `out`.
+// jb/njb: the parent's boundary-cancelable points; adds: a bound on the
+// events (partners and list entries of those points); box: the child's box
+// grown by the cells those points can add.
+cudaError_t down_child(MGraphHost &hp, const uint32_t *jb, uint32_t njb, unsigned long long adds, const dmsc_msc &C,
+                       const int box[4], ChildOut &out, uint32_t *status, cudaStream_t st) {
+  const MGraph &P = mg(hp);
+  const long long n0 = C.ncp, cap = n0 + (long long)adds + 1;
+  if (cap >= (1ll << 31)) return cudaErrorInvalidValue;
+  const int tw = box[2] - box[0] + 1, th = box[3] - box[1] + 1;
+  if (tw <= 0 || th <= 0) return cudaErrorInvalidValue;
+  const size_t cells = (size_t)tw * th;
   cudaError_t e = cudaSuccess;
-  if (e == cudaSuccess) e = C.cellid.ensure(n + 1, st);
-  if (e == cudaSuccess) e = C.fn.ensure(n + 1, st);
-  if (e == cudaSuccess) e = C.pair_idx.ensure(n + 1, st);
-  if (e == cudaSuccess) e = C.flags.ensure(n + 1, st);
-  if (e == cudaSuccess) e = C.aoff.ensure(n + 1, st);
-  if (e == cudaSuccess) e = C.doff.ensure(n + 1, st);
+  if (e == cudaSuccess) e = out.cellid.ensure(cap, st);
+  if (e == cudaSuccess) e = out.fn.ensure(cap, st);
+  if (e == cudaSuccess) e = out.pair_idx.ensure(cap, st);
+  if (e == cudaSuccess) e = out.flags.ensure(cap, st);
+  if (e == cudaSuccess) e = out.aoff.ensure(cap, st);
+  if (e == cudaSuccess) e = out.doff.ensure(cap, st);
   if (e != cudaSuccess) return e;
   Scratch s;
-  s.sz = {4ull * (n + 1), 4ull * (n + 1), 4ull * (n + 1), (size_t)n + 1};
+  // tab, first, cnt, base, addsrc, kind, addf, rank, src, tot_a, tot_d, need, counters
+  s.sz = {4 * cells, 4 * cells, 4ull * (njb + 1), 4ull * (njb + 1), 4ull * (njb + 1), (size_t)njb + 1,
+          4ull * (adds + 1), 4ull * (adds + 1), 4ull * cap, 4ull * cap, 4ull * cap, (size_t)cap, 64};
   if ((e = s.alloc(st)) != cudaSuccess) return e;
-  uint32_t *repl = (uint32_t *)s.ptr[0], *tot_a = (uint32_t *)s.ptr[1], *tot_d = (uint32_t *)s.ptr[2];
-  uint8_t *need = (uint8_t *)s.ptr[3];
-  e = cudaMemsetAsync(repl, 0xFF, 4ull * (n + 1), st);
-  if (e == cudaSuccess && P.G.ncp) {
-    k_down_repl<<<nblk(P.G.ncp), 256, 0, st>>>(P, Cg, repl);
+  DcArgs a;
+  a.P = P;
+  a.jb = jb;
+  a.njb = njb;
+  a.c = csr_in(C);
+  a.tab = CellTab{(uint32_t *)s.ptr[0], box[0], box[1], tw, th};
+  a.first = CellTab{(uint32_t *)s.ptr[1], box[0], box[1], tw, th};
+  a.cnt = (uint32_t *)s.ptr[2];
+  a.base = (uint32_t *)s.ptr[3];
+  a.addsrc = (uint32_t *)s.ptr[4];
+  a.kind = (uint8_t *)s.ptr[5];
+  a.addf = (uint32_t *)s.ptr[6];
+  a.rank = (uint32_t *)s.ptr[7];
+  uint32_t *src = (uint32_t *)s.ptr[8], *tot_a = (uint32_t *)s.ptr[9], *tot_d = (uint32_t *)s.ptr[10];
+  uint8_t *need = (uint8_t *)s.ptr[11];
+  uint32_t *ctr = (uint32_t *)s.ptr[12];  // [0] events, [1] added points
+  a.o = CsrOut{out.cellid.p, out.pair_idx.p, out.aoff.p, nullptr, out.doff.p, nullptr, out.fn.p, out.flags.p};
+  a.ncp0 = (uint32_t)n0;
+  a.status = status;
+  e = cudaMemsetAsync(s.ptr[0], 0xFF, 4 * cells, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s.ptr[1], 0xFF, 4 * cells, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, 64, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(a.addf, 0, 4ull * (adds + 1), st);
+  if (e == cudaSuccess && n0) {
+    k_dc_table<<<nblk(n0), 256, 0, st>>>(a.c, a.tab, status);
     DMSC_LAUNCHED(1);
+    e = cudaMemcpyAsync(out.cellid.p, C.cellid.p, 4ull * n0, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out.fn.p, C.fn.p, 4ull * n0, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out.pair_idx.p, C.pair_idx.p, 4ull * n0, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out.flags.p, C.flags.p, n0, cudaMemcpyDeviceToDevice, st);
   }
-  if (e == cudaSuccess && n) {
-    k_down_count<<<nblk(n), 256, 0, st>>>(P, Cg, repl, tot_a, tot_d, need);
+  if (e == cudaSuccess && njb) {
+    k_dc_classify<<<nblk(njb), 256, 0, st>>>(a);
     DMSC_LAUNCHED(1);
+    e = scan_exclusive_u32(a.cnt, njb, a.base, ctr, st);
+    if (e == cudaSuccess) {
+      k_dc_first<<<nblk(njb), 256, 0, st>>>(a);
+      k_dc_addflags<<<nblk(njb), 256, 0, st>>>(a);
+      DMSC_LAUNCHED(2);
+      e = scan_exclusive_u32(a.addf, (long long)adds + 1, a.rank, ctr + 1, st);
+    }
+    if (e == cudaSuccess) {
+      k_dc_add<<<nblk(njb), 256, 0, st>>>(a);
+      k_dc_pairing<<<nblk(njb), 256, 0, st>>>(a);
+      DMSC_LAUNCHED(2);
+      e = cudaGetLastError();
+    }
   }
-  if (e == cudaSuccess) e = scan_exclusive_u32(tot_a, n, C.aoff.p, C.aoff.p + n, st);
-  if (e == cudaSuccess) e = scan_exclusive_u32(tot_d, n, C.doff.p, C.doff.p + n, st);
-  uint32_t tot[2] = {0, 0};
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&tot[0], C.aoff.p + n, 4, cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&tot[1], C.doff.p + n, 4, cudaMemcpyDeviceToHost, st);
+  uint32_t hc[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hc, ctr, 8, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e == cudaSuccess) e = C.asc.ensure((size_t)tot[0] + 1, st);
-  if (e == cudaSuccess) e = C.des.ensure((size_t)tot[1] + 1, st);
+  const long long n = n0 + hc[1];
+  if (e == cudaSuccess && (unsigned long long)hc[0] > adds) e = cudaErrorInvalidValue;  // the event bound failed
+  // the lists (:283-320): taken from the parent where it holds the cell
   if (e == cudaSuccess && n) {
-    k_down_write<<<nblk(n), 256, 0, st>>>(P, Cg, repl, csr_out(C));
+    k_dc_src<<<nblk(n), 256, 0, st>>>(a, (uint32_t)n, src);
+    k_dc_count<<<nblk(n), 256, 0, st>>>(a, (uint32_t)n, src, tot_a, tot_d, need);
+    DMSC_LAUNCHED(2);
+  }
+  if (e == cudaSuccess) e = scan_exclusive_u32(tot_a, n, out.aoff.p, out.aoff.p + n, st);
+  if (e == cudaSuccess) e = scan_exclusive_u32(tot_d, n, out.doff.p, out.doff.p + n, st);
+  uint32_t tot[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&tot[0], out.aoff.p + n, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&tot[1], out.doff.p + n, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = out.asc.ensure((size_t)tot[0] + 1, st);
+  if (e == cudaSuccess) e = out.des.ensure((size_t)tot[1] + 1, st);
+  if (e == cudaSuccess && n) {
+    a.o.asc = out.asc.p;
+    a.o.des = out.des.p;
+    k_dc_write<<<nblk(n), 256, 0, st>>>(a, (uint32_t)n, src);
     DMSC_LAUNCHED(1);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = sort_segments(n, C.aoff.p, C.asc.p, need, st);
-  if (e == cudaSuccess) e = sort_segments(n, C.doff.p, C.des.p, need, st);
+  if (e == cudaSuccess) e = sort_segments(n, out.aoff.p, out.asc.p, need, st);
+  if (e == cudaSuccess) e = sort_segments(n, out.doff.p, out.des.p, need, st);
   s.free(st);
   if (e != cudaSuccess) return e;
-  C.ncp = n;
-  C.nasc = tot[0];
-  C.ndes = tot[1];
-  C.any_bcancel = true;
+  out.ncp = n;
+  out.nasc = tot[0];
+  out.ndes = tot[1];
   return cudaSuccess;
 }
 
@@ -762,7 +952,7 @@ cudaError_t merge_up_level_par(const std::vector<MergeJob> &jobs, unsigned long 
   for (int k = 0; k < nj; ++k) {
     const int *x = jobs[k].ixn;
     gp.push_back(&g[k]);
-    seq.push_back(SeqJob{SEQ_UP_CANCEL, k, -1, CRect{x[0], x[1], x[2], x[3]}, nullptr, nullptr});
+    seq.push_back(SeqJob{SEQ_UP_CANCEL, k, CRect{x[0], x[1], x[2], x[3]}});
   }
   e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS, [&](int k, cudaStream_t s) {
     const dmsc_msc &O = *jobs[k].parent;
@@ -789,14 +979,14 @@ cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned lon
   *stw = 0;
   const int nj = (int)jobs.size(), dev = current_device();
   cudaError_t e = cudaMemsetAsync(status, 0, 4, st);
-  // graphs: 3 per job (parent, child a, child b)
-  std::vector<MGraphHost> g(3 * nj);
+  // the parents' graphs
+  std::vector<MGraphHost> g(nj);
   std::vector<MGraphHost *> gp;
   for (auto &h : g) gp.push_back(&h);
   std::vector<SeqJob> seq;
   for (int k = 0; k < nj; ++k) {
     const int *x = jobs[k].ixn;
-    seq.push_back(SeqJob{SEQ_DOWN_BOUNDARY, 3 * k, -1, CRect{x[0], x[1], x[2], x[3]}, nullptr, nullptr});
+    seq.push_back(SeqJob{SEQ_DOWN_BOUNDARY, k, CRect{x[0], x[1], x[2], x[3]}});
   }
   // scratch: per job the boundary-cancelable flags, positions and list; counters
   Scratch s;
@@ -820,15 +1010,15 @@ cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned lon
   if (e == cudaSuccess)
     e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS, [&](int k, cudaStream_t q) {
       const dmsc_msc &P = *jobs[k].parent;
-      g[3 * k].status = status;
-      return (int)mgraph_alloc(g[3 * k], P, (uint32_t)P.ncp, P.nasc + P.ndes + grow * boundary_room(jobs[k].ixn), q, 0);
+      g[k].status = status;
+      return (int)mgraph_alloc(g[k], P, (uint32_t)P.ncp, P.nasc + P.ndes + grow * boundary_room(jobs[k].ixn), q, 0);
     }));
   // the uncancellations along each shared boundary (:172-201)
   if (e == cudaSuccess) e = run_seq(gp, seq, status, st, seq_ms);
   // checks, the boundary-cancelable lists and the bounds of the children's growth
   if (e == cudaSuccess)
     e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS, [&](int k, cudaStream_t q) {
-      MGraph &P = mg(g[3 * k]);
+      MGraph &P = mg(g[k]);
       uint32_t *bflag = (uint32_t *)s.ptr[3 * k], *pos = (uint32_t *)s.ptr[3 * k + 1], *jb = (uint32_t *)s.ptr[3 * k + 2];
       uint32_t *njb = (uint32_t *)(ctr + 2 * k);
       if (!P.G.ncp) return 0;
@@ -845,7 +1035,8 @@ cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned lon
   std::vector<unsigned long long> hc(2 * (nj + 1), 0);
   if (e == cudaSuccess) e = cudaMemcpy(hc.data(), ctr, 16ull * nj, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(hbox.data(), boxes, 16ull * nj, cudaMemcpyDeviceToHost);
-  // each child's table covers its own cells and the cells its parent's boundary points can add
+  if (e == cudaSuccess) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
+  // each child's box grows by the cells its parent's boundary points can add
   std::vector<int> cbox(8 * nj);
   for (int k = 0; k < nj; ++k)
     for (int c = 0; c < 2; ++c) {
@@ -858,42 +1049,23 @@ cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned lon
         o[2] = std::max(o[2], t[2]); o[3] = std::max(o[3], t[3]);
       }
     }
-  if (e == cudaSuccess) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
-  // the children's graphs, with room for what the parent's boundary points add
-  seq.clear();
-  for (int k = 0; k < nj; ++k)
-    if (hc[2 * k])
-      for (int c = 0; c < 2; ++c)
-        seq.push_back(SeqJob{SEQ_DOWN_LOOP1, 3 * k, 3 * k + 1 + c, CRect{0, 0, 0, 0}, (const uint32_t *)s.ptr[3 * k + 2],
-                             (const uint32_t *)(ctr + 2 * k)});
+  // the parent into each child (:207-320), beside the child
+  std::vector<ChildOut> outs(2 * nj);
   if (e == cudaSuccess && !*stw)
     e = as_cuda(for_each_on_streams(dev, 2 * nj, MERGE_WORKERS, [&](int kc, cudaStream_t q) {
       const int k = kc / 2, c = kc % 2;
-      const unsigned long long adds = hc[2 * k + 1];
       const dmsc_msc &C = *(c ? jobs[k].b : jobs[k].a);
-      const unsigned long long cap = (unsigned long long)C.ncp + adds + 16;
-      if (cap > 0xffffffffull) return (int)cudaErrorInvalidValue;
-      g[3 * k + 1 + c].status = status;
-      return (int)mgraph_alloc(g[3 * k + 1 + c], C, (uint32_t)cap, C.nasc + C.ndes + grow * (4 * adds + (1ull << 20)),
-                               q, 0, nullptr, &cbox[8 * k + 4 * c]);
+      return (int)down_child(g[k], (const uint32_t *)s.ptr[3 * k + 2], (uint32_t)hc[2 * k], hc[2 * k + 1], C,
+                             &cbox[8 * k + 4 * c], outs[kc], status, q);
     }));
-  // the parent's boundary-cancelable points into each child (:207-281)
-  if (e == cudaSuccess && !*stw) e = run_seq(gp, seq, status, st, seq_ms);
   if (e == cudaSuccess && !*stw) e = cudaMemcpy(stw, status, 4, cudaMemcpyDeviceToHost);
-  // every other point the child holds (:283-320), straight into the child's
-  // CSR arrays; then the parent's own write-back
-  if (e == cudaSuccess && !*stw)
-    e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS, [&](int k, cudaStream_t q) {
-      cudaError_t r = down_child_out(g[3 * k], g[3 * k + 1], *jobs[k].a, q);
-      if (r == cudaSuccess) r = down_child_out(g[3 * k], g[3 * k + 2], *jobs[k].b, q);
-      if (r == cudaSuccess) r = mgraph_to_csr(g[3 * k], *jobs[k].parent, q);
-      if (r == cudaSuccess)
-        for (int c = 0; c < 2; ++c) {
-          dmsc_msc &C = *(c ? jobs[k].b : jobs[k].a);
-          for (int i = 0; i < 4; ++i) C.bbox[i] = cbox[8 * k + 4 * c + i];
-        }
-      return (int)r;
-    }));
+  // every merge of the level succeeded: the children take their new
+  // complexes and the parents are written back
+  if (e == cudaSuccess && !*stw) {
+    for (int kc = 0; kc < 2 * nj; ++kc) child_take(*(kc % 2 ? jobs[kc / 2].b : jobs[kc / 2].a), outs[kc], &cbox[4 * kc]);
+    e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS,
+                                    [&](int k, cudaStream_t q) { return (int)mgraph_to_csr(g[k], *jobs[k].parent, q); }));
+  }
   s.free(st);
   for (auto &h : g) mgraph_free(h, st);
   cudaStreamSynchronize(st);

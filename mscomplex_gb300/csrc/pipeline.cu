@@ -141,8 +141,9 @@ static int run_level_par(dmsc_pipeline *P, bool up, const std::vector<int> &node
     if (e != cudaSuccess)
       return perr(e == cudaErrorMemoryAllocation ? DMSC_ERR_OOM : DMSC_ERR_CUDA,
                   std::string("parallel merge level: ") + cudaGetErrorString(e));
-    if (stw & ST_FALLBACK) {
-      for (auto &J : jobs) J.parent->ncp = J.parent->nasc = J.parent->ndes = 0;  // the one-thread merge_up starts empty
+    if (stw & ST_FALLBACK) {  // nothing was written back; the one-thread merge_up starts from an empty parent
+      if (up)
+        for (auto &J : jobs) J.parent->ncp = J.parent->nasc = J.parent->ndes = 0;
       return LEVEL_FALLBACK;
     }
     if (stw == ST_SIMPLIFY_LIMIT && attempt + 1 < 4) continue;
