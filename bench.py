@@ -268,16 +268,16 @@ def serve_requests(count: int, seed: int = 4):
     return reqs
 
 
-def bench_served(M, torch, count=300, rates=(None, 200.0), max_ops=2_000_000):
+def bench_served(M, torch, count=300, rates=(None, 200.0), max_ops=2_000_000, lanes=4):
     """The request server under a Poisson stream (rate None = every request
     submitted at once, i.e. saturation) against plain one-request-at-a-time
     processing through the per-grid API.  Latency = submit -> result ready."""
     reqs = serve_requests(count)
-    out = {"workload": SERVE_WORKLOAD, "requests": count, "max_ops_per_request": max_ops, "runs": []}
+    out = {"workload": SERVE_WORKLOAD, "requests": count, "max_ops_per_request": max_ops, "lanes": lanes, "runs": []}
     for rate in rates:
         rng = np.random.default_rng(11)
         gaps = np.zeros(count) if rate is None else rng.exponential(1.0 / rate, count)
-        srv = M.GridServer(arena_bytes=150 << 30, lanes=2, max_batch=128, max_ops=max_ops)
+        srv = M.GridServer(arena_bytes=150 << 30, lanes=lanes, max_batch=128, max_ops=max_ops)
         t0 = time.perf_counter()
         ids = []
         next_t = 0.0

@@ -207,9 +207,12 @@ int dmsc_batch_export_all(dmsc_batch *b, uint32_t *cp_base, uint32_t *asc_base, 
  * copied at submit) are admitted in arrival order by their device footprint
  * against arena_bytes and run as batches (dmsc_batch_run) by `lanes` worker
  * threads, each with its own stream, so one batch is admitted and copied
- * while another computes.  A request's result equals its grid's complex
- * computed alone.  max_ops bounds each grid's simplification (<= 0: the
- * default of dmsc_msc_simplify_un_simplify). */
+ * while another computes.  With two or more lanes, lanes / 2 of them take
+ * the requests whose exact simplification is expected to be long (tresh > 0
+ * and more than 1% equal neighbour pairs) and the others the rest.  A
+ * request's result equals its grid's complex computed alone.  max_ops bounds
+ * each grid's simplification (<= 0: the default of
+ * dmsc_msc_simplify_un_simplify). */
 typedef struct dmsc_server dmsc_server;
 int dmsc_server_create(dmsc_ctx *ctx, int64_t arena_bytes, int lanes, int max_batch, int64_t max_ops, dmsc_server **out);
 int dmsc_server_submit(dmsc_server *s, const float *heights, int nx, int ny, double tresh, int64_t *id);

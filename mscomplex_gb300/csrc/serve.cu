@@ -16,11 +16,13 @@
 // with many exact ties (its heap replays the reference's tie order), and a
 // batch completes with its slowest grid.  So requests with tresh > 0 whose
 // heights have more than 1% equal neighbour pairs are "heavy" and queue for
-// lane 0 alone (when there are two or more lanes); the other lanes never wait
-// behind them.  A request whose simplification exhausts the operation budget
+// the first half of the lanes (when there are two or more lanes: lanes / 2 of
+// them); the other lanes never wait behind them, and a heavy request that
+// arrives while a heavy batch runs starts on the next free heavy lane.  A request whose simplification exhausts the operation budget
 // fails alone (DMSC_ERR_PARTIAL from the batch); its batch mates complete.
 // Only a batch that fails as a whole (NaN heights, an allocation) is rerun
 // one grid at a time.
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -91,14 +93,22 @@ struct dmsc_server {
 };
 
 void dmsc_server::lane(int k) {
-  // lane 0 takes the heavy queue when there are other lanes; a single lane takes both
-  const bool heavy_lane = lanes >= 2 && k == 0, light_lane = lanes == 1 || k != 0;
+  // the first lanes / 2 lanes take the heavy queue when there are other lanes;
+  // a single lane takes both
+  const int nheavy = lanes >= 2 ? lanes / 2 : 0;
+  const bool heavy_lane = k < nheavy, light_lane = lanes == 1 || k >= nheavy;
   cudaSetDevice(ctx->device);
   cudaStream_t st = nullptr;
   cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
   dmsc_batch *batch = nullptr;
   float *staging = nullptr;
   size_t staging_n = 0;
+  uint32_t *ex = nullptr;  // pinned export buffer (words)
+  size_t ex_n = 0, staging_n_prev = 0;
+  // Pinned buffers outgrown while the server runs: freeing pinned memory
+  // waits for the whole device (every lane's work), so they are kept until
+  // the lane stops.
+  std::vector<void *> retired;
   std::vector<std::shared_ptr<Request>> take;
   for (;;) {
     take.clear();
@@ -143,12 +153,14 @@ void dmsc_server::lane(int k) {
       tr.push_back(r->tresh);
     }
     int rc = DMSC_OK;
+    bool partial = false;
     std::string err;
-    if (nv > staging_n) {
-      if (staging) cudaFreeHost(staging);
+    if (nv > staging_n) {  // grow (x2); the old buffer is freed when the lane stops
+      if (staging) retired.push_back(staging);
       staging = nullptr;
       staging_n = 0;
-      if (cudaMallocHost((void **)&staging, sizeof(float) * nv) == cudaSuccess) staging_n = nv;
+      const size_t want = std::max(nv, 2 * staging_n_prev);
+      if (cudaMallocHost((void **)&staging, sizeof(float) * want) == cudaSuccess) staging_n = staging_n_prev = want;
       else { rc = DMSC_ERR_OOM; err = "pinned staging"; }
     }
     if (rc == DMSC_OK) {
@@ -158,7 +170,7 @@ void dmsc_server::lane(int k) {
         o += r->heights.size();
       }
       rc = dmsc_batch_run(ctx, (int)take.size(), sizes.data(), staging, 0, tr.data(), max_ops, &batch, st);
-      if (rc == DMSC_ERR_PARTIAL) rc = DMSC_OK;  // a failed grid's export returns its own error
+      if (rc == DMSC_ERR_PARTIAL) { rc = DMSC_OK; partial = true; }  // a failed grid's export returns its own error
       else if (rc) err = dmsc_last_error();
     }
     // a failed batch of several grids is rerun one grid at a time, so that
@@ -203,7 +215,54 @@ void dmsc_server::lane(int k) {
       }
       for (auto &r : take) { r->heights.clear(); r->heights.shrink_to_fit(); }
     }
-    for (size_t i = 0; i < take.size() && !(rc != DMSC_OK && take.size() > 1); ++i) {
+    // a batch without failed grids comes back in one set of copies into pinned
+    // memory, split per request on the host
+    bool bulk = false;
+    if (rc == DMSC_OK && !partial && take.size() > 1) {
+      int64_t tot[3] = {0, 0, 0};
+      if (dmsc_batch_totals(batch, tot) == DMSC_OK) {
+        const size_t g1 = take.size() + 1, ncp = (size_t)tot[0], na = (size_t)tot[1], nd = (size_t)tot[2];
+        const size_t need = 3 * g1 + 4 * ncp + ncp + 2 * (ncp + 1) + na + nd + (ncp + 3) / 4 + 16;  // words
+        if (need > ex_n) {  // grow (x2); the old buffer is freed when the lane stops
+          if (ex) retired.push_back(ex);
+          ex = nullptr;
+          const size_t want = std::max(need, 2 * ex_n);
+          ex_n = 0;
+          if (cudaMallocHost((void **)&ex, sizeof(uint32_t) * want) == cudaSuccess) ex_n = want;
+        }
+        if (ex) {
+          uint32_t *cpb = ex, *ab = cpb + g1, *db = ab + g1, *cell = db + g1, *fnb = cell + ncp, *pair = fnb + ncp;
+          uint32_t *ao = pair + ncp, *asc = ao + ncp + 1, *dof = asc + na, *des = dof + ncp + 1;
+          uint8_t *fl = (uint8_t *)(des + nd);
+          bulk = dmsc_batch_export_all(batch, cpb, ab, db, cell, (float *)fnb, pair, fl, ao, asc, dof, des, st) == DMSC_OK;
+          for (size_t i = 0; bulk && i < take.size(); ++i) {
+            Request &r = *take[i];
+            const size_t c0 = cpb[i], n = cpb[i + 1] - c0, a0 = ab[i], a1 = ab[i + 1], d0 = db[i], d1 = db[i + 1];
+            r.t_start = t_start;
+            r.sizes[0] = (int64_t)n; r.sizes[1] = (int64_t)(a1 - a0); r.sizes[2] = (int64_t)(d1 - d0);
+            r.cellid.assign(cell + c0, cell + c0 + n);
+            r.fn.assign((float *)fnb + c0, (float *)fnb + c0 + n);
+            r.pair_idx.assign(pair + c0, pair + c0 + n);
+            r.flags.assign(fl + c0, fl + c0 + n);
+            r.asc.assign(asc + a0, asc + a1);
+            r.des.assign(des + d0, des + d1);
+            r.aoff.resize(n + 1);
+            r.doff.resize(n + 1);
+            for (size_t k = 0; k <= n; ++k) {
+              r.aoff[k] = ao[c0 + k] - (uint32_t)a0;
+              r.doff[k] = dof[c0 + k] - (uint32_t)d0;
+            }
+            r.heights.clear();
+            r.heights.shrink_to_fit();
+            r.error.clear();
+            r.t_done = now_ms();
+            std::lock_guard<std::mutex> lk(mu);
+            r.status = DMSC_OK;
+          }
+        }
+      }
+    }
+    for (size_t i = 0; !bulk && i < take.size() && !(rc != DMSC_OK && take.size() > 1); ++i) {
       Request &r = *take[i];
       r.t_start = t_start;
       int rrc = rc;
@@ -235,6 +294,8 @@ void dmsc_server::lane(int k) {
   }
   if (batch) dmsc_batch_destroy(batch);
   if (staging) cudaFreeHost(staging);
+  if (ex) cudaFreeHost(ex);
+  for (void *p : retired) cudaFreeHost(p);
   cudaStreamDestroy(st);
 }
 
