@@ -90,3 +90,33 @@ def test_par_equals_sequential(gpu_lib, par_ctx, seq_ctx, n, levels, split2d):
     a = gpu_lib.GridDataManager(f, levels=levels, tresh=0.0, split2d=split2d, ctx=par_ctx)
     b = gpu_lib.GridDataManager(f, levels=levels, tresh=0.0, split2d=split2d, ctx=seq_ctx)
     compare(a, b, f"noise{n} par vs seq")
+
+
+@pytest.mark.parametrize("shape,levels,split2d", [((9, 7), 2, True), ((12, 40), 2, False), ((33, 5), 2, True),
+                                                   ((17, 17), 3, True), ((40, 9), 3, False)])
+def test_par_thin_and_tiny(gpu_lib, oracle, par_ctx, shape, levels, split2d):
+    """Pieces only a few vertices wide (shared boundaries next to the outer one)."""
+    f = smooth_field(shape[0], shape[1], 11)
+    check(gpu_lib, oracle, par_ctx, f, levels, 0.05, split2d, f"par tiny {shape} L{levels}")
+
+
+@pytest.mark.parametrize("kind", ["constant", "ramp", "checker"])
+def test_par_degenerate_fields(gpu_lib, oracle, par_ctx, kind):
+    ny, nx = 40, 56
+    y, x = np.mgrid[0:ny, 0:nx]
+    if kind == "constant":
+        f = np.zeros((ny, nx), np.float32)
+    elif kind == "ramp":
+        f = (x + 0.5 * y).astype(np.float32)
+    else:
+        f = ((x + y) % 2).astype(np.float32)
+    check(gpu_lib, oracle, par_ctx, f, 2, 0.1, True, f"par {kind}")
+
+
+def test_par_too_thin_pieces_fail_like_the_reference(gpu_lib, oracle, par_ctx):
+    """Strips one or two rows high break a reference invariant (its logic_error); both report it."""
+    f = smooth_field(6, 40, 11)
+    with pytest.raises(RuntimeError):
+        oracle.Pipeline(f, levels=3, tresh=0.05, split2d=False)
+    with pytest.raises(gpu_lib.DmscError):
+        gpu_lib.GridDataManager(f, levels=3, tresh=0.05, split2d=False, ctx=par_ctx)
