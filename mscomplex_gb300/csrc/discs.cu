@@ -789,209 +789,304 @@ static cudaError_t hops_attr() {
   return attr;
 }
 
-cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
+// Everything both disc kinds share: the hop structure, the redirections, the
+// owner keys of the vertex and face grids.
+struct DiscShared {
   DiscArgs a;
-  a.g = io.g; a.codes = io.codes; a.labels = io.labels; a.ncp_ds = (uint32_t)io.ncp_ds; a.ncp = (uint32_t)io.ncp;
-  a.cellid = io.cellid; a.flags = io.flags; a.pair_idx = io.pair_idx;
-  a.aoff = io.aoff; a.asc = io.asc; a.doff = io.doff; a.des = io.des; a.status = io.status;
-  const long long ncp = io.ncp;
-  const GridGeom &g = io.g;
-  const long long nV = (long long)((g.rx1 - g.rx0) / 2 + 1) * ((g.ry1 - g.ry0) / 2 + 1);
-  const long long nF = (long long)((g.rx1 - g.rx0) / 2) * ((g.ry1 - g.ry0) / 2);
-  const long long nmax = std::max(std::max(nV, nF), std::max(io.nasc, io.ndes)) + 1;
-  const long long nE = 2ll * g.vnx * g.vny;  // edge ids of the ext window
-  // words: 7 ncp + 8 | 4 nmax | 2 (nV + nF) | 3 ncp + 1 (kc, mc, cbase) | ncp / 4 (big) | 2.75 nE (hops)
-  size_t words = (size_t)ncp * 7 + 8 + (size_t)nmax * 4 + (size_t)(nV + nF) * 2 + (size_t)ncp * 3 + 1 +
-                 (size_t)ncp / 4 + 1 + 2 * (size_t)nE + (size_t)nE / 2 + (size_t)nE / 4 + 64;
-  uint32_t *buf = nullptr;
-  cudaError_t e = hops_attr();
-  if (e != cudaSuccess) return e;
-  e = cudaMallocAsync((void **)&buf, sizeof(uint32_t) * words, st);
-  if (e != cudaSuccess) return e;
-  uint32_t *redir = buf, *acnt = buf + ncp, *dcnt = buf + 2 * ncp, *slen = buf + 3 * ncp;
-  uint32_t *sstart = buf + 4 * ncp, *scount = buf + 5 * ncp, *soff = buf + 6 * ncp;  // soff: ncp+1
-  uint32_t *key = buf + 7 * ncp + 8, *val = key + nmax, *kt = val + nmax, *vt = kt + nmax;
-  uint32_t *gkey[2] = {vt + nmax, vt + nmax + nV}, *gval[2] = {vt + nmax + nV + nF, vt + nmax + 2 * nV + nF};
-  uint32_t *kc = gval[1] + nF, *mc = kc + ncp, *cbase = mc + ncp;  // cbase: ncp+1
-  uint8_t *big = (uint8_t *)(cbase + ncp + 1);
-  uint32_t *hop_to = cbase + ncp + 1 + ncp / 4 + 1, *jseg = hop_to + nE;
-  uint16_t *hop_len = (uint16_t *)(jseg + nE);
-  uint8_t *nextd = (uint8_t *)(hop_len + nE);
-  const long long gn[2] = {nV, nF};
-  auto L = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-  uint32_t *chain_buf = nullptr, *tmp = nullptr;
+  const DiscIO *io;
+  long long ncp, nmax, gn[2];
+  int gw[2];
+  uint32_t *redir, *hop_to, *jseg, *gkey[2], *gval[2];
+  uint16_t *hop_len;
+  uint8_t *nextd;
+};
+
+// One disc kind (0 asc, 1 des) as a sequence of stages on its own stream;
+// a stage ends where the host needs a count back.  Two kinds interleave on
+// one host thread: while it waits for one kind's count, the other kind's
+// launches keep the GPU busy.
+struct DiscKind {
+  int kind = 0;
+  cudaStream_t st = nullptr;
+  const DiscShared *sh = nullptr;
+  // per-kind scratch (device)
+  uint32_t *cnt = nullptr, *slen = nullptr, *sstart = nullptr, *scount = nullptr, *soff = nullptr;
+  uint32_t *key = nullptr, *val = nullptr, *kt = nullptr, *vt = nullptr, *kc = nullptr, *mc = nullptr, *cbase = nullptr;
+  uint8_t *big = nullptr;
+  uint32_t *hbuf = nullptr;  // pinned host counts: [0] runs, [1] seeds, [2] chains, [3..5] totals
+  uint32_t *runbuf = nullptr, *chain_buf = nullptr, *tmp = nullptr;
   uint4 *segs = nullptr, *blocks = nullptr;
-  auto release = [&]() {
+  uint32_t *rp = nullptr, *rstart = nullptr;
+  uint32_t nrun = 0, ns = 0, nch = 0, tot[3] = {0, 0, 0};
+  ChainArgs c{};
+  int stage = 0;
+  cudaError_t e = cudaSuccess;
+
+  void L(cudaError_t x) { if (e == cudaSuccess) e = x; }
+  void release() {
     if (segs) cudaFreeAsync(segs, st);
     if (tmp) cudaFreeAsync(tmp, st);
     if (blocks) cudaFreeAsync(blocks, st);
     if (chain_buf) cudaFreeAsync(chain_buf, st);
-    segs = nullptr; tmp = nullptr; blocks = nullptr; chain_buf = nullptr;
-  };
+    if (runbuf) cudaFreeAsync(runbuf, st);
+    segs = nullptr; tmp = nullptr; blocks = nullptr; chain_buf = nullptr; runbuf = nullptr;
+  }
+  // Runs the next stage; returns true while more stages remain (the caller
+  // synchronises the stream before the next one).
+  bool step() {
+    if (e != cudaSuccess) return false;
+    const DiscShared &S = *sh;
+    const DiscArgs &a = S.a;
+    const DiscIO &io = *S.io;
+    const long long ncp = S.ncp, n = S.gn[kind];
+    switch (stage++) {
+      case 0: {  // runs of one owner along the rows, numbered row-major (gval holds the run ids)
+        if (n > 0 && ncp) {
+          k_run_flags<<<nb(n), 256, 0, st>>>(S.gkey[kind], n, S.gw[kind], S.gval[kind]);
+          DMSC_LAUNCHED(1);
+          L(scan_exclusive_u32(S.gval[kind], n, S.gval[kind], soff, st));
+          L(cudaMemcpyAsync(&hbuf[0], soff, 4, cudaMemcpyDeviceToHost, st));
+        } else {
+          hbuf[0] = 0;
+        }
+        return true;
+      }
+      case 1: {  // the runs in owner order (stable: row-major within an owner); seeds pushed by cancelled extrema
+        nrun = hbuf[0];
+        const size_t R = nrun;
+        L(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * ncp, st));
+        if (R) {
+          // rkey ridx rstart rend len_s spos rpos + sort scratch (2 R); gbase (ncp)
+          L(cudaMallocAsync((void **)&runbuf, sizeof(uint32_t) * (9 * R + (size_t)ncp + 16), st));
+          if (e != cudaSuccess) return false;
+          uint32_t *rkey = runbuf, *ridx = runbuf + R, *rend = runbuf + 3 * R, *len_s = runbuf + 4 * R;
+          uint32_t *spos = runbuf + 5 * R, *tk = runbuf + 7 * R, *tv = runbuf + 8 * R, *gbase = runbuf + 9 * R;
+          rstart = runbuf + 2 * R;
+          rp = runbuf + 6 * R;
+          k_run_records<<<nb(n), 256, 0, st>>>(S.gkey[kind], n, S.gw[kind], S.gval[kind], rkey, rstart, rend);
+          k_iota_u32<<<nb(R), 256, 0, st>>>(R, ridx);
+          DMSC_LAUNCHED(2);
+          L(radix_sort_pairs(rkey, ridx, tk, tv, R, nbits_for(ncp + 1), st));
+          k_runs_sorted_len<<<nb(R), 256, 0, st>>>(R, (uint32_t)ncp, rkey, ridx, rstart, rend, len_s);
+          DMSC_LAUNCHED(1);
+          L(scan_exclusive_u32(len_s, R, spos, nullptr, st));
+          k_runs_group_base<<<nb(R), 256, 0, st>>>(R, (uint32_t)ncp, rkey, spos, gbase);
+          k_runs_place<<<nb(R), 256, 0, st>>>(R, (uint32_t)ncp, rkey, ridx, spos, len_s, gbase, rp, cnt);
+          DMSC_LAUNCHED(2);
+        }
+        hbuf[1] = 0;
+        if (!io.no_cancel) {  // a complex without boundary-cancelable points has no seeds
+          k_seed_count<<<nb(ncp), 256, 0, st>>>(a, kind, slen);
+          DMSC_LAUNCHED(1);
+          L(scan_exclusive_u32(slen, ncp, soff, soff + ncp, st));
+          L(cudaMemcpyAsync(&hbuf[1], soff + ncp, 4, cudaMemcpyDeviceToHost, st));
+          return true;
+        }
+        return step();  // nothing to wait for
+      }
+      case 2: {  // chains per saddle
+        ns = hbuf[1];
+        if ((long long)ns > S.nmax) { e = cudaErrorInvalidValue; return false; }
+        if (ns) {
+          k_seed_write<<<nb(ncp), 256, 0, st>>>(a, kind, soff, key, val);
+          DMSC_LAUNCHED(1);
+          L(radix_sort_pairs(key, val, kt, vt, ns, nbits_for(ncp), st));  // stable: pushers stay in index order
+        }
+        L(cudaMemsetAsync(scount, 0, sizeof(uint32_t) * ncp, st));
+        if (ns) {
+          k_seed_runs<<<nb(ns), 256, 0, st>>>(ns, (uint32_t)ncp, key, sstart);
+          k_run_len<<<nb(ns), 256, 0, st>>>(ns, (uint32_t)ncp, key, sstart, scount, 0);
+          DMSC_LAUNCHED(2);
+        }
+        c.hop_to = S.hop_to; c.hop_len = S.hop_len; c.jseg = S.jseg; c.nextd = S.nextd;
+        c.kc = kc; c.mc = mc; c.big = big; c.cbase = cbase; c.limit = io.limit;
+        k_chain_count<<<nb(ncp), 128, 0, st>>>(a, kind, SeedRuns{val, sstart, scount}, c);
+        DMSC_LAUNCHED(1);
+        L(scan_exclusive_u32(kc, ncp, cbase, cbase + ncp, st));
+        // chain slots: the exact count, or without seeds from cancelled extrema the
+        // bound of two chains per saddle (two own seeds, one successor each), with
+        // the unused slots zeroed -- saving a synchronisation
+        if (ns || !io.no_cancel) {
+          L(cudaMemcpyAsync(&hbuf[2], cbase + ncp, 4, cudaMemcpyDeviceToHost, st));
+          return true;
+        }
+        hbuf[2] = (uint32_t)std::min<long long>(2 * ncp, 0xFFFFFFF0ll);
+        return step();
+      }
+      case 3: {  // chain lengths, pieces, disc sizes
+        nch = hbuf[2];
+        c.cap = nch;
+        // per chain: cstart csaddle clen cnseg | csegoff cofs (nch + 1 each)
+        L(cudaMallocAsync((void **)&chain_buf, sizeof(uint32_t) * (6ull * nch + 8), st));
+        L(cudaMallocAsync((void **)&blocks, sizeof(uint4) * (2 * (size_t)nch + 2), st));
+        if (e != cudaSuccess) return false;
+        if (!ns && io.no_cancel) {
+          L(cudaMemsetAsync(chain_buf, 0, sizeof(uint32_t) * 4ull * nch, st));
+          L(cudaMemsetAsync(blocks, 0, sizeof(uint4) * 2ull * nch, st));
+        }
+        c.cstart = chain_buf; c.csaddle = chain_buf + nch; c.clen = chain_buf + 2 * nch; c.cnseg = chain_buf + 3 * nch;
+        c.csegoff = chain_buf + 4 * nch;      // nch + 1
+        c.cofs = chain_buf + 5 * nch + 1;     // nch + 1
+        c.blocks = blocks;
+        const SeedRuns sr{val, sstart, scount};
+        k_chain_len<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, slen);
+        k_saddle_disc_count<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, slen, io.limit);
+        k_add_counts<<<nb(ncp), 256, 0, st>>>((uint32_t)ncp, slen, cnt);
+        DMSC_LAUNCHED(3);
+        uint32_t *offs = kind ? io.ddoff : io.adoff;
+        L(scan_exclusive_u32(cnt, ncp, offs, offs + ncp, st));
+        L(scan_exclusive_u32(c.cnseg, nch, c.csegoff, c.csegoff + nch, st));
+        L(scan_exclusive_u32(c.clen, nch, c.cofs, c.cofs + nch, st));
+        L(cudaMemcpyAsync(&hbuf[3], offs + ncp, 4, cudaMemcpyDeviceToHost, st));
+        L(cudaMemcpyAsync(&hbuf[4], c.csegoff + nch, 4, cudaMemcpyDeviceToHost, st));
+        L(cudaMemcpyAsync(&hbuf[5], c.cofs + nch, 4, cudaMemcpyDeviceToHost, st));
+        return true;
+      }
+      case 4: {  // the cells
+        for (int q = 0; q < 3; ++q) tot[q] = hbuf[3 + q];
+        uint32_t *offs = kind ? io.ddoff : io.adoff;
+        DevBuf<uint32_t> *ob = kind ? io.ddisc : io.adisc;
+        L(ob->ensure((size_t)tot[0] + 1, st));
+        L(cudaMallocAsync((void **)&segs, sizeof(uint4) * ((size_t)tot[1] + 1), st));
+        L(cudaMallocAsync((void **)&tmp, sizeof(uint32_t) * ((size_t)tot[2] + 1), st));
+        if (e != cudaSuccess) return false;
+        c.segs = segs;
+        c.tmp = tmp;
+        const SeedRuns sr{val, sstart, scount};
+        if (nch) {
+          k_chain_segs<<<nb(nch), 128, 0, st>>>(nch, c);
+          DMSC_LAUNCHED(1);
+        }
+        if (tot[1]) {
+          k_seg_write<<<nb((tot[1] + 31) / 32 * 32), SEG_WARPS * 32, 0, st>>>(a, c, tot[1]);
+          DMSC_LAUNCHED(1);
+        }
+        k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c, offs);
+        k_level0<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, offs, ob->p);
+        k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);
+        DMSC_LAUNCHED(3);
+        if (nch) {
+          k_zip<<<nb(32ll * nch), 256, 0, st>>>(a, c, nch, ob->p, (unsigned long long)tot[0]);
+          DMSC_LAUNCHED(1);
+        }
+        if (n > 0 && nrun) {  // extremum discs of this kind
+          k_runs_scatter<<<nb(n), 256, 0, st>>>(a.g, kind, S.gkey[kind], n, S.gw[kind], (uint32_t)ncp, S.gval[kind], rp,
+                                                rstart, offs, ob->p);
+          DMSC_LAUNCHED(1);
+        }
+        release();
+        return false;
+      }
+    }
+    return false;
+  }
+};
 
+cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
+  DiscShared S;
+  DiscArgs &a = S.a;
+  a.g = io.g; a.codes = io.codes; a.labels = io.labels; a.ncp_ds = (uint32_t)io.ncp_ds; a.ncp = (uint32_t)io.ncp;
+  a.cellid = io.cellid; a.flags = io.flags; a.pair_idx = io.pair_idx;
+  a.aoff = io.aoff; a.asc = io.asc; a.doff = io.doff; a.des = io.des; a.status = io.status;
+  S.io = &io;
+  const long long ncp = io.ncp;
+  S.ncp = ncp;
+  const GridGeom &g = io.g;
+  const long long nV = (long long)((g.rx1 - g.rx0) / 2 + 1) * ((g.ry1 - g.ry0) / 2 + 1);
+  const long long nF = (long long)((g.rx1 - g.rx0) / 2) * ((g.ry1 - g.ry0) / 2);
+  const long long nmax = std::max(std::max(nV, nF), std::max(io.nasc, io.ndes)) + 1;
+  S.nmax = nmax;
+  S.gn[0] = nV; S.gn[1] = nF;
+  S.gw[0] = (g.rx1 - g.rx0) / 2 + 1; S.gw[1] = (g.rx1 - g.rx0) / 2;
+  const long long nE = 2ll * g.vnx * g.vny;  // edge ids of the ext window
+  const bool seeds = !io.no_cancel;
+  // shared words: redir (ncp) | owner keys and run ids 2 (nV + nF) | hops 2.75 nE
+  // per kind: cnt slen sstart scount (4 ncp) soff (ncp + 8) kc mc cbase (3 ncp + 1) big (ncp / 4 + 1)
+  //           seed sort 4 nmax (only with seeds) | pinned counts
+  const size_t kwords = (size_t)ncp * 8 + 16 + (size_t)ncp / 4 + 1 + (seeds ? 4 * (size_t)nmax : 0);
+  size_t words = (size_t)ncp + 8 + (size_t)(nV + nF) * 2 + 2 * (size_t)nE + (size_t)nE / 2 + (size_t)nE / 4 + 64 +
+                 2 * kwords;
+  uint32_t *buf = nullptr;
+  cudaError_t e = hops_attr();
+  if (e != cudaSuccess) return e;
+  if (!io.aux || !io.ev[0] || !io.ev[1]) return cudaErrorInvalidValue;
+  e = cudaMallocAsync((void **)&buf, sizeof(uint32_t) * words, st);
+  if (e != cudaSuccess) return e;
+  uint32_t *p = buf;
+  S.redir = p; p += ncp + 8;
+  S.gkey[0] = p; p += nV;
+  S.gkey[1] = p; p += nF;
+  S.gval[0] = p; p += nV;
+  S.gval[1] = p; p += nF;
+  S.hop_to = p; p += nE;
+  S.jseg = p; p += nE;
+  S.hop_len = (uint16_t *)p; p += nE / 2 + 1;
+  S.nextd = (uint8_t *)p; p += nE / 4 + 1;
+  DiscKind K[2];
+  for (int k = 0; k < 2; ++k) {
+    DiscKind &D = K[k];
+    D.kind = k;
+    D.st = k ? io.aux : st;
+    D.sh = &S;
+    D.hbuf = io.hcounts + 8 * k;
+    D.cnt = p; p += ncp;
+    D.slen = p; p += ncp;
+    D.sstart = p; p += ncp;
+    D.scount = p; p += ncp;
+    D.soff = p; p += ncp + 8;
+    D.kc = p; p += ncp;
+    D.mc = p; p += ncp;
+    D.cbase = p; p += ncp + 1;
+    D.big = (uint8_t *)p; p += ncp / 4 + 1;
+    if (seeds) {
+      D.key = p; p += nmax;
+      D.val = p; p += nmax;
+      D.kt = p; p += nmax;
+      D.vt = p; p += nmax;
+    }
+  }
+  auto L = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
   if (ncp) {
-    k_redir_init<<<nb(ncp), 256, 0, st>>>((uint32_t)ncp, redir);
+    k_redir_init<<<nb(ncp), 256, 0, st>>>((uint32_t)ncp, S.redir);
     DMSC_LAUNCHED(1);
-    if (!io.no_cancel) {
-      k_redir_saddles<<<nb(ncp), 256, 0, st>>>(a, redir);
+    if (seeds) {
+      k_redir_saddles<<<nb(ncp), 256, 0, st>>>(a, S.redir);
       DMSC_LAUNCHED(1);
     }
   }
   if (io.ev_hops[0]) L(cudaEventRecord(io.ev_hops[0], st));
-  k_disc_hops<<<dim3(g.ntx, g.nty), HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, hop_to, hop_len, jseg, nextd,
-                                                                        io.status);
+  k_disc_hops<<<dim3(g.ntx, g.nty), HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, S.hop_to, S.hop_len, S.jseg,
+                                                                        S.nextd, io.status);
   DMSC_LAUNCHED(1);
   if (io.ev_hops[1]) L(cudaEventRecord(io.ev_hops[1], st));
-  L(cudaMemsetAsync(acnt, 0, sizeof(uint32_t) * ncp * 2, st));
   // extremum discs: vertices -> minima (asc_disc), faces -> maxima (des_disc),
   // grouped by owner with a stable sort (row-major order is the append order)
   if (ncp) {
-    k_owner_final<<<nb(ncp), 256, 0, st>>>(a, redir, scount);  // scount is free until the saddle passes
-    k_disc_keys<<<nb(nV), 256, 0, st>>>(a, scount, gkey[0], gkey[1]);
+    k_owner_final<<<nb(ncp), 256, 0, st>>>(a, S.redir, K[0].scount);  // free until the saddle passes
+    k_disc_keys<<<nb(nV), 256, 0, st>>>(a, K[0].scount, S.gkey[0], S.gkey[1]);
     DMSC_LAUNCHED(2);
   }
-  // runs of one owner along the rows, numbered row-major (gval holds the run ids)
-  const int gw[2] = {(g.rx1 - g.rx0) / 2 + 1, (g.rx1 - g.rx0) / 2};
-  uint32_t nrun[2] = {0, 0};
-  for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind) {
-    const long long n = gn[kind];
-    if (n <= 0 || !ncp) continue;
-    k_run_flags<<<nb(n), 256, 0, st>>>(gkey[kind], n, gw[kind], gval[kind]);
-    DMSC_LAUNCHED(1);
-    L(scan_exclusive_u32(gval[kind], n, gval[kind], soff, st));
-    L(cudaMemcpyAsync(&nrun[kind], soff, 4, cudaMemcpyDeviceToHost, st));
+  // the des kind runs on the auxiliary stream once the shared part is done
+  L(cudaEventRecord(io.ev[0], st));
+  L(cudaStreamWaitEvent(io.aux, io.ev[0], 0));
+  if (e == cudaSuccess) {
+    bool more[2] = {true, true};
+    while (more[0] || more[1])
+      for (int k = 0; k < 2; ++k) {
+        if (!more[k]) continue;
+        more[k] = K[k].step();
+        if (more[k] && K[k].e == cudaSuccess) K[k].L(cudaStreamSynchronize(K[k].st));
+      }
+    for (int k = 0; k < 2; ++k) {
+      if (K[k].e != cudaSuccess && e == cudaSuccess) e = K[k].e;
+      K[k].release();
+    }
+    io.nadisc = K[0].tot[0];
+    io.nddisc = K[1].tot[0];
   }
-  L(cudaStreamSynchronize(st));
-  uint32_t *runbuf = nullptr, *rpos[2] = {nullptr, nullptr}, *rstart_k[2] = {nullptr, nullptr};
-  {
-    const size_t R0 = nrun[0], R1 = nrun[1];
-    // per kind: rkey ridx rstart rend len_s spos rpos + sort scratch (2 R); gbase (ncp)
-    L(cudaMallocAsync((void **)&runbuf, sizeof(uint32_t) * (9 * (R0 + R1) + (size_t)ncp + 16), st));
-  }
-  for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind) {
-    const long long n = gn[kind], R = nrun[kind];
-    if (n <= 0 || R == 0) continue;
-    uint32_t *base = runbuf + (kind ? 9 * (size_t)nrun[0] : 0);
-    uint32_t *rkey = base, *ridx = base + R, *rstart = base + 2 * R, *rend = base + 3 * R, *len_s = base + 4 * R;
-    uint32_t *spos = base + 5 * R, *rp = base + 6 * R, *tk = base + 7 * R, *tv = base + 8 * R;
-    uint32_t *gbase = runbuf + 9 * ((size_t)nrun[0] + nrun[1]);
-    k_run_records<<<nb(n), 256, 0, st>>>(gkey[kind], n, gw[kind], gval[kind], rkey, rstart, rend);
-    k_iota_u32<<<nb(R), 256, 0, st>>>(R, ridx);
-    DMSC_LAUNCHED(2);
-    L(radix_sort_pairs(rkey, ridx, tk, tv, R, nbits_for(ncp + 1), st));  // stable: runs stay row-major
-    k_runs_sorted_len<<<nb(R), 256, 0, st>>>(R, (uint32_t)ncp, rkey, ridx, rstart, rend, len_s);
-    DMSC_LAUNCHED(1);
-    L(scan_exclusive_u32(len_s, R, spos, nullptr, st));
-    k_runs_group_base<<<nb(R), 256, 0, st>>>(R, (uint32_t)ncp, rkey, spos, gbase);
-    k_runs_place<<<nb(R), 256, 0, st>>>(R, (uint32_t)ncp, rkey, ridx, spos, len_s, gbase, rp, kind ? dcnt : acnt);
-    DMSC_LAUNCHED(2);
-    rpos[kind] = rp;
-    rstart_k[kind] = rstart;
-  }
-  // saddle discs
-  for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind) {
-    // seeds pushed by cancelled extrema: asc from maxima (via des), des from minima (via asc);
-    // a complex without boundary-cancelable points has none
-    uint32_t ns = 0;
-    if (!io.no_cancel) {
-      k_seed_count<<<nb(ncp), 256, 0, st>>>(a, kind, slen);
-      DMSC_LAUNCHED(1);
-      L(scan_exclusive_u32(slen, ncp, soff, soff + ncp, st));
-      L(cudaMemcpyAsync(&ns, soff + ncp, 4, cudaMemcpyDeviceToHost, st));
-      L(cudaStreamSynchronize(st));
-    }
-    if (e != cudaSuccess) break;
-    if ((long long)ns > nmax) { e = cudaErrorInvalidValue; break; }
-    if (ns) {
-      k_seed_write<<<nb(ncp), 256, 0, st>>>(a, kind, soff, key, val);
-      DMSC_LAUNCHED(1);
-      L(radix_sort_pairs(key, val, kt, vt, ns, nbits_for(ncp), st));  // stable: pushers stay in index order
-    }
-    L(cudaMemsetAsync(scount, 0, sizeof(uint32_t) * ncp, st));
-    if (ns) {
-      k_seed_runs<<<nb(ns), 256, 0, st>>>(ns, (uint32_t)ncp, key, sstart);
-      k_run_len<<<nb(ns), 256, 0, st>>>(ns, (uint32_t)ncp, key, sstart, scount, 0);
-      DMSC_LAUNCHED(2);
-    }
-    SeedRuns sr{val, sstart, scount};
-    ChainArgs c{};
-    c.hop_to = hop_to; c.hop_len = hop_len; c.jseg = jseg; c.nextd = nextd;
-    c.kc = kc; c.mc = mc; c.big = big; c.cbase = cbase; c.limit = io.limit;
-    k_chain_count<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c);
-    DMSC_LAUNCHED(1);
-    L(scan_exclusive_u32(kc, ncp, cbase, cbase + ncp, st));
-    // chain slots: the exact count, or without seeds from cancelled extrema the
-    // bound of two chains per saddle (two own seeds, one successor each), with
-    // the unused slots zeroed -- saving a synchronisation
-    uint32_t nch = 0;
-    if (ns || !io.no_cancel) {
-      L(cudaMemcpyAsync(&nch, cbase + ncp, 4, cudaMemcpyDeviceToHost, st));
-      L(cudaStreamSynchronize(st));
-    } else {
-      nch = (uint32_t)std::min<long long>(2 * ncp, 0xFFFFFFF0ll);
-    }
-    if (e != cudaSuccess) break;
-    c.cap = nch;
-    // per chain: cstart csaddle clen cnseg | csegoff cofs (nch + 1 each)
-    L(cudaMallocAsync((void **)&chain_buf, sizeof(uint32_t) * (6ull * nch + 8), st));
-    L(cudaMallocAsync((void **)&blocks, sizeof(uint4) * (2 * (size_t)nch + 2), st));
-    if (e != cudaSuccess) break;
-    if (!ns && io.no_cancel) {
-      L(cudaMemsetAsync(chain_buf, 0, sizeof(uint32_t) * 4ull * nch, st));
-      L(cudaMemsetAsync(blocks, 0, sizeof(uint4) * 2ull * nch, st));
-    }
-    c.cstart = chain_buf; c.csaddle = chain_buf + nch; c.clen = chain_buf + 2 * nch; c.cnseg = chain_buf + 3 * nch;
-    c.csegoff = chain_buf + 4 * nch;      // nch + 1
-    c.cofs = chain_buf + 5 * nch + 1;     // nch + 1
-    c.blocks = blocks;
-    k_chain_len<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, slen);
-    k_saddle_disc_count<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, slen, io.limit);
-    k_add_counts<<<nb(ncp), 256, 0, st>>>((uint32_t)ncp, slen, kind ? dcnt : acnt);
-    DMSC_LAUNCHED(3);
-    uint32_t *offs = kind ? io.ddoff : io.adoff;
-    L(scan_exclusive_u32(kind ? dcnt : acnt, ncp, offs, offs + ncp, st));
-    L(scan_exclusive_u32(c.cnseg, nch, c.csegoff, c.csegoff + nch, st));
-    L(scan_exclusive_u32(c.clen, nch, c.cofs, c.cofs + nch, st));
-    uint32_t tot[3] = {0, 0, 0};
-    L(cudaMemcpyAsync(&tot[0], offs + ncp, 4, cudaMemcpyDeviceToHost, st));
-    L(cudaMemcpyAsync(&tot[1], c.csegoff + nch, 4, cudaMemcpyDeviceToHost, st));
-    L(cudaMemcpyAsync(&tot[2], c.cofs + nch, 4, cudaMemcpyDeviceToHost, st));
-    L(cudaStreamSynchronize(st));
-    if (e != cudaSuccess) break;
-    DevBuf<uint32_t> *ob = kind ? io.ddisc : io.adisc;
-    L(ob->ensure((size_t)tot[0] + 1, st));
-    L(cudaMallocAsync((void **)&segs, sizeof(uint4) * ((size_t)tot[1] + 1), st));
-    L(cudaMallocAsync((void **)&tmp, sizeof(uint32_t) * ((size_t)tot[2] + 1), st));
-    if (e != cudaSuccess) break;
-    c.segs = segs;
-    c.tmp = tmp;
-    if (nch) {
-      k_chain_segs<<<nb(nch), 128, 0, st>>>(nch, c);
-      DMSC_LAUNCHED(1);
-    }
-    if (tot[1]) {
-      k_seg_write<<<nb((tot[1] + 31) / 32 * 32), SEG_WARPS * 32, 0, st>>>(a, c, tot[1]);
-      DMSC_LAUNCHED(1);
-    }
-    k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c, offs);
-    k_level0<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, offs, ob->p);
-    k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);
-    DMSC_LAUNCHED(3);
-    if (nch) {
-      k_zip<<<nb(32ll * nch), 256, 0, st>>>(a, c, nch, ob->p, (unsigned long long)tot[0]);
-      DMSC_LAUNCHED(1);
-    }
-    const long long n = gn[kind];
-    if (n > 0 && nrun[kind]) {  // extremum discs of this kind
-      k_runs_scatter<<<nb(n), 256, 0, st>>>(g, kind, gkey[kind], n, gw[kind], (uint32_t)ncp, gval[kind], rpos[kind],
-                                            rstart_k[kind], offs, ob->p);
-      DMSC_LAUNCHED(1);
-    }
-    (kind ? io.nddisc : io.nadisc) = tot[0];
-    release();
-  }
-  release();
-  if (runbuf) cudaFreeAsync(runbuf, st);
+  // the caller's stream waits for the auxiliary one
+  cudaEventRecord(io.ev[1], io.aux);
+  cudaStreamWaitEvent(st, io.ev[1], 0);
   cudaFreeAsync(buf, st);
   if (e == cudaSuccess) e = cudaGetLastError();
   return e;

@@ -50,6 +50,11 @@ static int status_to_error(uint32_t st) {
   return fail(DMSC_ERR_INVARIANT, "device invariant violated (status " + std::to_string(st) + ")");
 }
 
+namespace {
+uint32_t *pin_take();  // pinned 16-word slots (below)
+void pin_give(uint32_t *p);
+}  // namespace
+
 extern "C" {
 
 const char *dmsc_last_error(void) { return g_err.c_str(); }
@@ -409,6 +414,14 @@ int dmsc_dataset_fill_discs(dmsc_dataset *d, dmsc_msc *m, void *stream) {
   // a gradient path visits each cell at most once: bounds every chain of a disc
   io.limit = (unsigned long long)(d->g.cx + 1) * (d->g.cy + 1) + 16;
   io.no_cancel = !m->any_bcancel;
+  if (!d->disc_aux) CK(cudaStreamCreateWithFlags(&d->disc_aux, cudaStreamNonBlocking));
+  for (auto &ev : d->disc_ev)
+    if (!ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  if (!d->host_disc && !(d->host_disc = pin_take())) return fail(DMSC_ERR_OOM, "pinned count slot");
+  io.aux = d->disc_aux;
+  io.ev[0] = d->disc_ev[0];
+  io.ev[1] = d->disc_ev[1];
+  io.hcounts = d->host_disc;
   const bool tm = d->ctx->timing && d->ev_ready;
   if (tm) {
     io.ev_hops[0] = d->ev[7];
@@ -496,9 +509,10 @@ int dmsc_kernel_launches(uint64_t *count) {
 // ---------------------------------------------------------------------------
 // member functions of the handle types
 // ---------------------------------------------------------------------------
-// Pinned 16-byte slots for the status read-back of datasets, carved from
-// pinned blocks that live as long as the process (pinning a small buffer per
-// dataset would serialise on the driver when many pieces start at once).
+// Pinned 64-byte slots for the status and count read-backs of datasets,
+// carved from pinned blocks that live as long as the process (pinning a small
+// buffer per dataset would serialise on the driver when many pieces start at
+// once).
 namespace {
 std::mutex &pin_mu() {
   static std::mutex *m = new std::mutex;
@@ -512,10 +526,10 @@ uint32_t *pin_take() {
   std::lock_guard<std::mutex> lk(pin_mu());
   auto &f = pin_free();
   if (f.empty()) {
-    constexpr int SLOTS = 1024;
+    constexpr int SLOTS = 1024, WORDS = 16;
     uint32_t *blk = nullptr;
-    if (cudaMallocHost((void **)&blk, sizeof(uint32_t) * 4 * SLOTS) != cudaSuccess) return nullptr;
-    for (int i = SLOTS - 1; i >= 0; --i) f.push_back(blk + 4 * i);
+    if (cudaMallocHost((void **)&blk, sizeof(uint32_t) * WORDS * SLOTS) != cudaSuccess) return nullptr;
+    for (int i = SLOTS - 1; i >= 0; --i) f.push_back(blk + WORDS * i);
   }
   uint32_t *p = f.back();
   f.pop_back();
@@ -554,6 +568,10 @@ int dmsc_dataset::alloc_cps(long long n, cudaStream_t st) {
 
 dmsc_dataset::~dmsc_dataset() {
   if (host_scal) pin_give(host_scal);
+  if (host_disc) pin_give(host_disc);
+  if (disc_aux) cudaStreamDestroy(disc_aux);
+  for (auto &e : disc_ev)
+    if (e) cudaEventDestroy(e);
   if (ev_ready)
     for (auto &e : ev) cudaEventDestroy(e);
 }

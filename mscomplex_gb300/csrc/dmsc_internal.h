@@ -140,6 +140,11 @@ struct DiscIO {
   cudaEvent_t ev_hops[2] = {nullptr, nullptr};  // recorded around the hop kernel when set
   bool no_cancel = false;  // the complex has no boundary-cancelable critical point
   long long nadisc = 0, nddisc = 0;
+  // the des discs run on `aux` beside the asc discs on the caller's stream;
+  // ev[0]/ev[1] order the two streams; hcounts: 16 words of pinned host memory
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  uint32_t *hcounts = nullptr;
 };
 cudaError_t fill_discs(DiscIO &io, cudaStream_t st);
 

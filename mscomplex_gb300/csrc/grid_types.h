@@ -71,6 +71,9 @@ struct dmsc_dataset {
   DevBuf<uint64_t> table;      // border table
   DevBuf<uint32_t> scal;       // [0] status word, [1] number of critical points
   uint32_t *host_scal = nullptr;
+  uint32_t *host_disc = nullptr;  // pinned counts of fill_discs (16 words)
+  cudaStream_t disc_aux = nullptr;  // fill_discs' second stream and its two ordering events
+  cudaEvent_t disc_ev[2] = {nullptr, nullptr};
   long long cap = 0;           // capacity of the cp arrays
   long long ncp = 0;
   bool worked = false;
