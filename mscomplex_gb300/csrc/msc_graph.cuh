@@ -51,7 +51,15 @@ struct Graph {
   __host__ __device__ __forceinline__ uint2 *runs(uint32_t l) const { return L.pool + L.off[l]; }
   __host__ __device__ uint32_t find_run(uint32_t l, uint32_t x) const {  // first run with value >= x
     const uint2 *p = runs(l);
-    uint32_t lo = 0, hi = L.nrun[l];
+    const uint32_t n = L.nrun[l];
+    if (n <= 8) {  // short list: the runs below x counted from independent loads (one memory round trip)
+      uint32_t i = 0;
+#pragma unroll
+      for (uint32_t k = 0; k < 8; ++k)
+        if (k < n && p[k].x < x) ++i;
+      return i;
+    }
+    uint32_t lo = 0, hi = n;
     while (lo < hi) { uint32_t m = (lo + hi) >> 1; if (p[m].x < x) lo = m + 1; else hi = m; }
     return lo;
   }

@@ -359,7 +359,16 @@ int dmsc_pipeline_run(dmsc_ctx *ctx, const float *heights, int64_t pitch, int on
 
 int dmsc_pipeline_destroy(dmsc_pipeline *p) {
   if (!p) return perr(DMSC_ERR_BAD_ARG, "pipeline is null");
+  const int device = p->ctx->device;
+  cudaSetDevice(device);
   delete p;
+  // A pipeline over a large field leaves tens of GB of differently sized
+  // blocks in the stream-ordered pool, which the next one cannot always
+  // reuse; keep a working set cached and hand the rest back.
+  cudaMemPool_t pool;
+  size_t total = 0, free_b = 0;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess && cudaMemGetInfo(&free_b, &total) == cudaSuccess)
+    cudaMemPoolTrimTo(pool, total / 2);
   return DMSC_OK;
 }
 
