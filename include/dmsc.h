@@ -277,6 +277,10 @@ int dmsc_set_timing(dmsc_ctx *ctx, int enable);
  * arcs, [4] connectivity CSR; and of its last fill_discs: [5] the hop kernel,
  * [6] the whole pass.  Writes min(n, 7) floats. */
 int dmsc_dataset_stage_times(dmsc_dataset *ds, float *ms, int n);
+/* The device's stream-ordered memory pool, which holds the library's device
+ * buffers: bytes [0] reserved now, [1] reserved at most, [2] in use now,
+ * [3] in use at most. */
+int dmsc_pool_stats(dmsc_ctx *ctx, int64_t stats[4]);
 /* Kernels launched by this library so far in this process. */
 int dmsc_kernel_launches(uint64_t *count);
 

@@ -60,6 +60,7 @@ SIGNATURES = {
     "dmsc_batch_totals": ([_vp, _vp], _i32),
     "dmsc_set_merge_parallel_min": ([_vp, _i64], _i32),
     "dmsc_pipeline_merge_times": ([_vp, _vp], _i32),
+    "dmsc_pool_stats": ([_vp, _vp], _i32),
     "dmsc_batch_grid_status": ([_vp, _i64, _vp, C.c_char_p, _i32], _i32),
     "dmsc_batch_export_all": ([_vp] + [_vp] * 11 + [_vp], _i32),
     "dmsc_server_create": ([_vp, _i64, _i32, _i32, _i64, _vp], _i32),

@@ -328,6 +328,20 @@ int dmsc_set_timing(dmsc_ctx *ctx, int enable) {
   return DMSC_OK;
 }
 
+int dmsc_pool_stats(dmsc_ctx *ctx, int64_t stats[4]) {
+  if (!ctx || !stats) return fail(DMSC_ERR_BAD_ARG, "null argument");
+  cudaMemPool_t pool;
+  CK(cudaDeviceGetDefaultMemPool(&pool, ctx->device));
+  const cudaMemPoolAttr a[4] = {cudaMemPoolAttrReservedMemCurrent, cudaMemPoolAttrReservedMemHigh,
+                                cudaMemPoolAttrUsedMemCurrent, cudaMemPoolAttrUsedMemHigh};
+  for (int i = 0; i < 4; ++i) {
+    uint64_t v = 0;
+    CK(cudaMemPoolGetAttribute(pool, a[i], &v));
+    stats[i] = (int64_t)v;
+  }
+  return DMSC_OK;
+}
+
 int dmsc_set_merge_parallel_min(dmsc_ctx *ctx, int64_t min_cps) {
   if (!ctx || min_cps < 0) return fail(DMSC_ERR_BAD_ARG, "ctx is null or min_cps negative");
   ctx->merge_parallel_min = min_cps;

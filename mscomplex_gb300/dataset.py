@@ -37,6 +37,12 @@ class Context:
     def set_timing(self, enable: bool = True):
         check(self.lib.dmsc_set_timing(self.h, int(enable)))
 
+    def pool_stats(self) -> dict:
+        """Bytes of the device's stream-ordered pool (the library's buffers)."""
+        a = np.zeros(4, np.int64)
+        check(self.lib.dmsc_pool_stats(self.h, _ptr(a)))
+        return dict(zip(("reserved", "reserved_high", "used", "used_high"), (int(v) for v in a)))
+
     def set_merge_parallel_min(self, min_cps: int):
         """Pipeline tree levels whose largest merge involves at least min_cps
         critical points take the parallel merges (default 2048)."""
