@@ -54,9 +54,19 @@ struct SimpArgs {
   unsigned long long *stats;  // [0] pushes [1] pops [2] cancels [3] ops [4] status
 };
 
+// The top HEAP_TOP entries of the heap (its first 14 levels, which every pop
+// walks) live in shared memory; the rest in global memory.  Same layout and
+// the same operations, only the storage of those indices differs.
+constexpr unsigned long long HEAP_TOP = (1u << 14) - 1;
+constexpr size_t HEAP_TOP_BYTES = sizeof(HeapEnt) * HEAP_TOP;
+
 struct Simp {
   SimpArgs A;
   unsigned long long nheap = 0, nres = 0, ncanc = 0;
+  HeapEnt *top = nullptr;         // shared-memory part of the heap (null: all in global memory)
+  unsigned long long ntop = 0;    // indices below ntop are in `top`
+
+  __host__ __device__ __forceinline__ HeapEnt &H(unsigned long long i) { return i < ntop ? top[i] : A.heap[i]; }
 
   __host__ __device__ __forceinline__ bool on_boundary(uint32_t k) const {  // m_rect.isOnBoundry
     uint32_t c = A.G.cellid[k];
@@ -72,47 +82,45 @@ struct Simp {
   // ---- heap (binary heap of the standard library, comparator d1 > d2) ----
   __host__ __device__ __forceinline__ static bool comp(const HeapEnt &x, const HeapEnt &y) { return x.d > y.d; }
   __host__ __device__ void push_at(unsigned long long hole, unsigned long long topi, HeapEnt val) {
-    HeapEnt *v = A.heap;
     unsigned long long parent = (hole - 1) / 2;
-    while (hole > topi && comp(v[parent], val)) {
-      v[hole] = v[parent];
+    while (hole > topi && comp(H(parent), val)) {
+      H(hole) = H(parent);
       hole = parent;
       parent = (hole - 1) / 2;
     }
-    v[hole] = val;
+    H(hole) = val;
   }
   __host__ __device__ void push(uint32_t a, uint32_t b) {
     if (nheap >= A.heap_cap) { A.G.fail = true; return; }
     HeapEnt x{pers(a, b), a, b};
-    A.heap[nheap] = x;
+    H(nheap) = x;
     push_at(nheap, 0, x);
     ++nheap;
     ++A.stats[0];
   }
   __host__ __device__ HeapEnt pop() {
-    HeapEnt *v = A.heap;
-    HeapEnt top = v[0];
+    HeapEnt first = H(0);
     if (nheap > 1) {
       unsigned long long len = nheap - 1;
-      HeapEnt val = v[len];
-      v[len] = v[0];
+      HeapEnt val = H(len);
+      H(len) = H(0);
       unsigned long long hole = 0, second = 0;
       while (second < (len - 1) / 2) {
         second = 2 * (second + 1);
-        if (comp(v[second], v[second - 1])) second--;
-        v[hole] = v[second];
+        if (comp(H(second), H(second - 1))) second--;
+        H(hole) = H(second);
         hole = second;
       }
       if ((len & 1) == 0 && second == (len - 2) / 2) {
         second = 2 * (second + 1);
-        v[hole] = v[second - 1];
+        H(hole) = H(second - 1);
         hole = second - 1;
       }
       push_at(hole, 0, val);
     }
     --nheap;
     ++A.stats[1];
-    return top;
+    return first;
   }
 
   // simplify (grid_mscomplex.cpp:384-512) followed by un_simplify (:514-526)
@@ -191,9 +199,12 @@ struct Simp {
 };
 
 __global__ void k_simplify(SimpArgs a) {
+  extern __shared__ HeapEnt heap_top[];
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   Simp s;
   s.A = a;
+  s.top = heap_top;
+  s.ntop = HEAP_TOP;
   s.run();
   a.stats[3] = s.A.G.ops;
   if (s.A.G.fail) a.stats[4] |= ST_SIMPLIFY_LIMIT;
@@ -309,7 +320,10 @@ cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st) {
     k_lists_from_csr<<<blocks_for(ncp), 256, 0, st>>>(ncp, io.aoff, io.asc, io.doff, io.des, des_base, G.L.off,
                                                        G.L.nrun, G.L.cap, G.L.total, G.L.pool);
     DMSC_LAUNCHED(1);
-    k_simplify<<<1, 32, 0, st>>>(a);
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_simplify, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)HEAP_TOP_BYTES);
+    if (attr != cudaSuccess) return attr;
+    k_simplify<<<1, 32, HEAP_TOP_BYTES, st>>>(a);
     DMSC_LAUNCHED(1);
   }
   e = cudaMemcpyAsync(io.host_stats, a.stats, sizeof(unsigned long long) * 5, cudaMemcpyDeviceToHost, st);
@@ -356,10 +370,13 @@ void simplify_release(SimplifyIO &io, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 // batches: one block per complex to simplify, all in one launch
 // ---------------------------------------------------------------------------
-__global__ void k_simplify_batch(SimpArgs *args, int n) {
+__global__ void k_simplify_batch(SimpArgs *args, int n, unsigned ntop) {
+  extern __shared__ HeapEnt heap_top[];
   if (threadIdx.x != 0 || blockIdx.x >= (unsigned)n) return;
   Simp s;
   s.A = args[blockIdx.x];
+  s.top = heap_top;
+  s.ntop = ntop;
   s.run();
   s.A.stats[3] = s.A.G.ops;
   if (s.A.G.fail) s.A.stats[4] |= ST_SIMPLIFY_LIMIT;
@@ -467,7 +484,13 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
   }
   if (e == cudaSuccess && ns) e = cudaMemcpyAsync(w->dargs, args.data(), sizeof(SimpArgs) * ns, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && ns) {
-    k_simplify_batch<<<ns, 32, 0, st>>>(w->dargs, ns);
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_simplify_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)HEAP_TOP_BYTES);
+    if (attr != cudaSuccess) return attr;
+    // one grid per SM can keep 14 heap levels in shared memory; more grids
+    // than SMs keep 12, so that four fit on an SM and all start at once
+    const unsigned ntop = ns <= 152 ? (unsigned)HEAP_TOP : (1u << 12) - 1;
+    k_simplify_batch<<<ns, 32, sizeof(HeapEnt) * ntop, st>>>(w->dargs, ns, ntop);
     DMSC_LAUNCHED(1);
     e = cudaGetLastError();
   }
