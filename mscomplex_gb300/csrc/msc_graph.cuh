@@ -26,6 +26,34 @@ struct Lists {  // list 2*cp = asc, 2*cp+1 = des
   unsigned long long top, pool_cap;
 };
 
+// Moves n runs from src to dst (the ranges may overlap), eight at a time:
+// the eight loads of a group are issued before its stores, so one thread
+// waits for one memory round trip per group instead of one per run.
+__host__ __device__ __forceinline__ void move_runs(uint2 *dst, const uint2 *src, unsigned long long n) {
+  if (n == 0 || dst == src) return;
+  if (dst < src) {  // forward
+    unsigned long long i = 0;
+    for (; i + 8 <= n; i += 8) {
+      uint2 t[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) t[k] = src[i + k];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) dst[i + k] = t[k];
+    }
+    for (; i < n; ++i) dst[i] = src[i];
+  } else {  // backward
+    unsigned long long i = n;
+    for (; i >= 8; i -= 8) {
+      uint2 t[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) t[k] = src[i - 8 + k];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) dst[i - 8 + k] = t[k];
+    }
+    for (; i > 0; --i) dst[i - 1] = src[i - 1];
+  }
+}
+
 struct Graph {
   uint32_t ncp;
   uint32_t *cellid;
@@ -74,7 +102,7 @@ struct Graph {
     while (nc < need) nc *= 2;
     if (L.top + nc > L.pool_cap) { fail = true; return false; }
     uint2 *src = runs(l), *dst = L.pool + L.top;
-    for (uint32_t i = 0; i < L.nrun[l]; ++i) dst[i] = src[i];
+    move_runs(dst, src, L.nrun[l]);
     L.off[l] = (uint32_t)L.top;
     L.cap[l] = nc;
     L.top += nc;
@@ -89,7 +117,7 @@ struct Graph {
     } else {
       if (!reserve(l, n + 1)) return;
       uint2 *p = runs(l);
-      for (uint32_t k = n; k > i; --k) p[k] = p[k - 1];
+      move_runs(p + i + 1, p + i, n - i);
       p[i] = make_uint2(x, c);
       L.nrun[l] = n + 1;
       tick(n - i);
@@ -102,7 +130,7 @@ struct Graph {
     if (i >= n || runs(l)[i].x != x) return;
     uint2 *p = runs(l);
     L.total[l] -= p[i].y;
-    for (uint32_t k = i + 1; k < n; ++k) p[k - 1] = p[k];
+    move_runs(p + i, p + i + 1, n - i - 1);
     L.nrun[l] = n - 1;
     tick(n - i);
   }
@@ -140,7 +168,7 @@ struct Graph {
     }
     if (tot > 0xffffffffull || m > 0xffffffffull || !reserve(l, (uint32_t)m)) { fail = true; return false; }
     uint2 *p = runs(l);
-    for (unsigned long long u = 0; u < m; ++u) p[u] = tmp[u];
+    move_runs(p, tmp, m);
     L.nrun[l] = (uint32_t)m;
     L.total[l] = (uint32_t)tot;
     return true;

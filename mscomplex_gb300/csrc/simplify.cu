@@ -52,6 +52,11 @@ struct SimpArgs {
   int rx0, ry0, rx1, ry1;  // m_rect of the complex (cell coordinates)
   double tresh;
   unsigned long long *stats;  // [0] pushes [1] pops [2] cancels [3] ops [4] status
+  // the complex's CSR lists (offsets may be based anywhere) and the entries of
+  // its first pushes, one per des arc in that order (k_simp_prep)
+  const uint32_t *aoff, *asc, *doff, *des;
+  HeapEnt *init;
+  unsigned long long ninit;
 };
 
 // The top HEAP_TOP entries of the heap (its first 14 levels, which every pop
@@ -90,14 +95,14 @@ struct Simp {
     }
     H(hole) = val;
   }
-  __host__ __device__ void push(uint32_t a, uint32_t b) {
+  __host__ __device__ void push_ent(const HeapEnt &x) {
     if (nheap >= A.heap_cap) { A.G.fail = true; return; }
-    HeapEnt x{pers(a, b), a, b};
     H(nheap) = x;
     push_at(nheap, 0, x);
     ++nheap;
     ++A.stats[0];
   }
+  __host__ __device__ void push(uint32_t a, uint32_t b) { push_ent(HeapEnt{pers(a, b), a, b}); }
   __host__ __device__ HeapEnt pop() {
     HeapEnt first = H(0);
     if (nheap > 1) {
@@ -127,23 +132,17 @@ struct Simp {
   __host__ __device__ void run() {
     Graph &G = A.G;
     const uint32_t n = G.ncp;
+    // (:396-428) the strangulation marks and the entries of the first pushes
+    // come from k_simp_prep; the value range and the pushes, in the
+    // reference's order, here
     float max_val = 1.17549435e-38f;  // std::numeric_limits<float>::min(), as in the reference (:399)
     float min_val = 3.40282347e+38f;
-    for (uint32_t i = 0; i < n && !G.fail; ++i) {
-      if (G.dim(i) == 1) {
-        for (int j = 0; j < 2; ++j) {
-          uint32_t l = 2 * i + j;
-          if (G.L.total[l] != 2) continue;
-          if (G.runs(l)[0].y == 2) G.flags[i] |= F_STRANG;  // both elements equal
-        }
-      }
-      float f = A.fn[i];
+    for (uint32_t i = 0; i < n; ++i) {
+      const float f = A.fn[i];
       max_val = (max_val < f) ? f : max_val;  // std::max
       min_val = (f < min_val) ? f : min_val;  // std::min
-      const uint32_t ld = 2 * i + 1;
-      for (uint32_t k = 0; k < G.L.nrun[ld] && !G.fail; ++k)
-        for (uint32_t c = 0; c < G.runs(ld)[k].y && !G.fail; ++c) push(i, G.runs(ld)[k].x);
     }
+    for (unsigned long long q = 0; q < A.ninit && !G.fail; ++q) push_ent(A.init[q]);
     const float max_persistence = fsub_rn(max_val, min_val);
     while (nheap != 0 && !G.fail) {
       if (!G.tick()) break;
@@ -197,6 +196,25 @@ struct Simp {
     }
   }
 };
+
+// In parallel, per critical point of args[blockIdx.y]: the strangulation
+// mark of a saddle whose asc or des multiset holds one point twice (:404-417),
+// and the heap entries of its des arcs, at their places in the push order.
+__global__ void k_simp_prep(SimpArgs *args) {
+  SimpArgs &A = args[blockIdx.y];
+  const uint32_t n = A.G.ncp, base = A.doff[0];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (A.G.dim(i) == 1) {
+      if ((A.aoff[i + 1] - A.aoff[i] == 2 && A.asc[A.aoff[i]] == A.asc[A.aoff[i] + 1]) ||
+          (A.doff[i + 1] - A.doff[i] == 2 && A.des[A.doff[i]] == A.des[A.doff[i] + 1]))
+        A.G.flags[i] |= F_STRANG;
+    }
+    for (uint32_t q = A.doff[i]; q < A.doff[i + 1]; ++q) {
+      const uint32_t b = A.des[q];
+      A.init[q - base] = HeapEnt{b < n ? fabsf(fsub_rn(A.fn[b], A.fn[i])) : 0.0f, i, b};
+    }
+  }
+}
 
 __global__ void k_simplify(SimpArgs a) {
   extern __shared__ HeapEnt heap_top[];
@@ -273,7 +291,8 @@ cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st) {
   size_t sizes[] = {sizeof(uint32_t) * 2 * ncp, sizeof(uint32_t) * 2 * ncp, sizeof(uint32_t) * 2 * ncp,
                     sizeof(uint32_t) * 2 * ncp, sizeof(uint2) * pool_cap, sizeof(uint2) * tmp_cap, sizeof(HeapEnt) * heap_cap,
                     sizeof(uint2) * heap_cap, sizeof(uint2) * (ncp + 1), sizeof(unsigned long long) * 8,
-                    sizeof(uint8_t) * (ncp + 1), sizeof(uint32_t) * (ncp + 1), sizeof(uint32_t) * (ncp + 1)};
+                    sizeof(uint8_t) * (ncp + 1), sizeof(uint32_t) * (ncp + 1), sizeof(uint32_t) * (ncp + 1),
+                    sizeof(HeapEnt) * ((size_t)io.ndes + 1), sizeof(SimpArgs)};
   size_t bytes = 0;
   for (size_t z : sizes) bytes += rnd(z);
   SimplifyWork *w = new SimplifyWork;
@@ -305,6 +324,10 @@ cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st) {
   G.flags = (uint8_t *)take();
   G.pair_idx = (uint32_t *)take();
   w->lens = (uint32_t *)take();
+  a.init = (HeapEnt *)take();
+  a.ninit = (unsigned long long)io.ndes;
+  a.aoff = io.aoff; a.asc = io.asc; a.doff = io.doff; a.des = io.des;
+  SimpArgs *dargs = (SimpArgs *)take();
   w->flags_in = io.flags;
   w->pair_in = io.pair_idx;
   a.rx0 = io.rect[0]; a.ry0 = io.rect[1]; a.rx1 = io.rect[2]; a.ry1 = io.rect[3];
@@ -320,11 +343,14 @@ cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st) {
     k_lists_from_csr<<<blocks_for(ncp), 256, 0, st>>>(ncp, io.aoff, io.asc, io.doff, io.des, des_base, G.L.off,
                                                        G.L.nrun, G.L.cap, G.L.total, G.L.pool);
     DMSC_LAUNCHED(1);
+    e = cudaMemcpyAsync(dargs, &a, sizeof(SimpArgs), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    k_simp_prep<<<blocks_for(ncp), 256, 0, st>>>(dargs);
     static const cudaError_t attr =
         cudaFuncSetAttribute(k_simplify, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)HEAP_TOP_BYTES);
     if (attr != cudaSuccess) return attr;
     k_simplify<<<1, 32, HEAP_TOP_BYTES, st>>>(a);
-    DMSC_LAUNCHED(1);
+    DMSC_LAUNCHED(2);
   }
   e = cudaMemcpyAsync(io.host_stats, a.stats, sizeof(unsigned long long) * 5, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -397,7 +423,7 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
   const unsigned long long base_top = des_base + (unsigned long long)io.ndes + 4ull * ncp;
   // per simplified grid: pool growth region, heap, resubmits, cancellations, scratch runs
   std::vector<int> which;
-  unsigned long long grow = 0, heap = 0, canc = 0, tmp = 0;
+  unsigned long long grow = 0, heap = 0, canc = 0, tmp = 0, init = 0;
   const unsigned long long sc = io.scale ? io.scale : 1;
   auto grow_of = [&](unsigned long long na, unsigned long long nd, unsigned long long n) {
     return sc * (4 * (na + nd + 8 * n) + 16384);
@@ -413,6 +439,7 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
     heap += heap_of(nd);
     canc += n + 1;
     tmp += tmp_of(na, nd);
+    init += nd + 1;
   }
   const unsigned long long pool_cap = base_top + grow;
   if (pool_cap > 0xffffffffull) return cudaErrorInvalidValue;  // list offsets are 32-bit
@@ -421,7 +448,7 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
   const size_t sizes[] = {4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * (ncp + 1),
                           sizeof(uint2) * pool_cap, sizeof(uint2) * tmp, sizeof(HeapEnt) * heap, sizeof(uint2) * heap,
                           sizeof(uint2) * canc, sizeof(unsigned long long) * 8 * (size_t)(ns + 1),
-                          sizeof(SimpArgs) * (size_t)(ns + 1)};
+                          sizeof(SimpArgs) * (size_t)(ns + 1), sizeof(HeapEnt) * (init + 1)};
   size_t bytes = 0;
   for (size_t z : sizes) bytes += rnd(z);
   BatchSimplifyWork *w = new BatchSimplifyWork;
@@ -440,6 +467,7 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
   uint2 *dcanc = (uint2 *)take();
   w->dstats = (unsigned long long *)take();
   w->dargs = (SimpArgs *)take();
+  HeapEnt *dinit = (HeapEnt *)take();
   w->nsimp = ns;
   if (ncp) {
     k_lists_from_csr<<<blocks_for(ncp), 256, 0, st>>>(ncp, io.aoff, io.asc, io.doff, io.des, des_base, w->off, w->nrun,
@@ -448,7 +476,7 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
   }
   e = cudaMemsetAsync(w->dstats, 0, sizeof(unsigned long long) * 8 * (size_t)(ns + 1), st);
   std::vector<SimpArgs> args(ns);
-  unsigned long long top = base_top, ho = 0, co = 0, to = 0;
+  unsigned long long top = base_top, ho = 0, co = 0, to = 0, io2 = 0;
   for (int k = 0; k < ns && e == cudaSuccess; ++k) {
     const int g = which[k];
     const unsigned long long c0 = io.cpb[g], n = io.cpb[g + 1] - c0;
@@ -478,6 +506,10 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
     ho += a.heap_cap;
     a.canc = dcanc + co;
     co += n + 1;
+    a.aoff = io.aoff + c0; a.asc = io.asc; a.doff = io.doff + c0; a.des = io.des;
+    a.init = dinit + io2;
+    a.ninit = nd;
+    io2 += nd + 1;
     a.rx0 = io.rect[4 * g]; a.ry0 = io.rect[4 * g + 1]; a.rx1 = io.rect[4 * g + 2]; a.ry1 = io.rect[4 * g + 3];
     a.tresh = io.tresh[g];
     a.stats = w->dstats + 8 * k;
@@ -490,8 +522,9 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
     // one grid per SM can keep 14 heap levels in shared memory; more grids
     // than SMs keep 12, so that four fit on an SM and all start at once
     const unsigned ntop = ns <= 152 ? (unsigned)HEAP_TOP : (1u << 12) - 1;
+    k_simp_prep<<<dim3(64, (unsigned)ns), 256, 0, st>>>(w->dargs);
     k_simplify_batch<<<ns, 32, sizeof(HeapEnt) * ntop, st>>>(w->dargs, ns, ntop);
-    DMSC_LAUNCHED(1);
+    DMSC_LAUNCHED(2);
     e = cudaGetLastError();
   }
   std::vector<unsigned long long> hs(8 * (size_t)(ns + 1), 0);
