@@ -180,6 +180,44 @@ struct Graph {
   // new edges of the 4-argument form are (d, a) for every occurrence of a in
   // asc(cp0) \ {cp1} (ascending) times every occurrence of d in des(cp1) \ {cp0}
   // (ascending); both lists are left intact, so a caller can enumerate them.
+  // The k runs tmp[0..k) (ascending, distinct values) inserted into list l
+  // as k insert() calls in that order would leave it -- same multiset, same
+  // operation count -- with one merge instead of k shifts of the list's tail;
+  // each value whose count reaches 2 marks itself and `a` strangulated.
+  __host__ __device__ void insert_sorted(uint32_t l, unsigned long long k, uint32_t a) {
+    const uint32_t n = L.nrun[l];
+    const uint2 *R = runs(l);
+    unsigned long long ticks = 0, nnew = 0, add = 0;
+    for (unsigned long long q = 0, i = 0; q < k; ++q) {  // the shifts the k inserts would make
+      const uint32_t x = tmp[q].x;
+      while (i < n && R[i].x < x) ++i;
+      if (!(i < n && R[i].x == x)) { ticks += n - i; ++nnew; }
+      add += tmp[q].y;
+    }
+    if (!tick(ticks)) return;
+    if (n + nnew > 0xffffffffull || L.total[l] + add > 0xffffffffull) { fail = true; return; }
+    if (!reserve(l, (uint32_t)(n + nnew))) return;
+    uint2 *P = runs(l);
+    long long i = (long long)n - 1, w = (long long)(n + nnew) - 1;
+    for (long long q = (long long)k - 1; q >= 0; --q) {  // merge from the back, in place
+      const uint32_t x = tmp[q].x, c = tmp[q].y;
+      while (i >= 0 && P[i].x > x) P[w--] = P[i--];
+      if (i >= 0 && P[i].x == x) {
+        uint2 r = P[i--];
+        if (r.y > 0xffffffffu - c) { fail = true; return; }
+        r.y += c;
+        P[w--] = r;
+        flags[a] |= F_STRANG;
+        flags[x] |= F_STRANG;
+      } else {
+        P[w--] = make_uint2(x, c);
+        if (c >= 2) { flags[a] |= F_STRANG; flags[x] |= F_STRANG; }
+      }
+    }
+    L.nrun[l] = (uint32_t)(n + nnew);
+    L.total[l] += (uint32_t)add;
+  }
+
   __host__ __device__ bool cancel_pairs(uint32_t &cp0, uint32_t &cp1) {
     if (!contains(2 * cp0, cp1)) { uint32_t t = cp0; cp0 = cp1; cp1 = t; }
     if (!contains(2 * cp0, cp1)) return false;
@@ -187,6 +225,24 @@ struct Graph {
     for (uint32_t i = 0; i < L.nrun[la0] && !fail; ++i) {
       uint2 ra = runs(la0)[i];
       if (ra.x == cp1) continue;
+      if (L.nrun[ld1] >= 8 && L.nrun[ld1] <= tmp_cap) {
+        // many new edges into des(a): (d, a) for every d of des(cp1) but cp0,
+        // ascending; asc(d) takes a one by one, des(a) takes all d at once
+        unsigned long long k = 0, cs = 0;
+        for (uint32_t j = 0; j < L.nrun[ld1] && !fail; ++j) {
+          const uint2 rd = runs(ld1)[j];
+          if (rd.x == cp0) continue;
+          const unsigned long long c = (unsigned long long)ra.y * rd.y;
+          if (c > 0xffffffffull) { fail = true; return true; }
+          insert(2 * rd.x, ra.x, (uint32_t)c);
+          tmp[k++] = make_uint2(rd.x, (uint32_t)c);
+          cs += c;
+        }
+        if (fail) return true;
+        insert_sorted(2 * ra.x + 1, k, ra.x);
+        if (!tick(cs)) return true;
+        continue;
+      }
       for (uint32_t j = 0; j < L.nrun[ld1] && !fail; ++j) {
         uint2 rd = runs(ld1)[j];
         if (rd.x == cp0) continue;
