@@ -149,7 +149,7 @@ struct DiscIO {
 cudaError_t fill_discs(DiscIO &io, cudaStream_t st);
 
 // Piece merges (merge.cu).  MGraphHost is host-side storage of a device
-// MGraph (a complex as a mutable graph with its cell-id hash).
+// MGraph (a complex as a mutable graph with its cell table).
 struct MGraphHost {
   uint32_t *buf = nullptr;
   uint32_t *tab = nullptr;     // its cell table (owned)

@@ -1,5 +1,6 @@
 // merge_graph.cuh -- a complex being merged, as a mutable graph (msc_graph.cuh)
-// plus a hash table from cell id to critical-point index standing in for
+// plus a table from cell id to critical-point index (over the box of its
+// cells) standing in for
 // m_id_cp_map (std::map), and the reference's two merges restated step by
 // step on it: GridMSComplex::merge_up and merge_down
 // (dmsc/src/grid_mscomplex.cpp:7-322), including its std::map::operator[]
