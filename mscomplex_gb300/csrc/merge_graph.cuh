@@ -1,8 +1,7 @@
 // merge_graph.cuh -- a complex being merged, as a mutable graph (msc_graph.cuh)
-// plus a table from cell id to critical-point index (over the box of its
-// cells) standing in for
-// m_id_cp_map (std::map), and the reference's two merges restated step by
-// step on it: GridMSComplex::merge_up and merge_down
+// plus a table from cell id to critical-point index over the box of its
+// cells, standing in for m_id_cp_map (std::map), and the reference's two
+// merges restated step by step on it: GridMSComplex::merge_up and merge_down
 // (dmsc/src/grid_mscomplex.cpp:7-322), including its std::map::operator[]
 // (a missing key is inserted with index 0).  Shared by the level-at-a-time
 // merges (merge.cu) and the parallel merges (merge_par.cu), which run the
