@@ -122,6 +122,21 @@ __global__ void __launch_bounds__(512) k_ss_block(const uint32_t *__restrict__ o
   const uint32_t count = *nq;
   for (uint32_t k = blockIdx.x; k < count; k += gridDim.x) {
     const uint32_t s = q[k], b = off[s], n = off[s + 1] - b;
+    if (n <= 1024) {  // rank sort: each value's place is the count of values before it
+      for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) sh[i] = vals[b + i];
+      __syncthreads();
+      for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint32_t v = sh[i];
+        uint32_t r = 0;
+        for (uint32_t j = 0; j < n; ++j) {
+          const uint32_t u = sh[j];
+          r += (u < v) || (u == v && j < i);
+        }
+        vals[b + r] = v;
+      }
+      __syncthreads();
+      continue;
+    }
     uint32_t p2 = 1;
     while (p2 < n) p2 <<= 1;
     for (uint32_t i = threadIdx.x; i < p2; i += blockDim.x) sh[i] = i < n ? vals[b + i] : 0xFFFFFFFFu;

@@ -472,6 +472,21 @@ __global__ void __launch_bounds__(512) k_seg_sort_block(const uint32_t *__restri
     const int dim = cell_dim(cellid[k]);
     uint32_t *seg = dim == 0 ? asc + aoff[k] : des + doff[k];
     const uint32_t n = dim == 0 ? aoff[k + 1] - aoff[k] : doff[k + 1] - doff[k];
+    if (n <= 1024) {  // rank sort: each value's place is the count of values before it
+      for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) sh[i] = seg[i];
+      __syncthreads();
+      for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint32_t v = sh[i];
+        uint32_t r = 0;
+        for (uint32_t j = 0; j < n; ++j) {
+          const uint32_t u = sh[j];
+          r += (u < v) || (u == v && j < i);
+        }
+        seg[r] = v;
+      }
+      __syncthreads();
+      continue;
+    }
     uint32_t p2 = 1;
     while (p2 < n) p2 <<= 1;
     for (uint32_t i = threadIdx.x; i < p2; i += blockDim.x) sh[i] = i < n ? seg[i] : 0xFFFFFFFFu;
