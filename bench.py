@@ -144,6 +144,22 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """The maximum of x over all ranks (the job's time is its slowest rank's)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(units_per_rank: float, world: int, seconds: float) -> float:
+    """Whole-job throughput of N replicas: all ranks' units over the slowest rank's time."""
+    return units_per_rank * world / seconds
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -502,12 +518,8 @@ def main():
     launches = kernel_launches() - launches0
     barrier()
     clk = clocks.stop()
-    total_ms = sum(times)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = nverts * args.steps * world / (total_ms / 1e3) / 1e6
+    total_ms = max_over_ranks(sum(times), world)
+    value = replicas_value(nverts * args.steps, world, total_ms / 1e3) / 1e6
 
     # roofline of the dominant kernel (median stage time, live CUDA events)
     med = {k: statistics.median(v) for k, v in stages.items()}
@@ -547,12 +559,8 @@ def main():
         out = m.export(pinned)
         e2e_times.append(time.perf_counter() - s0)
         d2h = sum(v.nbytes for v in out.values())
-    e2e_total = sum(e2e_times)
-    if world > 1:
-        t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = nverts * args.steps * world / e2e_total / 1e6
+    e2e_total = max_over_ranks(sum(e2e_times), world)
+    e2e_value = replicas_value(nverts * args.steps, world, e2e_total) / 1e6
 
     line = None
     if rank == 0:
