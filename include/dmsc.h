@@ -103,6 +103,15 @@ int dmsc_msc_sizes(dmsc_msc *msc, int64_t sizes[5]);
 int dmsc_msc_export(dmsc_msc *msc, int16_t rect_ext[8], int16_t *cellid, float *fn, uint32_t *pair_idx,
                     uint8_t *flags, uint32_t *asc_off, uint32_t *asc, uint32_t *des_off, uint32_t *des,
                     uint32_t *adisc_off, int16_t *adisc, uint32_t *ddisc_off, int16_t *ddisc, void *stream);
+/* dmsc_msc_export without waiting: the copies are queued on `stream`, behind
+ * what is already queued there, and the host buffers (pinned, so that the
+ * copies run asynchronously) hold the complex once the stream reaches that
+ * point.  Until then the complex must not be changed or destroyed, and the
+ * buffers must stay allocated.  No reference counterpart: it lets a caller
+ * overlap one grid's device-to-host copies with the next grid's work. */
+int dmsc_msc_export_async(dmsc_msc *msc, int16_t rect_ext[8], int16_t *cellid, float *fn, uint32_t *pair_idx,
+                          uint8_t *flags, uint32_t *asc_off, uint32_t *asc, uint32_t *des_off, uint32_t *des,
+                          uint32_t *adisc_off, int16_t *adisc, uint32_t *ddisc_off, int16_t *ddisc, void *stream);
 
 /* GridMSComplex::simplify_un_simplify(tresh) (dmsc/src/grid_mscomplex.cpp:
  * 384-535): persistence cancellation in the reference's exact pop order,

@@ -38,6 +38,7 @@ SIGNATURES = {
     "dmsc_msc_destroy": ([_vp], _i32),
     "dmsc_msc_sizes": ([_vp, _vp], _i32),
     "dmsc_msc_export": ([_vp] * 15, _i32),
+    "dmsc_msc_export_async": ([_vp] * 15, _i32),
     "dmsc_set_timing": ([_vp, _i32], _i32),
     "dmsc_dataset_stage_times": ([_vp, _vp, _i32], _i32),
     "dmsc_kernel_launches": ([_vp], _i32),

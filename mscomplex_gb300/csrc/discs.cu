@@ -845,7 +845,8 @@ struct DiscKind {
           k_run_flags<<<nb(n), 256, 0, st>>>(S.gkey[kind], n, S.gw[kind], S.gval[kind]);
           DMSC_LAUNCHED(1);
           L(scan_exclusive_u32(S.gval[kind], n, S.gval[kind], soff, st));
-          L(cudaMemcpyAsync(&hbuf[0], soff, 4, cudaMemcpyDeviceToHost, st));
+          const uint32_t *w[1] = {soff};
+          L(read_words(&hbuf[0], w, 1, st));
         } else {
           hbuf[0] = 0;
         }
@@ -879,7 +880,8 @@ struct DiscKind {
           k_seed_count<<<nb(ncp), 256, 0, st>>>(a, kind, slen);
           DMSC_LAUNCHED(1);
           L(scan_exclusive_u32(slen, ncp, soff, soff + ncp, st));
-          L(cudaMemcpyAsync(&hbuf[1], soff + ncp, 4, cudaMemcpyDeviceToHost, st));
+          const uint32_t *w[1] = {soff + ncp};
+          L(read_words(&hbuf[1], w, 1, st));
           return true;
         }
         return step();  // nothing to wait for
@@ -907,7 +909,8 @@ struct DiscKind {
         // bound of two chains per saddle (two own seeds, one successor each), with
         // the unused slots zeroed -- saving a synchronisation
         if (ns || !io.no_cancel) {
-          L(cudaMemcpyAsync(&hbuf[2], cbase + ncp, 4, cudaMemcpyDeviceToHost, st));
+          const uint32_t *w[1] = {cbase + ncp};
+          L(read_words(&hbuf[2], w, 1, st));
           return true;
         }
         hbuf[2] = (uint32_t)std::min<long long>(2 * ncp, 0xFFFFFFF0ll);
@@ -937,9 +940,8 @@ struct DiscKind {
         L(scan_exclusive_u32(cnt, ncp, offs, offs + ncp, st));
         L(scan_exclusive_u32(c.cnseg, nch, c.csegoff, c.csegoff + nch, st));
         L(scan_exclusive_u32(c.clen, nch, c.cofs, c.cofs + nch, st));
-        L(cudaMemcpyAsync(&hbuf[3], offs + ncp, 4, cudaMemcpyDeviceToHost, st));
-        L(cudaMemcpyAsync(&hbuf[4], c.csegoff + nch, 4, cudaMemcpyDeviceToHost, st));
-        L(cudaMemcpyAsync(&hbuf[5], c.cofs + nch, 4, cudaMemcpyDeviceToHost, st));
+        const uint32_t *w[3] = {offs + ncp, c.csegoff + nch, c.cofs + nch};
+        L(read_words(&hbuf[3], w, 3, st));
         return true;
       }
       case 4: {  // the cells

@@ -5,6 +5,7 @@
 // device memory, dmsc_msc is a GridMSComplex (dmsc/include/grid_mscomplex.h)
 // held as flat device arrays.  There is no CPU fallback: every computation
 // here is a CUDA kernel launch.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -184,7 +185,10 @@ int dmsc_dataset_work(dmsc_dataset *d, void *stream) {
     if (tm) CK(cudaEventRecord(d->ev[3], st));
     CK(launch_labels(d->codes.p, d->terms.p, d->hgt, g, d->offsets.p, d->table.p, d->labels.p, cp, d->scal.p, st));
     if (tm) CK(cudaEventRecord(d->ev[4], st));
-    CK(cudaMemcpyAsync(d->host_scal, d->scal.p, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, st));
+    {
+      const uint32_t *w[4] = {d->scal.p, d->scal.p + 1, d->scal.p + 2, d->scal.p + 3};
+      CK(read_words(d->host_scal, w, 4, st));
+    }
     CK(cudaStreamSynchronize(st));
     d->ncp = d->host_scal[1];
     if (!(d->host_scal[0] & ST_CAPACITY)) break;
@@ -201,7 +205,8 @@ int dmsc_dataset_work(dmsc_dataset *d, void *stream) {
     if (d->ncp) CK(cudaMemsetAsync(d->cp_pair_idx.p, 0xFF, sizeof(uint32_t) * d->ncp, st));
   } else {
     CK(launch_pair_index(d->ncp, d->cp_cellid.p, d->cp_flags.p, d->cp_pair_cell.p, d->cp_pair_idx.p, d->scal.p, st));
-    CK(cudaMemcpyAsync(d->host_scal, d->scal.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    const uint32_t *w[1] = {d->scal.p};
+    CK(read_words(d->host_scal, w, 1, st));
     CK(cudaStreamSynchronize(st));
     rc = status_to_error(d->host_scal[0]);
     if (rc) return rc;
@@ -292,9 +297,9 @@ int dmsc_msc_sizes(dmsc_msc *m, int64_t sizes[5]) {
   return DMSC_OK;
 }
 
-int dmsc_msc_export(dmsc_msc *m, int16_t rect_ext[8], int16_t *cellid, float *fn, uint32_t *pair_idx, uint8_t *flags,
-                    uint32_t *asc_off, uint32_t *asc, uint32_t *des_off, uint32_t *des, uint32_t *adisc_off,
-                    int16_t *adisc, uint32_t *ddisc_off, int16_t *ddisc, void *stream) {
+static int msc_export(dmsc_msc *m, int16_t rect_ext[8], int16_t *cellid, float *fn, uint32_t *pair_idx, uint8_t *flags,
+                      uint32_t *asc_off, uint32_t *asc, uint32_t *des_off, uint32_t *des, uint32_t *adisc_off,
+                      int16_t *adisc, uint32_t *ddisc_off, int16_t *ddisc, void *stream, bool sync) {
   if (!m) return fail(DMSC_ERR_BAD_ARG, "complex is null");
   CK(cudaSetDevice(m->ctx->device));
   cudaStream_t st = pick(m->ctx, stream);
@@ -316,10 +321,25 @@ int dmsc_msc_export(dmsc_msc *m, int16_t rect_ext[8], int16_t *cellid, float *fn
   CK(cp(adisc, m->adisc.p, 4 * (size_t)m->nadisc));
   CK(cp(ddisc_off, m->ddoff.p, m->ddoff.p ? 4 * (n + 1) : 0));
   CK(cp(ddisc, m->ddisc.p, 4 * (size_t)m->nddisc));
-  CK(cudaStreamSynchronize(st));
+  if (sync) CK(cudaStreamSynchronize(st));
+  // no discs: zero offsets (host buffers no copy writes)
   if (adisc_off && !m->adoff.p) std::memset(adisc_off, 0, 4 * (n + 1));
   if (ddisc_off && !m->ddoff.p) std::memset(ddisc_off, 0, 4 * (n + 1));
   return DMSC_OK;
+}
+
+int dmsc_msc_export(dmsc_msc *m, int16_t rect_ext[8], int16_t *cellid, float *fn, uint32_t *pair_idx, uint8_t *flags,
+                    uint32_t *asc_off, uint32_t *asc, uint32_t *des_off, uint32_t *des, uint32_t *adisc_off,
+                    int16_t *adisc, uint32_t *ddisc_off, int16_t *ddisc, void *stream) {
+  return msc_export(m, rect_ext, cellid, fn, pair_idx, flags, asc_off, asc, des_off, des, adisc_off, adisc, ddisc_off,
+                    ddisc, stream, true);
+}
+
+int dmsc_msc_export_async(dmsc_msc *m, int16_t rect_ext[8], int16_t *cellid, float *fn, uint32_t *pair_idx,
+                          uint8_t *flags, uint32_t *asc_off, uint32_t *asc, uint32_t *des_off, uint32_t *des,
+                          uint32_t *adisc_off, int16_t *adisc, uint32_t *ddisc_off, int16_t *ddisc, void *stream) {
+  return msc_export(m, rect_ext, cellid, fn, pair_idx, flags, asc_off, asc, des_off, des, adisc_off, adisc, ddisc_off,
+                    ddisc, stream, false);
 }
 
 int dmsc_set_timing(dmsc_ctx *ctx, int enable) {
@@ -445,10 +465,10 @@ int dmsc_dataset_fill_discs(dmsc_dataset *d, dmsc_msc *m, void *stream) {
   CK(cudaMemsetAsync(d->scal.p, 0, sizeof(uint32_t), st));
   CK(fill_discs(io, st));
   if (tm) CK(cudaEventRecord(d->ev[9], st));
-  uint32_t stw = 0;
-  CK(cudaMemcpyAsync(&stw, d->scal.p, 4, cudaMemcpyDeviceToHost, st));
+  const uint32_t *w[1] = {d->scal.p};
+  CK(read_words(d->host_scal, w, 1, st));
   CK(cudaStreamSynchronize(st));
-  if (stw) return status_to_error(stw);
+  if (const uint32_t stw = d->host_scal[0]) return status_to_error(stw);
   m->nadisc = io.nadisc;
   m->nddisc = io.nddisc;
   return DMSC_OK;
@@ -603,9 +623,9 @@ int dmsc_msc::writeout_from(const dmsc_dataset &d, cudaStream_t st) {
   CK(asc.ensure(4 * n + 1, st));
   CK(des.ensure(4 * n + 1, st));
   if (n) {
-    CK(cudaMemcpyAsync(cellid.p, d.cp_cellid.p, 4 * n, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(fn.p, d.cp_fn.p, 4 * n, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(pair_idx.p, d.cp_pair_idx.p, 4 * n, cudaMemcpyDeviceToDevice, st));
+    CK(copy_u32(cellid.p, d.cp_cellid.p, (long long)n, st));
+    CK(copy_u32((uint32_t *)fn.p, (const uint32_t *)d.cp_fn.p, (long long)n, st));
+    CK(copy_u32(pair_idx.p, d.cp_pair_idx.p, (long long)n, st));
     CK(launch_msc_flags(ncp, d.cp_flags.p, flags.p, st));
   }
   CK(scan_exclusive_u32(d.cp_acnt.p, ncp, aoff.p, aoff.p + n, st));
@@ -613,16 +633,18 @@ int dmsc_msc::writeout_from(const dmsc_dataset &d, cudaStream_t st) {
   CK(cudaMemsetAsync(d.scal.p, 0, sizeof(uint32_t), st));
   CK(build_csr(ncp, d.cp_cellid.p, d.cp_des2.p, d.cp_asc2.p, aoff.p, doff.p, asc.p, des.p, 4 * (long long)n + 1,
                d.scal.p, st));
-  uint32_t tot[3] = {0, 0, 0};
-  CK(cudaMemcpyAsync(&tot[0], aoff.p + n, 4, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(&tot[1], doff.p + n, 4, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(&tot[2], d.scal.p, 4, cudaMemcpyDeviceToHost, st));
+  uint32_t *tot = d.host_scal;  // the dataset's pinned slot: [0] asc, [1] des entries, [2] status
+  {
+    const uint32_t *w[3] = {aoff.p + n, doff.p + n, d.scal.p};
+    CK(read_words(tot, w, 3, st));
+  }
   CK(cudaStreamSynchronize(st));
   if (tot[2] == ST_CAPACITY) {  // an extremum segment too long for the in-place sorts
     CK(cudaMemsetAsync(d.scal.p, 0, sizeof(uint32_t), st));
     CK(build_csr_radix(ncp, d.cp_cellid.p, d.cp_des2.p, d.cp_asc2.p, aoff.p, doff.p, asc.p, des.p,
                        4 * (long long)n + 1, d.scal.p, st));
-    CK(cudaMemcpyAsync(&tot[2], d.scal.p, 4, cudaMemcpyDeviceToHost, st));
+    const uint32_t *w[1] = {d.scal.p};
+    CK(read_words(tot + 2, w, 1, st));
     CK(cudaStreamSynchronize(st));
   }
   nasc = tot[0];

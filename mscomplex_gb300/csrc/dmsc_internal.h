@@ -52,6 +52,16 @@ cudaError_t launch_labels(const uint32_t *codes, const uint32_t *terms, const fl
 
 cudaError_t scan_exclusive_u8(const uint8_t *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st);
 cudaError_t scan_exclusive_u32(const uint32_t *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st);
+// dst[0..n) = src[0..n) on the device with a kernel (no copy engine: see
+// read_words)
+cudaError_t copy_u32(uint32_t *dst, const uint32_t *src, long long n, cudaStream_t st);
+// Reads up to 8 device words src[0..n) into host[0..n) with a one-warp kernel
+// that stores into the pinned host memory directly (memory from
+// cudaMallocHost / cudaHostAlloc, which kernels address by the same pointer).
+// A small read-back done this way does not use a copy engine, so it does not
+// queue behind large device-to-host copies that other streams have in flight.
+// host[] holds the words once `st` is synchronised.
+cudaError_t read_words(uint32_t *host, const uint32_t *const *src, int n, cudaStream_t st);
 long long scan_scratch_words(long long n);
 cudaError_t scan_exclusive_u32_scratch(const uint32_t *in, long long n, uint32_t *out, uint32_t *total,
                                        uint32_t *scratch, cudaStream_t st);

@@ -114,6 +114,37 @@ cudaError_t scan_exclusive_t(const T *in, long long n, uint32_t *out, uint32_t *
 cudaError_t scan_exclusive_u8(const uint8_t *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st) {
   return scan_exclusive_t<uint8_t>(in, n, out, total, st);
 }
+__global__ void k_copy_u32(long long n, const uint32_t *__restrict__ src, uint32_t *__restrict__ dst) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+cudaError_t copy_u32(uint32_t *dst, const uint32_t *src, long long n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  long long b = (n + 255) / 256;
+  if (b > 152 * 8) b = 152 * 8;
+  k_copy_u32<<<(unsigned)b, 256, 0, st>>>(n, src, dst);
+  DMSC_LAUNCHED(1);
+  return cudaGetLastError();
+}
+
+struct Words8 {
+  const uint32_t *src[8];
+};
+__global__ void k_read_words(Words8 w, int n, uint32_t *host) {
+  const int i = threadIdx.x;
+  if (i < n) host[i] = *w.src[i];
+}
+
+cudaError_t read_words(uint32_t *host, const uint32_t *const *src, int n, cudaStream_t st) {
+  if (n < 1 || n > 8 || !host) return cudaErrorInvalidValue;
+  Words8 w{};
+  for (int i = 0; i < n; ++i) w.src[i] = src[i];
+  k_read_words<<<1, 32, 0, st>>>(w, n, host);
+  DMSC_LAUNCHED(1);
+  return cudaGetLastError();
+}
+
 cudaError_t scan_exclusive_u32(const uint32_t *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st) {
   return scan_exclusive_t<uint32_t>(in, n, out, total, st);
 }
@@ -236,8 +267,8 @@ cudaError_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *ktmp, uin
     std::swap(va, vb);
   }
   if (e == cudaSuccess && ka != keys) {
-    cudaMemcpyAsync(keys, ka, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(vals, va, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+    e = copy_u32(keys, ka, n, st);
+    if (e == cudaSuccess) e = copy_u32(vals, va, n, st);
   }
   cudaFreeAsync(hist, st);
   if (e != cudaSuccess) return e;
@@ -307,8 +338,8 @@ cudaError_t sort_pairs_batched(uint32_t *dk, uint32_t *dv, const uint32_t *sk, c
       DMSC_LAUNCHED(1);
       k_gather_u32<<<gb, 256, 0, st>>>(n, t1, perm, t3);  // original indices in final order
       DMSC_LAUNCHED(1);
-      cudaMemcpyAsync(k, t2, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
-      cudaMemcpyAsync(perm, t3, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+      e = copy_u32(k, t2, n, st);
+      if (e == cudaSuccess) e = copy_u32(perm, t3, n, st);
     }
   }
   if (e == cudaSuccess) {
@@ -316,8 +347,7 @@ cudaError_t sort_pairs_batched(uint32_t *dk, uint32_t *dv, const uint32_t *sk, c
     DMSC_LAUNCHED(1);
     k_sort_finish<<<gb, 256, 0, st>>>(n, dir, k, dk);
     DMSC_LAUNCHED(1);
-    cudaMemcpyAsync(dv, t2, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
-    e = cudaGetLastError();
+    e = copy_u32(dv, t2, n, st);
   }
   cudaFreeAsync(buf, st);
   return e;
@@ -543,7 +573,8 @@ cudaError_t build_csr_radix(long long ncp, const uint32_t *cellid, const uint32_
   uint32_t *start = buf + 6 * n;
   k_fill_saddles<<<grid_for(ncp, 256), 256, 0, st>>>(ncp, cellid, des2, asc2, aoff, doff, asc, des, kmin, kmax, vmin);
   DMSC_LAUNCHED(1);
-  cudaMemcpyAsync(vmax, vmin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+  e = copy_u32(vmax, vmin, n, st);
+  if (e != cudaSuccess) { cudaFreeAsync(buf, st); return e; }
   int nbits = 1;
   while ((1ll << nbits) <= ncp) ++nbits;
   // minima: asc side; maxima: des side -- ascending saddle index within each run (stable sort)

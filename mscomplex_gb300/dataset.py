@@ -215,11 +215,16 @@ class GridMSComplex:
                     adisc_off=((n + 1,), np.uint32), adisc=((nad, 2), np.int16),
                     ddisc_off=((n + 1,), np.uint32), ddisc=((ndd, 2), np.int16))
 
-    def export(self, out: dict | None = None) -> dict:
+    def export(self, out: dict | None = None, stream=None, wait: bool = True) -> dict:
         """Flat arrays with the same keys as the oracle's complex dump.  `out`
         may hold preallocated flat host buffers (e.g. pinned) per key, large
-        enough: the result is then views into them."""
+        enough: the result is then views into them.  With wait=False the
+        copies are only queued on `stream` (dmsc_msc_export_async): the views
+        hold the complex once that stream has reached them, and neither the
+        complex nor the buffers may change before; `out` must then be pinned."""
         shapes = self.export_shapes()
+        if not wait and out is None:
+            raise ValueError("export(wait=False) needs preallocated pinned buffers in `out`")
         if out is None:
             d = {k: np.zeros(sh, dt) for k, (sh, dt) in shapes.items()}
         else:
@@ -230,7 +235,8 @@ class GridMSComplex:
                 if buf.size < n:
                     raise ValueError(f"export buffer {k} holds {buf.size} < {n} elements")
                 d[k] = buf[:n].reshape(sh)
-        check(self.lib.dmsc_msc_export(self.h, *(_ptr(d[k]) for k in self.EXPORT_KEYS), None))
+        fn = self.lib.dmsc_msc_export if wait else self.lib.dmsc_msc_export_async
+        check(fn(self.h, *(_ptr(d[k]) for k in self.EXPORT_KEYS), stream))
         return d
 
 

@@ -67,3 +67,42 @@ def test_write_discs_files(gpu_lib, oracle, tmp_path):
     assert set(got) == set(want)
     for k in want:
         assert np.array_equal(got[k], want[k]), k
+
+
+def test_export_async_overlapping_next_grid(gpu_lib, oracle):
+    """export(wait=False): each grid's device-to-host copies run on a copy
+    stream while the next grid computes; two complexes and two pinned buffer
+    sets alternate, a complex is rewritten only after its previous copies are
+    done.  Every result equals the oracle's complex with discs."""
+    import torch
+    fields = [smooth_field(70, 90, s) for s in range(4)]
+    r = full_rect(fields[0])
+    want = [oracle.Dataset(f, r, r, fill_discs=True).msc() for f in fields]
+    ds = gpu_lib.GridDataset(r, r)
+    need = {}
+    for f in fields:  # buffer sizes: the largest result per key
+        m = ds.init(f).work().writeout_connectivity()
+        ds.post_merge_fill_discs(m)
+        for k, (shape, dt) in m.export_shapes().items():
+            need[k] = max(need.get(k, 0), int(np.prod(shape)) * np.dtype(dt).itemsize)
+    pinned = [{k: torch.empty(n + 64, dtype=torch.uint8).pin_memory().numpy() for k, n in need.items()}
+              for _ in range(2)]
+    comp, cp = torch.cuda.Stream(), torch.cuda.Stream()
+    slots, freed, outs = [None, None], [None, None], [None] * len(fields)
+    for i, f in enumerate(fields):
+        k = i & 1
+        ds.init(f, stream=comp.cuda_stream).work(stream=comp.cuda_stream)
+        if freed[k] is not None:
+            comp.wait_event(freed[k])
+        m = slots[k] = ds.writeout_connectivity(slots[k], stream=comp.cuda_stream)
+        ds.post_merge_fill_discs(m, stream=comp.cuda_stream)
+        cp.wait_event(comp.record_event())
+        outs[i] = m.export(pinned[k], stream=cp.cuda_stream, wait=False)
+        freed[k] = cp.record_event()
+        if i > 0:  # the previous grid's buffers are read before the next export reuses them
+            freed[1 - k].synchronize()
+            assert_same_complex(outs[i - 1], want[i - 1], f"grid {i - 1}")
+    freed[(len(fields) - 1) & 1].synchronize()
+    assert_same_complex(outs[-1], want[-1], f"grid {len(fields) - 1}")
+    with pytest.raises(ValueError):
+        slots[0].export(None, wait=False)
