@@ -473,8 +473,6 @@ struct ChainArgs {
   uint32_t *cbase;      // exclusive scan of kc
   uint32_t *cstart, *csaddle, *clen, *cnseg, *csegoff;  // per chain
   uint4 *segs;          // (chain, first edge, first level, cells)
-  uint32_t *cofs;       // exclusive scan of clen: each chain's cells in tmp
-  uint32_t *tmp;        // chain-major cells
   uint4 *blocks;        // per chain slot of a saddle, 2 uint4: an interleave record (k_zip_blocks)
   uint32_t cap;         // chain slots allocated
   unsigned long long limit;
@@ -572,26 +570,70 @@ __global__ void k_level0(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, const u
   }
 }
 
-// Pieces of at most SEG_MAX cells of one chain.  Each lane of a warp follows
-// the 1-byte successor offsets of one piece into shared memory, then the
-// warp copies the 32 pieces out one after another with coalesced stores into
-// their chains' spans of tmp (a lane's own stores would each touch a
-// different sector).
+// Per saddle: the level ranges over which the set of alive chains is
+// constant.  Between consecutive distinct chain lengths the disc is a
+// regular interleave of the alive chains.  Each range becomes a record of
+// two uint4: (first output position, cells, alive chains, alive mask) and
+// (first level, 0, 0, 0); the saddle's unused record slots are zeroed.
+__global__ void k_zip_blocks(DiscArgs a, ChainArgs c, const uint32_t *off) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < a.ncp; s += gridDim.x * blockDim.x) {
+    const uint32_t K = c.kc[s], cb = c.cbase[s];
+    if (!K) continue;
+    if (cb + K > c.cap) { atomicOr(a.status, ST_CAPACITY); continue; }
+    uint32_t L[KMAX];
+    for (uint32_t q = 0; q < K; ++q) L[q] = c.clen[cb + q];
+    const uint32_t base = off[s] + c.mc[s];
+    uint32_t prev = 0, P = 0, nb = 0;
+    for (;;) {
+      uint32_t u = 0xFFFFFFFFu, mask = 0;
+      for (uint32_t q = 0; q < K; ++q)
+        if (L[q] > prev) { mask |= 1u << q; u = L[q] < u ? L[q] : u; }
+      if (!mask) break;
+      const uint32_t na = (uint32_t)__popc(mask), n = (u - prev) * na;
+      c.blocks[2 * (cb + nb)] = make_uint4(base + P, n, na, mask);
+      c.blocks[2 * (cb + nb) + 1] = make_uint4(prev + 1, 0, 0, 0);
+      ++nb;
+      P += n;
+      prev = u;
+    }
+    for (; nb < K; ++nb) c.blocks[2 * (cb + nb)] = make_uint4(0, 0, 0, 0);
+  }
+}
+
+// Pieces of at most SEG_MAX cells of one chain, stored straight at their
+// places in the disc.  Each lane of a warp follows the 1-byte successor
+// offsets of one piece into shared memory; then the warp stores the 32
+// pieces one after another, one cell per lane.  The cell at level t of the
+// saddle's j-th chain goes to the interleave record (k_zip_blocks) whose
+// level range holds t: start + (t - first level) * alive + (alive chains
+// before j), the order of the reference's breadth-first disc.
 constexpr int SEG_WARPS = 4;
-__global__ void __launch_bounds__(SEG_WARPS * 32) k_seg_write(DiscArgs a, ChainArgs c, long long nsegs) {
+__global__ void __launch_bounds__(SEG_WARPS * 32) k_seg_place(DiscArgs a, ChainArgs c, long long nsegs, uint32_t *out,
+                                                              unsigned long long out_len) {
   __shared__ uint32_t buf[SEG_WARPS][32][SEG_MAX + 1];  // +1: lanes' rows fall in different banks
   const GridGeom &g = a.g;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const long long gw = ((long long)blockIdx.x * SEG_WARPS + w), nwarps = (long long)gridDim.x * SEG_WARPS;
   for (long long k0 = gw * 32; k0 < nsegs; k0 += nwarps * 32) {
     const long long k = k0 + lane;
-    uint32_t len = 0, dst = 0;
+    uint32_t len = 0, t0 = 0, cb = 0, K = 0, j = 0;
     if (k < nsegs) {
       const uint4 sg = c.segs[k];
       const uint32_t ch = sg.x;
-      if (sg.z - 1 + sg.w > c.clen[ch]) atomicOr(a.status, ST_INVARIANT);
-      else {
-        dst = c.cofs[ch] + (sg.z - 1);
+      bool ok = ch < c.cap;
+      uint32_t s = 0;
+      if (ok) { s = c.csaddle[ch]; ok = s < a.ncp; }
+      if (ok) {
+        cb = c.cbase[s];
+        K = c.kc[s];
+        j = ch - cb;  // wraps (and fails j < K) for a chain below the saddle's slots
+        t0 = sg.z;
+        ok = sg.z >= 1 && sg.w <= (uint32_t)SEG_MAX && sg.z - 1 + sg.w <= c.clen[ch] && j < K && K <= (uint32_t)KMAX &&
+             cb + K <= c.cap;
+      }
+      if (!ok) {
+        atomicOr(a.status, ST_INVARIANT);
+      } else {
         int rx, ry;
         edge_cell(g, sg.y, rx, ry);
         for (uint32_t i = 0; i < sg.w; ++i) {
@@ -608,79 +650,27 @@ __global__ void __launch_bounds__(SEG_WARPS * 32) k_seg_write(DiscArgs a, ChainA
     }
     __syncwarp();
     for (int p = 0; p < 32; ++p) {
-      const uint32_t n = __shfl_sync(0xffffffffu, len, p), o = __shfl_sync(0xffffffffu, dst, p);
-      for (uint32_t i = lane; i < n; i += 32) c.tmp[o + i] = buf[w][p][i];
+      const uint32_t n = __shfl_sync(0xffffffffu, len, p), tp = __shfl_sync(0xffffffffu, t0, p);
+      const uint32_t cbp = __shfl_sync(0xffffffffu, cb, p), Kp = __shfl_sync(0xffffffffu, K, p);
+      const uint32_t jp = __shfl_sync(0xffffffffu, j, p);
+      if ((uint32_t)lane >= n) continue;
+      const uint32_t t = tp + lane;
+      unsigned long long pos = ~0ull;
+      for (uint32_t b = 0; b < Kp; ++b) {  // the records ascend in level
+        const uint4 r0 = c.blocks[2 * (cbp + b)];
+        if (!r0.y || !r0.z) break;
+        const uint32_t first = c.blocks[2 * (cbp + b) + 1].x, nlev = r0.y / r0.z;
+        if (t < first) break;
+        if (t - first < nlev) {
+          if (r0.w & (1u << jp))
+            pos = (unsigned long long)r0.x + (unsigned long long)(t - first) * r0.z + __popc(r0.w & ((1u << jp) - 1u));
+          break;
+        }
+      }
+      if (pos >= out_len) atomicOr(a.status, ST_INVARIANT);
+      else out[pos] = buf[w][p][lane];
     }
     __syncwarp();
-  }
-}
-
-// Per saddle: the level ranges over which the set of alive chains is
-// constant.  Between consecutive distinct chain lengths the disc is a
-// regular interleave of the alive chains.  Each range becomes a record of
-// two uint4: (first output position, cells, alive chains, alive mask) and
-// (tmp start of the first and second alive chain at the range's first level,
-// the saddle's first chain slot, the first level).
-__global__ void k_zip_blocks(DiscArgs a, ChainArgs c, const uint32_t *off) {
-  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < a.ncp; s += gridDim.x * blockDim.x) {
-    const uint32_t K = c.kc[s], cb = c.cbase[s];
-    if (!K) continue;
-    if (cb + K > c.cap) { atomicOr(a.status, ST_CAPACITY); continue; }
-    uint32_t L[KMAX];
-    for (uint32_t q = 0; q < K; ++q) L[q] = c.clen[cb + q];
-    const uint32_t base = off[s] + c.mc[s];
-    uint32_t prev = 0, P = 0, nb = 0;
-    for (;;) {
-      uint32_t u = 0xFFFFFFFFu, mask = 0;
-      for (uint32_t q = 0; q < K; ++q)
-        if (L[q] > prev) { mask |= 1u << q; u = L[q] < u ? L[q] : u; }
-      if (!mask) break;
-      const uint32_t na = (uint32_t)__popc(mask), n = (u - prev) * na;
-      const uint32_t j0 = (uint32_t)__ffs(mask) - 1, m1 = mask & (mask - 1);
-      const uint32_t j1 = m1 ? (uint32_t)__ffs(m1) - 1 : j0;
-      c.blocks[2 * (cb + nb)] = make_uint4(base + P, n, na, mask);
-      c.blocks[2 * (cb + nb) + 1] = make_uint4(c.cofs[cb + j0] + prev, c.cofs[cb + j1] + prev, cb, prev + 1);
-      ++nb;
-      P += n;
-      prev = u;
-    }
-    for (; nb < K; ++nb) c.blocks[2 * (cb + nb)] = make_uint4(0, 0, 0, 0);
-  }
-}
-
-// One warp per record: out[start + q] = the cell of level t_b + q / a of the
-// (q % a)-th alive chain, coalesced stores.
-__global__ void __launch_bounds__(256) k_zip(DiscArgs a, ChainArgs c, long long nch, uint32_t *out,
-                                             unsigned long long out_len) {
-  __shared__ uint32_t src[8][KMAX];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long k = w0; k < nch; k += nw) {
-    const uint4 r0 = c.blocks[2 * k];
-    if (!r0.y) continue;
-    const uint4 r1 = c.blocks[2 * k + 1];
-    const uint32_t n = r0.y, na = r0.z;
-    if ((unsigned long long)r0.x + n > out_len) { if (lane == 0) atomicOr(a.status, ST_INVARIANT); continue; }
-    uint32_t *o = out + r0.x;
-    if (na == 1) {
-      const uint32_t *p = c.tmp + r1.x;
-      for (uint32_t q = lane; q < n; q += 32) o[q] = p[q];
-    } else if (na == 2) {
-      for (uint32_t q = lane; q < n; q += 32) o[q] = c.tmp[((q & 1) ? r1.y : r1.x) + (q >> 1)];
-    } else {
-      __syncwarp();
-      if (lane < (int)na) {  // lane r: tmp start of the r-th alive chain
-        uint32_t m = r0.w;
-        for (int z = 0; z < lane; ++z) m &= m - 1;
-        src[wib][lane] = c.cofs[r1.z + (uint32_t)__ffs(m) - 1] + r1.w - 1;
-      }
-      __syncwarp();
-      for (uint32_t q = lane; q < n; q += 32) {
-        const uint32_t t = q / na;
-        o[q] = c.tmp[src[wib][q - t * na] + t];
-      }
-    }
   }
 }
 
@@ -814,10 +804,10 @@ struct DiscKind {
   uint32_t *key = nullptr, *val = nullptr, *kt = nullptr, *vt = nullptr, *kc = nullptr, *mc = nullptr, *cbase = nullptr;
   uint8_t *big = nullptr;
   uint32_t *hbuf = nullptr;  // pinned host counts: [0] runs, [1] seeds, [2] chains, [3..5] totals
-  uint32_t *runbuf = nullptr, *chain_buf = nullptr, *tmp = nullptr;
+  uint32_t *runbuf = nullptr, *chain_buf = nullptr;
   uint4 *segs = nullptr, *blocks = nullptr;
   uint32_t *rp = nullptr, *rstart = nullptr;
-  uint32_t nrun = 0, ns = 0, nch = 0, tot[3] = {0, 0, 0};
+  uint32_t nrun = 0, ns = 0, nch = 0, tot[2] = {0, 0};
   ChainArgs c{};
   int stage = 0;
   cudaError_t e = cudaSuccess;
@@ -825,11 +815,10 @@ struct DiscKind {
   void L(cudaError_t x) { if (e == cudaSuccess) e = x; }
   void release() {
     if (segs) cudaFreeAsync(segs, st);
-    if (tmp) cudaFreeAsync(tmp, st);
     if (blocks) cudaFreeAsync(blocks, st);
     if (chain_buf) cudaFreeAsync(chain_buf, st);
     if (runbuf) cudaFreeAsync(runbuf, st);
-    segs = nullptr; tmp = nullptr; blocks = nullptr; chain_buf = nullptr; runbuf = nullptr;
+    segs = nullptr; blocks = nullptr; chain_buf = nullptr; runbuf = nullptr;
   }
   // Runs the next stage; returns true while more stages remain (the caller
   // synchronises the stream before the next one).
@@ -919,8 +908,8 @@ struct DiscKind {
       case 3: {  // chain lengths, pieces, disc sizes
         nch = hbuf[2];
         c.cap = nch;
-        // per chain: cstart csaddle clen cnseg | csegoff cofs (nch + 1 each)
-        L(cudaMallocAsync((void **)&chain_buf, sizeof(uint32_t) * (6ull * nch + 8), st));
+        // per chain: cstart csaddle clen cnseg | csegoff (nch + 1)
+        L(cudaMallocAsync((void **)&chain_buf, sizeof(uint32_t) * (5ull * nch + 8), st));
         L(cudaMallocAsync((void **)&blocks, sizeof(uint4) * (2 * (size_t)nch + 2), st));
         if (e != cudaSuccess) return false;
         if (!ns && io.no_cancel) {
@@ -929,7 +918,6 @@ struct DiscKind {
         }
         c.cstart = chain_buf; c.csaddle = chain_buf + nch; c.clen = chain_buf + 2 * nch; c.cnseg = chain_buf + 3 * nch;
         c.csegoff = chain_buf + 4 * nch;      // nch + 1
-        c.cofs = chain_buf + 5 * nch + 1;     // nch + 1
         c.blocks = blocks;
         const SeedRuns sr{val, sstart, scount};
         k_chain_len<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, slen);
@@ -939,38 +927,33 @@ struct DiscKind {
         uint32_t *offs = kind ? io.ddoff : io.adoff;
         L(scan_exclusive_u32(cnt, ncp, offs, offs + ncp, st));
         L(scan_exclusive_u32(c.cnseg, nch, c.csegoff, c.csegoff + nch, st));
-        L(scan_exclusive_u32(c.clen, nch, c.cofs, c.cofs + nch, st));
-        const uint32_t *w[3] = {offs + ncp, c.csegoff + nch, c.cofs + nch};
-        L(read_words(&hbuf[3], w, 3, st));
+        const uint32_t *w[2] = {offs + ncp, c.csegoff + nch};
+        L(read_words(&hbuf[3], w, 2, st));
         return true;
       }
       case 4: {  // the cells
-        for (int q = 0; q < 3; ++q) tot[q] = hbuf[3 + q];
+        for (int q = 0; q < 2; ++q) tot[q] = hbuf[3 + q];
         uint32_t *offs = kind ? io.ddoff : io.adoff;
         DevBuf<uint32_t> *ob = kind ? io.ddisc : io.adisc;
         L(ob->ensure((size_t)tot[0] + 1, st));
         L(cudaMallocAsync((void **)&segs, sizeof(uint4) * ((size_t)tot[1] + 1), st));
-        L(cudaMallocAsync((void **)&tmp, sizeof(uint32_t) * ((size_t)tot[2] + 1), st));
         if (e != cudaSuccess) return false;
         c.segs = segs;
-        c.tmp = tmp;
         const SeedRuns sr{val, sstart, scount};
         if (nch) {
           k_chain_segs<<<nb(nch), 128, 0, st>>>(nch, c);
           DMSC_LAUNCHED(1);
         }
+        k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c, offs);  // the records the pieces are placed by
+        DMSC_LAUNCHED(1);
         if (tot[1]) {
-          k_seg_write<<<nb((tot[1] + 31) / 32 * 32), SEG_WARPS * 32, 0, st>>>(a, c, tot[1]);
+          k_seg_place<<<nb((tot[1] + 31) / 32 * 32), SEG_WARPS * 32, 0, st>>>(a, c, tot[1], ob->p,
+                                                                             (unsigned long long)tot[0]);
           DMSC_LAUNCHED(1);
         }
-        k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c, offs);
         k_level0<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, offs, ob->p);
         k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);
-        DMSC_LAUNCHED(3);
-        if (nch) {
-          k_zip<<<nb(32ll * nch), 256, 0, st>>>(a, c, nch, ob->p, (unsigned long long)tot[0]);
-          DMSC_LAUNCHED(1);
-        }
+        DMSC_LAUNCHED(2);
         if (n > 0 && nrun) {  // extremum discs of this kind
           k_runs_scatter<<<nb(n), 256, 0, st>>>(a.g, kind, S.gkey[kind], n, S.gw[kind], (uint32_t)ncp, S.gval[kind], rp,
                                                 rstart, offs, ob->p);
