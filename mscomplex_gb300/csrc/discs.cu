@@ -276,9 +276,11 @@ __global__ void k_saddle_disc_write(DiscArgs a, int kind, SeedRuns sr, const uin
 // where L_j is the length of chain j.  Chains are followed in "hops": per
 // 64x64 vertex tile, list ranking in shared memory gives every edge the
 // number of cells to its tile exit, the edge after it and the edge SEG_MAX
-// cells ahead, so a chain's length costs one step per tile crossed and its
-// cells are written by one thread per piece of at most SEG_MAX cells, into a
-// chain-major buffer that a last pass interleaves.
+// cells ahead, so a chain's length costs one step per tile crossed.  The
+// lengths fix every cell's place before any cell is known: per saddle, the
+// level ranges over which its set of alive chains is constant are regular
+// interleaves (k_zip_blocks), and the cells, walked by one lane per piece of
+// at most SEG_MAX cells, are stored straight there (k_seg_place).
 // ---------------------------------------------------------------------------
 constexpr int KMAX = 32;                 // saddles with more chains take the serial pass
 constexpr uint32_t HOP_END = 0xFFFFFFFFu;
