@@ -372,7 +372,7 @@ def bench_pipeline(M, torch, n=16384, levels=8, runs=2, cpu_side=1024):
     stages, seq, root = last
     out = {"workload": PIPE_WORKLOAD, "Mvert_per_s": round(n * n / wall / 1e6, 2), "s_per_run": round(wall, 3),
            "runs": runs, "stages_ms": {k: round(v, 1) for k, v in stages.items()},
-           "one_thread_boundary_steps_ms": {k: round(v, 1) for k, v in seq.items()},
+           "boundary_steps_ms": {k: round(v, 1) for k, v in seq.items()},
            "root_complex": {"critical_points": root[0], "asc": root[1], "des": root[2]}}
     if cpu_side:
         # the oracle's whole pipeline (one thread) on a smaller field of the same kind, 2 levels of splits

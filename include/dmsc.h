@@ -166,8 +166,9 @@ int dmsc_pipeline_write_discs(dmsc_pipeline *p, const char *prefix);
 /* Host wall time (ms) of the last run's stages: pieces, merge up, simplify,
  * merge down, discs. */
 int dmsc_pipeline_stage_times(dmsc_pipeline *p, double ms[5]);
-/* Of merge up and merge down, the host wall time (ms) spent in the steps
- * that run one thread per merge (the boundary cancellations). */
+/* Of merge up and merge down, the host wall time (ms) spent in the boundary
+ * steps: merge up's cancellations (ordered-parallel rounds) and merge down's
+ * uncancellations (one thread per merge). */
 int dmsc_pipeline_merge_times(dmsc_pipeline *p, double ms[2]);
 /* Tree levels whose largest merge involves at least min_cps critical points
  * (default 2048) run the parallel merges; smaller levels run every merge on

@@ -124,21 +124,27 @@ inline __host__ __device__ void merge_up_one(MGraph *in[2], MGraph &out, CRect i
   merge_up_cancel(out, ixn, status);
 }
 
+// One cell (x, y) of merge_up's boundary loop (:125-152); false where the
+// loop stops on a reference logic_error condition (status set).
+inline __host__ __device__ bool merge_up_cell(MGraph &out, int x, int y, uint32_t *status) {
+  uint32_t si = out.find(pack_cellid(x, y));
+  if (si == NO_CP) { set_status(status, ST_INVARIANT); return false; }  // "missing common bndry cp"
+  if ((out.G.flags[si] & F_CANCELLED) || !(out.G.flags[si] & F_BCANCEL)) return true;
+  uint32_t pi = out.G.pair_idx[si];
+  if (pi >= out.G.ncp) { set_status(status, ST_INVARIANT); return false; }
+  uint32_t p = out.G.cellid[pi];
+  if (!out.rect.interior(x, y) && !out.ext.boundary(x, y)) return true;
+  if (!out.rect.interior(px_(p), py_(p)) && !out.ext.boundary(px_(p), py_(p))) return true;
+  uint32_t a = si, b = pi;
+  out.G.cancel_pairs(a, b);
+  return true;
+}
+
 // merge_up's cancellation along the shared boundary (:124-153), row-major
 inline __host__ __device__ void merge_up_cancel(MGraph &out, CRect ixn, uint32_t *status) {
   for (int y = ixn.b; y <= ixn.t && !out.G.fail; ++y)
-    for (int x = ixn.l; x <= ixn.r && !out.G.fail; ++x) {
-      uint32_t si = out.find(pack_cellid(x, y));
-      if (si == NO_CP) { set_status(status, ST_INVARIANT); return; }  // "missing common bndry cp"
-      if ((out.G.flags[si] & F_CANCELLED) || !(out.G.flags[si] & F_BCANCEL)) continue;
-      uint32_t pi = out.G.pair_idx[si];
-      if (pi >= out.G.ncp) { set_status(status, ST_INVARIANT); return; }
-      uint32_t p = out.G.cellid[pi];
-      if (!out.rect.interior(x, y) && !out.ext.boundary(x, y)) continue;
-      if (!out.rect.interior(px_(p), py_(p)) && !out.ext.boundary(px_(p), py_(p))) continue;
-      uint32_t a = si, b = pi;
-      out.G.cancel_pairs(a, b);
-    }
+    for (int x = ixn.l; x <= ixn.r && !out.G.fail; ++x)
+      if (!merge_up_cell(out, x, y, status)) return;
 }
 
 // merge_down (grid_mscomplex.cpp:158-322) of parent P into one child C; the

@@ -626,6 +626,160 @@ __global__ void k_merge_seq(MGraph *graphs, const SeqJob *jobs, int njobs, uint3
   graphs[jb.g0] = g0;
 }
 
+// ---------------------------------------------------------------------------
+// merge_up's boundary cancellations in ordered-parallel rounds.  Task t is
+// cell t of the shared boundary in row-major order.  Each round, every
+// pending task reserves its footprint -- the critical points whose lists or
+// flags its cancellation reads or writes -- with the round-tagged key
+// (round, t) in a per-point slot (atomicMin: the round's smallest task
+// touching the point wins); tasks sharing a slot are joined in a union-find
+// that hooks the larger root under the smaller; and the root of each group,
+// its smallest task, runs.  Edges are only added inside a running task's
+// footprint, so groups cannot merge through growth and every task sees the
+// graph the row-major loop would show it.  One block per merge; the rounds
+// are separated by barriers of the block.  Each thread allocates list room
+// from its own slice of the pool's free part, so the graph code stays that of
+// one thread.
+// ---------------------------------------------------------------------------
+constexpr int ROUND_THREADS = 512, ROUND_TASKS = 32768;
+struct RoundSmem {
+  uint32_t parent[ROUND_TASKS];
+  uint32_t done[ROUND_TASKS / 32];
+};
+
+__device__ __forceinline__ uint32_t uf_root(uint32_t *parent, uint32_t a) {
+  for (int guard = 0; guard < ROUND_TASKS; ++guard) {  // parents only point to smaller tasks
+    const uint32_t p = ((volatile uint32_t *)parent)[a];
+    if (p == a) return a;
+    a = p;
+  }
+  return a;
+}
+__device__ __forceinline__ void uf_join(uint32_t *parent, uint32_t a, uint32_t b) {
+  for (int guard = 0; guard < 4 * ROUND_TASKS; ++guard) {
+    a = uf_root(parent, a);
+    b = uf_root(parent, b);
+    if (a == b) return;
+    if (a > b) { const uint32_t t = a; a = b; b = t; }
+    if (atomicCAS(&parent[b], b, a) == b) return;
+  }
+}
+
+// The cell's point and, while it may still cancel, its partner and both
+// points' neighbours.
+template <class F>
+__device__ void up_footprint(const MGraph &M, uint32_t si, F f) {
+  f(si);
+  const uint8_t fl = M.G.flags[si];
+  if ((fl & F_CANCELLED) || !(fl & F_BCANCEL)) return;
+  const uint32_t pi = M.G.pair_idx[si];
+  if (pi >= M.G.ncp) return;
+  f(pi);
+  const uint32_t c2[2] = {si, pi};
+  for (int k = 0; k < 2; ++k)
+    for (int w = 0; w < 2; ++w) {
+      const uint32_t l = 2 * c2[k] + w, n = M.G.L.nrun[l];
+      const uint2 *r = M.G.L.pool + M.G.L.off[l];
+      for (uint32_t q = 0; q < n; ++q) f(r[q].x);
+    }
+}
+
+// Whether cell (x, y) can ever act: the rect / ext test of the loop on it and
+// its partner (fixed for the whole loop; flags are not).
+__device__ __forceinline__ bool up_cell_static(const MGraph &M, int x, int y, uint32_t si) {
+  if (si >= M.G.ncp) return true;  // left to the loop body, which reports it
+  const uint32_t pi = M.G.pair_idx[si];
+  if (pi >= M.G.ncp) return true;
+  const uint32_t p = M.G.cellid[pi];
+  return (M.rect.interior(x, y) || M.ext.boundary(x, y)) && (M.rect.interior(px_(p), py_(p)) || M.ext.boundary(px_(p), py_(p)));
+}
+
+__global__ void __launch_bounds__(ROUND_THREADS, 1) k_merge_up_rounds(MGraph *graphs, const SeqJob *jobs, int njobs,
+                                                                      unsigned long long *const *slots, uint32_t *status) {
+  extern __shared__ __align__(16) unsigned char round_smem[];
+  RoundSmem &S = *reinterpret_cast<RoundSmem *>(round_smem);
+  __shared__ int abort_all;
+  const int b = blockIdx.x;
+  if (b >= njobs) return;
+  const SeqJob jb = jobs[b];
+  MGraph g = graphs[jb.g0];  // every thread's own descriptor copy, read before any write-back
+  const long long w = jb.ixn.r - jb.ixn.l + 1, h = jb.ixn.t - jb.ixn.b + 1, n = w * h;
+  unsigned long long *slot = slots[b];
+  if (n > ROUND_TASKS || !slot) {  // one thread, as k_merge_seq
+    if (threadIdx.x == 0) {
+      merge_up_cancel(g, jb.ixn, status);
+      if (g.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+      graphs[jb.g0] = g;
+    }
+    return;
+  }
+  if (threadIdx.x == 0) abort_all = 0;
+  for (long long t = threadIdx.x; t < ROUND_TASKS / 32; t += blockDim.x) S.done[t] = 0;
+  __syncthreads();
+  const unsigned long long room = (g.G.L.pool_cap - g.G.L.top) / blockDim.x, pool_end = g.G.L.pool_cap;
+  g.G.L.top += room * threadIdx.x;  // this thread's slice of the free pool
+  g.G.L.pool_cap = g.G.L.top + room;
+  g.G.tmp_cap = 0;  // no shared scratch: cancel_pairs takes its per-entry path (the same result)
+  auto cell_of = [&](long long t, int &x, int &y) { x = jb.ixn.l + (int)(t % w); y = jb.ixn.b + (int)(t / w); };
+  auto is_done = [&](long long t) { return (S.done[t >> 5] >> (t & 31)) & 1u; };
+  // cells that can never act are done from the start
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    int x, y;
+    cell_of(t, x, y);
+    const uint32_t si = g.find(pack_cellid(x, y));
+    if (si != NO_CP && !up_cell_static(g, x, y, si)) atomicOr(&S.done[t >> 5], 1u << (t & 31));
+  }
+  for (uint32_t round = 0; round < (uint32_t)n + 1; ++round) {
+    int mine = 0;
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) mine |= !is_done(t);
+    if (!__syncthreads_or(mine) || abort_all) break;
+    const unsigned long long hi = (unsigned long long)(0xFFFFFFFFu - round) << 32;
+    // reserve
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+      if (is_done(t)) continue;
+      S.parent[t] = (uint32_t)t;
+      int x, y;
+      cell_of(t, x, y);
+      const uint32_t si = g.find(pack_cellid(x, y));
+      if (si >= g.G.ncp) continue;  // the loop body reports it when the task runs
+      up_footprint(g, si, [&](uint32_t c) { if (c < g.G.ncp) atomicMin(&slot[c], hi | (unsigned long long)t); });
+    }
+    __syncthreads();
+    // join the tasks that share a point
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+      if (is_done(t)) continue;
+      int x, y;
+      cell_of(t, x, y);
+      const uint32_t si = g.find(pack_cellid(x, y));
+      if (si >= g.G.ncp) continue;
+      up_footprint(g, si, [&](uint32_t c) {
+        if (c >= g.G.ncp) return;
+        const unsigned long long v = slot[c];
+        if ((v & 0xFFFFFFFF00000000ull) == hi && (v & 0xFFFFFFFFull) < (unsigned long long)n)
+          uf_join(S.parent, (uint32_t)t, (uint32_t)(v & 0xFFFFFFFFull));
+      });
+    }
+    __syncthreads();
+    // the smallest task of each group runs
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+      if (is_done(t) || uf_root(S.parent, (uint32_t)t) != (uint32_t)t) continue;
+      int x, y;
+      cell_of(t, x, y);
+      if (!merge_up_cell(g, x, y, status) || g.G.fail) abort_all = 1;
+      atomicOr(&S.done[t >> 5], 1u << (t & 31));
+    }
+    __syncthreads();
+  }
+  if (g.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+  __syncthreads();
+  if (threadIdx.x == 0) {  // the slices are used up: later allocations of this graph find no room
+    g.G.L.top = pool_end;
+    g.G.L.pool_cap = pool_end;
+    g.G.tmp_cap = graphs[jb.g0].G.tmp_cap;
+    graphs[jb.g0] = g;
+  }
+}
+
 MGraph &mg(MGraphHost &h) { return *reinterpret_cast<MGraph *>(h.raw); }
 
 // List pool (runs) beyond the lists themselves for the one-thread steps
@@ -653,20 +807,49 @@ cudaError_t run_seq(std::vector<MGraphHost *> &graphs, const std::vector<SeqJob>
   } acc{ms, t0};
   const size_t ng = graphs.size();
   char *buf = nullptr;
-  const size_t gb = sizeof(MGraph) * ng, jbytes = sizeof(SeqJob) * jobs.size();
-  cudaError_t e = cudaMallocAsync((void **)&buf, gb + jbytes + 64, st);
+  const size_t nj = jobs.size();
+  const size_t gb = sizeof(MGraph) * ng, jbytes = sizeof(SeqJob) * nj;
+  // merge_up's jobs run in rounds: per job a slot per critical point of its
+  // graph (round-tagged keys, all ones = empty) and a pool top
+  const bool rounds = jobs[0].kind == SEQ_UP_CANCEL;
+  std::vector<size_t> soff(nj, 0);
+  size_t sbytes = 0;
+  if (rounds)
+    for (size_t k = 0; k < nj; ++k) {
+      soff[k] = sbytes;
+      sbytes += 8ull * ((mg(*graphs[jobs[k].g0]).G.ncp + 1 + 31) / 32 * 32);
+    }
+  const size_t head = (gb + 15) / 16 * 16 + (jbytes + 15) / 16 * 16, pbytes = rounds ? (8ull * nj + 15) / 16 * 16 : 0;
+  cudaError_t e = cudaMallocAsync((void **)&buf, head + pbytes + sbytes + 64, st);
   if (e != cudaSuccess) return e;
   MGraph *dg = (MGraph *)buf;
   SeqJob *dj = (SeqJob *)(buf + ((gb + 15) / 16) * 16);
+  unsigned long long **dslot = (unsigned long long **)(buf + head);
+  unsigned long long *slots = (unsigned long long *)(buf + head + pbytes);
   std::vector<MGraph> hg(ng);
   for (size_t i = 0; i < ng; ++i) hg[i] = mg(*graphs[i]);
   e = cudaMemcpyAsync(dg, hg.data(), gb, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dj, jobs.data(), jbytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && rounds) {
+    std::vector<unsigned long long *> hp(nj);
+    for (size_t k = 0; k < nj; ++k) hp[k] = slots + soff[k] / 8;
+    e = cudaMemcpyAsync(dslot, hp.data(), 8ull * nj, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(slots, 0xFF, sbytes, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // hp is read before it goes out of scope
+  }
   if (e == cudaSuccess) {
-    k_seq_prefetch<<<dim3(64, (unsigned)jobs.size()), 256, 0, st>>>(dg, dj, nullptr);
-    k_merge_seq<<<(unsigned)jobs.size(), 32, 0, st>>>(dg, dj, (int)jobs.size(), status);
+    k_seq_prefetch<<<dim3(64, (unsigned)nj), 256, 0, st>>>(dg, dj, nullptr);
+    if (rounds) {
+      static const cudaError_t attr = cudaFuncSetAttribute(k_merge_up_rounds, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                           (int)sizeof(RoundSmem));
+      e = attr;
+      if (e == cudaSuccess)
+        k_merge_up_rounds<<<(unsigned)nj, ROUND_THREADS, sizeof(RoundSmem), st>>>(dg, dj, (int)nj, dslot, status);
+    } else {
+      k_merge_seq<<<(unsigned)nj, 32, 0, st>>>(dg, dj, (int)nj, status);
+    }
     DMSC_LAUNCHED(2);
-    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(hg.data(), dg, gb, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -301,7 +301,9 @@ class GridDataManager:
         return dict(zip(self.STAGES, (float(v) for v in ms)))
 
     def merge_seq_times(self) -> dict:
-        """Of merge up / down, the ms spent in the one-thread boundary steps."""
+        """Of merge up / down, the ms spent in the boundary steps (merge up's
+        cancellations in ordered-parallel rounds, merge down's uncancellations
+        on one thread per merge)."""
         ms = np.zeros(2, np.float64)
         check(self.lib.dmsc_pipeline_merge_times(self.h, _ptr(ms)))
         return {"merge_up": float(ms[0]), "merge_down": float(ms[1])}
