@@ -639,7 +639,11 @@ __global__ void k_merge_seq(MGraph *graphs, const SeqJob *jobs, int njobs, uint3
 // graph the row-major loop would show it.  One block per merge; the rounds
 // are separated by barriers of the block.  Each thread allocates list room
 // from its own slice of the pool's free part, so the graph code stays that of
-// one thread.
+// one thread.  Where the groups stay large (one point in most footprints), the
+// rounds would cost the square of the boundary: past a budget of pending-task
+// evaluations, thread 0 runs the remaining tasks in row-major order, which is
+// exact at any round boundary (every task that ran commutes with every
+// earlier one still pending), from a quarter of the free pool kept for it.
 // ---------------------------------------------------------------------------
 constexpr int ROUND_THREADS = 512, ROUND_TASKS = 32768;
 struct RoundSmem {
@@ -699,6 +703,7 @@ __global__ void __launch_bounds__(ROUND_THREADS, 1) k_merge_up_rounds(MGraph *gr
   extern __shared__ __align__(16) unsigned char round_smem[];
   RoundSmem &S = *reinterpret_cast<RoundSmem *>(round_smem);
   __shared__ int abort_all;
+  __shared__ unsigned long long work;  // pending-task evaluations so far
   const int b = blockIdx.x;
   if (b >= njobs) return;
   const SeqJob jb = jobs[b];
@@ -713,10 +718,13 @@ __global__ void __launch_bounds__(ROUND_THREADS, 1) k_merge_up_rounds(MGraph *gr
     }
     return;
   }
-  if (threadIdx.x == 0) abort_all = 0;
+  if (threadIdx.x == 0) { abort_all = 0; work = 0; }
   for (long long t = threadIdx.x; t < ROUND_TASKS / 32; t += blockDim.x) S.done[t] = 0;
   __syncthreads();
-  const unsigned long long room = (g.G.L.pool_cap - g.G.L.top) / blockDim.x, pool_end = g.G.L.pool_cap;
+  const unsigned long long free_runs = g.G.L.pool_cap - g.G.L.top, pool_end = g.G.L.pool_cap;
+  const unsigned long long room = (free_runs - free_runs / 4) / blockDim.x, fin_start = g.G.L.top + room * blockDim.x;
+  const unsigned long long budget = 128ull * (unsigned long long)n;
+  const unsigned long long tmp_cap0 = g.G.tmp_cap;
   g.G.L.top += room * threadIdx.x;  // this thread's slice of the free pool
   g.G.L.pool_cap = g.G.L.top + room;
   g.G.tmp_cap = 0;  // no shared scratch: cancel_pairs takes its per-entry path (the same result)
@@ -731,8 +739,11 @@ __global__ void __launch_bounds__(ROUND_THREADS, 1) k_merge_up_rounds(MGraph *gr
   }
   for (uint32_t round = 0; round < (uint32_t)n + 1; ++round) {
     int mine = 0;
-    for (long long t = threadIdx.x; t < n; t += blockDim.x) mine |= !is_done(t);
-    if (!__syncthreads_or(mine) || abort_all) break;
+    unsigned long long cnt = 0;
+    for (long long t = threadIdx.x; t < n; t += blockDim.x)
+      if (!is_done(t)) { mine = 1; ++cnt; }
+    atomicAdd(&work, cnt);
+    if (!__syncthreads_or(mine) || abort_all || work > budget) break;
     const unsigned long long hi = (unsigned long long)(0xFFFFFFFFu - round) << 32;
     // reserve
     for (long long t = threadIdx.x; t < n; t += blockDim.x) {
@@ -772,10 +783,25 @@ __global__ void __launch_bounds__(ROUND_THREADS, 1) k_merge_up_rounds(MGraph *gr
   }
   if (g.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
   __syncthreads();
-  if (threadIdx.x == 0) {  // the slices are used up: later allocations of this graph find no room
+  if (threadIdx.x == 0) {
+    if (!abort_all) {  // tasks left by the budget, in row-major order on this thread
+      MGraph f = g;
+      f.G.L.top = fin_start;
+      f.G.L.pool_cap = pool_end;
+      f.G.tmp_cap = tmp_cap0;
+      f.G.fail = false;
+      for (long long t = 0; t < n && !f.G.fail; ++t) {
+        if (is_done(t)) continue;
+        int x, y;
+        cell_of(t, x, y);
+        if (!merge_up_cell(f, x, y, status)) break;
+      }
+      if (f.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
+    }
+    // the slices are used up: later allocations of this graph find no room
     g.G.L.top = pool_end;
     g.G.L.pool_cap = pool_end;
-    g.G.tmp_cap = graphs[jb.g0].G.tmp_cap;
+    g.G.tmp_cap = tmp_cap0;
     graphs[jb.g0] = g;
   }
 }
