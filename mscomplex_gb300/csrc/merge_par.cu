@@ -723,7 +723,7 @@ __global__ void __launch_bounds__(ROUND_THREADS, 1) k_merge_up_rounds(MGraph *gr
   __syncthreads();
   const unsigned long long free_runs = g.G.L.pool_cap - g.G.L.top, pool_end = g.G.L.pool_cap;
   const unsigned long long room = (free_runs - free_runs / 4) / blockDim.x, fin_start = g.G.L.top + room * blockDim.x;
-  const unsigned long long budget = 128ull * (unsigned long long)n;
+  const unsigned long long budget = 512ull * (unsigned long long)n;
   const unsigned long long tmp_cap0 = g.G.tmp_cap;
   g.G.L.top += room * threadIdx.x;  // this thread's slice of the free pool
   g.G.L.pool_cap = g.G.L.top + room;
