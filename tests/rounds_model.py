@@ -177,3 +177,91 @@ def same(G, H):
             if {x: v for x, v in a.items() if v} != {x: v for x, v in b.items() if v}:
                 return False
     return True
+
+
+# merge_down's uncancellation along the boundary (grid_mscomplex.cpp:172-201,
+# uncancel_pairs in discreteMorseAlgorithm.h:1006-1089), on the merged parent.
+
+def down_tasks(G, rect, ext, ixn):
+    """One task per boundary cell, reverse row-major."""
+    out = []
+    for y in range(ixn.t, ixn.b - 1, -1):
+        for x in range(ixn.r, ixn.l - 1, -1):
+            si = G["idx"][(x, y)]
+            pi = G["pair"][si]
+            ok = pi is not None and (rect.interior(x, y) or ext.boundary(x, y)) and \
+                (rect.interior(*G["cid"][pi]) or ext.boundary(*G["cid"][pi]))
+            out.append((si, pi if ok else None))
+    return out
+
+
+def down_footprint(G, t):
+    si, pi = t
+    if pi is None or not (G["flags"][si] & CANC):
+        return {si}
+    s = {si, pi}
+    for c in (si, pi):
+        for L in (G["asc"][c], G["des"][c]):
+            for r in L:
+                s.add(r)
+                if G["flags"][r] & BC and G["pair"][r] is not None:
+                    s.add(G["pair"][r])
+    return s
+
+
+def run_down(G, t):
+    si, pi = t
+    flags, asc, des, pair = G["flags"], G["asc"], G["des"], G["pair"]
+    if pi is None or not (flags[si] & CANC):
+        return
+    c1, c2 = si, pi
+    if c2 not in asc[c1]:
+        c1, c2 = c2, c1
+    for i, (L, other) in enumerate(((asc[c1], c2), (des[c2], c1))):
+        assert other in L, "cancellable pair is not connected"
+        new = defaultdict(int)
+        for rx, cx in list(L.items()):
+            if rx == other:
+                continue
+            if not (flags[rx] & BC):
+                new[rx] += cx
+                continue
+            assert not (flags[rx] & CANC)
+            p = pair[rx]
+            for ry, cy in (asc[p] if i == 0 else des[p]).items():
+                new[ry] += cx * cy
+        L.clear()
+        L.update(new)
+    flags[c1] &= ~CANC
+    flags[c2] &= ~CANC
+
+
+def run_down_rounds(G, T):
+    """The rounds schedule of run_rounds with the uncancellation's footprint."""
+    pending, rounds = list(range(len(T))), 0
+    while pending:
+        rounds += 1
+        fp = {t: down_footprint(G, T[t]) for t in pending}
+        slot = {}
+        for t in pending:
+            for c in fp[t]:
+                slot.setdefault(c, t)
+        parent = {t: t for t in pending}
+
+        def root(a):
+            while parent[a] != a:
+                parent[a] = parent[parent[a]]
+                a = parent[a]
+            return a
+
+        for t in pending:
+            for c in fp[t]:
+                ra, rb = root(t), root(slot[c])
+                if ra != rb:
+                    parent[max(ra, rb)] = min(ra, rb)
+        commit = [t for t in pending if root(t) == t]
+        for t in commit:
+            run_down(G, T[t])
+        done = set(commit)
+        pending = [t for t in pending if t not in done]
+    return rounds

@@ -49,3 +49,21 @@ def test_rounds_on_a_smooth_field(oracle):
     par = copy.deepcopy(G0)
     run_rounds(par, T)
     assert same(par, seq)
+
+
+@pytest.mark.parametrize("n,seed", [(96, 2), (128, 5)])
+def test_down_rounds_leave_the_loop_result(oracle, n, seed):
+    """merge_down's uncancellation in the same rounds (footprint: the pair, its
+    neighbours and their partners) on the parent that merge_up's loop leaves."""
+    from mscomplex_gb300 import synth
+    from rounds_model import down_tasks, run_down, run_down_rounds
+    G, rect, ext, ixn = two_pieces(oracle, synth.noise(n, seed=seed))
+    for t in tasks(G, rect, ext, ixn):
+        run(G, t)
+    T = down_tasks(G, rect, ext, ixn)
+    seq = copy.deepcopy(G)
+    for t in T:
+        run_down(seq, t)
+    par = copy.deepcopy(G)
+    run_down_rounds(par, T)
+    assert same(par, seq)
