@@ -44,23 +44,42 @@ SIMPLIFY_TRESH = 0.01
 # heap pushes + pops of the reference's simplification of this field at 1%,
 # counted by the oracle (2.956808816e9 pushes, 2.954259461e9 pops)
 SIMPLIFY_HEAP_OPS = 2956808816 + 2954259461
-# Algorithmic bytes of the single-kernel stages: (per vertex, per critical point, per arc, per disc cell).
+# The kernels of the step that the launch list ranks highest, each timed live
+# with its own CUDA events, with their algorithmic bytes (outputs and the
+# height input only; intermediate structures are not counted):
+#   (per vertex, per critical point, per arc, per saddle disc cell of the asc / des kind)
 KERNEL_BYTES = {
-    "gradient": (8.0, 0, 0, 0),        # k_gradient: 4 B height read + 4 B gradient codes written
-    "labels_arcs": (20.0, 12, 8, 0),   # k_labels: 4 B codes read + 16 B owner labels written; cp records, arcs
-    "disc_hops": (32.0, 0, 0, 0),      # k_disc_hops: 4 B codes read; per edge (2 a vertex) 14 B of hop data written
+    "gradient": (8.0, 0, 0, 0, 0),        # k_gradient: 4 B height read + 4 B gradient codes (1 B per cell)
+    "labels_arcs": (16.0, 12, 8, 0, 0),   # k_labels: 16 B owner labels (4 B per cell), cp records, arcs
+    "disc_hops": (0.0, 0, 0, 0, 0),       # k_disc_hops: writes only the hop structure (intermediate)
+    "seg_place_asc": (0.0, 0, 0, 4, 0),   # k_seg_place (asc): 4 B per saddle disc cell written
+    "seg_place_des": (0.0, 0, 0, 0, 4),   # k_seg_place (des)
 }
-KERNEL_NAMES = {"gradient": "k_gradient", "labels_arcs": "k_labels", "disc_hops": "k_disc_hops"}
+KERNEL_NAMES = {"gradient": "k_gradient", "labels_arcs": "k_labels", "disc_hops": "k_disc_hops",
+                "seg_place_asc": "k_seg_place", "seg_place_des": "k_seg_place"}
+TRAFFIC_KEYS = {"gradient": "k_gradient", "labels_arcs": "k_labels", "disc_hops": "k_disc_hops",
+                "seg_place_asc": "k_seg_place:asc", "seg_place_des": "k_seg_place:des"}
 # The whole step: 24 B/vertex (height, gradient, owner labels) + 12 B/cp + 8 B/arc + 4 B per disc cell written.
 PIPE_BYTES = (24.0, 12, 8, 4)
 
 
-def stage_bytes(stage, nverts, ncp, narcs, ndisc):
-    v, c, a, d = KERNEL_BYTES.get(stage, (0, 0, 0, 0)) if stage != "pipeline" else PIPE_BYTES
-    return v * nverts + c * ncp + a * narcs + d * ndisc
+def stage_bytes(stage, nverts, ncp, narcs, ndisc, sdisc=(0, 0)):
+    if stage == "pipeline":
+        v, c, a, d = PIPE_BYTES
+        return v * nverts + c * ncp + a * narcs + d * ndisc
+    v, c, a, sa, sd = KERNEL_BYTES.get(stage, (0, 0, 0, 0, 0))
+    return v * nverts + c * ncp + a * narcs + sa * sdisc[0] + sd * sdisc[1]
 
 
-def simplify_rate(M, ds, stream, sh, torch, budget=20_000_000):
+def saddle_disc_cells(ex: dict):
+    """Cells of the saddles' asc and des discs in an exported complex."""
+    c = ex["cellid"].astype(np.int64)
+    sad = ((c[:, 0] & 1) + (c[:, 1] & 1)) == 1
+    return (int(np.diff(ex["adisc_off"].astype(np.int64))[sad].sum()),
+            int(np.diff(ex["ddisc_off"].astype(np.int64))[sad].sum()))
+
+
+def simplify_rate(M, ds, stream, sh, torch, budget=5_000_000):
     """Runs the exact device replay of simplify_un_simplify at 1% on a fresh
     complex of the field until `budget` operations, and reports its rate."""
     m = ds.writeout_connectivity(stream=sh)
@@ -82,6 +101,28 @@ def simplify_rate(M, ds, stream, sh, torch, budget=20_000_000):
             "pops": st["pops"], "pushes": st["pushes"], "cancellations": st["cancels"], "ms": round(ms, 3),
             "heap_ops_per_s": round(rate, 1) if rate else None, "field_heap_ops": SIMPLIFY_HEAP_OPS,
             "field_est_s": round(SIMPLIFY_HEAP_OPS / rate, 1) if rate else None}
+
+
+def cpu_simplify_rate(field: np.ndarray, side: int = 1024):
+    """The oracle's simplify_un_simplify (one thread, libstdc++ heap) at 1% on
+    a window of the field, run to completion on the host: heap operations per
+    second (the time of the run with simplification minus the time without)."""
+    from oracle import oracle as O
+    O.build()
+    win = cpu_sample_field(field, side)
+    r = (0, 0, 2 * (side - 1), 2 * (side - 1))
+    t0 = time.perf_counter()
+    O.Dataset(win, r, r, tresh=0.0)
+    t1 = time.perf_counter()
+    O.simplify_stats()
+    O.Dataset(win, r, r, tresh=SIMPLIFY_TRESH)
+    t2 = time.perf_counter()
+    st = O.simplify_stats()
+    secs = max(1e-9, (t2 - t1) - (t1 - t0))
+    ops = st["pushes"] + st["pops"]
+    return {"cpu_heap_ops_per_s": round(ops / secs, 1), "cpu_cores": 1,
+            "cpu_sample": f"{side}x{side} window of the field at 1% of its range: {ops} heap operations, "
+                          f"{st['cancels']} cancellations, {secs:.2f} s"}
 
 
 def peaks():
@@ -284,20 +325,23 @@ def serve_requests(count: int, seed: int = 4):
     return reqs
 
 
-def bench_served(M, torch, count=300, rates=(None, 200.0), max_ops=2_000_000, lanes=4):
+def bench_served(M, torch, count=300, rates=((None, 300), (200.0, 300), (40.0, 120), (20.0, 120), (10.0, 120)),
+                 max_ops=2_000_000, lanes=4):
     """The request server under a Poisson stream (rate None = every request
-    submitted at once, i.e. saturation) against plain one-request-at-a-time
-    processing through the per-grid API.  Latency = submit -> result ready."""
+    submitted at once, i.e. saturation; each rate with its number of
+    requests, the first ones of the same mix) against plain
+    one-request-at-a-time processing through the per-grid API.  Latency =
+    submit -> result ready; grids_per_s counts completed requests only."""
     reqs = serve_requests(count)
     out = {"workload": SERVE_WORKLOAD, "requests": count, "max_ops_per_request": max_ops, "lanes": lanes, "runs": []}
-    for rate in rates:
+    for rate, nreq in rates:
         rng = np.random.default_rng(11)
-        gaps = np.zeros(count) if rate is None else rng.exponential(1.0 / rate, count)
+        gaps = np.zeros(nreq) if rate is None else rng.exponential(1.0 / rate, nreq)
         srv = M.GridServer(arena_bytes=150 << 30, lanes=lanes, max_batch=128, max_ops=max_ops)
         t0 = time.perf_counter()
         ids = []
         next_t = 0.0
-        for (f, t), gap in zip(reqs, gaps):
+        for (f, t), gap in zip(reqs[:nreq], gaps):
             next_t += gap
             while time.perf_counter() - t0 < next_t:
                 time.sleep(0.0002)
@@ -314,10 +358,11 @@ def bench_served(M, torch, count=300, rates=(None, 200.0), max_ops=2_000_000, la
         st = srv.stats()
         srv.close()
         lat = np.array(lat) if lat else np.zeros(1)
-        out["runs"].append({"rate_per_s": rate if rate is not None else "saturation",
-                            "grids_per_s": round(count / wall, 2), "p50_ms": round(float(np.percentile(lat, 50)), 2),
-                            "p99_ms": round(float(np.percentile(lat, 99)), 2), "failed": fails,
-                            "batches": st["batches"]})
+        out["runs"].append({"rate_per_s": rate if rate is not None else "saturation", "requests": nreq,
+                            "completed": nreq - fails, "failed": fails, "failed_frac": round(fails / nreq, 4),
+                            "grids_per_s": round((nreq - fails) / wall, 2),
+                            "p50_ms": round(float(np.percentile(lat, 50)), 2),
+                            "p99_ms": round(float(np.percentile(lat, 99)), 2), "batches": st["batches"]})
     # plain: one request at a time, each through dataset / writeout / simplify / export;
     # all submitted at t0 like the saturation run, so latency includes waiting
     t0 = time.perf_counter()
@@ -332,13 +377,15 @@ def bench_served(M, torch, count=300, rates=(None, 200.0), max_ops=2_000_000, la
             m.export()
         except M.DmscError:
             fails += 1
+            continue
         now = time.perf_counter()
         svc.append((now - s0) * 1e3)
         lat.append((now - t0) * 1e3)
     wall = time.perf_counter() - t0
     lat, svc = np.array(lat), np.array(svc)
-    out["plain"] = {"grids_per_s": round(count / wall, 2), "p50_ms": round(float(np.percentile(lat, 50)), 2),
-                    "p99_ms": round(float(np.percentile(lat, 99)), 2), "failed": fails,
+    out["plain"] = {"grids_per_s": round((count - fails) / wall, 2), "completed": count - fails, "failed": fails,
+                    "p50_ms": round(float(np.percentile(lat, 50)), 2),
+                    "p99_ms": round(float(np.percentile(lat, 99)), 2),
                     "service_p50_ms": round(float(np.percentile(svc, 50)), 2),
                     "service_p99_ms": round(float(np.percentile(svc, 99)), 2),
                     "note": "sequential, all submitted at once: latency = completion time since submission"}
@@ -496,6 +543,7 @@ def main():
         msc = step()
     torch.cuda.synchronize()
     ncp, nasc, ndes, nadisc, nddisc = msc.sizes()
+    sdisc = saddle_disc_cells(msc.export())
 
     # ---- device-resident timed region ----
     clocks = ClockSampler(local)
@@ -521,16 +569,21 @@ def main():
     total_ms = max_over_ranks(sum(times), world)
     value = replicas_value(nverts * args.steps, world, total_ms / 1e3) / 1e6
 
-    # roofline of the dominant kernel (median stage time, live CUDA events)
+    # roofline of the dominant kernel: the longest of the live-timed kernels
+    # (median over the steps), its algorithmic bytes over that time
     med = {k: statistics.median(v) for k, v in stages.items()}
     dom = max(KERNEL_BYTES, key=lambda k: med[k])
-    alg_bytes = stage_bytes(dom, nverts, ncp, nasc + ndes, nadisc + nddisc)
+    alg_bytes = stage_bytes(dom, nverts, ncp, nasc + ndes, nadisc + nddisc, sdisc)
     peak, peak_kind = peaks()
     achieved = alg_bytes / (med[dom] / 1e3) / 1e9
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
-        traffic = json.load(open(tp)).get(f"{KERNEL_NAMES[dom]}:bumps4096q")
+        traffic = json.load(open(tp)).get(f"{TRAFFIC_KEYS[dom]}:bumps4096q")
+    kernels = {k: {"kernel": KERNEL_NAMES[k], "ms": round(med[k], 4),
+                   "alg_bytes": int(stage_bytes(k, nverts, ncp, nasc + ndes, nadisc + nddisc, sdisc)),
+                   "frac": round(stage_bytes(k, nverts, ncp, nasc + ndes, nadisc + nddisc, sdisc)
+                                 / (med[k] / 1e3) / 1e9 / peak, 4)} for k in KERNEL_BYTES}
     pipe_bytes = stage_bytes("pipeline", nverts, ncp, nasc + ndes, nadisc + nddisc)
 
     # ---- persistence cancellation at 1%: device replay rate under an operation budget ----
@@ -605,13 +658,15 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "grid": [nx, ny], "levels": 0, "critical_points": ncp,
                        "arcs": [nasc, ndes], "disc_cells": [nadisc, nddisc],
+                       "saddle_disc_cells": list(sdisc),
                        "simplification": "excluded from the step; measured in simplify",
                        "l2": "flushed between steps (256 MB write)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "stages_ms": {k: round(v, 4) for k, v in med.items()},
-            "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": round(achieved, 1), "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+            "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "stage": dom, "achieved": round(achieved, 1),
+                         "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "alg_bytes_per_launch": int(alg_bytes), "traffic": traffic},
+            "kernels": kernels,
             "pipeline_roofline": {"alg_bytes": int(pipe_bytes),
                                   "frac": round(pipe_bytes / (total_ms / args.steps / 1e3) / 1e9 / peak, 4)},
             "simplify": simp,
@@ -622,6 +677,7 @@ def main():
         }
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(field)
+            line["simplify"].update(cpu_simplify_rate(field))
         if world == 1 and not args.no_batch:
             line["batched"] = bench_batched(M, torch, stream, sh)
             line["served"] = bench_served(M, torch)

@@ -69,9 +69,15 @@ int dmsc_dataset_destroy(dmsc_dataset *ds);
  * on_device = 0: host pointer (copied); 1: device pointer (borrowed, must stay
  * valid until the dataset is destroyed or re-initialised). */
 int dmsc_dataset_init(dmsc_dataset *ds, const float *heights, int64_t pitch, int on_device, void *stream);
-/* GridDataset::work() / work_ocl() (dmsc/src/grid_dataset.cpp:1734-1741,
- * 353-399): gradient, critical-cell collation and owner extrema. */
+/* GridDataset::work() (dmsc/src/grid_dataset.cpp:1734-1741): gradient,
+ * critical-cell collation and owner extrema of the reference's CPU path. */
 int dmsc_dataset_work(dmsc_dataset *ds, void *stream);
+/* GridDataset::work_ocl() (dmsc/src/grid_dataset.cpp:353-399): the gradient
+ * of the reference's OpenCL kernels, whose compareCells sorts a cell's
+ * vertices descending (dmsc/resources/assigngradient.cl:40-87; the CPU path
+ * sorts them ascending), then collation and owner extrema as the OpenCL
+ * kernels compute them (collate_critpts.cl, bfs_watershed.cl). */
+int dmsc_dataset_work_ocl(dmsc_dataset *ds, void *stream);
 /* m_critical_cells.size() (dmsc/include/grid_dataset.h:81). */
 int dmsc_dataset_num_critical(dmsc_dataset *ds, int64_t *n);
 /* m_cell_flags, m_cell_pairs, m_cell_own (dmsc/include/grid_dataset.h:78-80)
@@ -83,14 +89,29 @@ int dmsc_dataset_export_cells(dmsc_dataset *ds, int8_t *flags, int16_t *pairs, i
  * collation (row-major) order. */
 int dmsc_dataset_export_critical(dmsc_dataset *ds, int16_t *cellids, void *stream);
 /* GridDataset::writeout_connectivity(mscomplex_t *) (dmsc/src/grid_dataset.cpp:
- * 1858-1907) / writeout_connectivity_ocl (:1250-1283).  *out == NULL: a new
+ * 1858-1907).  *out == NULL: a new
  * complex is returned in *out.  *out != NULL: that complex (of the same
  * context) is overwritten in place, reusing its device buffers, as the
  * reference fills the mscomplex_t it is given. */
 int dmsc_dataset_writeout_connectivity(dmsc_dataset *ds, dmsc_msc **out, void *stream);
+/* GridDataset::writeout_connectivity_ocl(mscomplex_t *)
+ * (dmsc/src/grid_dataset.cpp:1250-1283, with collect_saddle_conn_ocl :907-1022):
+ * the complex from the saddle incidences of the dataset's last work_ocl.
+ * These read the same owners as writeout_connectivity, so both calls give
+ * the same complex for the same dataset. */
+int dmsc_dataset_writeout_connectivity_ocl(dmsc_dataset *ds, dmsc_msc **msc, void *stream);
 
 /* GridMSComplex::clear() (dmsc/src/grid_mscomplex.cpp:324-329). */
 int dmsc_msc_destroy(dmsc_msc *msc);
+/* GridMSComplex::serialize (dmsc/src/grid_mscomplex.cpp:604-695) as used by
+ * write_msgraph_to_archive / read_msgraph_from_archive
+ * (dmsc/src/grid_datamanager.cpp:91-119): the whole complex (points, values,
+ * pairs, flags, lists, discs) to a file and back.  The file layout is this
+ * library's own (documented in mscomplex_gb300/csrc/archive.cu): the
+ * reference's Boost binary archive cannot be reproduced without Boost.  A
+ * loaded complex is identical to the saved one. */
+int dmsc_msc_save(dmsc_msc *msc, const char *path);
+int dmsc_msc_load(dmsc_ctx *ctx, const char *path, dmsc_msc **out);
 /* Sizes of a complex: [0] critical points, [1] asc entries, [2] des entries,
  * [3] asc_disc cells, [4] des_disc cells. */
 int dmsc_msc_sizes(dmsc_msc *msc, int64_t sizes[5]);
@@ -174,6 +195,32 @@ int dmsc_pipeline_merge_times(dmsc_pipeline *p, double ms[2]);
  * (default 2048) run the parallel merges; smaller levels run every merge on
  * one thread (one block per merge).  Both give the same complexes. */
 int dmsc_set_merge_parallel_min(dmsc_ctx *ctx, int64_t min_cps);
+/* merge_up's cancellations along each shared boundary (the loop of
+ * dmsc/src/grid_mscomplex.cpp:124-153) on the parallel merges: rounds over
+ * the first `window` pending boundary cells (default 2048; 0 runs the loop on
+ * one thread per merge); after 8 rounds in a row that each commit fewer than
+ * `min_commits` cells (default 4), one thread finishes the rest in order.
+ * Every setting gives the same complexes. */
+int dmsc_set_merge_rounds(dmsc_ctx *ctx, int64_t window, int64_t min_commits);
+/* GridDataManager's `ocl` argument (the -ocl flag, dmsc/src/main.cpp:527-530;
+ * used at dmsc/src/grid_datamanager.cpp:123-132, 221-222, 433-434): pipelines
+ * run with this context compute their pieces with work_ocl (1) or work (0,
+ * the default). */
+int dmsc_set_use_ocl(dmsc_ctx *ctx, int use_ocl);
+/* GridDataManager's compute_out_of_core argument (--out-of-core,
+ * dmsc/src/grid_datamanager.cpp:91-119, 134-139, 258-395, 397-422): pipelines
+ * run with this context keep their pieces' complexes in archive files under
+ * `dir` (NULL or "" turns it off, the default) instead of device memory: a
+ * leaf's complex goes to its archive once computed and its dataset is freed;
+ * each merge-up level reads its inputs back and archives its new nodes (all
+ * but the root); each merge-down level reads its nodes and archives them
+ * again; the discs stage recomputes each leaf's gradient and reads its
+ * complex back.  A pipeline with levels == 0 stays in memory, as the
+ * reference's does.  After the run the complexes stay archived and are read
+ * back by dmsc_pipeline_piece and dmsc_pipeline_write_discs on first use;
+ * leaf datasets are not kept (dmsc_pipeline_piece returns NULL for them).
+ * The archive files are removed by dmsc_pipeline_destroy. */
+int dmsc_set_out_of_core(dmsc_ctx *ctx, const char *dir);
 
 /* ---- batches of whole grids ----
  * No counterpart in the reference, which builds one GridDataset at a time
@@ -261,7 +308,9 @@ int dmsc_prefix_scan(dmsc_ctx *ctx, uint32_t *d_out, const uint32_t *d_in, int64
  *    DMSC_ERR_BAD_ARG and a message naming the limit.
  *  - The first call on a device looks up the scratch array's device address
  *    (cudaGetSymbolAddress) with that device current; make that first call
- *    before any stream capture.
+ *    before any stream capture.  After a device reset the next call looks it
+ *    up again (the device's context has changed); make that call before any
+ *    capture as well.
  *  - All calls share the one scratch array: calls that overlap on the GPU
  *    (concurrent streams, or threads) race and corrupt each other's result.
  *  - The call only enqueues work on `stream`; the result is ready once that
@@ -285,7 +334,9 @@ int dmsc_set_timing(dmsc_ctx *ctx, int enable);
 /* Stage times in ms of the dataset's last work + writeout_connectivity:
  * [0] gradient, [1] collation scan, [2] border resolve, [3] owner labels and
  * arcs, [4] connectivity CSR; and of its last fill_discs: [5] the hop kernel,
- * [6] the whole pass.  Writes min(n, 7) floats. */
+ * [6] the whole pass, [7] / [8] the kernels that write the saddle discs of
+ * the asc / des kind (the chain cells' placement, the level-0 items and the
+ * discs of saddles with many chains).  Writes min(n, 9) floats. */
 int dmsc_dataset_stage_times(dmsc_dataset *ds, float *ms, int n);
 /* The device's stream-ordered memory pool, which holds the library's device
  * buffers: bytes [0] reserved now, [1] reserved at most, [2] in use now,

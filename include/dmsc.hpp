@@ -77,6 +77,8 @@ class Context {
     return *this;
   }
   dmsc_ctx *get() const noexcept { return c_; }
+  // GridDataManager's ocl argument (-ocl): pipelines of this context use work_ocl
+  void set_use_ocl(bool use_ocl) { check(dmsc_set_use_ocl(c_, use_ocl ? 1 : 0)); }
 
  private:
   dmsc_ctx *c_ = nullptr;
@@ -204,6 +206,9 @@ class GridDataset {
   }
   // GridDataset::work() (dmsc/src/grid_dataset.cpp:1734-1741)
   void work(void *stream = nullptr) { check(dmsc_dataset_work(d_, stream)); }
+  // GridDataset::work_ocl() (dmsc/src/grid_dataset.cpp:353-399): the OpenCL
+  // kernels' gradient (compareCells with vertices sorted descending)
+  void work_ocl(void *stream = nullptr) { check(dmsc_dataset_work_ocl(d_, stream)); }
   // m_critical_cells.size()
   int64_t num_critical() const {
     int64_t n = 0;
@@ -218,6 +223,12 @@ class GridDataset {
   GridMSComplex writeout_connectivity(void *stream = nullptr) {
     GridMSComplex m;
     writeout_connectivity(m, stream);
+    return m;
+  }
+  // GridDataset::writeout_connectivity_ocl(mscomplex_t *) (dmsc/src/grid_dataset.cpp:1250-1283)
+  GridMSComplex writeout_connectivity_ocl(void *stream = nullptr) {
+    GridMSComplex m;
+    check(dmsc_dataset_writeout_connectivity_ocl(d_, m.slot(), stream));
     return m;
   }
   // GridDataset::postMergeFillDiscs(mscomplex_t *) (dmsc/src/grid_dataset.cpp:1044-1231)

@@ -10,9 +10,12 @@ grid file, read by GridDataManager::readDataAndInit, grid_datamanager.cpp:
 strips along y, as -l; --split2d alternates y and x), merges, simplification
 at the root when tresh > 0, discs.  The disc files are written as the
 reference's collectSubdomainManifolds does (prefix "dp__disc_", :414-416) into
---outdir (default: the working directory).  -st, -ocl and --num-parallel
-select CPU threading or the OpenCL backend in the reference and are accepted
-without effect; --out-of-core is not supported.
+--outdir (default: the working directory).  -ocl computes the pieces with the
+gradient of the reference's OpenCL backend (GridDataset::work_ocl: cell
+vertices sorted descending in compareCells).  --out-of-core keeps the pieces'
+complexes in archive files (in --outdir) between the pipeline's stages, as the
+reference's compute_out_of_core does.  -st and --num-parallel select CPU
+threading in the reference and are accepted without effect.
 """
 from __future__ import annotations
 
@@ -38,8 +41,6 @@ def parse(argv):
     ap.add_argument("--out-of-core", action="store_true")
     ap.add_argument("--buffer-zone-width", type=int, default=1)
     a = ap.parse_args(argv)
-    if a.out_of_core:
-        ap.error("--out-of-core is not supported (the grid is read whole)")
     if a.dims[0] < 2 or a.dims[1] < 2:
         ap.error("-d needs at least 2 x 2 vertices")
     if a.levels < 0:
@@ -57,11 +58,15 @@ def load_raw(path: str, x: int, y: int) -> np.ndarray:
 
 def main(argv=None) -> int:
     a = parse(sys.argv[1:] if argv is None else argv)
-    from . import GridDataManager
+    from . import Context, GridDataManager
     field = load_raw(a.file, a.dims[0], a.dims[1])
     os.makedirs(a.outdir, exist_ok=True)
+    ctx = Context()
+    ctx.set_use_ocl(a.ocl)
+    if a.out_of_core:
+        ctx.set_out_of_core(a.outdir)
     t0 = time.perf_counter()
-    p = GridDataManager(field, levels=a.levels, tresh=a.tresh, split2d=a.split2d)
+    p = GridDataManager(field, levels=a.levels, tresh=a.tresh, split2d=a.split2d, ctx=ctx)
     t1 = time.perf_counter()
     p.write_discs(os.path.join(a.outdir, "dp__disc_"))
     t2 = time.perf_counter()

@@ -31,10 +31,12 @@ SIGNATURES = {
     "dmsc_dataset_destroy": ([_vp], _i32),
     "dmsc_dataset_init": ([_vp, _vp, _i64, _i32, _vp], _i32),
     "dmsc_dataset_work": ([_vp, _vp], _i32),
+    "dmsc_dataset_work_ocl": ([_vp, _vp], _i32),
     "dmsc_dataset_num_critical": ([_vp, _vp], _i32),
     "dmsc_dataset_export_cells": ([_vp, _vp, _vp, _vp, _vp], _i32),
     "dmsc_dataset_export_critical": ([_vp, _vp, _vp], _i32),
     "dmsc_dataset_writeout_connectivity": ([_vp, _vp, _vp], _i32),
+    "dmsc_dataset_writeout_connectivity_ocl": ([_vp, _vp, _vp], _i32),
     "dmsc_msc_destroy": ([_vp], _i32),
     "dmsc_msc_sizes": ([_vp, _vp], _i32),
     "dmsc_msc_export": ([_vp] * 15, _i32),
@@ -60,6 +62,11 @@ SIGNATURES = {
     "dmsc_batch_export": ([_vp, _i64] + [_vp] * 9 + [_vp], _i32),
     "dmsc_batch_totals": ([_vp, _vp], _i32),
     "dmsc_set_merge_parallel_min": ([_vp, _i64], _i32),
+    "dmsc_set_merge_rounds": ([_vp, _i64, _i64], _i32),
+    "dmsc_set_use_ocl": ([_vp, _i32], _i32),
+    "dmsc_set_out_of_core": ([_vp, C.c_char_p], _i32),
+    "dmsc_msc_save": ([_vp, C.c_char_p], _i32),
+    "dmsc_msc_load": ([_vp, C.c_char_p, _vp], _i32),
     "dmsc_pipeline_merge_times": ([_vp, _vp], _i32),
     "dmsc_pool_stats": ([_vp, _vp], _i32),
     "dmsc_batch_grid_status": ([_vp, _i64, _vp, C.c_char_p, _i32], _i32),

@@ -17,7 +17,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libdmsc.so")
-SOURCES = ["grid_kernels.cu", "primitives.cu", "simplify.cu", "discs.cu", "merge.cu", "merge_par.cu", "pipeline.cu", "batch.cu", "serve.cu", "dmsc_capi.cu", "dmsc_noalloc.cu"]
+SOURCES = ["grid_kernels.cu", "primitives.cu", "simplify.cu", "discs.cu", "merge.cu", "merge_par.cu", "pipeline.cu", "batch.cu", "serve.cu", "dmsc_capi.cu", "dmsc_noalloc.cu", "archive.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 

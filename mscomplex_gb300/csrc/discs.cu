@@ -948,6 +948,7 @@ struct DiscKind {
         }
         k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c, offs);  // the records the pieces are placed by
         DMSC_LAUNCHED(1);
+        if (S.io->ev_place[kind][0]) L(cudaEventRecord(S.io->ev_place[kind][0], st));
         if (tot[1]) {
           k_seg_place<<<nb((tot[1] + 31) / 32 * 32), SEG_WARPS * 32, 0, st>>>(a, c, tot[1], ob->p,
                                                                              (unsigned long long)tot[0]);
@@ -956,6 +957,8 @@ struct DiscKind {
         k_level0<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, offs, ob->p);
         k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);
         DMSC_LAUNCHED(2);
+        // between the two events: every saddle disc cell of this kind is written once
+        if (S.io->ev_place[kind][1]) L(cudaEventRecord(S.io->ev_place[kind][1], st));
         if (n > 0 && nrun) {  // extremum discs of this kind
           k_runs_scatter<<<nb(n), 256, 0, st>>>(a.g, kind, S.gkey[kind], n, S.gw[kind], (uint32_t)ncp, S.gval[kind], rp,
                                                 rstart, offs, ob->p);

@@ -152,10 +152,12 @@ int dmsc_dataset_init(dmsc_dataset *d, const float *heights, int64_t pitch, int 
 }
 
 // Runs K1 (gradient) -> scan -> K3 (resolve) -> K4 (labels) on `st`.
-// Returns after the device status is known.
-int dmsc_dataset_work(dmsc_dataset *d, void *stream) {
+// Returns after the device status is known.  desc: the OpenCL kernels'
+// compareCells (work_ocl) instead of the CPU path's (work).
+static int dataset_work(dmsc_dataset *d, void *stream, int desc) {
   if (!d) return fail(DMSC_ERR_BAD_ARG, "dataset is null");
   if (!d->hgt) return fail(DMSC_ERR_STATE, "dataset has no heights (call dmsc_dataset_init first)");
+  d->g.desc = desc;
   CK(cudaSetDevice(d->ctx->device));
   cudaStream_t st = pick(d->ctx, stream);
   int rc = d->alloc_cells(st);
@@ -250,6 +252,16 @@ int dmsc_dataset_export_critical(dmsc_dataset *d, int16_t *cellids, void *stream
   if (d->ncp) CK(cudaMemcpyAsync(cellids, d->cp_cellid.p, 4 * d->ncp, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   return DMSC_OK;
+}
+
+int dmsc_dataset_work(dmsc_dataset *d, void *stream) { return dataset_work(d, stream, 0); }
+int dmsc_dataset_work_ocl(dmsc_dataset *d, void *stream) { return dataset_work(d, stream, 1); }
+
+// writeout_connectivity_ocl builds the same complex from the same cells: its
+// saddle incidences (collect_saddle_conn_ocl) read the owners of a saddle's
+// facets and cofacets inside ext, as writeout_connectivity reads them.
+int dmsc_dataset_writeout_connectivity_ocl(dmsc_dataset *d, dmsc_msc **out, void *stream) {
+  return dmsc_dataset_writeout_connectivity(d, out, stream);
 }
 
 int dmsc_dataset_writeout_connectivity(dmsc_dataset *d, dmsc_msc **out, void *stream) {
@@ -368,13 +380,33 @@ int dmsc_set_merge_parallel_min(dmsc_ctx *ctx, int64_t min_cps) {
   return DMSC_OK;
 }
 
+int dmsc_set_out_of_core(dmsc_ctx *ctx, const char *dir) {
+  if (!ctx) return fail(DMSC_ERR_BAD_ARG, "ctx is null");
+  ctx->ooc_dir = dir ? dir : "";
+  return DMSC_OK;
+}
+
+int dmsc_set_use_ocl(dmsc_ctx *ctx, int use_ocl) {
+  if (!ctx) return fail(DMSC_ERR_BAD_ARG, "ctx is null");
+  ctx->use_ocl = use_ocl != 0;
+  return DMSC_OK;
+}
+
+int dmsc_set_merge_rounds(dmsc_ctx *ctx, int64_t window, int64_t min_commits) {
+  if (!ctx || window < 0 || min_commits < 0) return fail(DMSC_ERR_BAD_ARG, "ctx is null or a setting is negative");
+  ctx->merge_round_window = window;
+  ctx->merge_round_min_commits = min_commits;
+  return DMSC_OK;
+}
+
 int dmsc_dataset_stage_times(dmsc_dataset *d, float *ms, int n) {
   if (!d || !ms) return fail(DMSC_ERR_BAD_ARG, "null argument");
   if (!d->ev_ready) return fail(DMSC_ERR_STATE, "timing was not enabled for the last run");
   CK(cudaSetDevice(d->ctx->device));
-  // gradient, collate_scan, border_resolve, labels_arcs, connectivity, disc_hops, discs
-  const int pairs[7][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 4}, {5, 6}, {7, 8}, {7, 9}};
-  for (int i = 0; i < n && i < 7; ++i) {
+  // gradient, collate_scan, border_resolve, labels_arcs, connectivity, disc_hops, discs,
+  // the placement kernel of the asc and of the des discs
+  const int pairs[9][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 4}, {5, 6}, {7, 8}, {7, 9}, {10, 11}, {12, 13}};
+  for (int i = 0; i < n && i < 9; ++i) {
     CK(cudaEventSynchronize(d->ev[pairs[i][1]]));
     float t = 0;
     if (cudaEventElapsedTime(&t, d->ev[pairs[i][0]], d->ev[pairs[i][1]]) != cudaSuccess) { cudaGetLastError(); t = -1; }
@@ -460,6 +492,10 @@ int dmsc_dataset_fill_discs(dmsc_dataset *d, dmsc_msc *m, void *stream) {
   if (tm) {
     io.ev_hops[0] = d->ev[7];
     io.ev_hops[1] = d->ev[8];
+    io.ev_place[0][0] = d->ev[10];
+    io.ev_place[0][1] = d->ev[11];
+    io.ev_place[1][0] = d->ev[12];
+    io.ev_place[1][1] = d->ev[13];
     CK(cudaEventRecord(d->ev[7], st));
   }
   CK(cudaMemsetAsync(d->scal.p, 0, sizeof(uint32_t), st));

@@ -62,6 +62,10 @@ struct GridGeom {
   // a batch of grids (0 for a grid on its own): the border table's EXIT and
   // ROOT entries carry batch-wide indices.
   long long sbase = 0, gbase = 0;
+  // compareCells sorts a cell's vertices descending (the reference's OpenCL
+  // kernels, dmsc/resources/assigngradient.cl:40-87) instead of ascending
+  // (its CPU path, dmsc/src/grid_dataset.cpp:1530-1531)
+  int desc = 0;
 };
 
 __host__ __device__ __forceinline__ uint32_t pack_cellid(int x, int y) {

@@ -148,6 +148,7 @@ struct DiscIO {
   uint32_t *status = nullptr;
   unsigned long long limit = 1ull << 31;  // bound on one gradient chain (cells of the window)
   cudaEvent_t ev_hops[2] = {nullptr, nullptr};  // recorded around the hop kernel when set
+  cudaEvent_t ev_place[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // around k_seg_place, per kind, when set
   bool no_cancel = false;  // the complex has no boundary-cancelable critical point
   long long nadisc = 0, nddisc = 0;
   // the des discs run on `aux` beside the asc discs on the caller's stream;
@@ -195,7 +196,8 @@ struct MergeJob {
 };
 // seq_ms accumulates the host wall time of the one-thread steps.
 cudaError_t merge_up_level_par(const std::vector<MergeJob> &jobs, unsigned long long grow, uint32_t *status,
-                               uint32_t *stw, cudaStream_t st, double *seq_ms);
+                               uint32_t *stw, cudaStream_t st, double *seq_ms, long long round_window,
+                               long long round_min_commits);
 cudaError_t merge_down_level_par(const std::vector<MergeJob> &jobs, unsigned long long grow, uint32_t *status,
                                  uint32_t *stw, cudaStream_t st, double *seq_ms);
 }  // namespace dmsc

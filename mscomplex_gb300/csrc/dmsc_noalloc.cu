@@ -10,6 +10,8 @@
 // For them this file keeps the scratch in a fixed device array compiled into
 // the library.  Every GPU that loads libdmsc.so holds the array until the
 // process exits.
+#include <cuda.h>
+
 #include <mutex>
 #include <string>
 
@@ -26,7 +28,27 @@ constexpr long long kNoAllocScratchWords = 2 * (kNoAllocScanMax / 4096) + 64;
 constexpr int kMaxDevices = 64;
 
 std::mutex g_setup_mu;
-uint32_t *g_scratch_addr[kMaxDevices] = {};  // device address of the array, per device
+// Per device: the array's device address and the context it was looked up
+// in.  A device reset (cudaDeviceReset, or the primary context torn down and
+// created again) gives the device a new context in which the array may sit
+// elsewhere, so the address is looked up again when the context changes.
+uint32_t *g_scratch_addr[kMaxDevices] = {};
+CUcontext g_scratch_ctx[kMaxDevices] = {};
+
+// cuCtxGetCurrent through the runtime's driver entry point: the library does
+// not link the driver library itself.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return (CtxGetCurrentFn)p;
+  }();
+  return fn;
+}
 }  // namespace
 
 // The scratch itself.  In host code its name is only a stand-in for the
@@ -47,15 +69,20 @@ extern "C" int dmsc_prefix_scan_noalloc(dmsc_ctx *ctx, uint32_t *d_out, const ui
   if (e != cudaSuccess) return dmsc::set_last_error(DMSC_ERR_CUDA, cudaGetErrorString(e));
   uint32_t *scratch = nullptr;
   {
-    // First call on a device: look up the array's device address with that
-    // device current.  (This is why the first call should come before any
-    // stream capture.)
+    // First call on a device (or on its new context after a reset): look up
+    // the array's device address with that device current.  (This is why the
+    // first call should come before any stream capture.)
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_addr[ctx->device]) {
+    CUcontext cur = nullptr;
+    const CtxGetCurrentFn get = ctx_get_current();
+    if (get && get(&cur) != CUDA_SUCCESS) cur = nullptr;
+    if (!g_scratch_addr[ctx->device] || cur != g_scratch_ctx[ctx->device]) {
       void *p = nullptr;
       e = cudaGetSymbolAddress(&p, g_noalloc_scan_scratch);
       if (e != cudaSuccess) return dmsc::set_last_error(DMSC_ERR_CUDA, cudaGetErrorString(e));
       g_scratch_addr[ctx->device] = (uint32_t *)p;
+      if (get && get(&cur) != CUDA_SUCCESS) cur = nullptr;  // the lookup makes the context current
+      g_scratch_ctx[ctx->device] = cur;
     }
     scratch = g_scratch_addr[ctx->device];
   }

@@ -19,6 +19,18 @@
 //   * edge e=(P,Q) is >= every edge of a face whose other corners are U
 //     (adjacent to P) and W (adjacent to Q) iff U<Q, W<P and min(U,W) <
 //     min(P,Q) ("usable" test of lowestPairableCoFacet, :1344-1351).
+// The reference's OpenCL kernels (work_ocl) sort cell vertices DESCENDING
+// instead (dmsc/resources/assigngradient.cl:40-87); GridGeom::desc selects
+// their mirrored closed forms:
+//   * two faces sharing an edge are ordered by the LARGEST vertex of their
+//     symmetric difference: the face holding it is the larger one;
+//   * e=(P,Q) is the largest edge of the face iff the face's largest vertex
+//     is P or Q and the other end of e is that vertex's larger neighbour in
+//     the face: max(P,Q) > max(U,W) and (P > Q ? Q > U : P > W).
+// A vertex pairs with the edge to its lowest lower neighbour in both orders.
+// With either order the other steps of work_ocl (complete_pairings, the two
+// boundary-pair kernels, pointer-jumping owners, saddle incidences) give the
+// cells and owners of the CPU path's steps.
 //
 // Exactness of the parallel gradient.  The reference pairs cells in row-major
 // order and skips cells already marked.  A cell can only be chosen by its
@@ -80,6 +92,15 @@ __device__ __forceinline__ uint32_t finish_code(const GridGeom &g, bool piece, i
 // to P) and W (next to Q)
 __device__ __forceinline__ bool usable_face(uint64_t P, uint64_t Q, uint64_t U, uint64_t W) {
   return U < Q && W < P && min(U, W) < min(P, Q);
+}
+// the same test under the descending order of the OpenCL kernels
+__device__ __forceinline__ bool usable_face_desc(uint64_t P, uint64_t Q, uint64_t U, uint64_t W) {
+  return max(P, Q) > max(U, W) && (P > Q ? Q > U : P > W);
+}
+// the smaller of two usable faces of an edge, given each face's two corners
+// off the edge: true if face b (the second) is the smaller
+__device__ __forceinline__ bool second_face_smaller(bool desc, uint64_t Ua, uint64_t Wa, uint64_t Ub, uint64_t Wb) {
+  return desc ? max(Ua, Wa) > max(Ub, Wb) : min(Ub, Wb) < min(Ua, Wa);
 }
 
 // pointer-jumping words (uint16): tag in bits 14-15, local cell index below
@@ -238,8 +259,9 @@ __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, con
     if (hi + 1 < g.vnx && hj < g.vny && in_rect(g, 2 * hi + 1, 2 * hj) && hj != 0 && hj != g.vny - 1) {
       uint64_t P = KEY(i, j), Q = KEY(i + 1, j);
       uint64_t Ua = KEY(i, j + 1), Wa = KEY(i + 1, j + 1), Ub = KEY(i, j - 1), Wb = KEY(i + 1, j - 1);
-      bool u0 = usable_face(P, Q, Ua, Wa), u1 = usable_face(P, Q, Ub, Wb);  // cf[0] above, cf[1] below
-      if (u0 && u1) best = min(Ub, Wb) < min(Ua, Wa) ? DIR_MY : DIR_PY;
+      bool u0 = g.desc ? usable_face_desc(P, Q, Ua, Wa) : usable_face(P, Q, Ua, Wa);  // cf[0] above
+      bool u1 = g.desc ? usable_face_desc(P, Q, Ub, Wb) : usable_face(P, Q, Ub, Wb);  // cf[1] below
+      if (u0 && u1) best = second_face_smaller(g.desc, Ua, Wa, Ub, Wb) ? DIR_MY : DIR_PY;
       else if (u0) best = DIR_PY;
       else if (u1) best = DIR_MY;
     }
@@ -252,8 +274,9 @@ __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, con
     if (vi < g.vnx && vj + 1 < g.vny && in_rect(g, 2 * vi, 2 * vj + 1) && vi != 0 && vi != g.vnx - 1) {
       uint64_t P = KEY(i, j), Q = KEY(i, j + 1);
       uint64_t Ur = KEY(i + 1, j), Wr = KEY(i + 1, j + 1), Ul = KEY(i - 1, j), Wl = KEY(i - 1, j + 1);
-      bool u0 = usable_face(P, Q, Ur, Wr), u1 = usable_face(P, Q, Ul, Wl);  // cf[0] right, cf[1] left
-      if (u0 && u1) best = min(Ul, Wl) < min(Ur, Wr) ? DIR_MX : DIR_PX;
+      bool u0 = g.desc ? usable_face_desc(P, Q, Ur, Wr) : usable_face(P, Q, Ur, Wr);  // cf[0] right
+      bool u1 = g.desc ? usable_face_desc(P, Q, Ul, Wl) : usable_face(P, Q, Ul, Wl);  // cf[1] left
+      if (u0 && u1) best = second_face_smaller(g.desc, Ur, Wr, Ul, Wl) ? DIR_MX : DIR_PX;
       else if (u0) best = DIR_PX;
       else if (u1) best = DIR_MX;
     }

@@ -1,6 +1,7 @@
 // grid_types.h -- host-side handle types behind the C ABI (device-resident data).
 #pragma once
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "dmsc.h"
@@ -80,7 +81,7 @@ struct dmsc_dataset {
   DevBuf<uint32_t> cp_cellid, cp_pair_cell, cp_des2, cp_asc2, cp_acnt, cp_dcnt, cp_pair_idx;
   DevBuf<float> cp_fn;
   DevBuf<uint8_t> cp_flags;
-  cudaEvent_t ev[10] = {};    // stage events (only when the context has timing enabled)
+  cudaEvent_t ev[14] = {};    // stage events (only when the context has timing enabled)
   bool ev_ready = false;
 
   long long nslots() const { return (long long)g.ntx * g.nty * dmsc::SLOTS_PER_TILE; }
@@ -98,6 +99,13 @@ struct dmsc_ctx {
   cudaStream_t stream = nullptr;
   bool timing = false;
   long long merge_parallel_min = 2048;  // pipeline levels with merges this large take the parallel merges
+  // merge_up's boundary cancellations in ordered-parallel rounds: each round
+  // looks at the first merge_round_window pending boundary cells (0: one
+  // thread per merge); after 8 rounds in a row that each commit fewer than
+  // merge_round_min_commits cells, one thread finishes the rest in order
+  long long merge_round_window = 2048, merge_round_min_commits = 4;
+  bool use_ocl = false;  // pipeline pieces through work_ocl (GridDataManager's ocl flag)
+  std::string ooc_dir;   // pipelines spill their pieces' complexes to files here (empty: in memory)
 };
 
 struct dmsc_msc {

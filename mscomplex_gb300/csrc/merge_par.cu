@@ -571,6 +571,7 @@ enum SeqKind : int { SEQ_UP_CANCEL = 0, SEQ_DOWN_BOUNDARY = 1 };
 struct SeqJob {
   int kind, g0;
   CRect ixn;
+  int win = 0, min_commits = 0;  // SEQ_UP_CANCEL: rounds window (0: one thread) and hand-off rate
 };
 
 // Loads, across the GPU, what the one-thread step of a job will read -- the
@@ -628,45 +629,55 @@ __global__ void k_merge_seq(MGraph *graphs, const SeqJob *jobs, int njobs, uint3
 
 // ---------------------------------------------------------------------------
 // merge_up's boundary cancellations in ordered-parallel rounds.  Task t is
-// cell t of the shared boundary in row-major order.  Each round, every
-// pending task reserves its footprint -- the critical points whose lists or
-// flags its cancellation reads or writes -- with the round-tagged key
-// (round, t) in a per-point slot (atomicMin: the round's smallest task
-// touching the point wins); tasks sharing a slot are joined in a union-find
-// that hooks the larger root under the smaller; and the root of each group,
-// its smallest task, runs.  Edges are only added inside a running task's
-// footprint, so groups cannot merge through growth and every task sees the
-// graph the row-major loop would show it.  One block per merge; the rounds
-// are separated by barriers of the block.  Each thread allocates list room
-// from its own slice of the pool's free part, so the graph code stays that of
-// one thread.  Where the groups stay large (one point in most footprints), the
-// rounds would cost the square of the boundary: past a budget of pending-task
-// evaluations, thread 0 runs the remaining tasks in row-major order, which is
-// exact at any round boundary (every task that ran commutes with every
+// cell t of the shared boundary in row-major order.  Each round looks at a
+// window: the first `win` cells from the first pending task on.  Every
+// pending task of the window reserves its footprint -- the critical points
+// whose lists or flags its cancellation reads or writes -- with the
+// round-tagged key (round, t) in a per-point slot (atomicMin: the round's
+// smallest task touching the point wins); tasks sharing a slot are joined in
+// a union-find that hooks the larger root under the smaller; and the root of
+// each group, its smallest task, runs.  Every pending task earlier than a
+// window task is inside the window, so a root has no earlier pending task
+// that overlaps it.  Edges are only added inside a running task's footprint,
+// so groups cannot merge through growth and every task sees the graph the
+// row-major loop would show it.  The first pending task is always a root, so
+// every round commits at least one task.  One block per merge; the rounds are
+// separated by barriers of the block.  Each thread allocates list room from
+// its own slice of the pool's free part, so the graph code stays that of one
+// thread.  Where groups stay large (one point in most footprints, as a large
+// extremum on a smooth field), rounds commit few tasks each: after
+// ROUND_PATIENCE rounds in a row below `min_commits`, or if a union-find
+// guard runs out, thread 0 runs the remaining tasks in row-major order, which
+// is exact at any round boundary (every task that ran commutes with every
 // earlier one still pending), from a quarter of the free pool kept for it.
 // ---------------------------------------------------------------------------
-constexpr int ROUND_THREADS = 512, ROUND_TASKS = 32768;
+constexpr int ROUND_THREADS = 512, ROUND_TASKS = 32768, ROUND_PATIENCE = 8;
 struct RoundSmem {
   uint32_t parent[ROUND_TASKS];
   uint32_t done[ROUND_TASKS / 32];
 };
 
+// Parents only point to smaller tasks of the window, so a chain is shorter
+// than the window and the guard never ends a search early.
 __device__ __forceinline__ uint32_t uf_root(uint32_t *parent, uint32_t a) {
-  for (int guard = 0; guard < ROUND_TASKS; ++guard) {  // parents only point to smaller tasks
+  for (int guard = 0; guard < ROUND_TASKS; ++guard) {
     const uint32_t p = ((volatile uint32_t *)parent)[a];
     if (p == a) return a;
     a = p;
   }
   return a;
 }
-__device__ __forceinline__ void uf_join(uint32_t *parent, uint32_t a, uint32_t b) {
+// False if the join did not happen within the guard (each failed CAS means
+// another thread hooked a root meanwhile); the caller then stops the rounds.
+__device__ __forceinline__ bool uf_join(uint32_t *parent, uint32_t a, uint32_t b) {
   for (int guard = 0; guard < 4 * ROUND_TASKS; ++guard) {
     a = uf_root(parent, a);
     b = uf_root(parent, b);
-    if (a == b) return;
+    if (a == b) return true;
     if (a > b) { const uint32_t t = a; a = b; b = t; }
-    if (atomicCAS(&parent[b], b, a) == b) return;
+    if (atomicCAS(&parent[b], b, a) == b) return true;
   }
+  return false;
 }
 
 // The cell's point and, while it may still cancel, its partner and both
@@ -698,19 +709,31 @@ __device__ __forceinline__ bool up_cell_static(const MGraph &M, int x, int y, ui
   return (M.rect.interior(x, y) || M.ext.boundary(x, y)) && (M.rect.interior(px_(p), py_(p)) || M.ext.boundary(px_(p), py_(p)));
 }
 
+// The first task at or after `from` whose done bit is clear (n if none),
+// into *lo (which the caller set to n); all threads take part.
+__device__ __forceinline__ void first_pending(const RoundSmem &S, long long from, long long n, unsigned int *lo) {
+  const long long nw = (n + 31) / 32;
+  for (long long wi = from / 32 + threadIdx.x; wi < nw; wi += blockDim.x) {
+    uint32_t open = ~S.done[wi];
+    if (wi == from / 32) open &= ~0u << (from & 31);
+    if (wi == nw - 1 && (n & 31)) open &= (1u << (n & 31)) - 1;
+    if (open) atomicMin(lo, (unsigned int)(wi * 32 + __ffs(open) - 1));
+  }
+}
+
 __global__ void __launch_bounds__(ROUND_THREADS, 1) k_merge_up_rounds(MGraph *graphs, const SeqJob *jobs, int njobs,
                                                                       unsigned long long *const *slots, uint32_t *status) {
   extern __shared__ __align__(16) unsigned char round_smem[];
   RoundSmem &S = *reinterpret_cast<RoundSmem *>(round_smem);
-  __shared__ int abort_all;
-  __shared__ unsigned long long work;  // pending-task evaluations so far
+  __shared__ int abort_all, uf_bad;
+  __shared__ unsigned int lo_s, commits;
   const int b = blockIdx.x;
   if (b >= njobs) return;
   const SeqJob jb = jobs[b];
   MGraph g = graphs[jb.g0];  // every thread's own descriptor copy, read before any write-back
   const long long w = jb.ixn.r - jb.ixn.l + 1, h = jb.ixn.t - jb.ixn.b + 1, n = w * h;
   unsigned long long *slot = slots[b];
-  if (n > ROUND_TASKS || !slot) {  // one thread, as k_merge_seq
+  if (n > ROUND_TASKS || !slot || jb.win <= 0) {  // one thread, as k_merge_seq
     if (threadIdx.x == 0) {
       merge_up_cancel(g, jb.ixn, status);
       if (g.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
@@ -718,12 +741,12 @@ __global__ void __launch_bounds__(ROUND_THREADS, 1) k_merge_up_rounds(MGraph *gr
     }
     return;
   }
-  if (threadIdx.x == 0) { abort_all = 0; work = 0; }
+  const long long win = jb.win < ROUND_TASKS ? jb.win : ROUND_TASKS;
+  if (threadIdx.x == 0) { abort_all = 0; uf_bad = 0; lo_s = (unsigned int)n; }
   for (long long t = threadIdx.x; t < ROUND_TASKS / 32; t += blockDim.x) S.done[t] = 0;
   __syncthreads();
   const unsigned long long free_runs = g.G.L.pool_cap - g.G.L.top, pool_end = g.G.L.pool_cap;
   const unsigned long long room = (free_runs - free_runs / 4) / blockDim.x, fin_start = g.G.L.top + room * blockDim.x;
-  const unsigned long long budget = 512ull * (unsigned long long)n;
   const unsigned long long tmp_cap0 = g.G.tmp_cap;
   g.G.L.top += room * threadIdx.x;  // this thread's slice of the free pool
   g.G.L.pool_cap = g.G.L.top + room;
@@ -737,27 +760,30 @@ __global__ void __launch_bounds__(ROUND_THREADS, 1) k_merge_up_rounds(MGraph *gr
     const uint32_t si = g.find(pack_cellid(x, y));
     if (si != NO_CP && !up_cell_static(g, x, y, si)) atomicOr(&S.done[t >> 5], 1u << (t & 31));
   }
+  __syncthreads();
+  first_pending(S, 0, n, &lo_s);
+  __syncthreads();
+  int slow = 0;  // rounds in a row that committed fewer than min_commits tasks
   for (uint32_t round = 0; round < (uint32_t)n + 1; ++round) {
-    int mine = 0;
-    unsigned long long cnt = 0;
-    for (long long t = threadIdx.x; t < n; t += blockDim.x)
-      if (!is_done(t)) { mine = 1; ++cnt; }
-    atomicAdd(&work, cnt);
-    if (!__syncthreads_or(mine) || abort_all || work > budget) break;
-    const unsigned long long hi = (unsigned long long)(0xFFFFFFFFu - round) << 32;
+    const long long lo = lo_s;
+    if (lo >= n || abort_all || uf_bad || slow >= ROUND_PATIENCE) break;
+    const long long hi = lo + win < n ? lo + win : n;
+    const unsigned long long tag = (unsigned long long)(0xFFFFFFFFu - round) << 32;
+    __syncthreads();  // every thread has read lo_s and the flags
+    if (threadIdx.x == 0) { commits = 0; lo_s = (unsigned int)n; }
     // reserve
-    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x) {
       if (is_done(t)) continue;
       S.parent[t] = (uint32_t)t;
       int x, y;
       cell_of(t, x, y);
       const uint32_t si = g.find(pack_cellid(x, y));
       if (si >= g.G.ncp) continue;  // the loop body reports it when the task runs
-      up_footprint(g, si, [&](uint32_t c) { if (c < g.G.ncp) atomicMin(&slot[c], hi | (unsigned long long)t); });
+      up_footprint(g, si, [&](uint32_t c) { if (c < g.G.ncp) atomicMin(&slot[c], tag | (unsigned long long)t); });
     }
     __syncthreads();
     // join the tasks that share a point
-    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x) {
       if (is_done(t)) continue;
       int x, y;
       cell_of(t, x, y);
@@ -766,25 +792,30 @@ __global__ void __launch_bounds__(ROUND_THREADS, 1) k_merge_up_rounds(MGraph *gr
       up_footprint(g, si, [&](uint32_t c) {
         if (c >= g.G.ncp) return;
         const unsigned long long v = slot[c];
-        if ((v & 0xFFFFFFFF00000000ull) == hi && (v & 0xFFFFFFFFull) < (unsigned long long)n)
-          uf_join(S.parent, (uint32_t)t, (uint32_t)(v & 0xFFFFFFFFull));
+        if ((v & 0xFFFFFFFF00000000ull) == tag && (v & 0xFFFFFFFFull) < (unsigned long long)n)
+          if (!uf_join(S.parent, (uint32_t)t, (uint32_t)(v & 0xFFFFFFFFull))) uf_bad = 1;
       });
     }
     __syncthreads();
-    // the smallest task of each group runs
-    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
-      if (is_done(t) || uf_root(S.parent, (uint32_t)t) != (uint32_t)t) continue;
-      int x, y;
-      cell_of(t, x, y);
-      if (!merge_up_cell(g, x, y, status) || g.G.fail) abort_all = 1;
-      atomicOr(&S.done[t >> 5], 1u << (t & 31));
-    }
+    // the smallest task of each group runs (none if a join was lost)
+    if (!uf_bad)
+      for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x) {
+        if (is_done(t) || uf_root(S.parent, (uint32_t)t) != (uint32_t)t) continue;
+        int x, y;
+        cell_of(t, x, y);
+        if (!merge_up_cell(g, x, y, status) || g.G.fail) abort_all = 1;
+        atomicOr(&S.done[t >> 5], 1u << (t & 31));
+        atomicAdd(&commits, 1u);
+      }
     __syncthreads();
+    first_pending(S, lo, n, &lo_s);
+    __syncthreads();
+    slow = commits < (unsigned int)jb.min_commits ? slow + 1 : 0;
   }
   if (g.G.fail) set_status(status, ST_SIMPLIFY_LIMIT);
   __syncthreads();
   if (threadIdx.x == 0) {
-    if (!abort_all) {  // tasks left by the budget, in row-major order on this thread
+    if (!abort_all) {  // tasks left to one thread, in row-major order
       MGraph f = g;
       f.G.L.top = fin_start;
       f.G.L.pool_cap = pool_end;
@@ -1150,7 +1181,8 @@ int current_device() {
 // The merges of a level run side by side on their own streams (several host
 // threads); the one-thread steps of all of them run in one launch on `st`.
 cudaError_t merge_up_level_par(const std::vector<MergeJob> &jobs, unsigned long long grow, uint32_t *status,
-                               uint32_t *stw, cudaStream_t st, double *seq_ms) {
+                               uint32_t *stw, cudaStream_t st, double *seq_ms, long long round_window,
+                               long long round_min_commits) {
   *stw = 0;
   const int nj = (int)jobs.size(), dev = current_device();
   cudaError_t e = cudaMemsetAsync(status, 0, 4, st);
@@ -1176,7 +1208,10 @@ cudaError_t merge_up_level_par(const std::vector<MergeJob> &jobs, unsigned long 
   for (int k = 0; k < nj; ++k) {
     const int *x = jobs[k].ixn;
     gp.push_back(&g[k]);
-    seq.push_back(SeqJob{SEQ_UP_CANCEL, k, CRect{x[0], x[1], x[2], x[3]}});
+    SeqJob j{SEQ_UP_CANCEL, k, CRect{x[0], x[1], x[2], x[3]}};
+    j.win = (int)std::min<long long>(std::max<long long>(round_window, 0), 1 << 30);
+    j.min_commits = (int)std::min<long long>(std::max<long long>(round_min_commits, 0), 1 << 30);
+    seq.push_back(j);
   }
   e = as_cuda(for_each_on_streams(dev, nj, MERGE_WORKERS, [&](int k, cudaStream_t s) {
     const dmsc_msc &O = *jobs[k].parent;

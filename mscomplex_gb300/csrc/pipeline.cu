@@ -16,6 +16,8 @@
 #include <thread>
 #include <vector>
 
+#include <unistd.h>
+
 #include "dmsc.h"
 #include "dmsc_internal.h"
 #include "grid_types.h"
@@ -74,10 +76,17 @@ struct dmsc_pipeline {
   double ms[5] = {0, 0, 0, 0, 0};
   double seq_ms[2] = {0, 0};  // one-thread steps of the parallel merges: up, down
   unsigned long long simp[5] = {0, 0, 0, 0, 0};
+  // out of core (GridDataManager's compute_out_of_core): the archive file
+  // prefix of this run, and per tree node whether its archive exists
+  std::string ooc;
+  std::vector<char> archived;
   ~dmsc_pipeline() {
-    for (auto *d : ds) dmsc_dataset_destroy(d);
+    for (auto *d : ds)
+      if (d) dmsc_dataset_destroy(d);
     for (auto *m : msc)
       if (m) dmsc_msc_destroy(m);
+    for (size_t i = 0; i < archived.size(); ++i)
+      if (archived[i]) std::remove((ooc + std::to_string(i)).c_str());
   }
 };
 
@@ -93,6 +102,28 @@ static int perr(int code, const std::string &m) { return set_last_error(code, m.
     int r_ = (call);           \
     if (r_ != DMSC_OK) return r_; \
   } while (0)
+
+// Out of core, as write_msgraph_to_archive / read_msgraph_from_archive
+// (dmsc/src/grid_datamanager.cpp:91-119): a node's complex goes to its
+// archive file and leaves the device; it is read back when a stage needs it.
+static int archive_node(dmsc_pipeline *P, int node) {  // write, then free the device copy
+  PRC(dmsc_msc_save(P->msc[node], (P->ooc + std::to_string(node)).c_str()));
+  dmsc_msc_destroy(P->msc[node]);
+  P->msc[node] = nullptr;
+  P->archived[node] = 1;
+  return DMSC_OK;
+}
+static int unarchive_node(dmsc_pipeline *P, int node) {
+  if (P->msc[node]) return DMSC_OK;
+  if (!P->archived[node]) return perr(DMSC_ERR_STATE, "piece " + std::to_string(node) + " has no complex");
+  return dmsc_msc_load(P->ctx, (P->ooc + std::to_string(node)).c_str(), &P->msc[node]);
+}
+static void drop_node(dmsc_pipeline *P, int node) {  // its archive is current: free the device copy
+  if (P->archived[node] && P->msc[node]) {
+    dmsc_msc_destroy(P->msc[node]);
+    P->msc[node] = nullptr;
+  }
+}
 
 static dmsc_msc *new_msc(dmsc_ctx *c, const R4 &r, const R4 &e) {
   dmsc_msc *m = new dmsc_msc;
@@ -136,7 +167,8 @@ static int run_level_par(dmsc_pipeline *P, bool up, const std::vector<int> &node
   for (int attempt = 0; attempt < 4; ++attempt) {
     const unsigned long long grow = 1ull << (2 * attempt);
     uint32_t stw = 0;
-    cudaError_t e = up ? merge_up_level_par(jobs, grow, P->status.p, &stw, st, &P->seq_ms[0])
+    cudaError_t e = up ? merge_up_level_par(jobs, grow, P->status.p, &stw, st, &P->seq_ms[0],
+                                            P->ctx->merge_round_window, P->ctx->merge_round_min_commits)
                        : merge_down_level_par(jobs, grow, P->status.p, &stw, st, &P->seq_ms[1]);
     if (e != cudaSuccess)
       return perr(e == cudaErrorMemoryAllocation ? DMSC_ERR_OOM : DMSC_ERR_CUDA,
@@ -273,6 +305,31 @@ int dmsc_pipeline_run(dmsc_ctx *ctx, const float *heights, int64_t pitch, int on
   create_pieces(P->pieces, whole, whole, levels, 0, split2d != 0);
   const int N = (int)P->pieces.size();
   P->msc.assign(2 * N - 1, nullptr);
+  P->archived.assign(2 * N - 1, 0);
+  // out of core only with pieces to merge (grid_datamanager.cpp:640-641)
+  const bool ooc = !ctx->ooc_dir.empty() && levels > 0;
+  if (ooc) {
+    static std::atomic<unsigned long long> serial{0};
+    P->ooc = ctx->ooc_dir + "/dp_msgraph_" + std::to_string((long long)getpid()) + "_" + std::to_string(serial++) + "_";
+  }
+  // a leaf's dataset: its window of the field, the gradient (work or work_ocl)
+  auto leaf_dataset = [&](int i, cudaStream_t s) {
+    const R4 &r = P->pieces[i].first, &e = P->pieces[i].second;
+    int16_t rr[4] = {(int16_t)r.l, (int16_t)r.b, (int16_t)r.r, (int16_t)r.t};
+    int16_t ee[4] = {(int16_t)e.l, (int16_t)e.b, (int16_t)e.r, (int16_t)e.t};
+    int q = dmsc_dataset_create(ctx, rr, ee, &P->ds[i]);
+    if (!q) q = dmsc_dataset_init(P->ds[i], dev + (long long)(e.b / 2) * pitch + e.l / 2, pitch, 1, s);
+    if (!q) q = P->ctx->use_ocl ? dmsc_dataset_work_ocl(P->ds[i], s) : dmsc_dataset_work(P->ds[i], s);
+    return q;
+  };
+  // out of core: the leaf's complex to its archive, its dataset freed (dataset->clear())
+  auto leaf_out = [&](int i, cudaStream_t s) {
+    int q = cudaStreamSynchronize(s) == cudaSuccess ? DMSC_OK : perr(DMSC_ERR_CUDA, "leaf stream");
+    if (!q) q = archive_node(P, i);
+    dmsc_dataset_destroy(P->ds[i]);
+    P->ds[i] = nullptr;
+    return q;
+  };
   double t0 = now_ms();
   // computeSubdomainMsgraphs (:493-528): every leaf independently, several at a time
   if (cudaStreamSynchronize(st) != cudaSuccess) return fail(perr(DMSC_ERR_CUDA, "field copy"));
@@ -281,13 +338,9 @@ int dmsc_pipeline_run(dmsc_ctx *ctx, const float *heights, int64_t pitch, int on
     std::string msg;
     std::mutex mu;
     const int rc = for_each_on_streams(ctx->device, N, PIECE_WORKERS, [&](int i, cudaStream_t s) {
-      const R4 &r = P->pieces[i].first, &e = P->pieces[i].second;
-      int16_t rr[4] = {(int16_t)r.l, (int16_t)r.b, (int16_t)r.r, (int16_t)r.t};
-      int16_t ee[4] = {(int16_t)e.l, (int16_t)e.b, (int16_t)e.r, (int16_t)e.t};
-      int q = dmsc_dataset_create(ctx, rr, ee, &P->ds[i]);
-      if (!q) q = dmsc_dataset_init(P->ds[i], dev + (long long)(e.b / 2) * pitch + e.l / 2, pitch, 1, s);
-      if (!q) q = dmsc_dataset_work(P->ds[i], s);
+      int q = leaf_dataset(i, s);
       if (!q) q = dmsc_dataset_writeout_connectivity(P->ds[i], &P->msc[i], s);
+      if (!q && ooc) q = leaf_out(i, s);
       if (q) { std::lock_guard<std::mutex> lk(mu); msg = dmsc_last_error(); }
       return q;
     });
@@ -301,6 +354,12 @@ int dmsc_pipeline_run(dmsc_ctx *ctx, const float *heights, int64_t pitch, int on
       // node N+k merges 2k and 2k+1; this level's inputs are [lo, lo+cnt)
       std::vector<int> nodes;
       for (int j = lo; j < lo + cnt; j += 2) nodes.push_back(N + j / 2);
+      if (ooc)  // the level's inputs back from their archives
+        for (int node : nodes) {
+          int rc = unarchive_node(P, 2 * (node - N));
+          if (!rc) rc = unarchive_node(P, 2 * (node - N) + 1);
+          if (rc) return fail(rc);
+        }
       for (int node : nodes) {
         int k = node - N;
         dmsc_msc *a = P->msc[2 * k], *b = P->msc[2 * k + 1];
@@ -314,6 +373,12 @@ int dmsc_pipeline_run(dmsc_ctx *ctx, const float *heights, int64_t pitch, int on
       }
       int rc = run_level(P, true, nodes, st);
       if (rc) return fail(rc);
+      if (ooc)  // inputs stay in their archives; new nodes but the root go to theirs
+        for (int node : nodes) {
+          drop_node(P, 2 * (node - N));
+          drop_node(P, 2 * (node - N) + 1);
+          if (cnt > 2 && (rc = archive_node(P, node))) return fail(rc);
+        }
       lo += cnt;
       cnt /= 2;
     }
@@ -334,8 +399,17 @@ int dmsc_pipeline_run(dmsc_ctx *ctx, const float *heights, int64_t pitch, int on
     for (size_t q = lv.size(); q-- > 0;) {
       std::vector<int> nodes;
       for (int n2 = lv[q].second; n2 >= lv[q].first; --n2) nodes.push_back(n2);
-      int rc = run_level(P, false, nodes, st);
+      int rc = DMSC_OK;
+      if (ooc)
+        for (int node : nodes)
+          for (int x : {node, 2 * (node - N), 2 * (node - N) + 1})
+            if ((rc = unarchive_node(P, x))) return fail(rc);
+      rc = run_level(P, false, nodes, st);
       if (rc) return fail(rc);
+      if (ooc)  // the parents and children changed: all back to their archives
+        for (int node : nodes)
+          for (int x : {node, 2 * (node - N), 2 * (node - N) + 1})
+            if ((rc = archive_node(P, x))) return fail(rc);
     }
   }
   double t4 = now_ms();
@@ -345,7 +419,13 @@ int dmsc_pipeline_run(dmsc_ctx *ctx, const float *heights, int64_t pitch, int on
     std::string msg;
     std::mutex mu;
     const int rc = for_each_on_streams(ctx->device, N, PIECE_WORKERS, [&](int i, cudaStream_t s) {
-      const int q = dmsc_dataset_fill_discs(P->ds[i], P->msc[i], s);
+      int q = DMSC_OK;
+      if (ooc) {  // collectManifold (:397-422): the gradient again, the complex from its archive
+        q = leaf_dataset(i, s);
+        if (!q) q = unarchive_node(P, i);
+      }
+      if (!q) q = dmsc_dataset_fill_discs(P->ds[i], P->msc[i], s);
+      if (!q && ooc) q = leaf_out(i, s);
       if (q) { std::lock_guard<std::mutex> lk(mu); msg = dmsc_last_error(); }
       return q;
     });
@@ -380,6 +460,7 @@ int dmsc_pipeline_num_pieces(dmsc_pipeline *p, int64_t *n) {
 
 int dmsc_pipeline_piece(dmsc_pipeline *p, int64_t i, dmsc_msc **msc, dmsc_dataset **ds) {
   if (!p || i < 0 || i >= (int64_t)p->msc.size()) return perr(DMSC_ERR_BAD_ARG, "no such piece");
+  if (msc) PRC(unarchive_node(p, (int)i));  // out of core: read back on first use
   if (msc) *msc = p->msc[i];
   if (ds) *ds = i < (int64_t)p->ds.size() ? p->ds[i] : nullptr;
   return DMSC_OK;
@@ -387,7 +468,10 @@ int dmsc_pipeline_piece(dmsc_pipeline *p, int64_t i, dmsc_msc **msc, dmsc_datase
 
 int dmsc_pipeline_write_discs(dmsc_pipeline *p, const char *prefix) {
   if (!p || !prefix) return perr(DMSC_ERR_BAD_ARG, "null argument");
-  for (size_t i = 0; i < p->pieces.size(); ++i) PRC(dmsc_msc_write_discs(p->msc[i], prefix));
+  for (size_t i = 0; i < p->pieces.size(); ++i) {
+    PRC(unarchive_node(p, (int)i));
+    PRC(dmsc_msc_write_discs(p->msc[i], prefix));
+  }
   return DMSC_OK;
 }
 

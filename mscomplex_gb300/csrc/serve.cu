@@ -62,12 +62,22 @@ struct Request {
 // labels per vertex, row counts / offsets and the border table per tile,
 // and a bound on its critical points and arcs (a critical cell per 4
 // vertices at most in practice; checked by the engine, which grows buffers
-// when needed).
-long long footprint_of(int nx, int ny) {
+// when needed).  With a threshold, the simplification's first allocation for
+// that many points and arcs (n = v/4 points, v arcs): list pool 4 (arcs +
+// 8 n) runs of 8 B, heap and resubmit list 8 * (v/2) entries of 12 + 8 B,
+// scratch runs 4 * arcs of 8 B, list descriptors 32 B per point.  A
+// simplification that outgrows it retries with larger buffers, beyond this
+// estimate.
+long long footprint_of(int nx, int ny, bool simplify) {
   const long long v = (long long)nx * ny;
   const long long tiles = (long long)((nx + dmsc::TX - 1) / dmsc::TX) * ((ny + dmsc::TY - 1) / dmsc::TY);
-  return v * (4 + 4 + 4 + 16) + 2ll * ny * (long long)((nx + dmsc::TX - 1) / dmsc::TX) * 5 +
-         tiles * dmsc::SLOTS_PER_TILE * 8 + (v / 4) * 64 + (1 << 16);
+  long long b = v * (4 + 4 + 4 + 16) + 2ll * ny * (long long)((nx + dmsc::TX - 1) / dmsc::TX) * 5 +
+                tiles * dmsc::SLOTS_PER_TILE * 8 + (v / 4) * 64 + (1 << 16);
+  if (simplify) {
+    const long long n = v / 4, arcs = v;
+    b += 8 * 4 * (arcs + 8 * n) + 20 * 8 * (v / 2) + 8 * 4 * arcs + 32 * n + (1 << 20);
+  }
+  return b;
 }
 
 }  // namespace
@@ -323,7 +333,7 @@ int dmsc_server_submit(dmsc_server *s, const float *heights, int nx, int ny, dou
   auto r = std::make_shared<Request>();
   r->nx = nx; r->ny = ny; r->tresh = tresh;
   r->heights.assign(heights, heights + (size_t)nx * ny);
-  r->footprint = footprint_of(nx, ny);
+  r->footprint = footprint_of(nx, ny, tresh > 0.0);
   if (tresh > 0.0) {  // equal neighbour pairs along x and y
     size_t ties = 0;
     const float *h = r->heights.data();

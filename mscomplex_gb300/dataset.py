@@ -48,6 +48,24 @@ class Context:
         critical points take the parallel merges (default 2048)."""
         check(self.lib.dmsc_set_merge_parallel_min(self.h, int(min_cps)))
 
+    def set_use_ocl(self, use_ocl: bool = True):
+        """GridDataManager's ocl flag (-ocl): pipelines of this context compute
+        their pieces with work_ocl."""
+        check(self.lib.dmsc_set_use_ocl(self.h, int(bool(use_ocl))))
+
+    def set_out_of_core(self, directory: str | None):
+        """GridDataManager's compute_out_of_core (--out-of-core): pipelines of
+        this context keep their pieces' complexes in archive files under
+        `directory` (None: in device memory)."""
+        check(self.lib.dmsc_set_out_of_core(self.h, directory.encode() if directory else None))
+
+    def set_merge_rounds(self, window: int = 2048, min_commits: int = 4):
+        """merge_up's boundary cancellations on the parallel merges: rounds over
+        the first `window` pending boundary cells (0: one thread per merge);
+        after 8 rounds in a row below `min_commits` commits, one thread
+        finishes in order.  Every setting gives the same complexes."""
+        check(self.lib.dmsc_set_merge_rounds(self.h, int(window), int(min_commits)))
+
     def close(self):
         if self.h:
             check(self.lib.dmsc_shutdown(self.h))
@@ -84,10 +102,22 @@ class GridDataset:
         self.vny = self.cny // 2 + 1
         self._keep = None
 
+    @classmethod
+    def _borrowed(cls, handle, ctx: Context, rect, ext, owner):
+        """A view of a dataset that another object owns (a pipeline's leaf)."""
+        self = cls.__new__(cls)
+        self.ctx, self.lib, self.h = ctx, ctx.lib, handle
+        self.rect, self.ext = _rect(rect), _rect(ext)
+        self.cnx = int(self.ext[2] - self.ext[0]) + 1
+        self.cny = int(self.ext[3] - self.ext[1]) + 1
+        self.vnx, self.vny = self.cnx // 2 + 1, self.cny // 2 + 1
+        self._keep, self._owner = None, owner
+        return self
+
     def __del__(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and getattr(self, "_owner", None) is None:
             self.lib.dmsc_dataset_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def init(self, heights, stream=None):
         """GridDataset::init: heights of the ext window, shape (vny, vnx), x fastest.
@@ -117,6 +147,13 @@ class GridDataset:
         check(self.lib.dmsc_dataset_work(self.h, stream))
         return self
 
+    def work_ocl(self, stream=None):
+        """GridDataset::work_ocl: the gradient of the reference's OpenCL
+        kernels (compareCells with vertices sorted descending), collation and
+        owner extrema."""
+        check(self.lib.dmsc_dataset_work_ocl(self.h, stream))
+        return self
+
     @property
     def num_critical(self) -> int:
         n = C.c_int64()
@@ -141,12 +178,14 @@ class GridDataset:
             check(self.lib.dmsc_dataset_export_critical(self.h, _ptr(out), None))
         return out
 
-    STAGES = ("gradient", "collate_scan", "border_resolve", "labels_arcs", "connectivity", "disc_hops", "discs")
+    STAGES = ("gradient", "collate_scan", "border_resolve", "labels_arcs", "connectivity", "disc_hops", "discs",
+              "seg_place_asc", "seg_place_des")
 
     def stage_times(self, with_discs: bool = False) -> dict:
         """Device times (ms) of the last work / writeout_connectivity (and, with
-        with_discs, post_merge_fill_discs: its hop kernel and the whole pass)."""
-        n = 7 if with_discs else 5
+        with_discs, post_merge_fill_discs: its hop kernel, the whole pass and
+        the placement kernel of each disc kind)."""
+        n = 9 if with_discs else 5
         ms = np.zeros(n, np.float32)
         check(self.lib.dmsc_dataset_stage_times(self.h, _ptr(ms), n))
         return dict(zip(self.STAGES, (float(v) for v in ms)))
@@ -165,6 +204,14 @@ class GridDataset:
             return msc
         h = C.c_void_p()
         check(self.lib.dmsc_dataset_writeout_connectivity(self.h, C.byref(h), stream))
+        return GridMSComplex(h, self.ctx)
+
+    def writeout_connectivity_ocl(self, stream=None) -> "GridMSComplex":
+        """GridDataset::writeout_connectivity_ocl: the complex from the saddle
+        incidences of the last work_ocl (the same complex as
+        writeout_connectivity gives)."""
+        h = C.c_void_p()
+        check(self.lib.dmsc_dataset_writeout_connectivity_ocl(self.h, C.byref(h), stream))
         return GridMSComplex(h, self.ctx)
 
 
@@ -198,6 +245,17 @@ class GridMSComplex:
     def write_discs(self, prefix: str):
         """GridMSComplex::write_discs: one binary file per disc, appended."""
         check(self.lib.dmsc_msc_write_discs(self.h, prefix.encode()))
+
+    def save(self, path: str):
+        """The whole complex to an archive file (this library's layout)."""
+        check(self.lib.dmsc_msc_save(self.h, path.encode()))
+
+    @classmethod
+    def load(cls, path: str, ctx: Context | None = None) -> "GridMSComplex":
+        ctx = ctx or default_context()
+        h = C.c_void_p()
+        check(ctx.lib.dmsc_msc_load(ctx.h, path.encode(), C.byref(h)))
+        return cls(h, ctx)
 
     def sizes(self):
         s = np.zeros(5, np.int64)
@@ -290,6 +348,16 @@ class GridDataManager:
         m = C.c_void_p()
         check(self.lib.dmsc_pipeline_piece(self.h, int(i), C.byref(m), None))
         return GridMSComplex(m, self.ctx, owner=self)
+
+    def leaf_dataset(self, i: int) -> GridDataset:
+        """Leaf i's dataset (gradient, owners, critical cells of its window),
+        owned by the pipeline."""
+        if not 0 <= i < self.num_pieces:
+            raise IndexError(f"leaf {i} out of range")
+        m, d = C.c_void_p(), C.c_void_p()
+        check(self.lib.dmsc_pipeline_piece(self.h, int(i), C.byref(m), C.byref(d)))
+        re = self.piece(i).export()["rect_ext"]
+        return GridDataset._borrowed(d, self.ctx, re[:4], re[4:], owner=self)
 
     def write_discs(self, prefix: str):
         """collectSubdomainManifolds: write_discs of every piece in leaf order."""

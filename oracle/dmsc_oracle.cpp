@@ -134,6 +134,12 @@ struct GridDataset {
   std::vector<cellid_t> pairs, own;
   std::vector<cellid_t> m_critical_cells;
   int64_t pair_overwrites = 0;  // oracle-only assertion counter (pairCells overwriting a pair)
+  // compareCells with the cell's vertices sorted DESCENDING, as the
+  // reference's OpenCL kernels sort them (dmsc/resources/assigngradient.cl:
+  // 40-87); false: the CPU path's ascending sort (grid_dataset.cpp:1530-1531)
+  bool desc_cmp = false;
+  // work_ocl's saddle incidences (grid_dataset.h:83-84)
+  std::vector<uint> m_saddle_incidence_idx_offset, m_saddle_incidence_idx;
 
   GridDataset(rect_t r, rect_t e) : m_rect(r), m_ext_rect(e) {}
 
@@ -236,14 +242,23 @@ struct GridDataset {
     return dir == 0 ? getCellFacets(c, out) : getCellCofacets(c, out);
   }
 
-  // :1519-1536 (ascending vertex sort, then lexicographical_compare)
+  // :1519-1536 (ascending vertex sort, then lexicographical_compare); with
+  // desc_cmp the OpenCL kernels' compareCells (assigngradient.cl:62-87):
+  // ins_sort_pts puts the largest vertex first (max_pt_idx, :40-60), then the
+  // same lexicographic compare, a shorter list being the smaller
   bool compareCells(cellid_t c1, cellid_t c2) const {
     if (getCellDim(c1) == 0) return ptLt(c1, c2);
     cellid_t p1[4], p2[4];
     uint n1 = getCellPoints(c1, p1), n2 = getCellPoints(c2, p2);
     auto lt = [this](cellid_t a, cellid_t b) { return ptLt(a, b); };
-    std::sort(p1, p1 + n1, lt);
-    std::sort(p2, p2 + n2, lt);
+    if (desc_cmp) {
+      auto gt = [this](cellid_t a, cellid_t b) { return ptLt(b, a); };
+      std::sort(p1, p1 + n1, gt);
+      std::sort(p2, p2 + n2, gt);
+    } else {
+      std::sort(p1, p1 + n1, lt);
+      std::sort(p2, p2 + n2, lt);
+    }
     return std::lexicographical_compare(p1, p1 + n1, p2, p2 + n2, lt);
   }
   // :1538-1552
@@ -379,6 +394,8 @@ struct GridDataset {
 
   void writeout_connectivity(GridMSComplex *msc);
   int postMergeFillDiscs(GridMSComplex *msc);
+  void work_ocl(bool collect_cps = true);
+  void writeout_connectivity_ocl(GridMSComplex *msc);
 };
 
 // discreteMorseAlgorithm.h:244-268
@@ -427,6 +444,221 @@ void GridDataset::writeout_connectivity(GridMSComplex *msc) {
     msc->m_cps[cp_idx]->isBoundryCancelable = true;
     msc->m_cps[cp_idx]->pair_idx = msc->m_id_cp_map[getCellPairId(c)];
   }
+}
+
+// ---------------------------------------------------------------------------
+// GridDataset::work_ocl (grid_dataset.cpp:353-399) restated on the CPU: the
+// OpenCL kernels of assigngradient.cl, collate_critpts.cl and
+// bfs_watershed.cl run one work-item at a time over ext-local coordinates,
+// each reading the images as they were before the kernel (the host binds the
+// same image as input and output, :476-479, 502-504, 529-531; the kernels'
+// results do not depend on the order their work-items run in).  Images hold
+// cells in the host arrays' [x][y] layout; pairs and owners in global
+// coordinates, owners with a -1 coordinate stored as they are
+// (common_funcs.cl:218-261).
+// ---------------------------------------------------------------------------
+namespace ocl {
+struct L2 { int x, y; };
+static inline bool eq(L2 a, L2 b) { return a.x == b.x && a.y == b.y; }
+static inline int dim(L2 c) { return (c.x & 1) + (c.y & 1); }
+static int facets(L2 c, L2 *f) {  // common_funcs.cl:15-49
+  if (dim(c) == 1) { f[0] = {c.x + c.x % 2, c.y + c.y % 2}; f[1] = {c.x - c.x % 2, c.y - c.y % 2}; return 2; }
+  if (dim(c) == 2) { f[0] = {c.x + 1, c.y}; f[1] = {c.x - 1, c.y}; f[2] = {c.x, c.y + 1}; f[3] = {c.x, c.y - 1}; return 4; }
+  return 0;
+}
+static int cofacets(L2 c, L2 *cf) {  // :51-85
+  if (dim(c) == 0) { cf[0] = {c.x + 1, c.y}; cf[1] = {c.x - 1, c.y}; cf[2] = {c.x, c.y + 1}; cf[3] = {c.x, c.y - 1}; return 4; }
+  if (dim(c) == 1) { cf[0] = {c.x + c.y % 2, c.y + c.x % 2}; cf[1] = {c.x - c.y % 2, c.y - c.x % 2}; return 2; }
+  return 0;
+}
+static bool on_tb(L2 c, L2 sz) { return c.x == 0 || c.y == 0 || c.x == sz.x || c.y == sz.y; }   // :134-142
+static bool outside_tb(L2 c, L2 sz) { return c.x < 0 || c.y < 0 || c.x > sz.x || c.y > sz.y; }  // :144-152
+}  // namespace ocl
+
+void GridDataset::work_ocl(bool collect_cps) {
+  using namespace ocl;
+  const L2 sz{m_ext_rect.size(0), m_ext_rect.size(1)};
+  const L2 eb{m_ext_rect.left(), m_ext_rect.bottom()};
+  const L2 ib{m_rect.left() - eb.x, m_rect.bottom() - eb.y}, it{m_rect.right() - eb.x, m_rect.top() - eb.y};
+  auto at = [&](L2 c) { return (size_t)c.x * cny + (size_t)c.y; };
+  auto G = [&](L2 c) { return cellid_t(c.x + eb.x, c.y + eb.y); };
+  auto Lc = [&](cellid_t c) { return L2{c[0] - eb.x, c[1] - eb.y}; };
+  const bool saved = desc_cmp;
+  desc_cmp = true;  // the kernels' compareCells (assigngradient.cl:62-87)
+  // create_pair_flag_imgs_ocl (:248-279): images from the host arrays
+  std::vector<uint8_t> fimg(flags.begin(), flags.end());
+  std::vector<cellid_t> pimg(pairs);
+  // assign_gradient (assigngradient.cl:89-183), over m_rect
+  for (int gy = 0; gy <= it.y - ib.y; ++gy)
+    for (int gx = 0; gx <= it.x - ib.x; ++gx) {
+      const L2 c{gx + ib.x, gy + ib.y};
+      L2 cf[4];
+      const int cf_ct = cofacets(c, cf);
+      int usable[4];
+      const bool c_tb = on_tb(c, sz);
+      for (int i = 0; i < 4; ++i) {
+        usable[i] = i < cf_ct;
+        if (!usable[i]) continue;
+        if (outside_tb(cf[i], sz)) usable[i] = 0;
+        if (c_tb && !on_tb(cf[i], sz)) usable[i] = 0;
+        if (!usable[i]) continue;
+        L2 f[4];
+        const int f_ct = facets(cf[i], f);
+        for (int j = 0; j < f_ct; ++j)
+          if (compareCells(G(c), G(f[j]))) usable[i] = 0;
+      }
+      bool paired = false;
+      L2 p{0, 0};
+      for (int i = 0; i < 4; ++i) {
+        if (!usable[i]) continue;
+        if (!paired) { p = cf[i]; paired = true; }
+        else if (compareCells(G(cf[i]), G(p))) p = cf[i];
+      }
+      if (paired) { pimg[at(c)] = G(p); fimg[at(c)] = 1; }
+      else fimg[at(c)] = 2;
+    }
+  // complete_pairings (:184-238), over ext
+  {
+    const std::vector<uint8_t> fin(fimg);
+    const std::vector<cellid_t> pin(pimg);
+    for (int y = 0; y <= sz.y; ++y)
+      for (int x = 0; x <= sz.x; ++x) {
+        const L2 c{x, y};
+        L2 f[4];
+        const int f_ct = facets(c, f);
+        for (int i = 0; i < f_ct; ++i) {
+          if (outside_tb(f[i], sz)) continue;  // (a 2D image read out of range; never taken for ext cells)
+          const L2 fp = Lc(pin[at(f[i])]);
+          if (eq(fp, c) && (fin[at(f[i])] & 1)) { pimg[at(c)] = G(f[i]); fimg[at(c)] = 1; break; }
+        }
+      }
+  }
+  // mark_boundrypairs_critical_1 (:240-301) and _2 (:303-336), over ext
+  {
+    const std::vector<uint8_t> fin(fimg);
+    for (int y = 0; y <= sz.y; ++y)
+      for (int x = 0; x <= sz.x; ++x) {
+        const L2 c{x, y};
+        if (!(fin[at(c)] & 1)) continue;
+        L2 cf[4];
+        const int cf_ct = cofacets(c, cf);
+        bool out = false;
+        for (int i = 0; i < cf_ct; ++i) {
+          if (outside_tb(cf[i], sz)) continue;
+          out |= cf[i].x < ib.x || cf[i].y < ib.y || cf[i].x > it.x || cf[i].y > it.y;
+        }
+        if (out) fimg[at(c)] = 3;
+      }
+  }
+  {
+    const std::vector<uint8_t> fin(fimg);
+    for (int y = 0; y <= sz.y; ++y)
+      for (int x = 0; x <= sz.x; ++x) {
+        const L2 c{x, y};
+        if (!(fin[at(c)] & 1)) continue;
+        const uint8_t pf = fin[at(Lc(pimg[at(c)]))];
+        if ((pf & 2) && (pf & 1)) fimg[at(c)] = 3;
+      }
+  }
+  desc_cmp = saved;
+  // read_pair_img_ocl / read_flag_img_ocl (:372-373)
+  pairs = pimg;
+  for (size_t k = 0; k < flags.size(); ++k) flags[k] = (int8_t)fimg[k];
+  // collateCritcalPoints_ocl (:550-657): row-major over ext
+  m_critical_cells.clear();
+  std::map<std::pair<int, int>, uint> crit_idx;  // the index collate_cps_writeids writes into the pair image
+  for (int y = 0; y <= sz.y; ++y)
+    for (int x = 0; x <= sz.x; ++x)
+      if (fimg[at(L2{x, y})] & 2) {
+        crit_idx[{x, y}] = (uint)m_critical_cells.size();
+        m_critical_cells.push_back(G(L2{x, y}));
+      }
+  // assignCellOwnerExtrema_ocl (:763-890): dobfs_markowner_extrema_init, then
+  // dobfs_markowner_extrema until nothing changes (bfs_watershed.cl:6-98)
+  auto store = [&](L2 v) { return (v.x != -1 && v.y != -1) ? cellid_t(v.x + eb.x, v.y + eb.y) : cellid_t(v.x, v.y); };
+  auto load = [&](cellid_t v) { return (v[0] != -1 && v[1] != -1) ? L2{v[0] - eb.x, v[1] - eb.y} : L2{v[0], v[1]}; };
+  std::vector<cellid_t> oimg(flags.size());
+  for (int y = 0; y <= sz.y; ++y)
+    for (int x = 0; x <= sz.x; ++x) {
+      const L2 c{x, y};
+      L2 inf{-1, -1};
+      const uint8_t fl = fimg[at(c)];
+      if (fl & 2) inf = c;
+      if (!(fl & 2) && (fl & 1)) {
+        const L2 p = Lc(pimg[at(c)]);
+        const int d = dim(c), pd = dim(p);
+        if (d == 0 || d == 2) inf = p;
+        else {
+          L2 cets[4];
+          if (pd == 0) facets(c, cets);
+          else cofacets(c, cets);
+          const int k = eq(cets[0], p) ? 1 : 0;
+          if (cets[k].x <= sz.x && cets[k].y <= sz.y) inf = cets[k];
+        }
+      }
+      oimg[at(c)] = store(inf);
+    }
+  for (int iter = 0;; ++iter) {
+    if (iter > 64) throw std::logic_error("work_ocl: owner pointers did not converge");
+    const std::vector<cellid_t> oin(oimg);
+    bool changed = false;
+    for (int y = 0; y <= sz.y; ++y)
+      for (int x = 0; x <= sz.x; ++x) {
+        const L2 c{x, y};
+        const L2 o = load(oin[at(c)]);
+        L2 oo = o;
+        if (!outside_tb(o, sz)) oo = load(oin[at(o)]);
+        oimg[at(c)] = store(oo);
+        if (!eq(oo, o)) changed = true;
+      }
+    if (!changed) break;
+  }
+  // collect_saddle_conn_ocl (:907-1022): count_critpt_incidences and
+  // write_critpt_incidences (collate_critpts.cl:101-195)
+  m_saddle_incidence_idx_offset.assign(m_critical_cells.size() + 1, 0);
+  m_saddle_incidence_idx.clear();
+  if (collect_cps) {
+    for (size_t k = 0; k < m_critical_cells.size(); ++k) {
+      const L2 c = Lc(m_critical_cells[k]);
+      if (dim(c) == 1) {
+        L2 n[4];
+        facets(c, n);
+        cofacets(c, n + 2);
+        for (int i = 0; i < 4; ++i) {
+          if (outside_tb(n[i], sz)) continue;
+          const L2 o = load(oimg[at(n[i])]);
+          if (outside_tb(o, sz)) continue;
+          auto f = crit_idx.find({o.x, o.y});
+          if (f == crit_idx.end()) throw std::logic_error("work_ocl: an incidence owner is not critical");
+          m_saddle_incidence_idx.push_back(f->second);
+        }
+      }
+      m_saddle_incidence_idx_offset[k + 1] = (uint)m_saddle_incidence_idx.size();
+    }
+  }
+  // read_own_img_ocl (:392)
+  own = oimg;
+}
+
+// grid_dataset.cpp:1250-1283 with the index overload of connectCps (:1233-1248)
+void GridDataset::writeout_connectivity_ocl(GridMSComplex *msc) {
+  addCriticalPointsToMSComplex(msc, m_critical_cells);
+  msc->m_cp_fns.resize(m_critical_cells.size());
+  for (size_t k = 0; k < m_critical_cells.size(); ++k) {
+    cellid_t c = m_critical_cells[k];
+    uint cp_idx = msc->m_id_cp_map[c];
+    msc->m_cp_fns[cp_idx] = get_cell_fn(c);
+    if (!isCellPaired(c)) continue;
+    msc->m_cps[cp_idx]->isBoundryCancelable = true;
+    msc->m_cps[cp_idx]->pair_idx = msc->m_id_cp_map[getCellPairId(c)];
+  }
+  for (size_t i = 1; i < m_saddle_incidence_idx_offset.size(); ++i)
+    for (uint j = m_saddle_incidence_idx_offset[i - 1]; j < m_saddle_incidence_idx_offset[i]; ++j) {
+      uint a = m_saddle_incidence_idx[j], b = (uint)(i - 1);
+      if (s_getCellDim(msc->m_cps[a]->cellid) < s_getCellDim(msc->m_cps[b]->cellid)) std::swap(a, b);
+      msc->m_cps[a]->des.insert(b);
+      msc->m_cps[b]->asc.insert(a);
+    }
 }
 
 // grid_dataset.cpp:1044-1231
@@ -880,6 +1112,7 @@ struct Piece {
 
 struct Pipeline {
   int X = 0, Y = 0, levels = 0, split2d = 0;
+  int ocl = 0;  // GridDataManager's ocl flag (-ocl): pieces through work_ocl (grid_datamanager.cpp:123-132, 221-222, 433-434)
   double tresh = 0;
   std::vector<Piece> pieces;
   size_t nleaves = 0;
@@ -943,8 +1176,13 @@ static void run_pipeline(Pipeline &P, const float *full) {
   for (size_t i = 0; i < P.nleaves; ++i) {
     Piece &p = P.pieces[i];
     init_piece_data(full, P.X, p.ds);
-    p.ds->work();
-    p.ds->writeout_connectivity(p.msc);
+    if (P.ocl) {
+      p.ds->work_ocl();
+      p.ds->writeout_connectivity_ocl(p.msc);
+    } else {
+      p.ds->work();
+      p.ds->writeout_connectivity(p.msc);
+    }
     P.pair_overwrites += p.ds->pair_overwrites;
   }
   double t1 = now_ms();
@@ -978,7 +1216,8 @@ static void run_pipeline(Pipeline &P, const float *full) {
     Piece &p = P.pieces[i];
     GridDataset *ds = new GridDataset(p.ds->m_rect, p.ds->m_ext_rect);
     init_piece_data(full, P.X, ds);
-    ds->work();
+    if (P.ocl) ds->work_ocl(false);
+    else ds->work();
     ds->postMergeFillDiscs(p.msc);
     delete ds;
     for (auto *cp : p.msc->m_cps) {
@@ -1013,15 +1252,24 @@ static thread_local std::string g_err;
 const char *orc_last_error() { return g_err.c_str(); }
 
 // One GridDataset: init + work + writeout_connectivity (+ optional simplify
-// and postMergeFillDiscs on its own complex, as with levels = 0).
-void *orc_ds_run(const float *window, const int16_t rect[4], const int16_t ext[4], double tresh, int fill_discs) {
+// and postMergeFillDiscs on its own complex, as with levels = 0).  mode 0:
+// the CPU path; 1: the CPU path with the OpenCL kernels' compareCells
+// (descending vertex sort); 2: work_ocl + writeout_connectivity_ocl.
+void *orc_ds_run_mode(const float *window, const int16_t rect[4], const int16_t ext[4], double tresh, int fill_discs,
+                      int mode) {
   try {
     orc_ds_h *h = new orc_ds_h;
     h->ds = new GridDataset(rect_t(rect[0], rect[1], rect[2], rect[3]), rect_t(ext[0], ext[1], ext[2], ext[3]));
     h->ds->init(window);
-    h->ds->work();
     h->msc = new GridMSComplex(h->ds->m_rect, h->ds->m_ext_rect);
-    h->ds->writeout_connectivity(h->msc);
+    if (mode == 2) {
+      h->ds->work_ocl();
+      h->ds->writeout_connectivity_ocl(h->msc);
+    } else {
+      h->ds->desc_cmp = mode == 1;
+      h->ds->work();
+      h->ds->writeout_connectivity(h->msc);
+    }
     if (tresh > 0.0) {
       canc_list_t canc;
       simplify(h->msc, canc, tresh, nullptr);
@@ -1033,6 +1281,9 @@ void *orc_ds_run(const float *window, const int16_t rect[4], const int16_t ext[4
     g_err = e.what();
     return nullptr;
   }
+}
+void *orc_ds_run(const float *window, const int16_t rect[4], const int16_t ext[4], double tresh, int fill_discs) {
+  return orc_ds_run_mode(window, rect, ext, tresh, fill_discs, 0);
 }
 void orc_ds_free(void *p) {
   orc_ds_h *h = (orc_ds_h *)p;
@@ -1082,17 +1333,21 @@ void orc_dump_fill(void *p, int16_t *rect_ext, int16_t *cellid, float *fn, uint3
 }
 void orc_dump_free(void *p) { delete (MscDump *)p; }
 
-// Whole pipeline (GridDataManager ctor), full field x-fastest X*Y.
-void *orc_pipeline_run(const float *full, int X, int Y, int levels, double tresh, int split2d) {
+// Whole pipeline (GridDataManager ctor), full field x-fastest X*Y; ocl as
+// the -ocl flag.
+void *orc_pipeline_run_ocl(const float *full, int X, int Y, int levels, double tresh, int split2d, int ocl) {
   try {
     Pipeline *P = new Pipeline;
-    P->X = X; P->Y = Y; P->levels = levels; P->tresh = tresh; P->split2d = split2d;
+    P->X = X; P->Y = Y; P->levels = levels; P->tresh = tresh; P->split2d = split2d; P->ocl = ocl;
     run_pipeline(*P, full);
     return P;
   } catch (std::exception &e) {
     g_err = e.what();
     return nullptr;
   }
+}
+void *orc_pipeline_run(const float *full, int X, int Y, int levels, double tresh, int split2d) {
+  return orc_pipeline_run_ocl(full, X, Y, levels, tresh, split2d, 0);
 }
 void orc_pipeline_free(void *p) { delete (Pipeline *)p; }
 int64_t orc_pipeline_nleaves(void *p) { return (int64_t)((Pipeline *)p)->nleaves; }

@@ -43,6 +43,8 @@ def lib():
         L.orc_last_error.restype = C.c_char_p
         L.orc_ds_run.restype = vp
         L.orc_ds_run.argtypes = [vp, vp, vp, f64, i32]
+        L.orc_ds_run_mode.restype = vp
+        L.orc_ds_run_mode.argtypes = [vp, vp, vp, f64, i32, i32]
         L.orc_ds_free.argtypes = [vp]
         L.orc_ds_ncells.restype = i64
         L.orc_ds_ncells.argtypes = [vp]
@@ -56,6 +58,8 @@ def lib():
         L.orc_dump_free.argtypes = [vp]
         L.orc_pipeline_run.restype = vp
         L.orc_pipeline_run.argtypes = [vp, i32, i32, i32, f64, i32]
+        L.orc_pipeline_run_ocl.restype = vp
+        L.orc_pipeline_run_ocl.argtypes = [vp, i32, i32, i32, f64, i32, i32]
         L.orc_pipeline_free.argtypes = [vp]
         for f in ("orc_pipeline_nleaves", "orc_pipeline_npieces", "orc_pipeline_ncancel",
                   "orc_pipeline_overwrites", "orc_pipeline_ndisc_files", "orc_pipeline_disc_cells"):
@@ -103,18 +107,28 @@ def _check(h):
     return h
 
 
+# Dataset modes: the CPU path; the CPU path with the OpenCL kernels'
+# compareCells (vertices sorted descending, dmsc/resources/assigngradient.cl:
+# 40-87); the OpenCL path itself restated (GridDataset::work_ocl +
+# writeout_connectivity_ocl, dmsc/src/grid_dataset.cpp:353-1022, 1250-1283).
+MODE_CPU, MODE_CPU_DESC, MODE_OCL = 0, 1, 2
+
+
 class Dataset:
     """One GridDataset run: init + work + writeout_connectivity
     (dmsc/src/grid_dataset.cpp:1461, 1734, 1858), optionally followed by
-    simplify_un_simplify and postMergeFillDiscs on its own complex."""
+    simplify_un_simplify and postMergeFillDiscs on its own complex.  With
+    mode=MODE_OCL: work_ocl + writeout_connectivity_ocl instead."""
 
-    def __init__(self, window: np.ndarray, rect, ext, tresh: float = 0.0, fill_discs: bool = False):
+    def __init__(self, window: np.ndarray, rect, ext, tresh: float = 0.0, fill_discs: bool = False,
+                 mode: int = MODE_CPU):
         window = np.ascontiguousarray(window, dtype=np.float32)
         r = np.asarray(rect, np.int16)
         e = np.asarray(ext, np.int16)
         ny, nx = (e[3] - e[1]) // 2 + 1, (e[2] - e[0]) // 2 + 1
         assert window.shape == (ny, nx), (window.shape, (ny, nx))
-        self._h = _check(lib().orc_ds_run(_ptr(window), _ptr(r), _ptr(e), float(tresh), int(fill_discs)))
+        self._h = _check(lib().orc_ds_run_mode(_ptr(window), _ptr(r), _ptr(e), float(tresh), int(fill_discs),
+                                               int(mode)))
         self.rect, self.ext = r, e
         self.cnx, self.cny = int(e[2] - e[0]) + 1, int(e[3] - e[1]) + 1
 
@@ -143,10 +157,12 @@ class Dataset:
 class Pipeline:
     """GridDataManager (dmsc/src/grid_datamanager.cpp:596-662), single-threaded order."""
 
-    def __init__(self, field: np.ndarray, levels: int = 0, tresh: float = 0.0, split2d: bool = False):
+    def __init__(self, field: np.ndarray, levels: int = 0, tresh: float = 0.0, split2d: bool = False,
+                 ocl: bool = False):
         field = np.ascontiguousarray(field, dtype=np.float32)
         Y, X = field.shape
-        self._h = _check(lib().orc_pipeline_run(_ptr(field), X, Y, int(levels), float(tresh), int(split2d)))
+        self._h = _check(lib().orc_pipeline_run_ocl(_ptr(field), X, Y, int(levels), float(tresh), int(split2d),
+                                                    int(bool(ocl))))
 
     def __del__(self):
         if getattr(self, "_h", None):

@@ -16,9 +16,14 @@ def test_parse_rejects(capsys):
     with pytest.raises(SystemExit):
         parse(["-d", "4", "4"])  # no file
     with pytest.raises(SystemExit):
-        parse(["-gf", "f", "-d", "4", "4", "--out-of-core"])
-    with pytest.raises(SystemExit):
         parse(["-gf", "f", "-d", "1", "4"])
+    with pytest.raises(SystemExit):
+        parse(["-gf", "f", "-d", "4", "4", "-l", "-1"])
+
+
+def test_parse_backend_and_out_of_core_flags():
+    a = parse(["-gf", "f", "-d", "8", "8", "-ocl", "--out-of-core", "--outdir", "/tmp/x"])
+    assert a.ocl and a.out_of_core and a.outdir == "/tmp/x"
 
 
 def test_load_raw(tmp_path):

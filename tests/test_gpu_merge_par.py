@@ -120,3 +120,46 @@ def test_par_too_thin_pieces_fail_like_the_reference(gpu_lib, oracle, par_ctx):
         oracle.Pipeline(f, levels=3, tresh=0.05, split2d=False)
     with pytest.raises(gpu_lib.DmscError):
         gpu_lib.GridDataManager(f, levels=3, tresh=0.05, split2d=False, ctx=par_ctx)
+
+
+# merge_up's boundary cancellations in ordered-parallel rounds: every setting
+# of the rounds (window, hand-off rate) against the oracle, node by node.
+# window 0 runs the loop on one thread per merge; min_commits far above any
+# round's commits makes the rounds hand the rest to the in-order thread after
+# 8 rounds, so the finishing path runs on every merge with a boundary longer
+# than 8 windows; window 1 takes one task per round.
+ROUND_SETTINGS = [(2048, 4), (0, 0), (16, 1 << 30), (64, 1 << 30), (1, 0), (3, 2)]
+
+
+@pytest.fixture(scope="module", params=ROUND_SETTINGS, ids=lambda s: f"win{s[0]}-min{s[1]}")
+def rounds_ctx(gpu_lib, request):
+    ctx = gpu_lib.Context()
+    ctx.set_merge_parallel_min(0)
+    ctx.set_merge_rounds(*request.param)
+    yield ctx
+    ctx.close()
+
+
+def test_rounds_bumps256(gpu_lib, oracle, rounds_ctx):
+    """A smooth field: large extrema sit in most footprints, so groups stay large."""
+    from mscomplex_gb300 import synth
+    check(gpu_lib, oracle, rounds_ctx, synth.bumps256(), 3, 0.05, True, "rounds bumps256 L3")
+
+
+def test_rounds_noise(gpu_lib, oracle, rounds_ctx):
+    from mscomplex_gb300 import synth
+    check(gpu_lib, oracle, rounds_ctx, synth.noise(256, seed=3), 4, 0.0, True, "rounds noise256 L4")
+
+
+def test_rounds_quantized(gpu_lib, oracle, rounds_ctx):
+    from mscomplex_gb300 import synth
+    check(gpu_lib, oracle, rounds_ctx, synth.bumps4096q(n=256), 2, 0.01, False, "rounds bumps256q L2")
+
+
+def test_rounds_settings_rejected(gpu_lib):
+    ctx = gpu_lib.Context()
+    with pytest.raises(gpu_lib.DmscError):
+        ctx.set_merge_rounds(-1, 4)
+    with pytest.raises(gpu_lib.DmscError):
+        ctx.set_merge_rounds(16, -2)
+    ctx.close()

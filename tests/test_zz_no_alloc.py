@@ -32,8 +32,10 @@ def test_noalloc_scan_matches_allocating_scan(gpu_lib):
     lib = ctx.lib
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     rng = np.random.default_rng(20261203)
-    # two calls in a row: a large scan, then a smaller one over different data
-    for n in (3_000_017, 4096 * 37 + 5):
+    # calls in a row over different data: two-level scans, then the largest
+    # size the fixed scratch serves and a 4096^2 + 1 scan (three levels of
+    # partial sums in the fixed array)
+    for n in (3_000_017, 4096 * 37 + 5, 1 << 26, 4096 * 4096 + 1):
         x = rng.integers(0, 2 ** 32, size=n, dtype=np.uint64).astype(np.uint32)
         d_in = _u32_tensor(x)
         want, got = torch.empty_like(d_in), torch.full_like(d_in, -1)
