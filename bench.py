@@ -52,13 +52,15 @@ KERNEL_BYTES = {
     "gradient": (8.0, 0, 0, 0, 0),        # k_gradient: 4 B height read + 4 B gradient codes (1 B per cell)
     "labels_arcs": (16.0, 12, 8, 0, 0),   # k_labels: 16 B owner labels (4 B per cell), cp records, arcs
     "disc_hops": (0.0, 0, 0, 0, 0),       # k_disc_hops: writes only the hop structure (intermediate)
-    "seg_place_asc": (0.0, 0, 0, 4, 0),   # k_seg_place (asc): 4 B per saddle disc cell written
-    "seg_place_des": (0.0, 0, 0, 0, 4),   # k_seg_place (des)
+    # the saddle discs of one kind: pieces bucketed by tile, then k_tile_place (and the level-0 items and
+    # the discs of saddles with many chains); 4 B per saddle disc cell written
+    "seg_place_asc": (0.0, 0, 0, 4, 0),
+    "seg_place_des": (0.0, 0, 0, 0, 4),
 }
 KERNEL_NAMES = {"gradient": "k_gradient", "labels_arcs": "k_labels", "disc_hops": "k_disc_hops",
-                "seg_place_asc": "k_seg_place", "seg_place_des": "k_seg_place"}
+                "seg_place_asc": "k_tile_place", "seg_place_des": "k_tile_place"}
 TRAFFIC_KEYS = {"gradient": "k_gradient", "labels_arcs": "k_labels", "disc_hops": "k_disc_hops",
-                "seg_place_asc": "k_seg_place:asc", "seg_place_des": "k_seg_place:des"}
+                "seg_place_asc": "k_tile_place:asc", "seg_place_des": "k_tile_place:des"}
 # The whole step: 24 B/vertex (height, gradient, owner labels) + 12 B/cp + 8 B/arc + 4 B per disc cell written.
 PIPE_BYTES = (24.0, 12, 8, 4)
 

@@ -196,11 +196,12 @@ int dmsc_pipeline_merge_times(dmsc_pipeline *p, double ms[2]);
  * one thread (one block per merge).  Both give the same complexes. */
 int dmsc_set_merge_parallel_min(dmsc_ctx *ctx, int64_t min_cps);
 /* merge_up's cancellations along each shared boundary (the loop of
- * dmsc/src/grid_mscomplex.cpp:124-153) on the parallel merges: rounds over
- * the first `window` pending boundary cells (default 2048; 0 runs the loop on
- * one thread per merge); after 8 rounds in a row that each commit fewer than
- * `min_commits` cells (default 4), one thread finishes the rest in order.
- * Every setting gives the same complexes. */
+ * dmsc/src/grid_mscomplex.cpp:124-153) on the parallel merges: 0 (the
+ * default) runs the loop on one thread per merge; window > 0 runs it in
+ * ordered-parallel rounds over the first `window` pending boundary cells,
+ * and after 8 rounds in a row that each commit fewer than `min_commits` cells
+ * (default 4) one thread finishes the rest in order.  Every setting gives the
+ * same complexes; on white noise the one-thread loop is the faster. */
 int dmsc_set_merge_rounds(dmsc_ctx *ctx, int64_t window, int64_t min_commits);
 /* GridDataManager's `ocl` argument (the -ocl flag, dmsc/src/main.cpp:527-530;
  * used at dmsc/src/grid_datamanager.cpp:123-132, 221-222, 433-434): pipelines

@@ -280,7 +280,7 @@ __global__ void k_saddle_disc_write(DiscArgs a, int kind, SeedRuns sr, const uin
 // lengths fix every cell's place before any cell is known: per saddle, the
 // level ranges over which its set of alive chains is constant are regular
 // interleaves (k_zip_blocks), and the cells, walked by one lane per piece of
-// at most SEG_MAX cells, are stored straight there (k_seg_place).
+// at most SEG_MAX cells, are stored straight there (k_tile_place).
 // ---------------------------------------------------------------------------
 constexpr int KMAX = 32;                 // saddles with more chains take the serial pass
 constexpr uint32_t HOP_END = 0xFFFFFFFFu;
@@ -475,6 +475,7 @@ struct ChainArgs {
   uint32_t *cbase;      // exclusive scan of kc
   uint32_t *cstart, *csaddle, *clen, *cnseg, *csegoff;  // per chain
   uint4 *segs;          // (chain, first edge, first level, cells)
+  uint32_t *tile_cnt;   // pieces per 64x64 tile (the tile of their first edge)
   uint4 *blocks;        // per chain slot of a saddle, 2 uint4: an interleave record (k_zip_blocks)
   uint32_t cap;         // chain slots allocated
   unsigned long long limit;
@@ -542,21 +543,48 @@ __global__ void k_chain_len(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, uint
   }
 }
 
-// write pieces of every chain: its hops cut at every SEG_MAX cells
-__global__ void k_chain_segs(long long nchains, ChainArgs c) {
+// the 64x64 vertex tile of an edge
+__device__ __forceinline__ uint32_t edge_tile(const GridGeom &g, uint32_t e) {
+  const uint32_t v = e >> 1;
+  const uint32_t vx = v % (uint32_t)g.vnx, vy = v / (uint32_t)g.vnx;
+  return (vy / TY) * (uint32_t)g.ntx + vx / TX;
+}
+
+// write pieces of every chain: its hops (in-tile runs) cut at every SEG_MAX
+// cells; counts the pieces of each tile
+__global__ void k_chain_segs(long long nchains, GridGeom g, ChainArgs c) {
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nchains; k += (long long)gridDim.x * blockDim.x) {
     uint32_t o = c.csegoff[k], end = c.csegoff[k + 1], T = 1;
     for (uint32_t e = c.cstart[k]; e != HOP_END && o < end; e = c.hop_to[e]) {
       const uint32_t l = c.hop_len[e];
       if (l == 0) break;
       uint32_t x = e;
+      const uint32_t tile = edge_tile(g, e);
       for (uint32_t done = 0; done < l && o < end && x != HOP_END; done += SEG_MAX) {
         const uint32_t w = l - done < (uint32_t)SEG_MAX ? l - done : (uint32_t)SEG_MAX;
         c.segs[o++] = make_uint4((uint32_t)k, x, T + done, w);
+        atomicAdd(&c.tile_cnt[tile], 1u);
         if (done + SEG_MAX < l) x = c.jseg[x];
       }
       T += l;
     }
+    for (; o < end; ++o) c.segs[o] = make_uint4(0xFFFFFFFFu, 0, 0, 0);  // a chain cut short (status already set)
+  }
+}
+
+// the pieces grouped by tile (any order inside a tile: every cell's place in
+// its disc is fixed by its chain and level)
+__global__ void k_seg_bucket(long long nsegs, DiscArgs a, const uint4 *__restrict__ segs, const uint32_t *__restrict__ toff,
+                             uint32_t *__restrict__ cursor, uint4 *__restrict__ out) {
+  const GridGeom &g = a.g;
+  const uint32_t ntiles = (uint32_t)g.ntx * (uint32_t)g.nty;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nsegs; k += (long long)gridDim.x * blockDim.x) {
+    const uint4 sg = segs[k];
+    const uint32_t tile = sg.x == 0xFFFFFFFFu ? ntiles : edge_tile(g, sg.y);
+    if (tile >= ntiles) { atomicOr(a.status, ST_INVARIANT); continue; }
+    const uint32_t p = toff[tile] + atomicAdd(&cursor[tile], 1u);
+    if (p >= toff[tile + 1]) { atomicOr(a.status, ST_INVARIANT); continue; }
+    out[p] = sg;
   }
 }
 
@@ -603,77 +631,79 @@ __global__ void k_zip_blocks(DiscArgs a, ChainArgs c, const uint32_t *off) {
 }
 
 // Pieces of at most SEG_MAX cells of one chain, stored straight at their
-// places in the disc.  Each lane of a warp follows the 1-byte successor
-// offsets of one piece into shared memory; then the warp stores the 32
-// pieces one after another, one cell per lane.  The cell at level t of the
-// saddle's j-th chain goes to the interleave record (k_zip_blocks) whose
-// level range holds t: start + (t - first level) * alive + (alive chains
-// before j), the order of the reference's breadth-first disc.
-constexpr int SEG_WARPS = 4;
-__global__ void __launch_bounds__(SEG_WARPS * 32) k_seg_place(DiscArgs a, ChainArgs c, long long nsegs, uint32_t *out,
+// places in the disc.  One block per 64x64 tile takes the pieces that lie in
+// it (a piece is part of an in-tile run): the tile's successor offsets (1 byte
+// per edge) are loaded into shared memory once, and each thread follows its
+// pieces there, one cell per step.  The cell at level t of the saddle's j-th
+// chain goes to the interleave record (k_zip_blocks) whose level range holds
+// t: start + (t - first level) * alive + (alive chains before j), the order of
+// the reference's breadth-first disc.
+constexpr int PLACE_THREADS = 256;
+__global__ void __launch_bounds__(PLACE_THREADS) k_tile_place(DiscArgs a, ChainArgs c, const uint4 *__restrict__ segs,
+                                                              const uint32_t *__restrict__ toff, uint32_t *out,
                                                               unsigned long long out_len) {
-  __shared__ uint32_t buf[SEG_WARPS][32][SEG_MAX + 1];  // +1: lanes' rows fall in different banks
+  __shared__ uint8_t sd[HOP_SLOTS];
   const GridGeom &g = a.g;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const long long gw = ((long long)blockIdx.x * SEG_WARPS + w), nwarps = (long long)gridDim.x * SEG_WARPS;
-  for (long long k0 = gw * 32; k0 < nsegs; k0 += nwarps * 32) {
-    const long long k = k0 + lane;
-    uint32_t len = 0, t0 = 0, cb = 0, K = 0, j = 0;
-    if (k < nsegs) {
-      const uint4 sg = c.segs[k];
-      const uint32_t ch = sg.x;
-      bool ok = ch < c.cap;
-      uint32_t s = 0;
-      if (ok) { s = c.csaddle[ch]; ok = s < a.ncp; }
-      if (ok) {
-        cb = c.cbase[s];
-        K = c.kc[s];
-        j = ch - cb;  // wraps (and fails j < K) for a chain below the saddle's slots
-        t0 = sg.z;
-        ok = sg.z >= 1 && sg.w <= (uint32_t)SEG_MAX && sg.z - 1 + sg.w <= c.clen[ch] && j < K && K <= (uint32_t)KMAX &&
-             cb + K <= c.cap;
-      }
-      if (!ok) {
-        atomicOr(a.status, ST_INVARIANT);
-      } else {
-        int rx, ry;
-        edge_cell(g, sg.y, rx, ry);
-        for (uint32_t i = 0; i < sg.w; ++i) {
-          buf[w][lane][i] = pack_cellid(g.ex0 + rx, g.ey0 + ry);
-          ++len;
-          if (i + 1 < sg.w) {
-            const uint32_t d = c.nextd[edge_id(g, rx, ry)];
-            if (d == SUCC_NONE) { atomicOr(a.status, ST_INVARIANT); break; }
-            rx += (int)(d % 5) - 2;
-            ry += (int)(d / 5) - 2;
-          }
-        }
-      }
-    }
-    __syncwarp();
-    for (int p = 0; p < 32; ++p) {
-      const uint32_t n = __shfl_sync(0xffffffffu, len, p), tp = __shfl_sync(0xffffffffu, t0, p);
-      const uint32_t cbp = __shfl_sync(0xffffffffu, cb, p), Kp = __shfl_sync(0xffffffffu, K, p);
-      const uint32_t jp = __shfl_sync(0xffffffffu, j, p);
-      if ((uint32_t)lane >= n) continue;
-      const uint32_t t = tp + lane;
-      unsigned long long pos = ~0ull;
-      for (uint32_t b = 0; b < Kp; ++b) {  // the records ascend in level
-        const uint4 r0 = c.blocks[2 * (cbp + b)];
-        if (!r0.y || !r0.z) break;
-        const uint32_t first = c.blocks[2 * (cbp + b) + 1].x, nlev = r0.y / r0.z;
-        if (t < first) break;
-        if (t - first < nlev) {
-          if (r0.w & (1u << jp))
-            pos = (unsigned long long)r0.x + (unsigned long long)(t - first) * r0.z + __popc(r0.w & ((1u << jp) - 1u));
-          break;
-        }
-      }
-      if (pos >= out_len) atomicOr(a.status, ST_INVARIANT);
-      else out[pos] = buf[w][p][lane];
-    }
-    __syncwarp();
+  const uint32_t tile = blockIdx.x;
+  const uint32_t p0 = toff[tile], p1 = toff[tile + 1];
+  if (p0 >= p1) return;
+  const int tx0 = (int)(tile % (uint32_t)g.ntx) * TX, ty0 = (int)(tile / (uint32_t)g.ntx) * TY;
+  for (int i = threadIdx.x; i < HOP_SLOTS; i += blockDim.x) {  // slot 2 (lj TX + li) + t, rows of 2 TX bytes
+    const int lj = i / (2 * TX), r = i - lj * (2 * TX), vx = tx0 + (r >> 1), vy = ty0 + lj;
+    sd[i] = (vx < g.vnx && vy < g.vny) ? c.nextd[2 * ((long long)vy * g.vnx + vx) + (r & 1)] : SUCC_NONE;
   }
+  __syncthreads();
+  uint32_t st = 0;
+  for (uint32_t k = p0 + threadIdx.x; k < p1; k += blockDim.x) {
+    const uint4 sg = segs[k];
+    const uint32_t ch = sg.x;
+    if (ch >= c.cap) { st |= ST_INVARIANT; continue; }
+    const uint32_t s = c.csaddle[ch];
+    if (s >= a.ncp) { st |= ST_INVARIANT; continue; }
+    const uint32_t cb = c.cbase[s], K = c.kc[s], j = ch - cb;  // j wraps for a chain below the saddle's slots
+    if (!(sg.z >= 1 && sg.w >= 1 && sg.w <= (uint32_t)SEG_MAX && sg.z - 1 + sg.w <= c.clen[ch] && j < K &&
+          K <= (uint32_t)KMAX && cb + K <= c.cap)) {
+      st |= ST_INVARIANT;
+      continue;
+    }
+    // the record whose level range holds the piece's first level (records ascend in level)
+    uint32_t b = 0, first = 0, nlev = 0;
+    uint4 r0 = make_uint4(0, 0, 0, 0);
+    for (; b < K; ++b) {
+      r0 = c.blocks[2 * (cb + b)];
+      if (!r0.y || !r0.z) { b = K; break; }
+      first = c.blocks[2 * (cb + b) + 1].x;
+      nlev = r0.y / r0.z;
+      if (sg.z - first < nlev) break;
+    }
+    if (b >= K || sg.z < first) { st |= ST_INVARIANT; continue; }
+    int rx, ry;
+    edge_cell(g, sg.y, rx, ry);
+    for (uint32_t i = 0; i < sg.w; ++i) {
+      const uint32_t t = sg.z + i;
+      while (t - first >= nlev) {  // the next level range
+        if (++b >= K) break;
+        r0 = c.blocks[2 * (cb + b)];
+        first = c.blocks[2 * (cb + b) + 1].x;
+        nlev = r0.z ? r0.y / r0.z : 0;
+        if (!r0.y || !r0.z) { b = K; break; }
+      }
+      if (b >= K || !(r0.w & (1u << j))) { st |= ST_INVARIANT; break; }
+      const unsigned long long pos =
+          (unsigned long long)r0.x + (unsigned long long)(t - first) * r0.z + __popc(r0.w & ((1u << j) - 1u));
+      if (pos >= out_len) { st |= ST_INVARIANT; break; }
+      out[pos] = pack_cellid(g.ex0 + rx, g.ey0 + ry);
+      if (i + 1 < sg.w) {
+        const int li = (rx >> 1) - tx0, lj = (ry >> 1) - ty0;
+        if (li < 0 || li >= TX || lj < 0 || lj >= TY) { st |= ST_INVARIANT; break; }  // a piece stays in its tile
+        const uint32_t d = sd[2 * (lj * TX + li) + (ry & 1)];
+        if (d >= SUCC_TWO) { st |= ST_INVARIANT; break; }
+        rx += (int)(d % 5) - 2;
+        ry += (int)(d / 5) - 2;
+      }
+    }
+  }
+  if (st) atomicOr(a.status, st);
 }
 
 // 5. runs of equal sorted keys: the last element of each run writes (or adds)
@@ -938,21 +968,30 @@ struct DiscKind {
         uint32_t *offs = kind ? io.ddoff : io.adoff;
         DevBuf<uint32_t> *ob = kind ? io.ddisc : io.adisc;
         L(ob->ensure((size_t)tot[0] + 1, st));
-        L(cudaMallocAsync((void **)&segs, sizeof(uint4) * ((size_t)tot[1] + 1), st));
+        // pieces in chain order, then grouped by tile | per tile: count, offset (ntiles + 1), cursor
+        const long long ntiles = (long long)a.g.ntx * a.g.nty;
+        L(cudaMallocAsync((void **)&segs, sizeof(uint4) * (2 * (size_t)tot[1] + 2) + sizeof(uint32_t) * (3 * ntiles + 8),
+                          st));
         if (e != cudaSuccess) return false;
+        uint4 *bucketed = segs + tot[1] + 1;
+        uint32_t *tcnt = (uint32_t *)(bucketed + tot[1] + 1), *toff = tcnt + ntiles + 2, *tcur = toff + ntiles + 2;
+        L(cudaMemsetAsync(tcnt, 0, sizeof(uint32_t) * (3 * ntiles + 6), st));
         c.segs = segs;
+        c.tile_cnt = tcnt;
         const SeedRuns sr{val, sstart, scount};
-        if (nch) {
-          k_chain_segs<<<nb(nch), 128, 0, st>>>(nch, c);
-          DMSC_LAUNCHED(1);
-        }
         k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c, offs);  // the records the pieces are placed by
         DMSC_LAUNCHED(1);
+        if (nch) {
+          k_chain_segs<<<nb(nch), 128, 0, st>>>(nch, a.g, c);
+          DMSC_LAUNCHED(1);
+        }
         if (S.io->ev_place[kind][0]) L(cudaEventRecord(S.io->ev_place[kind][0], st));
         if (tot[1]) {
-          k_seg_place<<<nb((tot[1] + 31) / 32 * 32), SEG_WARPS * 32, 0, st>>>(a, c, tot[1], ob->p,
-                                                                             (unsigned long long)tot[0]);
-          DMSC_LAUNCHED(1);
+          L(scan_exclusive_u32(tcnt, ntiles, toff, toff + ntiles, st));
+          k_seg_bucket<<<nb(tot[1]), 256, 0, st>>>(tot[1], a, segs, toff, tcur, bucketed);
+          k_tile_place<<<(unsigned)ntiles, PLACE_THREADS, 0, st>>>(a, c, bucketed, toff, ob->p,
+                                                                   (unsigned long long)tot[0]);
+          DMSC_LAUNCHED(2);
         }
         k_level0<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, offs, ob->p);
         k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);

@@ -100,10 +100,11 @@ struct dmsc_ctx {
   bool timing = false;
   long long merge_parallel_min = 2048;  // pipeline levels with merges this large take the parallel merges
   // merge_up's boundary cancellations in ordered-parallel rounds: each round
-  // looks at the first merge_round_window pending boundary cells (0: one
-  // thread per merge); after 8 rounds in a row that each commit fewer than
-  // merge_round_min_commits cells, one thread finishes the rest in order
-  long long merge_round_window = 2048, merge_round_min_commits = 4;
+  // looks at the first merge_round_window pending boundary cells (0, the
+  // default: one thread per merge, measured faster on noise); after 8 rounds
+  // in a row that each commit fewer than merge_round_min_commits cells, one
+  // thread finishes the rest in order
+  long long merge_round_window = 0, merge_round_min_commits = 4;
   bool use_ocl = false;  // pipeline pieces through work_ocl (GridDataManager's ocl flag)
   std::string ooc_dir;   // pipelines spill their pieces' complexes to files here (empty: in memory)
 };

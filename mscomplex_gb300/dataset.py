@@ -59,11 +59,12 @@ class Context:
         `directory` (None: in device memory)."""
         check(self.lib.dmsc_set_out_of_core(self.h, directory.encode() if directory else None))
 
-    def set_merge_rounds(self, window: int = 2048, min_commits: int = 4):
-        """merge_up's boundary cancellations on the parallel merges: rounds over
-        the first `window` pending boundary cells (0: one thread per merge);
-        after 8 rounds in a row below `min_commits` commits, one thread
-        finishes in order.  Every setting gives the same complexes."""
+    def set_merge_rounds(self, window: int = 0, min_commits: int = 4):
+        """merge_up's boundary cancellations on the parallel merges: 0 (the
+        default) runs them on one thread per merge; window > 0 in rounds over
+        the first `window` pending boundary cells, one thread finishing in
+        order after 8 rounds in a row below `min_commits` commits.  Every
+        setting gives the same complexes."""
         check(self.lib.dmsc_set_merge_rounds(self.h, int(window), int(min_commits)))
 
     def close(self):

@@ -123,3 +123,16 @@ def test_batch_budget_failure_is_per_grid(gpu_lib, oracle):
     assert ei.value.code == 5
     with pytest.raises(gpu_lib.DmscError):
         b.export_all()
+
+
+def test_batch_largest_mixed_grids_vs_oracle(gpu_lib, oracle):
+    """The mixed-size workload's largest grids (sides 2034-2046, and two near
+    1024), generated as the batch workload generates them, in one batch with
+    small grids, each against the oracle at 2% of its range."""
+    from mscomplex_gb300 import synth
+    sides = synth.mixed_batch_sides(1000, 3)
+    order = np.argsort(-sides)
+    near_1k = np.argsort(np.abs(sides - 1024))[:2]
+    pick = [int(i) for i in order[:4]] + [int(i) for i in near_1k] + [int(i) for i in order[-3:]]
+    fields = [synth.mixed_grid(int(sides[i]), 3 * 1000003 + i) for i in pick]
+    check_batch(gpu_lib, oracle, fields, 0.02, "largest mixed grids")
