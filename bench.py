@@ -52,15 +52,15 @@ KERNEL_BYTES = {
     "gradient": (8.0, 0, 0, 0, 0),        # k_gradient: 4 B height read + 4 B gradient codes (1 B per cell)
     "labels_arcs": (16.0, 12, 8, 0, 0),   # k_labels: 16 B owner labels (4 B per cell), cp records, arcs
     "disc_hops": (0.0, 0, 0, 0, 0),       # k_disc_hops: writes only the hop structure (intermediate)
-    # the saddle discs of one kind: pieces bucketed by tile, then k_tile_place (and the level-0 items and
-    # the discs of saddles with many chains); 4 B per saddle disc cell written
+    # the saddle discs of one kind: k_seg_place (and the level-0 items and the discs of saddles with many
+    # chains); 4 B per saddle disc cell written
     "seg_place_asc": (0.0, 0, 0, 4, 0),
     "seg_place_des": (0.0, 0, 0, 0, 4),
 }
 KERNEL_NAMES = {"gradient": "k_gradient", "labels_arcs": "k_labels", "disc_hops": "k_disc_hops",
-                "seg_place_asc": "k_tile_place", "seg_place_des": "k_tile_place"}
+                "seg_place_asc": "k_seg_place", "seg_place_des": "k_seg_place"}
 TRAFFIC_KEYS = {"gradient": "k_gradient", "labels_arcs": "k_labels", "disc_hops": "k_disc_hops",
-                "seg_place_asc": "k_tile_place:asc", "seg_place_des": "k_tile_place:des"}
+                "seg_place_asc": "k_seg_place:asc", "seg_place_des": "k_seg_place:des"}
 # The whole step: 24 B/vertex (height, gradient, owner labels) + 12 B/cp + 8 B/arc + 4 B per disc cell written.
 PIPE_BYTES = (24.0, 12, 8, 4)
 
@@ -203,6 +203,45 @@ def replicas_value(units_per_rank: float, world: int, seconds: float) -> float:
     return units_per_rank * world / seconds
 
 
+def gpu_local_cpus(device: int):
+    """The host CPUs next to the GPU (sysfs local_cpulist of its PCI device),
+    intersected with the CPUs this process may use; empty if unknown."""
+    try:
+        import torch
+        pr = torch.cuda.get_device_properties(device)
+        bus = "%04x:%02x:%02x.0" % (getattr(pr, "pci_domain_id", 0), pr.pci_bus_id, pr.pci_device_id)
+        with open(f"/sys/bus/pci/devices/{bus}/local_cpulist") as fh:
+            spec = fh.read().strip()
+        cpus = set()
+        for part in spec.split(","):
+            if "-" in part:
+                lo, hi = part.split("-")
+                cpus.update(range(int(lo), int(hi) + 1))
+            elif part:
+                cpus.add(int(part))
+        return sorted(cpus & os.sched_getaffinity(0))
+    except Exception:
+        return []
+
+
+def host_link(torch, nbytes=800 << 20, reps=3):
+    """Pinned host <-> device copy bandwidth (GB/s) of one large copy each way."""
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, dst, src in (("d2h_gbs", h, d), ("h2d_gbs", d, h)):
+        best = 0.0
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            dst.copy_(src, non_blocking=True)
+            torch.cuda.synchronize()
+            best = max(best, nbytes / (time.perf_counter() - t0) / 1e9)
+        out[name] = round(best, 1)
+    del h, d
+    return out
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -301,12 +340,36 @@ def bench_batched(M, torch, stream, sh, steps=2, warmup=1, count=1000):
         d2h = sum(v.nbytes for v in out.values())
     e2e_s = (time.perf_counter() - t0) / steps
     st = [b.simplify_stats(i) for i in range(count)]
+    tile_ms = b.tile_times()
+    # the launch autotuner on the workload's own grids, then the batched pass again
+    t0 = time.perf_counter()
+    table = M.GridBatch.autotune(fields, repeats=2)
+    tune_s = time.perf_counter() - t0
+    bt = M.GridBatch()
+    bt.run(packed=dev, sizes=sizes, tresh=tresh, stream=sh)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        bt.run(packed=dev, sizes=sizes, tresh=tresh, stream=sh)
+    e1.record(stream)
+    e1.synchronize()
+    tuned_s = e0.elapsed_time(e1) / 1e3 / steps
+    tuned_tile_ms = bt.tile_times()
+    exact = exact and all(all(np.array_equal(np.asarray(bt.export(i)[k]).view(np.uint8),
+                                             np.asarray(ref[i][k]).view(np.uint8)) for k in keys) for i in ref)
+    M.GridBatch.autotune_reset()
     return {"workload": BATCH_WORKLOAD, "grids": count, "vertices": nverts, "critical_points": ncp,
             "batched_grids_per_s": round(count / batch_s, 2), "batched_mvert_per_s": round(nverts / batch_s / 1e6, 2),
             "batched_ms": round(batch_s * 1e3, 3), "plain_grids_per_s": round(count / plain_s, 2),
             "plain_ms": round(plain_s * 1e3, 3), "speedup_vs_plain": round(plain_s / batch_s, 2),
             "e2e_grids_per_s": round(count / e2e_s, 2), "e2e_h2d_bytes": int(packed.nbytes), "e2e_d2h_bytes": int(d2h),
             "bit_exact_vs_plain": bool(exact), "checked_grids": len(ref),
+            "tile_kernels_ms": [round(v, 3) for v in tile_ms],
+            "autotune": {"seconds": round(tune_s, 2), "per_class": {k: {"threads": v[0], "blocks_per_sm": v[1],
+                                                                        "tile_us": v[2], "default_tile_us": v[3]}
+                                                                    for k, v in table.items()},
+                         "batched_grids_per_s": round(count / tuned_s, 2), "batched_ms": round(tuned_s * 1e3, 3),
+                         "tile_kernels_ms": [round(v, 3) for v in tuned_tile_ms]},
             "max_simplify_pops": max(x["pops"] for x in st), "total_simplify_pops": sum(x["pops"] for x in st)}
 
 
@@ -510,6 +573,11 @@ def main():
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
+    # host threads and pinned buffers on the CPUs next to the GPU (first touch
+    # places pinned pages on the calling thread's node)
+    local_cpus = gpu_local_cpus(local)
+    if local_cpus:
+        os.sched_setaffinity(0, local_cpus)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
@@ -600,6 +668,7 @@ def main():
     # complexes and two sets of host buffers alternate; a buffer or complex is
     # rewritten only after what read it last is done.  The K steps are timed
     # as one span, from the first input copy to the last result copy.
+    link = host_link(torch)
     host = torch.from_numpy(field).pin_memory()
     in_stream = torch.cuda.Stream()
     dbuf, used, ready = [torch.empty_like(dev), torch.empty_like(dev)], [None, None], [None, None]
@@ -674,6 +743,7 @@ def main():
             "simplify": simp,
             "e2e": {"value": round(e2e_value, 3), "unit": "Mvert/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
+            "host_link": dict(link, cpus=len(local_cpus) or None),
             "gpu_launches": int(launches),
             "clocks": clk,
         }

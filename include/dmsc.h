@@ -259,6 +259,32 @@ int dmsc_batch_totals(dmsc_batch *b, int64_t totals[3]);
 int dmsc_batch_export_all(dmsc_batch *b, uint32_t *cp_base, uint32_t *asc_base, uint32_t *des_base, uint32_t *cellid,
                           float *fn, uint32_t *pair_idx, uint8_t *flags, uint32_t *asc_off, uint32_t *asc,
                           uint32_t *des_off, uint32_t *des, void *stream);
+/* Device times (ms) of the batch's last run: [0] the gradient tile kernel's
+ * launches, [1] the owner-label tile kernel's launches. */
+int dmsc_batch_tile_times(dmsc_batch *b, float ms[2]);
+/* No counterpart in the reference: the launch autotuner of the batched path.
+ * Grids are grouped into size classes by their larger side: below 128, 256,
+ * 512, 1024, 2048 vertices, and from 2048 on.  For every class present in
+ * the sample (ngrids grids packed as for dmsc_batch_run), each launch
+ * configuration of the two persistent tile kernels -- 256 or 512 threads per
+ * block, 1, 2 or 3 resident blocks per SM -- is timed over `repeats` batch
+ * runs of the class's grids (after one untimed run), and the configuration
+ * with the smallest median becomes the class's in the context.  From then on
+ * dmsc_batch_run launches the tile kernels once per size class present, each
+ * with its class's configuration.  Results never depend on the
+ * configuration.  table (may be NULL) receives per class 4 int32: threads,
+ * blocks per SM, the chosen configuration's median time and the default
+ * configuration's (512 threads, 3 blocks per SM), in microseconds; zeros for
+ * classes absent from the sample.  The tile shape (64 x 64 vertices) is not a
+ * parameter: it fixes the border table's layout and the 12-bit in-tile cell
+ * indices of the pointer jumping. */
+int dmsc_batch_autotune(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float *heights, int on_device,
+                        int repeats, int32_t table[24]);
+/* Sets one size class's configuration by hand (as the autotuner would);
+ * later batches launch per size class. */
+int dmsc_batch_set_launch(dmsc_ctx *ctx, int size_class, int threads, int blocks_per_sm);
+/* Back to one launch over all grids with the default configuration. */
+int dmsc_batch_autotune_reset(dmsc_ctx *ctx);
 
 /* ---- request server (continuous batching) ----
  * No counterpart in the reference.  Requests (one whole grid each, heights

@@ -71,6 +71,10 @@ SIGNATURES = {
     "dmsc_pool_stats": ([_vp, _vp], _i32),
     "dmsc_batch_grid_status": ([_vp, _i64, _vp, C.c_char_p, _i32], _i32),
     "dmsc_batch_export_all": ([_vp] + [_vp] * 11 + [_vp], _i32),
+    "dmsc_batch_tile_times": ([_vp, _vp], _i32),
+    "dmsc_batch_autotune": ([_vp, _i32, _vp, _vp, _i32, _i32, _vp], _i32),
+    "dmsc_batch_autotune_reset": ([_vp], _i32),
+    "dmsc_batch_set_launch": ([_vp, _i32, _i32, _i32], _i32),
     "dmsc_server_create": ([_vp, _i64, _i32, _i32, _i64, _vp], _i32),
     "dmsc_server_submit": ([_vp, _vp, _i32, _i32, C.c_double, _vp], _i32),
     "dmsc_server_wait": ([_vp, _i64, _i32, _vp, _vp], _i32),

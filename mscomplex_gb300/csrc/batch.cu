@@ -45,6 +45,13 @@ struct dmsc_batch {
   std::vector<int> gstat;                             // per grid: DMSC_OK or the grid's own error
   std::vector<std::string> gerr;                      // its message
   int ndead = 0;
+  // the grids regrouped by size class (per-class launches of a tuned context)
+  DevBuf<BatchGrid> grids_cls;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // around the gradient and the labels launches
+  ~dmsc_batch() {
+    for (auto e : ev)
+      if (e) cudaEventDestroy(e);
+  }
 };
 
 namespace {
@@ -58,6 +65,16 @@ int berr(int code, const std::string &m) { return set_last_error(code, m.c_str()
       return berr(e_ == cudaErrorMemoryAllocation ? DMSC_ERR_OOM : DMSC_ERR_CUDA,                       \
                   std::string(#call) + ": " + cudaGetErrorString(e_));                                  \
   } while (0)
+
+// Size class of a grid for the launch configurations: its larger side below
+// 128, 256, 512, 1024, 2048 vertices, or above.
+constexpr int NCLASS = 6;
+int size_class(int nx, int ny) {
+  const int s = nx > ny ? nx : ny;
+  int c = 0;
+  for (int lim = 128; c < NCLASS - 1 && s >= lim; lim *= 2) ++c;
+  return c;
+}
 
 unsigned nblk(long long n) {
   long long b = (n + 255) / 256;
@@ -183,8 +200,41 @@ int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float 
       cudaMemsetAsync(B->scal.p, 0, sizeof(uint32_t) * 4, st))
     return fail(berr(DMSC_ERR_CUDA, "batch descriptors"));
 
+  // the tile kernels' launches: one over all grids, or with a tuned context
+  // one per size class present, each with its class's configuration
+  struct ClassLaunch { int off, n; long long ntiles; BatchLaunch cfg; };
+  std::vector<ClassLaunch> cl;
+  const BatchGrid *lgrids = B->grids.p;
+  if (ctx->batch_tuned) {
+    std::vector<BatchGrid> hc;
+    for (int c = 0; c < NCLASS; ++c) {
+      ClassLaunch L{(int)hc.size(), 0, 0, BatchLaunch{ctx->batch_cfg[c][0], ctx->batch_cfg[c][1]}};
+      for (int g = 0; g < ngrids; ++g) {
+        if (size_class(sizes[2 * g], sizes[2 * g + 1]) != c) continue;
+        BatchGrid q = hg[g];
+        q.tile0 = L.ntiles;  // class-local tile numbering
+        L.ntiles += B->tile0[g + 1] - B->tile0[g];
+        hc.push_back(q);
+        ++L.n;
+      }
+      if (L.n) cl.push_back(L);
+    }
+    if (B->grids_cls.ensure(hc.size(), st) ||
+        cudaMemcpyAsync(B->grids_cls.p, hc.data(), sizeof(BatchGrid) * hc.size(), cudaMemcpyHostToDevice, st) ||
+        cudaStreamSynchronize(st))  // hc is read before it goes out of scope
+      return fail(berr(DMSC_ERR_CUDA, "batch class descriptors"));
+    lgrids = B->grids_cls.p;
+  } else {
+    cl.push_back(ClassLaunch{0, ngrids, NT, BatchLaunch()});
+  }
+  for (auto &e : B->ev)
+    if (!e && cudaEventCreate(&e) != cudaSuccess) return fail(berr(DMSC_ERR_CUDA, "batch events"));
   // K1 -> scan -> K3 over all grids, then the cp bases
-  if (launch_gradient_batch(B->grids.p, ngrids, NT, B->scal.p, st) != cudaSuccess ||
+  bool ok = cudaEventRecord(B->ev[0], st) == cudaSuccess;
+  for (const auto &L : cl)
+    ok = ok && launch_gradient_batch(lgrids + L.off, L.n, L.ntiles, B->scal.p, st, L.cfg) == cudaSuccess;
+  ok = ok && cudaEventRecord(B->ev[1], st) == cudaSuccess;
+  if (!ok ||
       scan_exclusive_u8(B->rowcnt.p, NR, B->offsets.p, B->offsets.p + NR, st) != cudaSuccess ||
       launch_resolve(B->table.p, NS, B->offsets.p, NR, B->scal.p, st) != cudaSuccess)
     return fail(berr(DMSC_ERR_CUDA, std::string("batch gradient: ") + cudaGetErrorString(cudaGetLastError())));
@@ -208,8 +258,12 @@ int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float 
   CpOut cp{B->cp_cellid.p, B->cp_fn.p, B->cp_flags.p, B->cp_pair_cell.p, B->cp_des2.p, B->cp_asc2.p,
            B->cp_acnt.p, B->cp_dcnt.p, ncp};
   if (cudaMemsetAsync(B->cp_acnt.p, 0, 4 * (n + 1), st) || cudaMemsetAsync(B->cp_dcnt.p, 0, 4 * (n + 1), st) ||
-      launch_labels_batch(B->grids.p, ngrids, NT, cp, B->scal.p, st) != cudaSuccess)
+      cudaEventRecord(B->ev[2], st))
     return fail(berr(DMSC_ERR_CUDA, "batch labels"));
+  for (const auto &L : cl)
+    if (launch_labels_batch(lgrids + L.off, L.n, L.ntiles, cp, B->scal.p, st, L.cfg) != cudaSuccess)
+      return fail(berr(DMSC_ERR_CUDA, "batch labels"));
+  if (cudaEventRecord(B->ev[3], st)) return fail(berr(DMSC_ERR_CUDA, "batch labels"));
 
   // writeout_connectivity of every grid: shared CSR, then local list values
   if (launch_msc_flags(ncp, B->cp_flags.p, B->flags.p, st) || cudaMemsetAsync(B->pair_idx.p, 0xFF, 4 * (n + 1), st) ||
@@ -332,6 +386,125 @@ int dmsc_batch_destroy(dmsc_batch *b) {
   cudaSetDevice(b->ctx->device);
   cudaStreamSynchronize(b->ctx->stream);
   delete b;
+  return DMSC_OK;
+}
+
+int dmsc_batch_tile_times(dmsc_batch *b, float ms[2]) {
+  if (!b || !ms) return berr(DMSC_ERR_BAD_ARG, "null argument");
+  if (!b->ev[3]) return berr(DMSC_ERR_STATE, "the batch has not run");
+  BCK(cudaSetDevice(b->ctx->device));
+  BCK(cudaEventSynchronize(b->ev[3]));
+  BCK(cudaEventElapsedTime(&ms[0], b->ev[0], b->ev[1]));
+  BCK(cudaEventElapsedTime(&ms[1], b->ev[2], b->ev[3]));
+  return DMSC_OK;
+}
+
+// Per size class present in the sample: every launch configuration of the
+// two tile kernels, `repeats` timed batch runs of the class's grids each
+// (after one untimed), the median of the tile kernels' time; the fastest
+// configuration becomes the class's.
+int dmsc_batch_autotune(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float *heights, int on_device,
+                        int repeats, int32_t *table) {
+  if (!ctx || !sizes || !heights || ngrids <= 0) return berr(DMSC_ERR_BAD_ARG, "null argument or empty sample");
+  if (repeats < 1 || repeats > 50) return berr(DMSC_ERR_BAD_ARG, "repeats must be 1..50");
+  for (int g = 0; g < ngrids; ++g)
+    if (sizes[2 * g] < 2 || sizes[2 * g + 1] < 2 || sizes[2 * g] > 16384 || sizes[2 * g + 1] > 16384)
+      return berr(DMSC_ERR_BAD_ARG, "sample grid " + std::to_string(g) + " has a bad size");
+  BCK(cudaSetDevice(ctx->device));
+  std::vector<long long> voff(ngrids + 1, 0);
+  for (int g = 0; g < ngrids; ++g) voff[g + 1] = voff[g] + (long long)sizes[2 * g] * sizes[2 * g + 1];
+  const BatchLaunch cand[] = {{512, 3}, {512, 2}, {512, 1}, {256, 3}, {256, 2}, {256, 1}};
+  const bool was_tuned = ctx->batch_tuned;
+  int saved[NCLASS][2], chosen[NCLASS][2];
+  std::memcpy(saved, ctx->batch_cfg, sizeof saved);
+  std::memcpy(chosen, ctx->batch_cfg, sizeof chosen);
+  std::vector<int32_t> out(4 * NCLASS, 0);
+  auto restore = [&](int rc) {
+    std::memcpy(ctx->batch_cfg, saved, sizeof saved);
+    ctx->batch_tuned = was_tuned;
+    return rc;
+  };
+  for (int c = 0; c < NCLASS; ++c) {
+    std::vector<int32_t> sz;
+    std::vector<float> hh;
+    float *dh = nullptr;
+    long long nv = 0;
+    std::vector<int> members;
+    for (int g = 0; g < ngrids; ++g)
+      if (size_class(sizes[2 * g], sizes[2 * g + 1]) == c) {
+        members.push_back(g);
+        sz.push_back(sizes[2 * g]);
+        sz.push_back(sizes[2 * g + 1]);
+        nv += voff[g + 1] - voff[g];
+      }
+    if (members.empty()) continue;
+    const int nc = (int)members.size();
+    if (on_device) {  // the class's grids packed into one device buffer
+      if (cudaMalloc((void **)&dh, sizeof(float) * nv) != cudaSuccess) return restore(berr(DMSC_ERR_OOM, "autotune sample"));
+      long long o = 0;
+      for (int g : members) {
+        const long long k = voff[g + 1] - voff[g];
+        if (cudaMemcpy(dh + o, heights + voff[g], sizeof(float) * k, cudaMemcpyDeviceToDevice) != cudaSuccess) {
+          cudaFree(dh);
+          return restore(berr(DMSC_ERR_CUDA, "autotune sample copy"));
+        }
+        o += k;
+      }
+    } else {
+      hh.reserve(nv);
+      for (int g : members) hh.insert(hh.end(), heights + voff[g], heights + voff[g + 1]);
+    }
+    const std::vector<double> zero(nc, 0.0);
+    dmsc_batch *b = nullptr;
+    float best = 3.4e38f, def = 0;
+    BatchLaunch pick;
+    int rc = DMSC_OK;
+    for (const BatchLaunch &cfg : cand) {
+      ctx->batch_tuned = true;
+      for (int k = 0; k < NCLASS; ++k) { ctx->batch_cfg[k][0] = cfg.threads; ctx->batch_cfg[k][1] = cfg.blocks_per_sm; }
+      std::vector<float> t;
+      for (int r = 0; r <= repeats && rc == DMSC_OK; ++r) {
+        rc = dmsc_batch_run(ctx, nc, sz.data(), on_device ? dh : hh.data(), on_device, zero.data(), 0, &b, nullptr);
+        float ms[2] = {0, 0};
+        if (rc == DMSC_OK) rc = dmsc_batch_tile_times(b, ms);
+        if (r) t.push_back(ms[0] + ms[1]);
+      }
+      if (rc != DMSC_OK) break;
+      std::sort(t.begin(), t.end());
+      const float med = t[t.size() / 2];
+      if (cfg.threads == 512 && cfg.blocks_per_sm == 3) def = med;
+      if (med < best) { best = med; pick = cfg; }
+    }
+    if (b) dmsc_batch_destroy(b);
+    if (dh) cudaFree(dh);
+    if (rc != DMSC_OK) return restore(rc);
+    chosen[c][0] = pick.threads;
+    chosen[c][1] = pick.blocks_per_sm;
+    out[4 * c] = pick.threads;
+    out[4 * c + 1] = pick.blocks_per_sm;
+    out[4 * c + 2] = (int32_t)(best * 1000.0f + 0.5f);
+    out[4 * c + 3] = (int32_t)(def * 1000.0f + 0.5f);
+  }
+  std::memcpy(ctx->batch_cfg, chosen, sizeof chosen);
+  ctx->batch_tuned = true;
+  if (table) std::memcpy(table, out.data(), sizeof(int32_t) * out.size());
+  return DMSC_OK;
+}
+
+int dmsc_batch_set_launch(dmsc_ctx *ctx, int size_class, int threads, int blocks_per_sm) {
+  if (!ctx || size_class < 0 || size_class >= NCLASS || (threads != 256 && threads != 512) || blocks_per_sm < 1 ||
+      blocks_per_sm > 3)
+    return berr(DMSC_ERR_BAD_ARG, "size class 0..5, threads 256 or 512, blocks per SM 1..3");
+  ctx->batch_cfg[size_class][0] = threads;
+  ctx->batch_cfg[size_class][1] = blocks_per_sm;
+  ctx->batch_tuned = true;
+  return DMSC_OK;
+}
+
+int dmsc_batch_autotune_reset(dmsc_ctx *ctx) {
+  if (!ctx) return berr(DMSC_ERR_BAD_ARG, "ctx is null");
+  ctx->batch_tuned = false;
+  for (int c = 0; c < NCLASS; ++c) { ctx->batch_cfg[c][0] = 512; ctx->batch_cfg[c][1] = 3; }
   return DMSC_OK;
 }
 

@@ -280,7 +280,9 @@ __global__ void k_saddle_disc_write(DiscArgs a, int kind, SeedRuns sr, const uin
 // lengths fix every cell's place before any cell is known: per saddle, the
 // level ranges over which its set of alive chains is constant are regular
 // interleaves (k_zip_blocks), and the cells, walked by one lane per piece of
-// at most SEG_MAX cells, are stored straight there (k_tile_place).
+// at most SEG_MAX cells (cut where the set of alive chains changes, with the
+// disc position of their first cell and their stride), are stored straight
+// there (k_seg_place).
 // ---------------------------------------------------------------------------
 constexpr int KMAX = 32;                 // saddles with more chains take the serial pass
 constexpr uint32_t HOP_END = 0xFFFFFFFFu;
@@ -475,7 +477,6 @@ struct ChainArgs {
   uint32_t *cbase;      // exclusive scan of kc
   uint32_t *cstart, *csaddle, *clen, *cnseg, *csegoff;  // per chain
   uint4 *segs;          // (chain, first edge, first level, cells)
-  uint32_t *tile_cnt;   // pieces per 64x64 tile (the tile of their first edge)
   uint4 *blocks;        // per chain slot of a saddle, 2 uint4: an interleave record (k_zip_blocks)
   uint32_t cap;         // chain slots allocated
   unsigned long long limit;
@@ -531,7 +532,9 @@ __global__ void k_chain_len(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, uint
           nseg += (l + SEG_MAX - 1) / SEG_MAX;
           if (L > c.limit) { bad = true; break; }
         }
-        if (j < c.cap) { c.cstart[j] = ch[b]; c.csaddle[j] = s; c.clen[j] = (uint32_t)L; c.cnseg[j] = nseg; }
+        // piece slots: one per SEG_MAX cells of each hop, and one more for each level
+        // where another of the saddle's chains ends inside this one (at most K - 1)
+        if (j < c.cap) { c.cstart[j] = ch[b]; c.csaddle[j] = s; c.clen[j] = (uint32_t)L; c.cnseg[j] = nseg + c.kc[s] - 1; }
         else atomicOr(a.status, ST_CAPACITY);
         ++j;
         total += L;
@@ -543,48 +546,70 @@ __global__ void k_chain_len(DiscArgs a, int kind, SeedRuns sr, ChainArgs c, uint
   }
 }
 
-// the 64x64 vertex tile of an edge
-__device__ __forceinline__ uint32_t edge_tile(const GridGeom &g, uint32_t e) {
-  const uint32_t v = e >> 1;
-  const uint32_t vx = v % (uint32_t)g.vnx, vy = v / (uint32_t)g.vnx;
-  return (vy / TY) * (uint32_t)g.ntx + vx / TX;
-}
-
-// write pieces of every chain: its hops (in-tile runs) cut at every SEG_MAX
-// cells; counts the pieces of each tile
-__global__ void k_chain_segs(long long nchains, GridGeom g, ChainArgs c) {
+// Pieces of every chain, each with the disc position of its first cell and
+// the step between its cells: the chain's hops cut at every SEG_MAX cells
+// and at the levels where the saddle's set of alive chains changes (the
+// interleave records of k_zip_blocks), so that a piece's cells are
+// `alive` apart in the disc.  A piece is (first edge, first position,
+// cells | alive << 8, chain); the chain's unused slots get 0 cells.
+__global__ void k_chain_segs(long long nchains, DiscArgs a, ChainArgs c) {
+  const GridGeom &g = a.g;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nchains; k += (long long)gridDim.x * blockDim.x) {
-    uint32_t o = c.csegoff[k], end = c.csegoff[k + 1], T = 1;
-    for (uint32_t e = c.cstart[k]; e != HOP_END && o < end; e = c.hop_to[e]) {
+    uint32_t o = c.csegoff[k], end = c.csegoff[k + 1];
+    if (o == end) continue;  // an unused chain slot (slots counted by the two-per-saddle bound)
+    const uint32_t s = c.csaddle[k];
+    bool ok = s < a.ncp;
+    const uint32_t cb = ok ? c.cbase[s] : 0, K = ok ? c.kc[s] : 0, j = (uint32_t)k - cb;
+    ok = ok && j < K && K <= (uint32_t)KMAX && cb + K <= c.cap;
+    uint32_t b = 0, first = 1, nlev = 0;
+    uint4 r0 = make_uint4(0, 0, 0, 0);
+    if (ok) {
+      r0 = c.blocks[2 * cb];
+      first = c.blocks[2 * cb + 1].x;
+      ok = r0.z != 0 && r0.y != 0;
+      nlev = ok ? r0.y / r0.z : 0;
+    }
+    uint32_t T = 1;
+    for (uint32_t e = c.cstart[k]; ok && e != HOP_END && o < end; e = c.hop_to[e]) {
       const uint32_t l = c.hop_len[e];
       if (l == 0) break;
-      uint32_t x = e;
-      const uint32_t tile = edge_tile(g, e);
-      for (uint32_t done = 0; done < l && o < end && x != HOP_END; done += SEG_MAX) {
-        const uint32_t w = l - done < (uint32_t)SEG_MAX ? l - done : (uint32_t)SEG_MAX;
-        c.segs[o++] = make_uint4((uint32_t)k, x, T + done, w);
-        atomicAdd(&c.tile_cnt[tile], 1u);
-        if (done + SEG_MAX < l) x = c.jseg[x];
+      uint32_t x = e, done = 0;
+      while (ok && done < l && o < end) {
+        const uint32_t t0 = T + done;
+        while (t0 - first >= nlev) {  // the record holding level t0 (records ascend in level)
+          if (++b >= K) { ok = false; break; }
+          r0 = c.blocks[2 * (cb + b)];
+          first = c.blocks[2 * (cb + b) + 1].x;
+          if (!r0.z || !r0.y || t0 < first) { ok = false; break; }
+          nlev = r0.y / r0.z;
+        }
+        if (!ok || !(r0.w & (1u << j))) { ok = false; break; }
+        uint32_t w = l - done < (uint32_t)SEG_MAX ? l - done : (uint32_t)SEG_MAX;
+        if (first + nlev - t0 < w) w = first + nlev - t0;
+        const uint32_t pos = r0.x + (t0 - first) * r0.z + __popc(r0.w & ((1u << j) - 1u));
+        c.segs[o++] = make_uint4(x, pos, w | (r0.z << 8), (uint32_t)k);
+        done += w;
+        if (done < l) {  // the next piece's first edge, w cells ahead in the run
+          if (w == (uint32_t)SEG_MAX) {
+            x = c.jseg[x];
+          } else {
+            int rx, ry;
+            edge_cell(g, x, rx, ry);
+            for (uint32_t i = 0; i < w && ok; ++i) {
+              const uint32_t d = c.nextd[edge_id(g, rx, ry)];
+              if (d >= SUCC_TWO) { ok = false; break; }
+              rx += (int)(d % 5) - 2;
+              ry += (int)(d / 5) - 2;
+            }
+            x = edge_id(g, rx, ry);
+          }
+          if (x == HOP_END) ok = false;
+        }
       }
       T += l;
     }
-    for (; o < end; ++o) c.segs[o] = make_uint4(0xFFFFFFFFu, 0, 0, 0);  // a chain cut short (status already set)
-  }
-}
-
-// the pieces grouped by tile (any order inside a tile: every cell's place in
-// its disc is fixed by its chain and level)
-__global__ void k_seg_bucket(long long nsegs, DiscArgs a, const uint4 *__restrict__ segs, const uint32_t *__restrict__ toff,
-                             uint32_t *__restrict__ cursor, uint4 *__restrict__ out) {
-  const GridGeom &g = a.g;
-  const uint32_t ntiles = (uint32_t)g.ntx * (uint32_t)g.nty;
-  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nsegs; k += (long long)gridDim.x * blockDim.x) {
-    const uint4 sg = segs[k];
-    const uint32_t tile = sg.x == 0xFFFFFFFFu ? ntiles : edge_tile(g, sg.y);
-    if (tile >= ntiles) { atomicOr(a.status, ST_INVARIANT); continue; }
-    const uint32_t p = toff[tile] + atomicAdd(&cursor[tile], 1u);
-    if (p >= toff[tile + 1]) { atomicOr(a.status, ST_INVARIANT); continue; }
-    out[p] = sg;
+    if (!ok) atomicOr(a.status, ST_INVARIANT);
+    for (; o < end; ++o) c.segs[o] = make_uint4(0, 0, 0, (uint32_t)k);
   }
 }
 
@@ -631,75 +656,55 @@ __global__ void k_zip_blocks(DiscArgs a, ChainArgs c, const uint32_t *off) {
 }
 
 // Pieces of at most SEG_MAX cells of one chain, stored straight at their
-// places in the disc.  One block per 64x64 tile takes the pieces that lie in
-// it (a piece is part of an in-tile run): the tile's successor offsets (1 byte
-// per edge) are loaded into shared memory once, and each thread follows its
-// pieces there, one cell per step.  The cell at level t of the saddle's j-th
-// chain goes to the interleave record (k_zip_blocks) whose level range holds
-// t: start + (t - first level) * alive + (alive chains before j), the order of
-// the reference's breadth-first disc.
-constexpr int PLACE_THREADS = 256;
-__global__ void __launch_bounds__(PLACE_THREADS) k_tile_place(DiscArgs a, ChainArgs c, const uint4 *__restrict__ segs,
-                                                              const uint32_t *__restrict__ toff, uint32_t *out,
-                                                              unsigned long long out_len) {
-  __shared__ uint8_t sd[HOP_SLOTS];
+// places in the disc.  A piece's cells are `alive` positions apart from its
+// first position (k_chain_segs), so a thread follows the 1-byte successor
+// offsets of the piece and stores each cell as it reaches it.  Each thread
+// walks PLACE_PIECES pieces side by side, so that their dependent successor
+// loads are in flight together.
+constexpr int PLACE_PIECES = 2;
+__global__ void __launch_bounds__(256) k_seg_place(DiscArgs a, ChainArgs c, long long nsegs, uint32_t *out,
+                                                   unsigned long long out_len) {
   const GridGeom &g = a.g;
-  const uint32_t tile = blockIdx.x;
-  const uint32_t p0 = toff[tile], p1 = toff[tile + 1];
-  if (p0 >= p1) return;
-  const int tx0 = (int)(tile % (uint32_t)g.ntx) * TX, ty0 = (int)(tile / (uint32_t)g.ntx) * TY;
-  for (int i = threadIdx.x; i < HOP_SLOTS; i += blockDim.x) {  // slot 2 (lj TX + li) + t, rows of 2 TX bytes
-    const int lj = i / (2 * TX), r = i - lj * (2 * TX), vx = tx0 + (r >> 1), vy = ty0 + lj;
-    sd[i] = (vx < g.vnx && vy < g.vny) ? c.nextd[2 * ((long long)vy * g.vnx + vx) + (r & 1)] : SUCC_NONE;
-  }
-  __syncthreads();
   uint32_t st = 0;
-  for (uint32_t k = p0 + threadIdx.x; k < p1; k += blockDim.x) {
-    const uint4 sg = segs[k];
-    const uint32_t ch = sg.x;
-    if (ch >= c.cap) { st |= ST_INVARIANT; continue; }
-    const uint32_t s = c.csaddle[ch];
-    if (s >= a.ncp) { st |= ST_INVARIANT; continue; }
-    const uint32_t cb = c.cbase[s], K = c.kc[s], j = ch - cb;  // j wraps for a chain below the saddle's slots
-    if (!(sg.z >= 1 && sg.w >= 1 && sg.w <= (uint32_t)SEG_MAX && sg.z - 1 + sg.w <= c.clen[ch] && j < K &&
-          K <= (uint32_t)KMAX && cb + K <= c.cap)) {
-      st |= ST_INVARIANT;
-      continue;
-    }
-    // the record whose level range holds the piece's first level (records ascend in level)
-    uint32_t b = 0, first = 0, nlev = 0;
-    uint4 r0 = make_uint4(0, 0, 0, 0);
-    for (; b < K; ++b) {
-      r0 = c.blocks[2 * (cb + b)];
-      if (!r0.y || !r0.z) { b = K; break; }
-      first = c.blocks[2 * (cb + b) + 1].x;
-      nlev = r0.y / r0.z;
-      if (sg.z - first < nlev) break;
-    }
-    if (b >= K || sg.z < first) { st |= ST_INVARIANT; continue; }
-    int rx, ry;
-    edge_cell(g, sg.y, rx, ry);
-    for (uint32_t i = 0; i < sg.w; ++i) {
-      const uint32_t t = sg.z + i;
-      while (t - first >= nlev) {  // the next level range
-        if (++b >= K) break;
-        r0 = c.blocks[2 * (cb + b)];
-        first = c.blocks[2 * (cb + b) + 1].x;
-        nlev = r0.z ? r0.y / r0.z : 0;
-        if (!r0.y || !r0.z) { b = K; break; }
+  const long long npairs = (nsegs + PLACE_PIECES - 1) / PLACE_PIECES;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npairs; p += (long long)gridDim.x * blockDim.x) {
+    int rx[PLACE_PIECES], ry[PLACE_PIECES];
+    uint32_t w[PLACE_PIECES], pos[PLACE_PIECES], na[PLACE_PIECES], W = 0;
+#pragma unroll
+    for (int q = 0; q < PLACE_PIECES; ++q) {
+      const long long k = p * PLACE_PIECES + q;
+      w[q] = 0; pos[q] = 0; na[q] = 0; rx[q] = 0; ry[q] = 0;
+      if (k >= nsegs) continue;
+      const uint4 sg = c.segs[k];
+      w[q] = sg.z & 0xffu;
+      na[q] = sg.z >> 8;
+      pos[q] = sg.y;
+      if (!w[q]) continue;
+      if (w[q] > (uint32_t)SEG_MAX || na[q] == 0 || na[q] > (uint32_t)KMAX ||
+          (unsigned long long)pos[q] + (unsigned long long)(w[q] - 1) * na[q] >= out_len) {
+        st |= ST_INVARIANT;
+        w[q] = 0;
+        continue;
       }
-      if (b >= K || !(r0.w & (1u << j))) { st |= ST_INVARIANT; break; }
-      const unsigned long long pos =
-          (unsigned long long)r0.x + (unsigned long long)(t - first) * r0.z + __popc(r0.w & ((1u << j) - 1u));
-      if (pos >= out_len) { st |= ST_INVARIANT; break; }
-      out[pos] = pack_cellid(g.ex0 + rx, g.ey0 + ry);
-      if (i + 1 < sg.w) {
-        const int li = (rx >> 1) - tx0, lj = (ry >> 1) - ty0;
-        if (li < 0 || li >= TX || lj < 0 || lj >= TY) { st |= ST_INVARIANT; break; }  // a piece stays in its tile
-        const uint32_t d = sd[2 * (lj * TX + li) + (ry & 1)];
-        if (d >= SUCC_TWO) { st |= ST_INVARIANT; break; }
-        rx += (int)(d % 5) - 2;
-        ry += (int)(d / 5) - 2;
+      edge_cell(g, sg.x, rx[q], ry[q]);
+      W = w[q] > W ? w[q] : W;
+    }
+    for (uint32_t i = 0; i < W; ++i) {
+      uint32_t d[PLACE_PIECES];
+#pragma unroll
+      for (int q = 0; q < PLACE_PIECES; ++q) {  // the loads first, then the stores
+        d[q] = SUCC_NONE;
+        if (i + 1 < w[q]) d[q] = c.nextd[edge_id(g, rx[q], ry[q])];
+      }
+#pragma unroll
+      for (int q = 0; q < PLACE_PIECES; ++q) {
+        if (i >= w[q]) continue;
+        out[pos[q] + i * na[q]] = pack_cellid(g.ex0 + rx[q], g.ey0 + ry[q]);
+        if (i + 1 < w[q]) {
+          if (d[q] >= SUCC_TWO) { st |= ST_INVARIANT; w[q] = i + 1; continue; }
+          rx[q] += (int)(d[q] % 5) - 2;
+          ry[q] += (int)(d[q] / 5) - 2;
+        }
       }
     }
   }
@@ -968,30 +973,21 @@ struct DiscKind {
         uint32_t *offs = kind ? io.ddoff : io.adoff;
         DevBuf<uint32_t> *ob = kind ? io.ddisc : io.adisc;
         L(ob->ensure((size_t)tot[0] + 1, st));
-        // pieces in chain order, then grouped by tile | per tile: count, offset (ntiles + 1), cursor
-        const long long ntiles = (long long)a.g.ntx * a.g.nty;
-        L(cudaMallocAsync((void **)&segs, sizeof(uint4) * (2 * (size_t)tot[1] + 2) + sizeof(uint32_t) * (3 * ntiles + 8),
-                          st));
+        L(cudaMallocAsync((void **)&segs, sizeof(uint4) * ((size_t)tot[1] + 1), st));
         if (e != cudaSuccess) return false;
-        uint4 *bucketed = segs + tot[1] + 1;
-        uint32_t *tcnt = (uint32_t *)(bucketed + tot[1] + 1), *toff = tcnt + ntiles + 2, *tcur = toff + ntiles + 2;
-        L(cudaMemsetAsync(tcnt, 0, sizeof(uint32_t) * (3 * ntiles + 6), st));
         c.segs = segs;
-        c.tile_cnt = tcnt;
         const SeedRuns sr{val, sstart, scount};
         k_zip_blocks<<<nb(ncp), 128, 0, st>>>(a, c, offs);  // the records the pieces are placed by
         DMSC_LAUNCHED(1);
         if (nch) {
-          k_chain_segs<<<nb(nch), 128, 0, st>>>(nch, a.g, c);
+          k_chain_segs<<<nb(nch), 128, 0, st>>>(nch, a, c);
           DMSC_LAUNCHED(1);
         }
         if (S.io->ev_place[kind][0]) L(cudaEventRecord(S.io->ev_place[kind][0], st));
         if (tot[1]) {
-          L(scan_exclusive_u32(tcnt, ntiles, toff, toff + ntiles, st));
-          k_seg_bucket<<<nb(tot[1]), 256, 0, st>>>(tot[1], a, segs, toff, tcur, bucketed);
-          k_tile_place<<<(unsigned)ntiles, PLACE_THREADS, 0, st>>>(a, c, bucketed, toff, ob->p,
-                                                                   (unsigned long long)tot[0]);
-          DMSC_LAUNCHED(2);
+          k_seg_place<<<nb((tot[1] + PLACE_PIECES - 1) / PLACE_PIECES), 256, 0, st>>>(a, c, tot[1], ob->p,
+                                                                                      (unsigned long long)tot[0]);
+          DMSC_LAUNCHED(1);
         }
         k_level0<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, offs, ob->p);
         k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);

@@ -36,9 +36,16 @@ struct BatchGrid {
   const uint32_t *offsets;  // the batch's cp offsets from this grid's first row segment on
   long long tile0;          // first tile of this grid in the batch's tile numbering
 };
-cudaError_t launch_gradient_batch(const BatchGrid *grids, int ngrids, long long ntiles, uint32_t *status, cudaStream_t st);
+// Launch configuration of the batch's persistent tile kernels (chosen per
+// size class by dmsc_batch_autotune): threads per block (256 or 512) and
+// resident blocks per SM (1..3).
+struct BatchLaunch {
+  int threads = 512, blocks_per_sm = 3;
+};
+cudaError_t launch_gradient_batch(const BatchGrid *grids, int ngrids, long long ntiles, uint32_t *status, cudaStream_t st,
+                                  BatchLaunch cfg = BatchLaunch());
 cudaError_t launch_labels_batch(const BatchGrid *grids, int ngrids, long long ntiles, const CpOut &cp, uint32_t *status,
-                                cudaStream_t st);
+                                cudaStream_t st, BatchLaunch cfg = BatchLaunch());
 
 size_t grad_smem_bytes();
 size_t label_smem_bytes();

@@ -108,15 +108,17 @@ constexpr uint16_t PJ_PTR = 0x0000, PJ_ROOT = 0x4000, PJ_EXIT = 0x8000, PJ_INVAL
 constexpr uint16_t PJ_TAG = 0xC000, PJ_IDX = 0x0FFF;
 
 // Jumps every pointer of pv[0..TX*TY) and pf[...] to its terminal.  Each
-// thread keeps a bit mask of its still-active entries.  Returns true if a
-// path failed to terminate (a cycle).
+// thread (THREADS per block) keeps a bit mask of its still-active entries.
+// Returns true if a path failed to terminate (a cycle).
+template <int THREADS>
 __device__ __forceinline__ bool pointer_jump(uint16_t *pv, uint16_t *pf) {
   constexpr int n = TX * TY;
-  constexpr int PER = 2 * n / GRAD_THREADS;  // 16 entries per thread
+  constexpr int PER = 2 * n / THREADS;  // 16 entries per thread with 512 threads, 32 with 256
+  static_assert(PER <= 32 && PER * THREADS == 2 * n, "one bit of the mask per entry");
   uint32_t active = 0;
 #pragma unroll
   for (int k = 0; k < PER; ++k) {
-    int e = threadIdx.x + k * GRAD_THREADS;
+    int e = threadIdx.x + k * THREADS;
     uint16_t v = e < n ? pv[e] : pf[e - n];
     if ((v & PJ_TAG) == PJ_PTR) active |= 1u << k;
   }
@@ -126,7 +128,7 @@ __device__ __forceinline__ bool pointer_jump(uint16_t *pv, uint16_t *pf) {
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
       if (!(active & (1u << k))) continue;
-      int e = threadIdx.x + k * GRAD_THREADS;
+      int e = threadIdx.x + k * THREADS;
       uint16_t *p = e < n ? pv : pf;
       int c = e < n ? e : e - n;
       uint16_t w = p[p[c] & PJ_IDX];
@@ -140,7 +142,7 @@ __device__ __forceinline__ bool pointer_jump(uint16_t *pv, uint16_t *pf) {
 #pragma unroll
     for (int k = 0; k < PER; ++k)
       if (active & (1u << k)) {
-        int e = threadIdx.x + k * GRAD_THREADS;
+        int e = threadIdx.x + k * THREADS;
         if (e < n) pv[e] = PJ_INVALID; else pf[e - n] = PJ_INVALID;
       }
     __syncthreads();
@@ -204,7 +206,8 @@ struct GradSmem {
   uint32_t code[TY][TX];
 };
 
-// K1 on tile (bx, by) of one grid.
+// K1 on tile (bx, by) of one grid, THREADS threads per block.
+template <int THREADS>
 __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, const GridGeom &g, uint32_t *__restrict__ codes,
                                               uint32_t *__restrict__ terms, uint8_t *__restrict__ rowcnt,
                                               uint64_t *__restrict__ table, uint32_t *__restrict__ status, int bx, int by) {
@@ -352,7 +355,7 @@ __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, con
     B.pf[e] = pff;
   }
   row_ranks(s.code, B.rankA, B.rankB, B.cntA, B.cntB, w, h);
-  if (pointer_jump(B.pv, B.pf)) st |= ST_CYCLE;  // (begins with a barrier)
+  if (pointer_jump<THREADS>(B.pv, B.pf)) st |= ST_CYCLE;  // (begins with a barrier)
 
   // 5. in-tile terminals of every vertex and face, per (cell row, tile) counts
   for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
@@ -398,7 +401,7 @@ __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, con
 __global__ void __launch_bounds__(GRAD_THREADS, 3)
 k_gradient(const float *__restrict__ hgt, GridGeom g, uint32_t *__restrict__ codes, uint32_t *__restrict__ terms,
            uint8_t *__restrict__ rowcnt, uint64_t *__restrict__ table, uint32_t *__restrict__ status) {
-  gradient_tile(hgt, g, codes, terms, rowcnt, table, status, blockIdx.x, blockIdx.y);
+  gradient_tile<GRAD_THREADS>(hgt, g, codes, terms, rowcnt, table, status, blockIdx.x, blockIdx.y);
 }
 
 // The grid of batch tile t (tiles numbered grid after grid).
@@ -411,13 +414,17 @@ __device__ __forceinline__ int batch_grid_of(const BatchGrid *G, int ngrids, lon
   return lo;
 }
 
-// K1 over a batch: a persistent grid of blocks takes (grid, tile) items in order.
-__global__ void __launch_bounds__(GRAD_THREADS, 3)
+// K1 over a batch: a persistent grid of blocks takes (grid, tile) items in
+// order; THREADS threads per block (the launch configurations of the batch's
+// autotuner).
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS, 3)
 k_gradient_batch(const BatchGrid *__restrict__ G, int ngrids, long long ntiles, uint32_t *__restrict__ status) {
   for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const BatchGrid &B = G[batch_grid_of(G, ngrids, t)];
     const long long lt = t - B.tile0;
-    gradient_tile(B.hgt, B.g, B.codes, B.terms, B.rowcnt, B.table, status, (int)(lt % B.g.ntx), (int)(lt / B.g.ntx));
+    gradient_tile<THREADS>(B.hgt, B.g, B.codes, B.terms, B.rowcnt, B.table, status, (int)(lt % B.g.ntx),
+                           (int)(lt / B.g.ntx));
     __syncthreads();  // shared memory is reused by the next item
   }
 }
@@ -638,7 +645,8 @@ k_labels(const uint32_t *__restrict__ codes, const uint32_t *__restrict__ terms,
 }
 
 // K4 over a batch; cp indices (and so labels) are batch-wide.
-__global__ void __launch_bounds__(GRAD_THREADS, 3)
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS, 3)
 k_labels_batch(const BatchGrid *__restrict__ G, int ngrids, long long ntiles, CpOut cp, uint32_t *__restrict__ status) {
   for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const BatchGrid &B = G[batch_grid_of(G, ngrids, t)];
@@ -689,27 +697,56 @@ cudaError_t launch_labels(const uint32_t *codes, const uint32_t *terms, const fl
   return cudaGetLastError();
 }
 
-cudaError_t launch_gradient_batch(const BatchGrid *grids, int ngrids, long long ntiles, uint32_t *status, cudaStream_t st) {
-  // once per process (thread-safe static initialisation)
-  static const cudaError_t attr = cudaFuncSetAttribute(k_gradient_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradSmem));
+// The persistent batch kernels' launch: `threads` per block (256 or 512) and
+// blocks_per_sm resident blocks per SM (1 to 3; the shared memory of a 64x64
+// tile allows 3) over the device's SMs.
+static long long persistent_blocks(long long ntiles, int blocks_per_sm) {
+  static const int sms = [] {
+    int dev = 0, n = 152;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      n = 152;
+    return n;
+  }();
+  const int bps = blocks_per_sm < 1 ? 1 : blocks_per_sm > 3 ? 3 : blocks_per_sm;
+  return std::min<long long>(ntiles, (long long)sms * bps);
+}
+
+template <int THREADS>
+static cudaError_t gradient_batch_t(const BatchGrid *grids, int ngrids, long long ntiles, int bps, uint32_t *status,
+                                    cudaStream_t st) {
+  static const cudaError_t attr =  // once per instantiation (thread-safe static initialisation)
+      cudaFuncSetAttribute(k_gradient_batch<THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradSmem));
   if (attr != cudaSuccess) return attr;
-  if (ntiles <= 0) return cudaSuccess;
-  const long long blocks = std::min<long long>(ntiles, 152LL * 3);
-  k_gradient_batch<<<(unsigned)blocks, GRAD_THREADS, sizeof(GradSmem), st>>>(grids, ngrids, ntiles, status);
+  k_gradient_batch<THREADS><<<(unsigned)persistent_blocks(ntiles, bps), THREADS, sizeof(GradSmem), st>>>(grids, ngrids,
+                                                                                                      ntiles, status);
   DMSC_LAUNCHED(1);
   return cudaGetLastError();
 }
 
-cudaError_t launch_labels_batch(const BatchGrid *grids, int ngrids, long long ntiles, const CpOut &cp, uint32_t *status,
-                                cudaStream_t st) {
-  // once per process (thread-safe static initialisation)
-  static const cudaError_t attr = cudaFuncSetAttribute(k_labels_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LabelSmem));
+template <int THREADS>
+static cudaError_t labels_batch_t(const BatchGrid *grids, int ngrids, long long ntiles, const CpOut &cp, int bps,
+                                  uint32_t *status, cudaStream_t st) {
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(k_labels_batch<THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LabelSmem));
   if (attr != cudaSuccess) return attr;
-  if (ntiles <= 0) return cudaSuccess;
-  const long long blocks = std::min<long long>(ntiles, 152LL * 3);
-  k_labels_batch<<<(unsigned)blocks, GRAD_THREADS, sizeof(LabelSmem), st>>>(grids, ngrids, ntiles, cp, status);
+  k_labels_batch<THREADS><<<(unsigned)persistent_blocks(ntiles, bps), THREADS, sizeof(LabelSmem), st>>>(grids, ngrids,
+                                                                                                     ntiles, cp, status);
   DMSC_LAUNCHED(1);
   return cudaGetLastError();
+}
+
+cudaError_t launch_gradient_batch(const BatchGrid *grids, int ngrids, long long ntiles, uint32_t *status, cudaStream_t st,
+                                  BatchLaunch cfg) {
+  if (ntiles <= 0) return cudaSuccess;
+  return cfg.threads == 256 ? gradient_batch_t<256>(grids, ngrids, ntiles, cfg.blocks_per_sm, status, st)
+                            : gradient_batch_t<GRAD_THREADS>(grids, ngrids, ntiles, cfg.blocks_per_sm, status, st);
+}
+
+cudaError_t launch_labels_batch(const BatchGrid *grids, int ngrids, long long ntiles, const CpOut &cp, uint32_t *status,
+                                cudaStream_t st, BatchLaunch cfg) {
+  if (ntiles <= 0) return cudaSuccess;
+  return cfg.threads == 256 ? labels_batch_t<256>(grids, ngrids, ntiles, cp, cfg.blocks_per_sm, status, st)
+                            : labels_batch_t<GRAD_THREADS>(grids, ngrids, ntiles, cp, cfg.blocks_per_sm, status, st);
 }
 
 }  // namespace dmsc

@@ -107,6 +107,10 @@ struct dmsc_ctx {
   long long merge_round_window = 0, merge_round_min_commits = 4;
   bool use_ocl = false;  // pipeline pieces through work_ocl (GridDataManager's ocl flag)
   std::string ooc_dir;   // pipelines spill their pieces' complexes to files here (empty: in memory)
+  // batch launch configurations per size class (dmsc_batch_autotune): threads
+  // per block and resident blocks per SM of the persistent tile kernels
+  bool batch_tuned = false;
+  int batch_cfg[6][2] = {{512, 3}, {512, 3}, {512, 3}, {512, 3}, {512, 3}, {512, 3}};
 };
 
 struct dmsc_msc {

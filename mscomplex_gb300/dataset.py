@@ -398,6 +398,38 @@ class GridBatch:
             self.lib.dmsc_batch_destroy(self.h)
             self.h = None
 
+    CLASSES = ("<128", "<256", "<512", "<1024", "<2048", ">=2048")
+
+    @staticmethod
+    def autotune(fields, repeats: int = 3, ctx: Context | None = None) -> dict:
+        """The batch launch autotuner (dmsc_batch_autotune): per size class of
+        the sample's grids (larger side <128, <256, <512, <1024, <2048,
+        >=2048), the fastest launch configuration of the two tile kernels
+        (threads per block, resident blocks per SM) becomes the context's.
+        Returns {class: (threads, blocks_per_sm, us, default_us)}."""
+        ctx = ctx or default_context()
+        packed, sizes = GridBatch.pack(fields)
+        t = np.zeros(24, np.int32)
+        check(ctx.lib.dmsc_batch_autotune(ctx.h, len(fields), _ptr(sizes), _ptr(packed), 0, int(repeats), _ptr(t)))
+        return {GridBatch.CLASSES[c]: tuple(int(v) for v in t[4 * c:4 * c + 4]) for c in range(6) if t[4 * c]}
+
+    @staticmethod
+    def set_launch(size_class: int, threads: int, blocks_per_sm: int, ctx: Context | None = None):
+        """Pins one size class's launch configuration (as the autotuner would)."""
+        ctx = ctx or default_context()
+        check(ctx.lib.dmsc_batch_set_launch(ctx.h, int(size_class), int(threads), int(blocks_per_sm)))
+
+    @staticmethod
+    def autotune_reset(ctx: Context | None = None):
+        ctx = ctx or default_context()
+        check(ctx.lib.dmsc_batch_autotune_reset(ctx.h))
+
+    def tile_times(self):
+        """Device ms of the last run's gradient and owner-label tile kernels."""
+        ms = np.zeros(2, np.float32)
+        check(self.lib.dmsc_batch_tile_times(self.h, _ptr(ms)))
+        return float(ms[0]), float(ms[1])
+
     @staticmethod
     def pack(fields):
         """(packed float32 heights, sizes int32[2n]) of a list of 2D fields."""
