@@ -300,6 +300,18 @@ __host__ __device__ __forceinline__ void edge_cell(const GridGeom &g, uint32_t e
   ry = 2 * vy + (int)(e & 1);
 }
 
+// Index of edge (rx, ry) (ext-local) in the successor-offset array, which is
+// laid out in 8x8-vertex blocks of 128 bytes (two edges per vertex), so that a
+// chain walked one cell at a time in any direction stays inside one cache
+// line for several steps.
+__host__ __device__ __forceinline__ uint32_t succ_idx(const GridGeom &g, int rx, int ry) {
+  const uint32_t vx = (uint32_t)(rx >> 1), vy = (uint32_t)(ry >> 1), nbx = ((uint32_t)g.vnx + 7u) >> 3;
+  return (((vy >> 3) * nbx + (vx >> 3)) << 7) | ((vy & 7u) << 4) | ((vx & 7u) << 1) | ((uint32_t)ry & 1u);
+}
+__host__ __device__ __forceinline__ size_t succ_bytes(const GridGeom &g) {
+  return (size_t)(((uint32_t)g.vnx + 7u) >> 3) * (size_t)(((uint32_t)g.vny + 7u) >> 3) * 128u;
+}
+
 // next_cells in ext-local coordinates with a code accessor: up to two
 // successors of edge (rx, ry); returns -1 on a non-critical unpaired rect cell.
 template <class CodeFn>
@@ -395,7 +407,7 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict
           active = 1;
         }
       }
-      nextd[edge_id(g, rx, ry)] = succ;
+      nextd[succ_idx(g, rx, ry)] = succ;
       S.sd[sl] = sd;
     } else {
       S.sd[sl] = SUCC_NONE;
@@ -476,7 +488,7 @@ struct ChainArgs {
   uint8_t *big;         // per cp: surviving saddle with more than KMAX chains
   uint32_t *cbase;      // exclusive scan of kc
   uint32_t *cstart, *csaddle, *clen, *cnseg, *csegoff;  // per chain
-  uint4 *segs;          // (chain, first edge, first level, cells)
+  uint4 *segs;          // (first edge, first disc position, cells | alive << 8, chain)
   uint4 *blocks;        // per chain slot of a saddle, 2 uint4: an interleave record (k_zip_blocks)
   uint32_t cap;         // chain slots allocated
   unsigned long long limit;
@@ -596,7 +608,7 @@ __global__ void k_chain_segs(long long nchains, DiscArgs a, ChainArgs c) {
             int rx, ry;
             edge_cell(g, x, rx, ry);
             for (uint32_t i = 0; i < w && ok; ++i) {
-              const uint32_t d = c.nextd[edge_id(g, rx, ry)];
+              const uint32_t d = c.nextd[succ_idx(g, rx, ry)];
               if (d >= SUCC_TWO) { ok = false; break; }
               rx += (int)(d % 5) - 2;
               ry += (int)(d / 5) - 2;
@@ -658,54 +670,40 @@ __global__ void k_zip_blocks(DiscArgs a, ChainArgs c, const uint32_t *off) {
 // Pieces of at most SEG_MAX cells of one chain, stored straight at their
 // places in the disc.  A piece's cells are `alive` positions apart from its
 // first position (k_chain_segs), so a thread follows the 1-byte successor
-// offsets of the piece and stores each cell as it reaches it.  Each thread
-// walks PLACE_PIECES pieces side by side, so that their dependent successor
-// loads are in flight together.
-constexpr int PLACE_PIECES = 2;
+// offsets of the piece (read through the 8x8-vertex blocked layout of
+// succ_idx) and stores each cell as it reaches it; a successor code d is a
+// fixed packed cell id delta (a shared-memory table).  One piece per thread:
+// the walk is bound by the latency of its dependent loads, which more
+// resident threads hide better than more pieces per thread (measured).
 __global__ void __launch_bounds__(256) k_seg_place(DiscArgs a, ChainArgs c, long long nsegs, uint32_t *out,
                                                    unsigned long long out_len) {
+  __shared__ int dcell[25];  // packed cell id delta of successor code d
   const GridGeom &g = a.g;
+  if (threadIdx.x < 25) dcell[threadIdx.x] = ((int)threadIdx.x / 5 - 2) * 65536 + ((int)threadIdx.x % 5 - 2);
+  __syncthreads();
   uint32_t st = 0;
-  const long long npairs = (nsegs + PLACE_PIECES - 1) / PLACE_PIECES;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npairs; p += (long long)gridDim.x * blockDim.x) {
-    int rx[PLACE_PIECES], ry[PLACE_PIECES];
-    uint32_t w[PLACE_PIECES], pos[PLACE_PIECES], na[PLACE_PIECES], W = 0;
-#pragma unroll
-    for (int q = 0; q < PLACE_PIECES; ++q) {
-      const long long k = p * PLACE_PIECES + q;
-      w[q] = 0; pos[q] = 0; na[q] = 0; rx[q] = 0; ry[q] = 0;
-      if (k >= nsegs) continue;
-      const uint4 sg = c.segs[k];
-      w[q] = sg.z & 0xffu;
-      na[q] = sg.z >> 8;
-      pos[q] = sg.y;
-      if (!w[q]) continue;
-      if (w[q] > (uint32_t)SEG_MAX || na[q] == 0 || na[q] > (uint32_t)KMAX ||
-          (unsigned long long)pos[q] + (unsigned long long)(w[q] - 1) * na[q] >= out_len) {
-        st |= ST_INVARIANT;
-        w[q] = 0;
-        continue;
-      }
-      edge_cell(g, sg.x, rx[q], ry[q]);
-      W = w[q] > W ? w[q] : W;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nsegs; k += (long long)gridDim.x * blockDim.x) {
+    const uint4 sg = c.segs[k];
+    const uint32_t w = sg.z & 0xffu, na = sg.z >> 8;
+    uint32_t pos = sg.y;
+    if (!w) continue;  // an unused slot
+    if (w > (uint32_t)SEG_MAX || na == 0 || na > (uint32_t)KMAX ||
+        (unsigned long long)pos + (unsigned long long)(w - 1) * na >= out_len) {
+      st |= ST_INVARIANT;
+      continue;
     }
-    for (uint32_t i = 0; i < W; ++i) {
-      uint32_t d[PLACE_PIECES];
-#pragma unroll
-      for (int q = 0; q < PLACE_PIECES; ++q) {  // the loads first, then the stores
-        d[q] = SUCC_NONE;
-        if (i + 1 < w[q]) d[q] = c.nextd[edge_id(g, rx[q], ry[q])];
-      }
-#pragma unroll
-      for (int q = 0; q < PLACE_PIECES; ++q) {
-        if (i >= w[q]) continue;
-        out[pos[q] + i * na[q]] = pack_cellid(g.ex0 + rx[q], g.ey0 + ry[q]);
-        if (i + 1 < w[q]) {
-          if (d[q] >= SUCC_TWO) { st |= ST_INVARIANT; w[q] = i + 1; continue; }
-          rx[q] += (int)(d[q] % 5) - 2;
-          ry[q] += (int)(d[q] / 5) - 2;
-        }
-      }
+    int rx, ry;
+    edge_cell(g, sg.x, rx, ry);
+    uint32_t cell = pack_cellid(g.ex0 + rx, g.ey0 + ry);
+    for (uint32_t i = 0;; ++i) {
+      const uint32_t d = i + 1 < w ? __ldg(c.nextd + succ_idx(g, rx, ry)) : 0u;  // the load first, then the store
+      __stcs(out + pos, cell);  // streaming: the disc is not read again here
+      if (i + 1 >= w) break;
+      pos += na;
+      if (d >= 25u) { st |= ST_INVARIANT; break; }
+      cell += (uint32_t)dcell[d];
+      rx = (int)(cell & 0xffffu) - g.ex0;
+      ry = (int)(cell >> 16) - g.ey0;
     }
   }
   if (st) atomicOr(a.status, st);
@@ -985,8 +983,7 @@ struct DiscKind {
         }
         if (S.io->ev_place[kind][0]) L(cudaEventRecord(S.io->ev_place[kind][0], st));
         if (tot[1]) {
-          k_seg_place<<<nb((tot[1] + PLACE_PIECES - 1) / PLACE_PIECES), 256, 0, st>>>(a, c, tot[1], ob->p,
-                                                                                      (unsigned long long)tot[0]);
+          k_seg_place<<<nb(tot[1]), 256, 0, st>>>(a, c, tot[1], ob->p, (unsigned long long)tot[0]);
           DMSC_LAUNCHED(1);
         }
         k_level0<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, offs, ob->p);
@@ -1029,7 +1026,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   // per kind: cnt slen sstart scount (4 ncp) soff (ncp + 8) kc mc cbase (3 ncp + 1) big (ncp / 4 + 1)
   //           seed sort 4 nmax (only with seeds) | pinned counts
   const size_t kwords = (size_t)ncp * 8 + 16 + (size_t)ncp / 4 + 1 + (seeds ? 4 * (size_t)nmax : 0);
-  size_t words = (size_t)ncp + 8 + (size_t)(nV + nF) * 2 + 2 * (size_t)nE + (size_t)nE / 2 + (size_t)nE / 4 + 64 +
+  size_t words = (size_t)ncp + 8 + (size_t)(nV + nF) * 2 + 2 * (size_t)nE + (size_t)nE / 2 + succ_bytes(g) / 4 + 64 +
                  2 * kwords;
   uint32_t *buf = nullptr;
   cudaError_t e = hops_attr();
@@ -1046,7 +1043,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   S.hop_to = p; p += nE;
   S.jseg = p; p += nE;
   S.hop_len = (uint16_t *)p; p += nE / 2 + 1;
-  S.nextd = (uint8_t *)p; p += nE / 4 + 1;
+  S.nextd = (uint8_t *)p; p += succ_bytes(g) / 4 + 1;
   DiscKind K[2];
   for (int k = 0; k < 2; ++k) {
     DiscKind &D = K[k];

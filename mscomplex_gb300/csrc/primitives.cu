@@ -48,37 +48,70 @@ __device__ __forceinline__ uint32_t block_exscan(uint32_t v, uint32_t &excl) {
   return total;
 }
 
+// A thread's SCAN_ITEMS consecutive items: one or two vector loads when the
+// array is aligned for them and the items are all in range, else scalars.
 template <typename T>
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const T *__restrict__ in, long long n, uint32_t *partial) {
+__device__ __forceinline__ void load_items(const T *__restrict__ in, long long base, long long n, bool vec,
+                                           uint32_t v[SCAN_ITEMS]) {
+  static_assert(SCAN_ITEMS == 8, "two 16-byte (u32) or one 8-byte (u8) vector per thread");
+  if (vec && base + SCAN_ITEMS <= n) {
+    if constexpr (sizeof(T) == 4) {
+      const uint4 a = reinterpret_cast<const uint4 *>(in + base)[0], b = reinterpret_cast<const uint4 *>(in + base)[1];
+      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    } else {
+      const uint2 a = *reinterpret_cast<const uint2 *>(in + base);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) { v[k] = (a.x >> (8 * k)) & 0xffu; v[4 + k] = (a.y >> (8 * k)) & 0xffu; }
+    }
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) v[k] = (base + k < n) ? (uint32_t)in[base + k] : 0u;
+}
+template <typename T>
+__host__ __forceinline__ bool items_aligned(const T *p) {
+  return ((uintptr_t)p % (sizeof(T) == 4 ? 16 : 8)) == 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const T *__restrict__ in, long long n, bool vec,
+                                                              uint32_t *partial) {
   long long base = (long long)blockIdx.x * SCAN_CHUNK + (long long)threadIdx.x * SCAN_ITEMS;
+  uint32_t v[SCAN_ITEMS];
+  load_items(in, base, n, vec, v);
   uint32_t s = 0;
 #pragma unroll
-  for (int k = 0; k < SCAN_ITEMS; ++k)
-    if (base + k < n) s += (uint32_t)in[base + k];
+  for (int k = 0; k < SCAN_ITEMS; ++k) s += v[k];
   uint32_t ex;
   uint32_t tot = block_exscan(s, ex);
   if (threadIdx.x == 0) partial[blockIdx.x] = tot;
 }
 
+// (in and out may be the same array: a thread reads its items before it
+// writes them, and no thread reads another's)
 template <typename T>
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const T *__restrict__ in, long long n,
-                                                            const uint32_t *__restrict__ block_off,
-                                                            uint32_t *__restrict__ out, uint32_t *total) {
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const T *in, long long n, bool vec_in,
+                                                            const uint32_t *__restrict__ block_off, uint32_t *out,
+                                                            bool vec_out, uint32_t *total) {
   long long base = (long long)blockIdx.x * SCAN_CHUNK + (long long)threadIdx.x * SCAN_ITEMS;
   uint32_t v[SCAN_ITEMS];
+  load_items(in, base, n, vec_in, v);
   uint32_t s = 0;
 #pragma unroll
-  for (int k = 0; k < SCAN_ITEMS; ++k) {
-    v[k] = (base + k < n) ? (uint32_t)in[base + k] : 0u;
-    s += v[k];
-  }
+  for (int k = 0; k < SCAN_ITEMS; ++k) s += v[k];
   uint32_t ex;
   uint32_t tot = block_exscan(s, ex);
   uint32_t run = (block_off ? block_off[blockIdx.x] : 0u) + ex;
+  uint32_t o[SCAN_ITEMS];
 #pragma unroll
-  for (int k = 0; k < SCAN_ITEMS; ++k) {
-    if (base + k < n) out[base + k] = run;
-    run += v[k];
+  for (int k = 0; k < SCAN_ITEMS; ++k) { o[k] = run; run += v[k]; }
+  if (vec_out && base + SCAN_ITEMS <= n) {
+    reinterpret_cast<uint4 *>(out + base)[0] = make_uint4(o[0], o[1], o[2], o[3]);
+    reinterpret_cast<uint4 *>(out + base)[1] = make_uint4(o[4], o[5], o[6], o[7]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k)
+      if (base + k < n) out[base + k] = o[k];
   }
   if (total && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total = (block_off ? block_off[blockIdx.x] : 0u) + tot;
 }
@@ -91,7 +124,7 @@ cudaError_t scan_exclusive_t(const T *in, long long n, uint32_t *out, uint32_t *
   }
   long long nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
   if (nb == 1) {
-    k_scan_down<T><<<1, SCAN_THREADS, 0, st>>>(in, n, nullptr, out, total);
+    k_scan_down<T><<<1, SCAN_THREADS, 0, st>>>(in, n, items_aligned(in), nullptr, out, items_aligned(out), total);
     DMSC_LAUNCHED(1);
     return cudaGetLastError();
   }
@@ -99,11 +132,11 @@ cudaError_t scan_exclusive_t(const T *in, long long n, uint32_t *out, uint32_t *
   cudaError_t e = cudaMallocAsync((void **)&part, sizeof(uint32_t) * nb * 2, st);
   if (e != cudaSuccess) return e;
   poff = part + nb;
-  k_scan_reduce<T><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, part);
+  k_scan_reduce<T><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, items_aligned(in), part);
   DMSC_LAUNCHED(1);
   e = scan_exclusive_t<uint32_t>(part, nb, poff, nullptr, st);
   if (e == cudaSuccess) {
-    k_scan_down<T><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, poff, out, total);
+    k_scan_down<T><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, items_aligned(in), poff, out, items_aligned(out), total);
     DMSC_LAUNCHED(1);
     e = cudaGetLastError();
   }
@@ -166,16 +199,17 @@ cudaError_t scan_exclusive_u32_scratch(const uint32_t *in, long long n, uint32_t
   }
   long long nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
   if (nb == 1) {
-    k_scan_down<uint32_t><<<1, SCAN_THREADS, 0, st>>>(in, n, nullptr, out, total);
+    k_scan_down<uint32_t><<<1, SCAN_THREADS, 0, st>>>(in, n, items_aligned(in), nullptr, out, items_aligned(out), total);
     DMSC_LAUNCHED(1);
     return cudaGetLastError();
   }
   uint32_t *part = scratch, *poff = scratch + nb;
-  k_scan_reduce<uint32_t><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, part);
+  k_scan_reduce<uint32_t><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, items_aligned(in), part);
   DMSC_LAUNCHED(1);
   cudaError_t e = scan_exclusive_u32_scratch(part, nb, poff, nullptr, scratch + 2 * nb, st);
   if (e != cudaSuccess) return e;
-  k_scan_down<uint32_t><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, poff, out, total);
+  k_scan_down<uint32_t><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, items_aligned(in), poff, out,
+                                                                items_aligned(out), total);
   DMSC_LAUNCHED(1);
   return cudaGetLastError();
 }
