@@ -77,8 +77,9 @@ __device__ __forceinline__ int dir_dy(uint32_t d) { return d == DIR_PY ? 1 : (d 
 // Gradient code of a cell after the pairing (assignGradients steps 2 and 3):
 // unmarked rect cells are critical; the boundary rule marks a paired rect
 // cell with an exterior cofacet, and its pair, critical as well.
+template <bool INTERIOR = false>
 __device__ __forceinline__ uint32_t finish_code(const GridGeom &g, bool piece, int x, int y, uint32_t dir, bool paired) {
-  bool inr = in_rect(g, x, y);
+  bool inr = INTERIOR || in_rect(g, x, y);
   bool crit = inr && !paired;
   if (piece && paired) {
     if (inr && has_ext_cofacet(g, x, y)) crit = true;
@@ -206,9 +207,20 @@ struct GradSmem {
   uint32_t code[TY][TX];
 };
 
-// K1 on tile (bx, by) of one grid, THREADS threads per block.
-template <int THREADS>
-__device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, const GridGeom &g, uint32_t *__restrict__ codes,
+// True if every cell of tile (bx, by), its one-vertex halo and the cells
+// paired across its border lie strictly inside rect and away from the grid's
+// border: the bounds tests, the grid-border rule of lowestPairableCoFacet and
+// the exterior-cofacet rule then all have fixed outcomes.
+__device__ __forceinline__ bool interior_tile(const GridGeom &g, int bx, int by) {
+  const int tx0 = bx * TX, ty0 = by * TY;
+  return tx0 >= 2 && ty0 >= 2 && tx0 + TX + 2 < g.vnx && ty0 + TY + 2 < g.vny && g.rx0 + 4 <= 2 * tx0 &&
+         g.ry0 + 4 <= 2 * ty0 && 2 * (tx0 + TX) + 4 <= g.rx1 && 2 * (ty0 + TY) + 4 <= g.ry1;
+}
+
+// K1 on tile (bx, by) of one grid, THREADS threads per block; INTERIOR:
+// the tile satisfies interior_tile (the same results with fewer tests).
+template <int THREADS, bool INTERIOR>
+__device__ __forceinline__ void gradient_tile_t(const float *__restrict__ hgt, const GridGeom &g, uint32_t *__restrict__ codes,
                                               uint32_t *__restrict__ terms, uint8_t *__restrict__ rowcnt,
                                               uint64_t *__restrict__ table, uint32_t *__restrict__ status, int bx, int by) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -218,7 +230,9 @@ __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, con
   int w, h, wf, hf;
   tile_extent(g, bx, by, 0, w, h);
   tile_extent(g, bx, by, 1, wf, hf);
-  const bool piece = !(g.rx0 == 0 && g.ry0 == 0 && g.rx1 == g.cx && g.ry1 == g.cy);
+  if (INTERIOR) { w = h = wf = hf = TX; }
+  const bool piece = !INTERIOR && !(g.rx0 == 0 && g.ry0 == 0 && g.rx1 == g.cx && g.ry1 == g.cy);
+  auto inr = [&](int x, int y) { return INTERIOR || in_rect(g, x, y); };
   uint32_t st = 0;
 
   // 1. vertex keys with a 1-vertex halo below/left and 2 above/right
@@ -226,7 +240,7 @@ __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, con
     int jj = e / (TX + 3), ii = e - jj * (TX + 3);
     int vi = tx0 - 1 + ii, vj = ty0 - 1 + jj;
     uint64_t k = 0;
-    if (vi >= 0 && vi < g.vnx && vj >= 0 && vj < g.vny) {
+    if (INTERIOR || (vi >= 0 && vi < g.vnx && vj >= 0 && vj < g.vny)) {
       float f = __ldg(hgt + (long long)vj * g.pitch + vi);
       if ((__float_as_uint(f) & 0x7fffffffu) > 0x7f800000u) st |= ST_NAN_INPUT;
       k = ((uint64_t)ord_key(f) << 32) | ((uint32_t)vi << 16) | (uint32_t)vj;
@@ -241,17 +255,17 @@ __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, con
     int j = e / (TX + 1), i = e - j * (TX + 1);
     int vi = tx0 + i, vj = ty0 + j;
     uint8_t best = CAND_NONE;
-    if (vi < g.vnx && vj < g.vny && in_rect(g, 2 * vi, 2 * vj)) {
+    if (INTERIOR || (vi < g.vnx && vj < g.vny && in_rect(g, 2 * vi, 2 * vj))) {
       uint64_t kv = KEY(i, j), bk = kv;
-      bool tbv = vi == 0 || vi == g.vnx - 1 || vj == 0 || vj == g.vny - 1;
+      bool tbv = !INTERIOR && (vi == 0 || vi == g.vnx - 1 || vj == 0 || vj == g.vny - 1);
       bool okv = !tbv || vi == 0 || vi == g.vnx - 1;  // vertical edges usable
       bool okh = !tbv || vj == 0 || vj == g.vny - 1;  // horizontal edges usable
       // cofacet order of getCellCofacets (:1626-1629): up, down, left, right;
       // minimum over lower neighbours (keys are distinct, order is irrelevant)
-      if (okv && vj + 1 < g.vny) { uint64_t k = KEY(i, j + 1); if (k < bk) { bk = k; best = DIR_PY; } }
-      if (okv && vj >= 1) { uint64_t k = KEY(i, j - 1); if (k < bk) { bk = k; best = DIR_MY; } }
-      if (okh && vi >= 1) { uint64_t k = KEY(i - 1, j); if (k < bk) { bk = k; best = DIR_MX; } }
-      if (okh && vi + 1 < g.vnx) { uint64_t k = KEY(i + 1, j); if (k < bk) { bk = k; best = DIR_PX; } }
+      if (okv && (INTERIOR || vj + 1 < g.vny)) { uint64_t k = KEY(i, j + 1); if (k < bk) { bk = k; best = DIR_PY; } }
+      if (okv && (INTERIOR || vj >= 1)) { uint64_t k = KEY(i, j - 1); if (k < bk) { bk = k; best = DIR_MY; } }
+      if (okh && (INTERIOR || vi >= 1)) { uint64_t k = KEY(i - 1, j); if (k < bk) { bk = k; best = DIR_MX; } }
+      if (okh && (INTERIOR || vi + 1 < g.vnx)) { uint64_t k = KEY(i + 1, j); if (k < bk) { bk = k; best = DIR_PX; } }
     }
     A.candV[j][i] = best;
   }
@@ -259,7 +273,7 @@ __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, con
     int j = e / TX, i = e - j * TX;  // H(i,j): P = V(i,j), Q = V(i+1,j)
     int hi = tx0 + i, hj = ty0 + j;
     uint8_t best = CAND_NONE;
-    if (hi + 1 < g.vnx && hj < g.vny && in_rect(g, 2 * hi + 1, 2 * hj) && hj != 0 && hj != g.vny - 1) {
+    if (INTERIOR || (hi + 1 < g.vnx && hj < g.vny && in_rect(g, 2 * hi + 1, 2 * hj) && hj != 0 && hj != g.vny - 1)) {
       uint64_t P = KEY(i, j), Q = KEY(i + 1, j);
       uint64_t Ua = KEY(i, j + 1), Wa = KEY(i + 1, j + 1), Ub = KEY(i, j - 1), Wb = KEY(i + 1, j - 1);
       bool u0 = g.desc ? usable_face_desc(P, Q, Ua, Wa) : usable_face(P, Q, Ua, Wa);  // cf[0] above
@@ -274,7 +288,7 @@ __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, con
     int j = e / (TX + 1), i = e - j * (TX + 1);  // Vt(i,j): P = V(i,j), Q = V(i,j+1)
     int vi = tx0 + i, vj = ty0 + j;
     uint8_t best = CAND_NONE;
-    if (vi < g.vnx && vj + 1 < g.vny && in_rect(g, 2 * vi, 2 * vj + 1) && vi != 0 && vi != g.vnx - 1) {
+    if (INTERIOR || (vi < g.vnx && vj + 1 < g.vny && in_rect(g, 2 * vi, 2 * vj + 1) && vi != 0 && vi != g.vnx - 1)) {
       uint64_t P = KEY(i, j), Q = KEY(i, j + 1);
       uint64_t Ur = KEY(i + 1, j), Wr = KEY(i + 1, j + 1), Ul = KEY(i - 1, j), Wl = KEY(i - 1, j + 1);
       bool u0 = g.desc ? usable_face_desc(P, Q, Ur, Wr) : usable_face(P, Q, Ur, Wr);  // cf[0] right
@@ -295,30 +309,30 @@ __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, con
     if (i < w && j < h) {
       int vi = tx0 + i, vj = ty0 + j, x = 2 * vi, y = 2 * vj;
       uint8_t cv = A.candV[j][i];
-      packed |= finish_code(g, piece, x, y, cv, cv != CAND_NONE);
-      if (vi + 1 < g.vnx) {  // H(i,j)
+      packed |= finish_code<INTERIOR>(g, piece, x, y, cv, cv != CAND_NONE);
+      if (INTERIOR || vi + 1 < g.vnx) {  // H(i,j)
         uint32_t d = CAND_NONE;
         if (cv == DIR_PX) d = DIR_MX;
         if (A.candV[j][i + 1] == DIR_MX) d = DIR_PX;
         uint8_t ce = A.candH[j][i];
         if (ce != CAND_NONE) { if (d != CAND_NONE) st |= ST_PAIR_CONFLICT; else d = ce; }
-        packed |= finish_code(g, piece, x + 1, y, d & 3, d != CAND_NONE) << 8;
+        packed |= finish_code<INTERIOR>(g, piece, x + 1, y, d & 3, d != CAND_NONE) << 8;
       }
-      if (vj + 1 < g.vny) {  // Vt(i,j)
+      if (INTERIOR || vj + 1 < g.vny) {  // Vt(i,j)
         uint32_t d = CAND_NONE;
         if (cv == DIR_PY) d = DIR_MY;
         if (A.candV[j + 1][i] == DIR_MY) d = DIR_PY;
         uint8_t ce = A.candVt[j][i];
         if (ce != CAND_NONE) { if (d != CAND_NONE) st |= ST_PAIR_CONFLICT; else d = ce; }
-        packed |= finish_code(g, piece, x, y + 1, d & 3, d != CAND_NONE) << 16;
+        packed |= finish_code<INTERIOR>(g, piece, x, y + 1, d & 3, d != CAND_NONE) << 16;
       }
-      if (vi + 1 < g.vnx && vj + 1 < g.vny) {  // F(i,j): chosen by at most one edge
+      if (INTERIOR || (vi + 1 < g.vnx && vj + 1 < g.vny)) {  // F(i,j): chosen by at most one edge
         uint32_t d = CAND_NONE;
         if (A.candH[j][i] == DIR_PY) d = DIR_MY;
         if (A.candH[j + 1][i] == DIR_MY) d = DIR_PY;
         if (A.candVt[j][i] == DIR_PX) d = DIR_MX;
         if (A.candVt[j][i + 1] == DIR_MX) d = DIR_PX;
-        packed |= finish_code(g, piece, x + 1, y + 1, d & 3, d != CAND_NONE) << 24;
+        packed |= finish_code<INTERIOR>(g, piece, x + 1, y + 1, d & 3, d != CAND_NONE) << 24;
       }
       codes[(long long)vj * g.vnx + vi] = packed;
     }
@@ -336,7 +350,7 @@ __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, con
     if (i < w && j < h) {
       uint32_t cvv = c & 0xff;
       if (cvv & CODE_CRIT) pvv = PJ_ROOT | e;
-      else if (in_rect(g, 2 * (tx0 + i), 2 * (ty0 + j))) {
+      else if (inr(2 * (tx0 + i), 2 * (ty0 + j))) {
         uint32_t d = cvv & 3;
         int ni = i + dir_dx(d), nj = j + dir_dy(d);
         pvv = (ni >= 0 && ni < w && nj >= 0 && nj < h) ? (uint16_t)(PJ_PTR | (nj * TX + ni)) : (uint16_t)(PJ_EXIT | e);
@@ -345,7 +359,7 @@ __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, con
     if (i < wf && j < hf) {
       uint32_t cf = c >> 24;
       if (cf & CODE_CRIT) pff = PJ_ROOT | e;
-      else if (in_rect(g, 2 * (tx0 + i) + 1, 2 * (ty0 + j) + 1)) {
+      else if (inr(2 * (tx0 + i) + 1, 2 * (ty0 + j) + 1)) {
         uint32_t d = cf & 3;
         int ni = i + dir_dx(d), nj = j + dir_dy(d);
         pff = (ni >= 0 && ni < wf && nj >= 0 && nj < hf) ? (uint16_t)(PJ_PTR | (nj * TX + ni)) : (uint16_t)(PJ_EXIT | e);
@@ -396,6 +410,15 @@ __device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, con
     table[tile_base + kind * SLOTS_SIDE + b] = entry;
   }
   if (st) atomicOr(status, st);
+}
+template <int THREADS>
+__device__ __forceinline__ void gradient_tile(const float *__restrict__ hgt, const GridGeom &g, uint32_t *__restrict__ codes,
+                                              uint32_t *__restrict__ terms, uint8_t *__restrict__ rowcnt,
+                                              uint64_t *__restrict__ table, uint32_t *__restrict__ status, int bx, int by) {
+  if (interior_tile(g, bx, by))
+    gradient_tile_t<THREADS, true>(hgt, g, codes, terms, rowcnt, table, status, bx, by);
+  else
+    gradient_tile_t<THREADS, false>(hgt, g, codes, terms, rowcnt, table, status, bx, by);
 }
 
 __global__ void __launch_bounds__(GRAD_THREADS, 3)
