@@ -104,26 +104,37 @@ __global__ void k_owner_final(DiscArgs a, const uint32_t *redir, uint32_t *fo) {
 
 // 2b. owner keys of the rect vertices (vertex grid) and faces (face grid),
 // row-major, from one read of the labels
-__global__ void k_disc_keys(DiscArgs a, const uint32_t *fo, uint32_t *key0, uint32_t *key1) {
+// one rect row of vertices per blockIdx.y, KEYS_ILP vertices per thread
+// (KEYS_THREADS apart) with their label loads issued together
+constexpr int KEYS_THREADS = 256, KEYS_ILP = 2, KEYS_SPAN = KEYS_THREADS * KEYS_ILP;
+__global__ void __launch_bounds__(KEYS_THREADS) k_disc_keys(DiscArgs a, const uint32_t *__restrict__ fo,
+                                                            uint32_t *__restrict__ key0, uint32_t *__restrict__ key1) {
   const GridGeom &g = a.g;
   const int nx = (g.rx1 - g.rx0) / 2 + 1, ny = (g.ry1 - g.ry0) / 2 + 1;
   const uint32_t n_ok = a.ncp_ds < a.ncp ? a.ncp_ds : a.ncp;
-  const long long n = (long long)nx * ny;
+  const int jj = blockIdx.y, ry = g.ry0 + 2 * jj;
+  const int i0 = blockIdx.x * KEYS_SPAN + threadIdx.x;
+  uint4 L[KEYS_ILP];
+#pragma unroll
+  for (int q = 0; q < KEYS_ILP; ++q) {
+    const int ii = i0 + q * KEYS_THREADS;
+    L[q] = ii < nx ? a.labels[(long long)(ry >> 1) * g.vnx + ((g.rx0 >> 1) + ii)] : make_uint4(0, 0, 0, 0);
+  }
   uint32_t bad = 0;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int jj = (int)(t / nx), ii = (int)(t - (long long)jj * nx);
-    const int rx = g.rx0 + 2 * ii, ry = g.ry0 + 2 * jj;
-    const uint4 L = a.labels[(long long)(ry >> 1) * g.vnx + (rx >> 1)];
+#pragma unroll
+  for (int q = 0; q < KEYS_ILP; ++q) {
+    const int ii = i0 + q * KEYS_THREADS;
+    if (ii >= nx) continue;
     for (int kind = 0; kind < 2; ++kind) {
       if (kind && (ii == nx - 1 || jj == ny - 1)) continue;
-      const uint32_t m = kind ? L.w : L.x;
+      const uint32_t m = kind ? L[q].w : L[q].x;
       uint32_t o = a.ncp;
       if (m != LABEL_NONE) {
         const uint32_t v = m < n_ok ? fo[m] : FO_BAD;
         if (v == FO_BAD || (v >> 30) != (uint32_t)kind) bad = 1;
         else o = v & 0x3FFFFFFFu;
       }
-      const long long fi = kind ? (long long)jj * (nx - 1) + ii : t;
+      const long long fi = kind ? (long long)jj * (nx - 1) + ii : (long long)jj * nx + ii;
       (kind ? key1 : key0)[fi] = o;
     }
   }
@@ -736,24 +747,56 @@ __global__ void k_seed_runs(long long n, uint32_t ncp, const uint32_t *key, uint
 // runs of one owner; the disc of an owner is its runs in row-major order, so
 // a stable sort of the runs (far fewer than the cells) by owner gives every
 // cell's place.
-__device__ __forceinline__ bool run_start(const uint32_t *key, long long t, int w) {
-  return (t % w) == 0 || key[t] != key[t - 1];
-}
-__device__ __forceinline__ bool run_end(const uint32_t *key, long long t, long long n, int w) {
-  return (t % w) == w - 1 || t + 1 == n || key[t + 1] != key[t];
-}
-__global__ void k_run_flags(const uint32_t *key, long long n, int w, uint32_t *flag) {
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-    flag[t] = run_start(key, t, w) ? 1u : 0u;
+// The row-wise run kernels take one grid row per blockIdx.y and RUN_SPAN
+// cells of it per block, RUN_ILP cells per thread (RUN_THREADS apart, so a
+// warp's loads stay coalesced) with all of a thread's loads issued before
+// any is used: one 4-byte load in flight per thread leaves these streaming
+// kernels far below the memory bandwidth.
+constexpr int RUN_THREADS = 256, RUN_ILP = 4, RUN_SPAN = RUN_THREADS * RUN_ILP;
+static dim3 run_grid(long long n, int w) { return dim3((unsigned)((w + RUN_SPAN - 1) / RUN_SPAN), (unsigned)(n / w)); }
+
+__global__ void __launch_bounds__(RUN_THREADS) k_run_flags(const uint32_t *__restrict__ key, int w, uint32_t *__restrict__ flag) {
+  const uint32_t *kr = key + (long long)blockIdx.y * w;
+  uint32_t *fr = flag + (long long)blockIdx.y * w;
+  const int c0 = blockIdx.x * RUN_SPAN + threadIdx.x;
+  uint32_t k[RUN_ILP], kp[RUN_ILP];
+#pragma unroll
+  for (int q = 0; q < RUN_ILP; ++q) {
+    const int c = c0 + q * RUN_THREADS;
+    k[q] = c < w ? kr[c] : 0u;
+    kp[q] = c > 0 && c < w ? kr[c - 1] : ~k[q];
+  }
+#pragma unroll
+  for (int q = 0; q < RUN_ILP; ++q) {
+    const int c = c0 + q * RUN_THREADS;
+    if (c < w) fr[c] = k[q] != kp[q] ? 1u : 0u;  // a run starts at a row start or a change of owner
+  }
 }
 // rid: exclusive scan of the start flags (the run of a start cell)
-__global__ void k_run_records(const uint32_t *key, long long n, int w, const uint32_t *rid, uint32_t *rkey,
-                              uint32_t *rstart, uint32_t *rend) {
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const bool s = run_start(key, t, w);
-    const uint32_t r = s ? rid[t] : rid[t] - 1u;  // the run holding t
-    if (s) { rkey[r] = key[t]; rstart[r] = (uint32_t)t; }
-    if (run_end(key, t, n, w)) rend[r] = (uint32_t)t + 1;
+__global__ void __launch_bounds__(RUN_THREADS) k_run_records(const uint32_t *__restrict__ key, int w,
+                                                             const uint32_t *__restrict__ rid, uint32_t *__restrict__ rkey,
+                                                             uint32_t *__restrict__ rstart, uint32_t *__restrict__ rend) {
+  const long long r0 = (long long)blockIdx.y * w;
+  const uint32_t *kr = key + r0, *ir = rid + r0;
+  const int c0 = blockIdx.x * RUN_SPAN + threadIdx.x;
+  uint32_t k[RUN_ILP], kp[RUN_ILP], kn[RUN_ILP], id[RUN_ILP];
+#pragma unroll
+  for (int q = 0; q < RUN_ILP; ++q) {
+    const int c = c0 + q * RUN_THREADS;
+    const bool in = c < w;
+    k[q] = in ? kr[c] : 0u;
+    kp[q] = in && c > 0 ? kr[c - 1] : ~k[q];
+    kn[q] = in && c + 1 < w ? kr[c + 1] : ~k[q];
+    id[q] = in ? ir[c] : 0u;
+  }
+#pragma unroll
+  for (int q = 0; q < RUN_ILP; ++q) {
+    const int c = c0 + q * RUN_THREADS;
+    if (c >= w) continue;
+    const bool st = k[q] != kp[q];
+    const uint32_t r = st ? id[q] : id[q] - 1u;  // the run holding the cell
+    if (st) { rkey[r] = k[q]; rstart[r] = (uint32_t)(r0 + c); }
+    if (k[q] != kn[q]) rend[r] = (uint32_t)(r0 + c) + 1u;
   }
 }
 __global__ void k_runs_sorted_len(long long R, uint32_t ncp, const uint32_t *rkey_s, const uint32_t *ridx,
@@ -779,17 +822,31 @@ __global__ void k_runs_place(long long R, uint32_t ncp, const uint32_t *rkey_s, 
   }
 }
 // every owned cell to its owner's disc: off[owner] + its run's place + offset in the run
-__global__ void k_runs_scatter(const GridGeom g, int kind, const uint32_t *key, long long n, int w, uint32_t ncp,
-                               const uint32_t *rid, const uint32_t *rpos, const uint32_t *rstart, const uint32_t *off,
-                               uint32_t *out) {
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const uint32_t k = key[t];
-    if (k >= ncp) continue;
-    const bool s = run_start(key, t, w);
-    const uint32_t r = s ? rid[t] : rid[t] - 1u;
-    const long long jj = t / w, ii = t - jj * w;
-    out[off[k] + rpos[r] + ((uint32_t)t - rstart[r])] =
-        pack_cellid(g.ex0 + g.rx0 + kind + 2 * (int)ii, g.ey0 + g.ry0 + kind + 2 * (int)jj);
+__global__ void __launch_bounds__(RUN_THREADS) k_runs_scatter(const GridGeom g, int kind, const uint32_t *__restrict__ key,
+                                                              int w, uint32_t ncp, const uint32_t *__restrict__ rid,
+                                                              const uint32_t *__restrict__ rpos,
+                                                              const uint32_t *__restrict__ rstart,
+                                                              const uint32_t *__restrict__ off, uint32_t *__restrict__ out) {
+  const int jj = blockIdx.y;
+  const long long r0 = (long long)jj * w;
+  const uint32_t *kr = key + r0, *ir = rid + r0;
+  const int c0 = blockIdx.x * RUN_SPAN + threadIdx.x;
+  uint32_t k[RUN_ILP], kp[RUN_ILP], id[RUN_ILP];
+#pragma unroll
+  for (int q = 0; q < RUN_ILP; ++q) {
+    const int c = c0 + q * RUN_THREADS;
+    const bool in = c < w;
+    k[q] = in ? kr[c] : ncp;
+    kp[q] = in && c > 0 ? kr[c - 1] : ~k[q];
+    id[q] = in ? ir[c] : 0u;
+  }
+#pragma unroll
+  for (int q = 0; q < RUN_ILP; ++q) {
+    const int c = c0 + q * RUN_THREADS;
+    if (k[q] >= ncp) continue;  // out of the row, or a cell without a disc owner
+    const uint32_t r = k[q] != kp[q] ? id[q] : id[q] - 1u;
+    out[off[k[q]] + rpos[r] + ((uint32_t)(r0 + c) - rstart[r])] =
+        pack_cellid(g.ex0 + g.rx0 + kind + 2 * c, g.ey0 + g.ry0 + kind + 2 * jj);
   }
 }
 __global__ void k_iota_u32(long long n, uint32_t *a) {
@@ -866,7 +923,7 @@ struct DiscKind {
     switch (stage++) {
       case 0: {  // runs of one owner along the rows, numbered row-major (gval holds the run ids)
         if (n > 0 && ncp) {
-          k_run_flags<<<nb(n), 256, 0, st>>>(S.gkey[kind], n, S.gw[kind], S.gval[kind]);
+          k_run_flags<<<run_grid(n, S.gw[kind]), RUN_THREADS, 0, st>>>(S.gkey[kind], S.gw[kind], S.gval[kind]);
           DMSC_LAUNCHED(1);
           L(scan_exclusive_u32(S.gval[kind], n, S.gval[kind], soff, st));
           const uint32_t *w[1] = {soff};
@@ -888,7 +945,8 @@ struct DiscKind {
           uint32_t *spos = runbuf + 5 * R, *tk = runbuf + 7 * R, *tv = runbuf + 8 * R, *gbase = runbuf + 9 * R;
           rstart = runbuf + 2 * R;
           rp = runbuf + 6 * R;
-          k_run_records<<<nb(n), 256, 0, st>>>(S.gkey[kind], n, S.gw[kind], S.gval[kind], rkey, rstart, rend);
+          k_run_records<<<run_grid(n, S.gw[kind]), RUN_THREADS, 0, st>>>(S.gkey[kind], S.gw[kind], S.gval[kind], rkey,
+                                                                          rstart, rend);
           k_iota_u32<<<nb(R), 256, 0, st>>>(R, ridx);
           DMSC_LAUNCHED(2);
           L(radix_sort_pairs(rkey, ridx, tk, tv, R, nbits_for(ncp + 1), st));
@@ -992,8 +1050,8 @@ struct DiscKind {
         // between the two events: every saddle disc cell of this kind is written once
         if (S.io->ev_place[kind][1]) L(cudaEventRecord(S.io->ev_place[kind][1], st));
         if (n > 0 && nrun) {  // extremum discs of this kind
-          k_runs_scatter<<<nb(n), 256, 0, st>>>(a.g, kind, S.gkey[kind], n, S.gw[kind], (uint32_t)ncp, S.gval[kind], rp,
-                                                rstart, offs, ob->p);
+          k_runs_scatter<<<run_grid(n, S.gw[kind]), RUN_THREADS, 0, st>>>(a.g, kind, S.gkey[kind], S.gw[kind], (uint32_t)ncp,
+                                                                          S.gval[kind], rp, rstart, offs, ob->p);
           DMSC_LAUNCHED(1);
         }
         release();
@@ -1085,7 +1143,9 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   // grouped by owner with a stable sort (row-major order is the append order)
   if (ncp) {
     k_owner_final<<<nb(ncp), 256, 0, st>>>(a, S.redir, K[0].scount);  // free until the saddle passes
-    k_disc_keys<<<nb(nV), 256, 0, st>>>(a, K[0].scount, S.gkey[0], S.gkey[1]);
+    const int knx = (a.g.rx1 - a.g.rx0) / 2 + 1, kny = (a.g.ry1 - a.g.ry0) / 2 + 1;
+    k_disc_keys<<<dim3((unsigned)((knx + KEYS_SPAN - 1) / KEYS_SPAN), (unsigned)kny), KEYS_THREADS, 0, st>>>(
+        a, K[0].scount, S.gkey[0], S.gkey[1]);
     DMSC_LAUNCHED(2);
   }
   // the des kind runs on the auxiliary stream once the shared part is done
