@@ -140,7 +140,7 @@ int dmsc_msc_export_async(dmsc_msc *msc, int16_t rect_ext[8], int16_t *cellid, f
  * the record of the simplified complex.  The reference heap's order among
  * equal persistences is replayed exactly, so the pass is sequential: it stops
  * with DMSC_ERR_DEVICE_TIMEOUT (complex unchanged) after max_ops heap pops
- * and cross-connections (max_ops <= 0: 20,000,000). */
+ * and cross-connections (max_ops <= 0: 2,000,000,000). */
 int dmsc_msc_simplify_un_simplify(dmsc_msc *msc, double tresh, int64_t max_ops, void *stream);
 /* Counters of the last simplification: [0] heap pushes, [1] pops,
  * [2] cancellations, [3] operations, [4] device status. */
@@ -232,7 +232,7 @@ int dmsc_set_out_of_core(dmsc_ctx *ctx, const char *dir);
  * simplify_un_simplify(tresh[g]) (skipped where tresh[g] == 0) in shared
  * launches.  Every grid's complex is identical to the one-grid path.
  * *out == NULL: a new batch; otherwise that batch is rerun in place (buffers
- * reused).  max_ops bounds each grid's simplification (<= 0: 20,000,000).
+ * reused).  max_ops bounds each grid's simplification (<= 0: 2,000,000,000).
  * A grid whose simplification exhausts max_ops (or breaks an invariant) fails
  * alone: the run returns DMSC_ERR_PARTIAL, the batch is still *out, the
  * other grids export as usual, and dmsc_batch_export of a failed grid returns

@@ -310,7 +310,7 @@ int dmsc_batch_run(dmsc_ctx *ctx, int ngrids, const int32_t *sizes, const float 
     io.aoff = B->aoff.p; io.asc = B->asc.p; io.doff = B->doff.p; io.des = B->des.p;
     io.ngrids = ngrids; io.cpb = B->cpb.data(); io.abase = B->abase.data(); io.dbase = B->dbase.data();
     io.tresh = B->tresh.data(); io.rect = B->rect.data();
-    io.max_ops = max_ops > 0 ? (unsigned long long)max_ops : 20000000ull;
+    io.max_ops = max_ops > 0 ? (unsigned long long)max_ops : 2000000000ull;
     io.host_stats = B->stats.data();
     int rc = DMSC_OK;
     std::vector<int> dead;

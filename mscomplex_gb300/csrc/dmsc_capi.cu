@@ -428,7 +428,7 @@ int dmsc_msc_simplify_un_simplify(dmsc_msc *m, double tresh, int64_t max_ops, vo
   io.aoff = m->aoff.p; io.asc = m->asc.p; io.doff = m->doff.p; io.des = m->des.p;
   for (int i = 0; i < 4; ++i) io.rect[i] = m->rect[i];
   io.tresh = tresh;
-  io.max_ops = max_ops > 0 ? (unsigned long long)max_ops : 20000000ull;
+  io.max_ops = max_ops > 0 ? (unsigned long long)max_ops : 2000000000ull;
   io.host_stats = hs;
   cudaError_t e = simplify_run(io, st);
   int rc = DMSC_OK;

@@ -184,7 +184,7 @@ struct Graph {
   // as k insert() calls in that order would leave it -- same multiset, same
   // operation count -- with one merge instead of k shifts of the list's tail;
   // each value whose count reaches 2 marks itself and `a` strangulated.
-  __host__ __device__ void insert_sorted(uint32_t l, unsigned long long k, uint32_t a) {
+  __host__ __device__ void insert_sorted(uint32_t l, unsigned long long k, uint32_t a, bool mark = true) {
     const uint32_t n = L.nrun[l];
     const uint2 *R = runs(l);
     unsigned long long ticks = 0, nnew = 0, add = 0;
@@ -207,11 +207,10 @@ struct Graph {
         if (r.y > 0xffffffffu - c) { fail = true; return; }
         r.y += c;
         P[w--] = r;
-        flags[a] |= F_STRANG;
-        flags[x] |= F_STRANG;
+        if (mark) { flags[a] |= F_STRANG; flags[x] |= F_STRANG; }
       } else {
         P[w--] = make_uint2(x, c);
-        if (c >= 2) { flags[a] |= F_STRANG; flags[x] |= F_STRANG; }
+        if (mark && c >= 2) { flags[a] |= F_STRANG; flags[x] |= F_STRANG; }
       }
     }
     L.nrun[l] = (uint32_t)(n + nnew);
@@ -222,6 +221,9 @@ struct Graph {
     if (!contains(2 * cp0, cp1)) { uint32_t t = cp0; cp0 = cp1; cp1 = t; }
     if (!contains(2 * cp0, cp1)) return false;
     const uint32_t la0 = 2 * cp0, ld1 = 2 * cp1 + 1;
+    // few d and many a (a minimum's saddles): the inserts into each asc(d)
+    // become one merge per d after the loop instead of one shift each
+    const bool batch_asc = L.nrun[ld1] < 8 && L.nrun[la0] >= 8 && L.nrun[la0] <= tmp_cap;
     for (uint32_t i = 0; i < L.nrun[la0] && !fail; ++i) {
       uint2 ra = runs(la0)[i];
       if (ra.x == cp1) continue;
@@ -243,6 +245,21 @@ struct Graph {
         if (!tick(cs)) return true;
         continue;
       }
+      if (batch_asc) {  // asc(d) takes every a at once below
+        for (uint32_t j = 0; j < L.nrun[ld1] && !fail; ++j) {
+          uint2 rd = runs(ld1)[j];
+          if (rd.x == cp0) continue;
+          unsigned long long c = (unsigned long long)ra.y * rd.y;
+          if (c > 0xffffffffull) { fail = true; return true; }
+          insert(2 * ra.x + 1, rd.x, (uint32_t)c);
+          if (count(2 * ra.x + 1, rd.x) >= 2) {
+            flags[ra.x] |= F_STRANG;
+            flags[rd.x] |= F_STRANG;
+          }
+          if (!tick(c)) return true;
+        }
+        continue;
+      }
       for (uint32_t j = 0; j < L.nrun[ld1] && !fail; ++j) {
         uint2 rd = runs(ld1)[j];
         if (rd.x == cp0) continue;
@@ -255,6 +272,23 @@ struct Graph {
           flags[rd.x] |= F_STRANG;
         }
         if (!tick(c)) return true;
+      }
+    }
+    if (batch_asc) {
+      // every d of des(cp1) but cp0 takes all a of asc(cp0) but cp1 (ascending,
+      // distinct) with counts ra.y * rd.y in one merge: the same multiset the
+      // inserts one by one leave (the strangulation marks were set above,
+      // from des(a))
+      for (uint32_t j = 0; j < L.nrun[ld1] && !fail; ++j) {
+        const uint2 rd = runs(ld1)[j];
+        if (rd.x == cp0) continue;
+        unsigned long long k = 0;
+        for (uint32_t i = 0; i < L.nrun[la0]; ++i) {
+          const uint2 ra = runs(la0)[i];
+          if (ra.x == cp1) continue;
+          tmp[k++] = make_uint2(ra.x, (uint32_t)((unsigned long long)ra.y * rd.y));
+        }
+        insert_sorted(2 * rd.x, k, rd.x, false);
       }
     }
     for (uint32_t i = 0; i < L.nrun[la0]; ++i) {

@@ -64,8 +64,8 @@ struct Request {
 // vertices at most in practice; checked by the engine, which grows buffers
 // when needed).  With a threshold, the simplification's first allocation for
 // that many points and arcs (n = v/4 points, v arcs): list pool 4 (arcs +
-// 8 n) runs of 8 B, heap and resubmit list 8 * (v/2) entries of 12 + 8 B,
-// scratch runs 4 * arcs of 8 B, list descriptors 32 B per point.  A
+// 8 n) runs of 8 B, heap and resubmit list 8 * (v/2) entries of 12 + 12 B,
+// scratch runs 4 * arcs of 8 B, list descriptors and entry words 36 B per point.  A
 // simplification that outgrows it retries with larger buffers, beyond this
 // estimate.
 long long footprint_of(int nx, int ny, bool simplify) {
@@ -75,7 +75,7 @@ long long footprint_of(int nx, int ny, bool simplify) {
                 tiles * dmsc::SLOTS_PER_TILE * 8 + (v / 4) * 64 + (1 << 16);
   if (simplify) {
     const long long n = v / 4, arcs = v;
-    b += 8 * 4 * (arcs + 8 * n) + 20 * 8 * (v / 2) + 8 * 4 * arcs + 32 * n + (1 << 20);
+    b += 8 * 4 * (arcs + 8 * n) + 24 * 8 * (v / 2) + 8 * 4 * arcs + 36 * n + (1 << 20);
   }
   return b;
 }

@@ -27,10 +27,19 @@
 
 namespace dmsc {
 
+// A heap entry: persistence and the pair (a, b).  The top three bits of a
+// and of b carry that critical point's static facts (on rect's boundary, cell
+// dimension), so that a popped pair is classified from the entry itself and
+// a resubmitted pair goes back on the heap without a load.  Critical point
+// indices are below 2^29.
 struct HeapEnt {
   float d;
   uint32_t a, b;
 };
+constexpr uint32_t IDX_MASK = (1u << 29) - 1u, META_BOUNDARY = 1u << 31;
+__host__ __device__ __forceinline__ uint32_t ent_idx(uint32_t x) { return x & IDX_MASK; }
+__host__ __device__ __forceinline__ int ent_dim(uint32_t x) { return (int)((x >> 29) & 3u); }
+__host__ __device__ __forceinline__ bool ent_boundary(uint32_t x) { return (x & META_BOUNDARY) != 0; }
 
 // IEEE single subtraction without contraction on either side of the compiler.
 __host__ __device__ __forceinline__ float fsub_rn(float a, float b) {
@@ -45,9 +54,10 @@ __host__ __device__ __forceinline__ float fsub_rn(float a, float b) {
 struct SimpArgs {
   Graph G;            // the complex as a mutable graph (msc_graph.cuh)
   const float *fn;
+  uint32_t *meta;     // per critical point: its index with the entry bits (k_simp_prep)
   HeapEnt *heap;
   unsigned long long heap_cap;
-  uint2 *resub;       // resubmit list (capacity heap_cap)
+  HeapEnt *resub;     // resubmit list (capacity heap_cap), whole entries
   uint2 *canc;        // cancellation list (capacity ncp)
   int rx0, ry0, rx1, ry1;  // m_rect of the complex (cell coordinates)
   double tresh;
@@ -68,21 +78,11 @@ constexpr size_t HEAP_TOP_BYTES = sizeof(HeapEnt) * HEAP_TOP;
 struct Simp {
   SimpArgs A;
   unsigned long long nheap = 0, nres = 0, ncanc = 0;
+  unsigned long long n_push = 0, n_pop = 0;  // heap operations (stats[0], stats[1] at the end)
   HeapEnt *top = nullptr;         // shared-memory part of the heap (null: all in global memory)
   unsigned long long ntop = 0;    // indices below ntop are in `top`
 
   __host__ __device__ __forceinline__ HeapEnt &H(unsigned long long i) { return i < ntop ? top[i] : A.heap[i]; }
-
-  __host__ __device__ __forceinline__ bool on_boundary(uint32_t k) const {  // m_rect.isOnBoundry
-    uint32_t c = A.G.cellid[k];
-    int x = (int16_t)(c & 0xffff), y = (int16_t)(c >> 16);
-    bool contains = x >= A.rx0 && y >= A.ry0 && x <= A.rx1 && y <= A.ry1;
-    bool interior = x > A.rx0 && y > A.ry0 && x < A.rx1 && y < A.ry1;
-    return contains && !interior;
-  }
-  __host__ __device__ __forceinline__ float pers(uint32_t a, uint32_t b) const {
-    return fabsf(fsub_rn(A.fn[b], A.fn[a]));
-  }
 
   // ---- heap (binary heap of the standard library, comparator d1 > d2) ----
   __host__ __device__ __forceinline__ static bool comp(const HeapEnt &x, const HeapEnt &y) { return x.d > y.d; }
@@ -100,31 +100,96 @@ struct Simp {
     H(nheap) = x;
     push_at(nheap, 0, x);
     ++nheap;
-    ++A.stats[0];
+    ++n_push;
   }
-  __host__ __device__ void push(uint32_t a, uint32_t b) { push_ent(HeapEnt{pers(a, b), a, b}); }
+  // a new pair: its two values and its two entry words from independent loads
+  __host__ __device__ void push(uint32_t a, uint32_t b) {
+    const float fa = A.fn[a], fb = A.fn[b];
+    const uint32_t ma = A.meta[a], mb = A.meta[b];
+    push_ent(HeapEnt{fabsf(fsub_rn(fb, fa)), ma, mb});
+  }
+  // pop_heap + pop_back: libstdc++'s __adjust_heap moves the hole from the
+  // root to a leaf along the smaller children (the right one unless the left
+  // is strictly smaller), then sifts the last element up from that leaf.  The
+  // sift-up restores every path entry below the place where the last element
+  // lands, so stopping the descent there -- at the first chosen child larger
+  // than the last element -- leaves the same heap with fewer steps.
+  //
+  // The path does not depend on the last element, so the shared-memory part
+  // is chosen first from the keys alone (while the last element, often in
+  // global memory, is still on its way), then shifted up to the stop; in
+  // global memory both children and all four grandchildren of the hole are
+  // loaded together, two levels per round trip.
   __host__ __device__ HeapEnt pop() {
+    ++n_pop;
     HeapEnt first = H(0);
-    if (nheap > 1) {
-      unsigned long long len = nheap - 1;
-      HeapEnt val = H(len);
-      H(len) = H(0);
-      unsigned long long hole = 0, second = 0;
-      while (second < (len - 1) / 2) {
-        second = 2 * (second + 1);
-        if (comp(H(second), H(second - 1))) second--;
-        H(hole) = H(second);
-        hole = second;
-      }
-      if ((len & 1) == 0 && second == (len - 2) / 2) {
-        second = 2 * (second + 1);
-        H(hole) = H(second - 1);
-        hole = second - 1;
-      }
-      push_at(hole, 0, val);
-    }
+    const unsigned long long len = nheap - 1;
     --nheap;
-    ++A.stats[1];
+    if (len == 0) return first;
+    const HeapEnt val = H(len);
+    unsigned long long hole = 0;
+    // shared-memory levels: the path while both children are in `top`
+    constexpr int PMAX = 16;  // HEAP_TOP holds 14 levels
+    uint32_t path[PMAX];
+    float pkey[PMAX];
+    int np = 0;
+    {
+      unsigned long long h = 0;
+      while (np < PMAX) {
+        const unsigned long long l = 2 * h + 1;
+        if (l >= len || l + 1 >= ntop) break;
+        unsigned long long c = l;
+        float dc = top[l].d;
+        if (l + 1 < len) {
+          const float dr = top[l + 1].d;
+          if (!(dr > dc)) { c = l + 1; dc = dr; }
+        }
+        path[np] = (uint32_t)c;
+        pkey[np] = dc;
+        ++np;
+        h = c;
+      }
+    }
+    int stop = np;
+    for (int i = 0; i < np; ++i)
+      if (pkey[i] > val.d) { stop = i; break; }
+    for (int i = 0; i < stop; ++i) {
+      top[hole] = top[path[i]];
+      hole = path[i];
+    }
+    if (stop < np) {  // the last element lands in shared memory
+      top[hole] = val;
+      return first;
+    }
+    // global levels (and the step from the last shared-memory node), two at a time
+    for (;;) {
+      const unsigned long long l = 2 * hole + 1;
+      if (l >= len) break;
+      const bool has_r = l + 1 < len;
+      const unsigned long long ll = 2 * l + 1, rl = 2 * (l + 1) + 1;
+      const HeapEnt L = H(l), R = has_r ? H(l + 1) : L;
+      HeapEnt g[4];
+      g[0] = ll < len ? H(ll) : L;
+      g[1] = ll + 1 < len ? H(ll + 1) : L;
+      g[2] = rl < len ? H(rl) : L;
+      g[3] = rl + 1 < len ? H(rl + 1) : L;
+      const bool right = has_r && !(R.d > L.d);
+      const unsigned long long c = right ? l + 1 : l;
+      const HeapEnt hc = right ? R : L;
+      if (hc.d > val.d) break;
+      H(hole) = hc;
+      hole = c;
+      // the next level from the loaded grandchildren
+      const unsigned long long l2 = 2 * c + 1;
+      if (l2 >= len) break;
+      const HeapEnt L2 = right ? g[2] : g[0], R2 = right ? g[3] : g[1];
+      const bool right2 = l2 + 1 < len && !(R2.d > L2.d);
+      const HeapEnt hc2 = right2 ? R2 : L2;
+      if (hc2.d > val.d) break;
+      H(hole) = hc2;
+      hole = right2 ? l2 + 1 : l2;
+    }
+    H(hole) = val;
     return first;
   }
 
@@ -147,18 +212,23 @@ struct Simp {
     while (nheap != 0 && !G.fail) {
       if (!G.tick()) break;
       HeapEnt e = pop();
-      uint32_t v1 = e.a, v2 = e.b;
       if ((double)e.d / (double)max_persistence > A.tresh) break;
-      if (G.dim(v2) == 1) { uint32_t t = v1; v1 = v2; v2 = t; }
-      const int cp2_dim = G.dim(v2);
-      if ((G.flags[v1] & F_CANCELLED) || (G.flags[v2] & F_CANCELLED)) continue;
-      bool b1 = on_boundary(v1), b2 = on_boundary(v2);
+      uint32_t w1 = e.a, w2 = e.b;
+      if (ent_dim(w2) == 1) { uint32_t t = w1; w1 = w2; w2 = t; }
+      const uint32_t v1 = ent_idx(w1), v2 = ent_idx(w2);
+      if (v1 >= n || v2 >= n) { A.stats[4] |= ST_INVARIANT; continue; }  // a list entry outside the complex
+      const int cp2_dim = ent_dim(w2);
+      // the pair's dynamic state, three independent loads
+      const uint8_t f1 = G.flags[v1], f2 = G.flags[v2];
+      const uint32_t tot2 = G.L.total[2 * v2 + cp2_dim / 2];
+      if ((f1 & F_CANCELLED) || (f2 & F_CANCELLED)) continue;
+      const bool b1 = ent_boundary(w1), b2 = ent_boundary(w2);
       if (b1 && !b2) continue;
       if (!b1 && b2) continue;
-      const bool strang = G.flags[v1] & F_STRANG;
-      if (strang && G.L.total[2 * v2 + cp2_dim / 2] != 1) {
+      const bool strang = f1 & F_STRANG;
+      if (strang && tot2 != 1) {
         if (nres >= A.heap_cap) { G.fail = true; break; }
-        A.resub[nres++] = make_uint2(e.a, e.b);
+        A.resub[nres++] = e;
         continue;
       }
       if (strang && b1) continue;
@@ -170,7 +240,7 @@ struct Simp {
       G.pair_idx[v1] = v2;
       G.pair_idx[v2] = v1;
       if (ncanc >= n) { G.fail = true; break; }
-      A.canc[ncanc++] = make_uint2(e.a, e.b);
+      A.canc[ncanc++] = make_uint2(ent_idx(e.a), ent_idx(e.b));
       if (connected) {  // new edges (d, a) in the reference's order
         const uint32_t la0 = 2 * cp0, ld1 = 2 * cp1 + 1;
         for (uint32_t i = 0; i < G.L.nrun[la0] && !G.fail; ++i) {
@@ -184,9 +254,11 @@ struct Simp {
             }
         }
       }
-      for (unsigned long long i = 0; i < nres && !G.fail; ++i) push(A.resub[i].x, A.resub[i].y);
+      for (unsigned long long i = 0; i < nres && !G.fail; ++i) push_ent(A.resub[i]);
       nres = 0;
     }
+    A.stats[0] = n_push;
+    A.stats[1] = n_pop;
     A.stats[2] = ncanc;
     if (G.fail) return;
     for (unsigned long long k = ncanc; k-- > 0;) {
@@ -200,6 +272,20 @@ struct Simp {
 // In parallel, per critical point of args[blockIdx.y]: the strangulation
 // mark of a saddle whose asc or des multiset holds one point twice (:404-417),
 // and the heap entries of its des arcs, at their places in the push order.
+// the entry word of critical point k: its index, dimension and boundary bit
+__device__ __forceinline__ uint32_t meta_of(const SimpArgs &A, uint32_t k) {
+  const uint32_t c = A.G.cellid[k];
+  const int x = (int16_t)(c & 0xffff), y = (int16_t)(c >> 16);
+  const bool contains = x >= A.rx0 && y >= A.ry0 && x <= A.rx1 && y <= A.ry1;
+  const bool interior = x > A.rx0 && y > A.ry0 && x < A.rx1 && y < A.ry1;
+  const uint32_t dim = (c & 1u) + ((c >> 16) & 1u);
+  return k | (dim << 29) | (contains && !interior ? META_BOUNDARY : 0u);
+}
+__global__ void k_simp_meta(SimpArgs *args) {
+  SimpArgs &A = args[blockIdx.y];
+  const uint32_t n = A.G.ncp;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) A.meta[i] = meta_of(A, i);
+}
 __global__ void k_simp_prep(SimpArgs *args) {
   SimpArgs &A = args[blockIdx.y];
   const uint32_t n = A.G.ncp, base = A.doff[0];
@@ -209,9 +295,10 @@ __global__ void k_simp_prep(SimpArgs *args) {
           (A.doff[i + 1] - A.doff[i] == 2 && A.des[A.doff[i]] == A.des[A.doff[i] + 1]))
         A.G.flags[i] |= F_STRANG;
     }
+    const uint32_t mi = A.meta[i];
     for (uint32_t q = A.doff[i]; q < A.doff[i + 1]; ++q) {
       const uint32_t b = A.des[q];
-      A.init[q - base] = HeapEnt{b < n ? fabsf(fsub_rn(A.fn[b], A.fn[i])) : 0.0f, i, b};
+      A.init[q - base] = b < n ? HeapEnt{fabsf(fsub_rn(A.fn[b], A.fn[i])), mi, A.meta[b]} : HeapEnt{0.0f, mi, b};
     }
   }
 }
@@ -287,12 +374,13 @@ cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st) {
   unsigned long long heap_cap = io.heap_cap ? io.heap_cap : (4ull * io.ndes + (1ull << 20));
   unsigned long long tmp_cap = io.tmp_cap ? io.tmp_cap : (1ull << 22);
   if (pool_cap > 0xffffffffull) return cudaErrorInvalidValue;  // list offsets are 32-bit
+  if (ncp > IDX_MASK) return cudaErrorInvalidValue;               // heap entries hold 29-bit indices
   auto rnd = [](size_t n) { return (n + 255) / 256 * 256; };
   size_t sizes[] = {sizeof(uint32_t) * 2 * ncp, sizeof(uint32_t) * 2 * ncp, sizeof(uint32_t) * 2 * ncp,
                     sizeof(uint32_t) * 2 * ncp, sizeof(uint2) * pool_cap, sizeof(uint2) * tmp_cap, sizeof(HeapEnt) * heap_cap,
-                    sizeof(uint2) * heap_cap, sizeof(uint2) * (ncp + 1), sizeof(unsigned long long) * 8,
+                    sizeof(HeapEnt) * heap_cap, sizeof(uint2) * (ncp + 1), sizeof(unsigned long long) * 8,
                     sizeof(uint8_t) * (ncp + 1), sizeof(uint32_t) * (ncp + 1), sizeof(uint32_t) * (ncp + 1),
-                    sizeof(HeapEnt) * ((size_t)io.ndes + 1), sizeof(SimpArgs)};
+                    sizeof(HeapEnt) * ((size_t)io.ndes + 1), sizeof(SimpArgs), sizeof(uint32_t) * (ncp + 1)};
   size_t bytes = 0;
   for (size_t z : sizes) bytes += rnd(z);
   SimplifyWork *w = new SimplifyWork;
@@ -318,7 +406,7 @@ cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st) {
   G.tmp_cap = tmp_cap;
   a.heap = (HeapEnt *)take();
   a.heap_cap = heap_cap;
-  a.resub = (uint2 *)take();
+  a.resub = (HeapEnt *)take();
   a.canc = (uint2 *)take();
   a.stats = (unsigned long long *)take();
   G.flags = (uint8_t *)take();
@@ -328,6 +416,7 @@ cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st) {
   a.ninit = (unsigned long long)io.ndes;
   a.aoff = io.aoff; a.asc = io.asc; a.doff = io.doff; a.des = io.des;
   SimpArgs *dargs = (SimpArgs *)take();
+  a.meta = (uint32_t *)take();
   w->flags_in = io.flags;
   w->pair_in = io.pair_idx;
   a.rx0 = io.rect[0]; a.ry0 = io.rect[1]; a.rx1 = io.rect[2]; a.ry1 = io.rect[3];
@@ -345,12 +434,13 @@ cudaError_t simplify_run(SimplifyIO &io, cudaStream_t st) {
     DMSC_LAUNCHED(1);
     e = cudaMemcpyAsync(dargs, &a, sizeof(SimpArgs), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
+    k_simp_meta<<<blocks_for(ncp), 256, 0, st>>>(dargs);
     k_simp_prep<<<blocks_for(ncp), 256, 0, st>>>(dargs);
     static const cudaError_t attr =
         cudaFuncSetAttribute(k_simplify, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)HEAP_TOP_BYTES);
     if (attr != cudaSuccess) return attr;
     k_simplify<<<1, 32, HEAP_TOP_BYTES, st>>>(a);
-    DMSC_LAUNCHED(2);
+    DMSC_LAUNCHED(3);
   }
   e = cudaMemcpyAsync(io.host_stats, a.stats, sizeof(unsigned long long) * 5, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -446,9 +536,9 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
   const int ns = (int)which.size();
   auto rnd = [](size_t x) { return (x + 255) / 256 * 256; };
   const size_t sizes[] = {4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * (ncp + 1),
-                          sizeof(uint2) * pool_cap, sizeof(uint2) * tmp, sizeof(HeapEnt) * heap, sizeof(uint2) * heap,
+                          sizeof(uint2) * pool_cap, sizeof(uint2) * tmp, sizeof(HeapEnt) * heap, sizeof(HeapEnt) * heap,
                           sizeof(uint2) * canc, sizeof(unsigned long long) * 8 * (size_t)(ns + 1),
-                          sizeof(SimpArgs) * (size_t)(ns + 1), sizeof(HeapEnt) * (init + 1)};
+                          sizeof(SimpArgs) * (size_t)(ns + 1), sizeof(HeapEnt) * (init + 1), 4ull * (ncp + 1)};
   size_t bytes = 0;
   for (size_t z : sizes) bytes += rnd(z);
   BatchSimplifyWork *w = new BatchSimplifyWork;
@@ -463,11 +553,12 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
   w->pool = (uint2 *)take();
   uint2 *dtmp = (uint2 *)take();
   HeapEnt *dheap = (HeapEnt *)take();
-  uint2 *dres = (uint2 *)take();
+  HeapEnt *dres = (HeapEnt *)take();
   uint2 *dcanc = (uint2 *)take();
   w->dstats = (unsigned long long *)take();
   w->dargs = (SimpArgs *)take();
   HeapEnt *dinit = (HeapEnt *)take();
+  uint32_t *dmeta = (uint32_t *)take();
   w->nsimp = ns;
   if (ncp) {
     k_lists_from_csr<<<blocks_for(ncp), 256, 0, st>>>(ncp, io.aoff, io.asc, io.doff, io.des, des_base, w->off, w->nrun,
@@ -500,6 +591,7 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
     G.ops = 0;
     G.fail = false;
     a.fn = io.fn + c0;
+    a.meta = dmeta + c0;
     a.heap = dheap + ho;
     a.resub = dres + ho;
     a.heap_cap = heap_of(nd);
@@ -522,9 +614,10 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
     // one grid per SM can keep 14 heap levels in shared memory; more grids
     // than SMs keep 12, so that four fit on an SM and all start at once
     const unsigned ntop = ns <= 152 ? (unsigned)HEAP_TOP : (1u << 12) - 1;
+    k_simp_meta<<<dim3(64, (unsigned)ns), 256, 0, st>>>(w->dargs);
     k_simp_prep<<<dim3(64, (unsigned)ns), 256, 0, st>>>(w->dargs);
     k_simplify_batch<<<ns, 32, sizeof(HeapEnt) * ntop, st>>>(w->dargs, ns, ntop);
-    DMSC_LAUNCHED(2);
+    DMSC_LAUNCHED(3);
     e = cudaGetLastError();
   }
   std::vector<unsigned long long> hs(8 * (size_t)(ns + 1), 0);

@@ -10,6 +10,11 @@
   leaves -- the four corners, two edges, two interior -- each against the
   oracle's GridDataset on the same rect / ext window: the leaf's cells and
   critical list as the pipeline computed them, and the leaf's complex.
+* The 4096² quantised field's persistence cancellation at 1% of the range
+  (GridMSComplex::simplify_un_simplify, dmsc/src/grid_mscomplex.cpp:384-535)
+  run to completion on its 1024² corner window: about 2*10^7 exact heap
+  operations and 3*10^4 cancellations, the simplified complex and its discs
+  against the oracle's.
 * The 4096² white-noise pipeline in 16 blocks of 1024² (2D splits, threshold
   0), node by node, against digests of the oracle's pipeline committed under
   tests/golden/ (the oracle needs several minutes for it; the script that
@@ -36,6 +41,22 @@ def same_cells(got, want, what):
         if not np.array_equal(a, b):
             bad = np.argwhere(a != b)[:5]
             raise AssertionError(f"{what}: {name} differs at {bad.tolist()}")
+
+
+def test_simplify_4096_quantised_window_to_completion(gpu_lib, oracle):
+    from mscomplex_gb300 import synth
+    f = np.ascontiguousarray(synth.bumps4096q()[:1024, :1024])
+    r = full_rect(f)
+    ds = gpu_lib.GridDataset(r, r).init(f).work()
+    m = ds.writeout_connectivity()
+    m.simplify_un_simplify(0.01)
+    st = m.simplify_stats()
+    assert st["pops"] + st["pushes"] > 10_000_000, st
+    ds.post_merge_fill_discs(m)
+    got = m.export()
+    del m, ds
+    want = oracle.Dataset(f, r, r, 0.01, True).msc()
+    assert_same_complex(got, want, "4096q 1024^2 window at 1%")
 
 
 def test_step_4096_quantised_vs_oracle(gpu_lib, oracle):
