@@ -83,6 +83,33 @@ struct Simp {
   unsigned long long ntop = 0;    // indices below ntop are in `top`
 
   __host__ __device__ __forceinline__ HeapEnt &H(unsigned long long i) { return i < ntop ? top[i] : A.heap[i]; }
+  // L1 prefetch of the global part of heap[lo..hi], one request per 128-byte line
+  __host__ __device__ __forceinline__ void prefetch_heap(unsigned long long lo, unsigned long long hi) {
+#ifdef __CUDA_ARCH__
+    if (lo < ntop) lo = ntop;
+    if (hi >= A.heap_cap) hi = A.heap_cap - 1;
+    if (lo > hi) return;
+    const char *p = reinterpret_cast<const char *>(A.heap + lo), *e = reinterpret_cast<const char *>(A.heap + hi + 1);
+    for (p = reinterpret_cast<const char *>(reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)127); p < e; p += 128)
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+#else
+    (void)lo; (void)hi;
+#endif
+  }
+  // before a burst of m pushes at the end: the lines of the three ancestor
+  // levels above the positions they take, and of the entries themselves
+  __host__ __device__ __forceinline__ void prefetch_pushes(const HeapEnt *src, unsigned long long m) {
+#ifdef __CUDA_ARCH__
+    if (m == 0) return;
+    const unsigned long long n0 = nheap, n1 = nheap + m;
+    for (int k = 1; k <= 3; ++k) prefetch_heap(((n0 + 1) >> k) - 1, ((n1 + 1) >> k) - 1);
+    const char *p = reinterpret_cast<const char *>(src), *e = reinterpret_cast<const char *>(src + m);
+    for (p = reinterpret_cast<const char *>(reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)127); p < e; p += 128)
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+#else
+    (void)src; (void)m;
+#endif
+  }
 
   // ---- heap (binary heap of the standard library, comparator d1 > d2) ----
   __host__ __device__ __forceinline__ static bool comp(const HeapEnt &x, const HeapEnt &y) { return x.d > y.d; }
@@ -127,33 +154,53 @@ struct Simp {
     --nheap;
     if (len == 0) return first;
     const HeapEnt val = H(len);
+    // the next pops' last elements are the entries below this one: keep
+    // their lines on their way into L1
+    if (len >= ntop + 16) prefetch_heap(len - 16, len - 16);
     unsigned long long hole = 0;
-    // shared-memory levels: the path while both children are in `top`
-    constexpr int PMAX = 16;  // HEAP_TOP holds 14 levels
+    // shared-memory levels: the path while both children are in `top`, two
+    // levels per step (children and grandchildren keys loaded together),
+    // kept in registers (fixed-size arrays indexed by unrolled constants)
+    constexpr int PMAX = 14;  // HEAP_TOP holds 14 levels
     uint32_t path[PMAX];
     float pkey[PMAX];
     int np = 0;
     {
       unsigned long long h = 0;
-      while (np < PMAX) {
+#pragma unroll
+      for (int q = 0; q < PMAX; q += 2) {
         const unsigned long long l = 2 * h + 1;
         if (l >= len || l + 1 >= ntop) break;
-        unsigned long long c = l;
-        float dc = top[l].d;
-        if (l + 1 < len) {
-          const float dr = top[l + 1].d;
-          if (!(dr > dc)) { c = l + 1; dc = dr; }
-        }
-        path[np] = (uint32_t)c;
-        pkey[np] = dc;
-        ++np;
+        const unsigned long long ll = 2 * l + 1, rl = ll + 2;  // first child of l and of l + 1
+        const bool g_ok = rl + 1 < ntop;                      // all four grandchildren in `top`
+        const float dl = top[l].d, dr = l + 1 < len ? top[l + 1].d : 0.0f;
+        float g0 = 0, g1 = 0, g2 = 0, g3 = 0;
+        if (g_ok) { g0 = top[ll].d; g1 = top[ll + 1].d; g2 = top[rl].d; g3 = top[rl + 1].d; }
+        const bool right = l + 1 < len && !(dr > dl);
+        const unsigned long long c = right ? l + 1 : l;
+        path[q] = (uint32_t)c;
+        pkey[q] = right ? dr : dl;
+        np = q + 1;
         h = c;
+        if (q + 1 >= PMAX || !g_ok) break;
+        const unsigned long long l2 = 2 * c + 1;
+        if (l2 >= len) break;
+        const float el = right ? g2 : g0, er = right ? g3 : g1;
+        const bool right2 = l2 + 1 < len && !(er > el);
+        const unsigned long long c2 = right2 ? l2 + 1 : l2;
+        path[q + 1] = (uint32_t)c2;
+        pkey[q + 1] = right2 ? er : el;
+        np = q + 2;
+        h = c2;
       }
     }
     int stop = np;
-    for (int i = 0; i < np; ++i)
-      if (pkey[i] > val.d) { stop = i; break; }
-    for (int i = 0; i < stop; ++i) {
+#pragma unroll
+    for (int i = PMAX - 1; i >= 0; --i)
+      if (i < np && pkey[i] > val.d) stop = i;
+#pragma unroll
+    for (int i = 0; i < PMAX; ++i) {
+      if (i >= stop) break;
       top[hole] = top[path[i]];
       hole = path[i];
     }
@@ -211,16 +258,19 @@ struct Simp {
     const float max_persistence = fsub_rn(max_val, min_val);
     while (nheap != 0 && !G.fail) {
       if (!G.tick()) break;
-      HeapEnt e = pop();
-      if ((double)e.d / (double)max_persistence > A.tresh) break;
-      uint32_t w1 = e.a, w2 = e.b;
+      // the entry on top and its pair's dynamic state (three independent
+      // loads), issued before the pop's descent so that they arrive during it
+      const HeapEnt top0 = H(0);
+      uint32_t w1 = top0.a, w2 = top0.b;
       if (ent_dim(w2) == 1) { uint32_t t = w1; w1 = w2; w2 = t; }
       const uint32_t v1 = ent_idx(w1), v2 = ent_idx(w2);
-      if (v1 >= n || v2 >= n) { A.stats[4] |= ST_INVARIANT; continue; }  // a list entry outside the complex
+      const bool inside = v1 < n && v2 < n;
       const int cp2_dim = ent_dim(w2);
-      // the pair's dynamic state, three independent loads
-      const uint8_t f1 = G.flags[v1], f2 = G.flags[v2];
-      const uint32_t tot2 = G.L.total[2 * v2 + cp2_dim / 2];
+      const uint8_t f1 = inside ? G.flags[v1] : 0, f2 = inside ? G.flags[v2] : 0;
+      const uint32_t tot2 = inside ? G.L.total[2 * v2 + cp2_dim / 2] : 0;
+      HeapEnt e = pop();
+      if ((double)e.d / (double)max_persistence > A.tresh) break;
+      if (!inside) { A.stats[4] |= ST_INVARIANT; continue; }  // a list entry outside the complex
       if ((f1 & F_CANCELLED) || (f2 & F_CANCELLED)) continue;
       const bool b1 = ent_boundary(w1), b2 = ent_boundary(w2);
       if (b1 && !b2) continue;
@@ -254,6 +304,7 @@ struct Simp {
             }
         }
       }
+      prefetch_pushes(A.resub, nres);
       for (unsigned long long i = 0; i < nres && !G.fail; ++i) push_ent(A.resub[i]);
       nres = 0;
     }
