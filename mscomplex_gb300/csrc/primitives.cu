@@ -116,6 +116,109 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const T *in, long lo
   if (total && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total = (block_off ? block_off[blockIdx.x] : 0u) + tot;
 }
 
+// Single-pass scan (decoupled look-back): a block takes the next tile from
+// an atomic counter, publishes its tile's sum, then warp 0 walks back over
+// the earlier tiles' published words -- adding sums until it meets a tile
+// that has published its inclusive prefix -- and publishes its own.  Tiles
+// are taken in counter order, so a block only waits for blocks that already
+// run.  A word is (flag << 32 | value) in one 64-bit store: 0 not yet, 1 the
+// tile's sum, 2 its inclusive prefix.  The wait is bounded: past
+// LOOKBACK_LIMIT polls the block sums the earlier tiles' inputs itself (the
+// same prefix, slower), which is why the input must not be the output.
+constexpr unsigned long long LOOKBACK_LIMIT = 1ull << 22;
+__device__ __forceinline__ unsigned long long ld_word(const unsigned long long *p) {
+  return *reinterpret_cast<const volatile unsigned long long *>(p);
+}
+__device__ __forceinline__ void st_word(unsigned long long *p, unsigned long long v) {
+  *reinterpret_cast<volatile unsigned long long *>(p) = v;
+}
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_onepass(const T *__restrict__ in, long long n, bool vec_in,
+                                                               uint32_t *__restrict__ out, bool vec_out,
+                                                               unsigned long long *__restrict__ word,
+                                                               uint32_t *__restrict__ counter, long long nb,
+                                                               uint32_t *__restrict__ total) {
+  __shared__ uint32_t tile_s, excl_s;
+  if (threadIdx.x == 0) tile_s = atomicAdd(counter, 1u);
+  __syncthreads();
+  const long long tile = tile_s;
+  if (tile >= nb) return;  // (block-uniform)
+  const long long base = tile * SCAN_CHUNK + (long long)threadIdx.x * SCAN_ITEMS;
+  uint32_t v[SCAN_ITEMS];
+  load_items(in, base, n, vec_in, v);
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) s += v[k];
+  uint32_t ex;
+  const uint32_t tot = block_exscan(s, ex);
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    uint32_t excl = 0;
+    bool fallback = false;
+    if (tile == 0) {
+      if (lane == 0) st_word(word, (2ull << 32) | tot);
+    } else {
+      if (lane == 0) st_word(word + tile, (1ull << 32) | tot);
+      long long j = tile - 1;
+      unsigned long long polls = 0;
+      for (;;) {
+        const long long idx = j - lane;  // lane 0: the nearest earlier tile
+        const unsigned long long w = idx >= 0 ? ld_word(word + idx) : (2ull << 32);
+        const uint32_t flag = (uint32_t)(w >> 32);
+        const unsigned pm = __ballot_sync(0xffffffffu, flag == 2u), zm = __ballot_sync(0xffffffffu, flag == 0u);
+        const int fp = pm ? __ffs(pm) - 1 : 32;  // the nearest tile with its prefix
+        const unsigned need = fp >= 31 ? 0xffffffffu : ((2u << fp) - 1u);
+        if (zm & need) {  // a tile before it has published nothing yet
+          if (++polls > LOOKBACK_LIMIT) { fallback = true; break; }
+          continue;
+        }
+        uint32_t c = lane <= fp ? (uint32_t)w : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        excl += c;
+        if (fp < 32) break;
+        j -= 32;
+      }
+      fallback = __any_sync(0xffffffffu, fallback);
+      if (!fallback && lane == 0) st_word(word + tile, (2ull << 32) | (excl + tot));
+    }
+    if (lane == 0) excl_s = fallback ? 0xFFFFFFFFu : excl;
+  }
+  __syncthreads();
+  uint32_t prefix = excl_s;
+  if (prefix == 0xFFFFFFFFu && tile > 0) {  // bounded wait ran out: the earlier tiles' sum from their inputs
+    __shared__ uint32_t red[32];
+    const long long upto = tile * SCAN_CHUNK;
+    uint32_t acc = 0;
+    for (long long i = threadIdx.x; i < upto; i += blockDim.x) acc += (uint32_t)in[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      uint32_t r = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0u;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+      if (threadIdx.x == 0) { excl_s = r; st_word(word + tile, (2ull << 32) | (r + tot)); }
+    }
+    __syncthreads();
+    prefix = excl_s;
+  }
+  uint32_t run = prefix + ex;
+  uint32_t o[SCAN_ITEMS];
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) { o[k] = run; run += v[k]; }
+  if (vec_out && base + SCAN_ITEMS <= n) {
+    reinterpret_cast<uint4 *>(out + base)[0] = make_uint4(o[0], o[1], o[2], o[3]);
+    reinterpret_cast<uint4 *>(out + base)[1] = make_uint4(o[4], o[5], o[6], o[7]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k)
+      if (base + k < n) out[base + k] = o[k];
+  }
+  if (total && tile == nb - 1 && threadIdx.x == 0) *total = prefix + tot;
+}
+
 template <typename T>
 cudaError_t scan_exclusive_t(const T *in, long long n, uint32_t *out, uint32_t *total, cudaStream_t st) {
   if (n <= 0) {
@@ -127,6 +230,20 @@ cudaError_t scan_exclusive_t(const T *in, long long n, uint32_t *out, uint32_t *
     k_scan_down<T><<<1, SCAN_THREADS, 0, st>>>(in, n, items_aligned(in), nullptr, out, items_aligned(out), total);
     DMSC_LAUNCHED(1);
     return cudaGetLastError();
+  }
+  if ((const void *)in != (const void *)out) {  // one pass (the look-back's fallback reads the input)
+    unsigned long long *word = nullptr;
+    cudaError_t e = cudaMallocAsync((void **)&word, sizeof(unsigned long long) * (nb + 1), st);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(word, 0, sizeof(unsigned long long) * (nb + 1), st);
+    if (e == cudaSuccess) {
+      k_scan_onepass<T><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, items_aligned(in), out, items_aligned(out), word,
+                                                                reinterpret_cast<uint32_t *>(word + nb), nb, total);
+      DMSC_LAUNCHED(1);
+      e = cudaGetLastError();
+    }
+    cudaFreeAsync(word, st);
+    return e;
   }
   uint32_t *part = nullptr, *poff = nullptr;
   cudaError_t e = cudaMallocAsync((void **)&part, sizeof(uint32_t) * nb * 2, st);

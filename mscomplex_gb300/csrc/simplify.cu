@@ -23,6 +23,7 @@
 #include "dmsc_internal.h"
 #include "msc_graph.cuh"
 
+#include <algorithm>
 #include <vector>
 
 namespace dmsc {
@@ -584,6 +585,15 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
   }
   const unsigned long long pool_cap = base_top + grow;
   if (pool_cap > 0xffffffffull) return cudaErrorInvalidValue;  // list offsets are 32-bit
+  // Blocks start roughly in index order and more grids than fit at once wait
+  // for a free slot, while the batch lasts as long as its longest replay: the
+  // complexes with the most arcs (the longest replays, as a rule) take the
+  // first blocks.
+  std::stable_sort(which.begin(), which.end(), [&](int x, int y) {
+    const unsigned long long ax = (io.abase[x + 1] - io.abase[x]) + (io.dbase[x + 1] - io.dbase[x]);
+    const unsigned long long ay = (io.abase[y + 1] - io.abase[y]) + (io.dbase[y + 1] - io.dbase[y]);
+    return ax > ay;
+  });
   const int ns = (int)which.size();
   auto rnd = [](size_t x) { return (x + 255) / 256 * 256; };
   const size_t sizes[] = {4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * 2 * ncp, 4ull * (ncp + 1),
@@ -663,8 +673,9 @@ cudaError_t simplify_batch_run(BatchSimplifyIO &io, cudaStream_t st) {
         cudaFuncSetAttribute(k_simplify_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)HEAP_TOP_BYTES);
     if (attr != cudaSuccess) return attr;
     // one grid per SM can keep 14 heap levels in shared memory; more grids
-    // than SMs keep 12, so that four fit on an SM and all start at once
-    const unsigned ntop = ns <= 152 ? (unsigned)HEAP_TOP : (1u << 12) - 1;
+    // than SMs keep 13, two per SM (measured on the 1000-grid workload: 13
+    // levels 108.8 ms, 12 levels (four per SM) 113.8, 14 levels 122.4)
+    const unsigned ntop = ns <= 152 ? (unsigned)HEAP_TOP : (1u << 13) - 1;
     k_simp_meta<<<dim3(64, (unsigned)ns), 256, 0, st>>>(w->dargs);
     k_simp_prep<<<dim3(64, (unsigned)ns), 256, 0, st>>>(w->dargs);
     k_simplify_batch<<<ns, 32, sizeof(HeapEnt) * ntop, st>>>(w->dargs, ns, ntop);
