@@ -4,8 +4,9 @@
 // The reference's scan is the OpenCL PrefixScan (dmsc/src/prefix_scan.cpp:
 // 340-465, kernels absent: dmsc/resources/scan_kernel.cl is empty) and its
 // sort slot is an unused bitonic sort (dmsc/src/bitonic_sort.cpp).  Both are
-// written here from scratch: the scan is reduce-then-scan with no inter-CTA
-// waiting, the radix sort is a stable 8-bit LSD sort (histogram, scan,
+// written here from scratch: the scan is a single pass with decoupled
+// look-back out of place (bounded waits on earlier tiles) and reduce-then-scan
+// in place, the radix sort is a stable 8-bit LSD sort (histogram, scan,
 // match_any-ranked scatter).
 #include "dmsc_common.cuh"
 #include "dmsc_internal.h"
