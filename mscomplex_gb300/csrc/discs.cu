@@ -290,10 +290,11 @@ __global__ void k_saddle_disc_write(DiscArgs a, int kind, SeedRuns sr, const uin
 // cells ahead, so a chain's length costs one step per tile crossed.  The
 // lengths fix every cell's place before any cell is known: per saddle, the
 // level ranges over which its set of alive chains is constant are regular
-// interleaves (k_zip_blocks), and the cells, walked by one lane per piece of
-// at most SEG_MAX cells (cut where the set of alive chains changes, with the
-// disc position of their first cell and their stride), are stored straight
-// there (k_seg_place).
+// interleaves (k_zip_blocks).  The chains are cut into pieces of at most
+// SEG_MAX cells (also where the set of alive chains changes), each with the
+// disc position of its first cell and its stride, and every block gathers the
+// cells of one window of disc positions in shared memory, walking the pieces
+// that reach it one lane each, and stores the window out (k_win_place).
 // ---------------------------------------------------------------------------
 constexpr int KMAX = 32;                 // saddles with more chains take the serial pass
 constexpr uint32_t HOP_END = 0xFFFFFFFFu;
@@ -311,16 +312,58 @@ __host__ __device__ __forceinline__ void edge_cell(const GridGeom &g, uint32_t e
   ry = 2 * vy + (int)(e & 1);
 }
 
-// Index of edge (rx, ry) (ext-local) in the successor-offset array, which is
-// laid out in 8x8-vertex blocks of 128 bytes (two edges per vertex), so that a
-// chain walked one cell at a time in any direction stays inside one cache
-// line for several steps.
+// Index of edge (rx, ry) (ext-local) in the successor-word array, which is
+// laid out in 8x8-vertex blocks of 128 words (two edges per vertex), so that a
+// chain walked in any direction stays inside one block for several steps.
 __host__ __device__ __forceinline__ uint32_t succ_idx(const GridGeom &g, int rx, int ry) {
   const uint32_t vx = (uint32_t)(rx >> 1), vy = (uint32_t)(ry >> 1), nbx = ((uint32_t)g.vnx + 7u) >> 3;
   return (((vy >> 3) * nbx + (vx >> 3)) << 7) | ((vy & 7u) << 4) | ((vx & 7u) << 1) | ((uint32_t)ry & 1u);
 }
-__host__ __device__ __forceinline__ size_t succ_bytes(const GridGeom &g) {
+__host__ __device__ __forceinline__ size_t succ_words(const GridGeom &g) {
   return (size_t)(((uint32_t)g.vnx + 7u) >> 3) * (size_t)(((uint32_t)g.vny + 7u) >> 3) * 128u;
+}
+
+// Successor words.  A chain step from an edge goes to another edge of the
+// face (asc) or vertex (des) it crosses: one of the four diagonal neighbours
+// (dx, dy = +-1) or one of the two edges 2 cells away along one axis, which
+// is y for an asc H edge or a des Vt edge and x otherwise.  So a step is a
+// 3-bit code: 0-3 diagonal (dx = +1 if bit 0, dy = +1 if bit 1), 4 / 5 the
+// +2 / -2 axis step, 7 no further step in this word.  Every edge keeps a
+// 16-bit word of the next WORD_STEPS steps of its chain inside its tile
+// (fewer where the chain leaves the tile or ends: the step out of the tile
+// is the word's last), so a walk makes one dependent load per WORD_STEPS
+// cells instead of one per cell.  A diagonal step changes the edge's
+// orientation, an axis step keeps it.
+constexpr int WORD_STEPS = 5;
+constexpr uint32_t WORD_END = 7u;
+__device__ __forceinline__ bool step_axis_y(int kind, int rx) { return ((rx & 1) != 0) == (kind == 0); }
+// code of the step (dx, dy); WORD_END if it is no chain step
+__device__ __forceinline__ uint32_t step_code(int dx, int dy) {
+  if ((dx == 1 || dx == -1) && (dy == 1 || dy == -1)) return (uint32_t)(dx > 0) | ((uint32_t)(dy > 0) << 1);
+  if ((dx == 0 && (dy == 2 || dy == -2)) || (dy == 0 && (dx == 2 || dx == -2))) return dx + dy > 0 ? 4u : 5u;
+  return WORD_END;
+}
+__device__ __forceinline__ void step_apply(uint32_t q, bool axis_y, int &rx, int &ry) {
+  if (q < 4u) {
+    rx += (q & 1u) ? 1 : -1;
+    ry += (q & 2u) ? 1 : -1;
+  } else {
+    const int s = q == 4u ? 2 : -2;
+    if (axis_y) ry += s; else rx += s;
+  }
+}
+// the same step as a packed cell id delta (x | y << 16)
+__device__ __forceinline__ uint32_t step_delta(uint32_t q, bool axis_y) {
+  if (q < 4u) return (uint32_t)(((q & 2u) ? 65536 : -65536) + ((q & 1u) ? 1 : -1));
+  const int s = q == 4u ? 2 : -2;
+  return (uint32_t)(axis_y ? s * 65536 : s);
+}
+static_assert(WORD_STEPS >= 1 && 3 * WORD_STEPS <= 16, "a word's steps fit its 16 bits");
+// a loaded word with the bits above its steps set, so that a used-up word reads WORD_END
+__device__ __forceinline__ uint32_t word_bits(uint16_t w) { return (uint32_t)w | (0xFFFFFFFFu << (3 * WORD_STEPS)); }
+// an ext-local cell whose successor word may be loaded
+__device__ __forceinline__ bool word_cell_ok(const GridGeom &g, int rx, int ry) {
+  return rx >= 0 && ry >= 0 && rx <= g.cx && ry <= g.cy && ((rx ^ ry) & 1);
 }
 
 // next_cells in ext-local coordinates with a code accessor: up to two
@@ -357,7 +400,7 @@ __device__ __forceinline__ int chain_kind(uint32_t code, int rx, int ry) {
 }
 
 constexpr int HOP_THREADS = 512;
-// successor of an edge along its chain as a cell offset (dx + 2) + 5 (dy + 2), |dx|, |dy| <= 2
+// successor of an edge along its chain as a step code (0-5, as in the successor words)
 constexpr uint8_t SUCC_NONE = 0xFF;
 constexpr int SEG_LOG = 5, SEG_MAX = 1 << SEG_LOG;  // cells of a write piece: the jump pointer distance
 
@@ -366,16 +409,17 @@ struct HopSmem {
   uint32_t code[(TX + 2) * (TY + 2)];
   uint32_t nv[HOP_SLOTS];     // next slot << 16 | cells counted so far
   uint16_t tail[HOP_SLOTS];
-  uint8_t sd[HOP_SLOTS];      // successor offset code of every slot (SUCC_NONE / SUCC_TWO)
+  uint8_t sd[HOP_SLOTS];      // successor step code of every slot (SUCC_NONE / SUCC_TWO)
 };
 
 // Per edge, for the chains of its own kind: hop_to (the edge after its
 // in-tile run, HOP_END if the chain ends in the tile), hop_len (cells of the
-// run, 0 for a branching cell) and jseg (the edge SEG_MAX cells ahead in the
-// same run, HOP_END if the run is shorter).  One block per tile.
+// run, 0 for a branching cell), jseg (the edge SEG_MAX cells ahead in the
+// same run, HOP_END if the run is shorter) and its successor word (wcode, at
+// succ_idx).  One block per tile.
 __global__ void __launch_bounds__(HOP_THREADS, 3)
 k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict__ to, uint16_t *__restrict__ len,
-            uint32_t *__restrict__ jseg, uint8_t *__restrict__ nextd, uint32_t *status) {
+            uint32_t *__restrict__ jseg, uint16_t *__restrict__ wcode, uint32_t *status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   HopSmem &S = *reinterpret_cast<HopSmem *>(smem_raw);
   const int tx0 = blockIdx.x * TX, ty0 = blockIdx.y * TY;
@@ -407,24 +451,63 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict
     uint32_t nx = SLOT_NIL;
     if (slot_cell(sl, rx, ry)) {
       const int kind = chain_kind(code(rx, ry), rx, ry);
-      uint8_t succ = SUCC_NONE, sd = SUCC_NONE;
+      uint8_t sd = SUCC_NONE;
       if (kind >= 0) {
         const int n = succ_local(g, kind, rx, ry, code, ox, oy);
         if (n < 0) st |= ST_INVARIANT;
-        if (n == 1) sd = succ = (uint8_t)((ox[0] - rx + 2) + 5 * (oy[0] - ry + 2));
+        if (n == 1) {
+          const int dx = ox[0] - rx, dy = oy[0] - ry;
+          const uint32_t q = step_code(dx, dy);
+          // the decoders take an axis step along the axis of the kind and orientation
+          if (q == WORD_END || (q >= 4u && (dy != 0) != step_axis_y(kind, rx))) st |= ST_INVARIANT;
+          else sd = (uint8_t)q;
+        }
         if (n == 2) sd = SUCC_TWO;
         if (n == 1 && in_tile(ox[0], oy[0])) {
           nx = (uint32_t)((((oy[0] >> 1) - ty0) * TX + ((ox[0] >> 1) - tx0)) << 1) | (uint32_t)(oy[0] & 1);
           active = 1;
         }
       }
-      nextd[succ_idx(g, rx, ry)] = succ;
       S.sd[sl] = sd;
     } else {
       S.sd[sl] = SUCC_NONE;
     }
     S.nv[sl] = (nx << 16) | 1u;
     S.tail[sl] = (uint16_t)sl;
+  }
+  __syncthreads();
+  // successor words: the next WORD_STEPS steps of each edge's chain inside the
+  // tile, from the successor pointers before the ranking rounds replace them;
+  // WORD_ILP slots per thread step together so that their loads overlap
+  constexpr int WORD_ILP = 4;
+  static_assert(HOP_SLOTS % (WORD_ILP * HOP_THREADS) == 0, "word pass covers the slots exactly");
+  for (int base = threadIdx.x; base < HOP_SLOTS; base += WORD_ILP * HOP_THREADS) {
+    int s[WORD_ILP], k[WORD_ILP];
+    uint32_t w[WORD_ILP];
+    bool on[WORD_ILP];
+#pragma unroll
+    for (int j = 0; j < WORD_ILP; ++j) { s[j] = base + j * HOP_THREADS; k[j] = 0; w[j] = 0; on[j] = true; }
+#pragma unroll
+    for (int t = 0; t < WORD_STEPS; ++t) {
+#pragma unroll
+      for (int j = 0; j < WORD_ILP; ++j) {
+        if (!on[j]) continue;
+        const uint32_t q = S.sd[s[j]];
+        const uint32_t n = S.nv[s[j]] >> 16;
+        if (q >= SUCC_TWO) { on[j] = false; continue; }
+        w[j] |= q << (3 * k[j]);
+        ++k[j];
+        if (n == SLOT_NIL) on[j] = false;  // the step left the tile, or the chain ends after it
+        else s[j] = (int)n;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < WORD_ILP; ++j) {
+      int rx, ry;
+      if (!slot_cell(base + j * HOP_THREADS, rx, ry)) continue;
+      if (k[j] < WORD_STEPS) w[j] |= WORD_END << (3 * k[j]);
+      wcode[succ_idx(g, rx, ry)] = (uint16_t)w[j];
+    }
   }
   // list ranking: at most 13 rounds (2^13 = HOP_SLOTS cells); after round
   // SEG_LOG every pointer still inside the tile is exactly SEG_MAX cells ahead
@@ -466,7 +549,7 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict
   }
   __syncthreads();
   for (int sl = threadIdx.x; sl < HOP_SLOTS; sl += blockDim.x) {
-    int rx, ry, ox[2], oy[2];
+    int rx, ry;
     if (!slot_cell(sl, rx, ry)) continue;
     const uint32_t e = edge_id(g, rx, ry);
     const uint32_t v = S.nv[sl];
@@ -477,9 +560,9 @@ k_disc_hops(GridGeom g, const uint32_t *__restrict__ codes, uint32_t *__restrict
     if (sd < SUCC_TWO) {  // the run leaves the tile after its tail
       int tx, ty;
       slot_cell(tl, tx, ty);
-      ox[0] = tx + (int)(sd % 5) - 2;
-      oy[0] = ty + (int)(sd / 5) - 2;
-      dst = edge_id(g, ox[0], oy[0]);
+      const int kind = chain_kind(code(tx, ty), tx, ty);
+      step_apply(sd, step_axis_y(kind, tx), tx, ty);
+      dst = edge_id(g, tx, ty);
     }
     to[e] = dst;
     // a cell with two successors ends no chain: length 0 marks it for the walkers
@@ -493,7 +576,8 @@ struct ChainArgs {
   const uint32_t *hop_to;
   const uint16_t *hop_len;
   const uint32_t *jseg;
-  const uint8_t *nextd;   // per edge: its chain successor as a cell offset (SUCC_NONE if none)
+  const uint16_t *wcode;  // per edge (at succ_idx): its successor word
+  int kind;               // the chains' kind (0 asc, 1 des)
   uint32_t *kc;         // per cp: chains of a saddle handled here (0 otherwise)
   uint32_t *mc;         // per cp: level-0 items
   uint8_t *big;         // per cp: surviving saddle with more than KMAX chains
@@ -615,14 +699,22 @@ __global__ void k_chain_segs(long long nchains, DiscArgs a, ChainArgs c) {
         if (done < l) {  // the next piece's first edge, w cells ahead in the run
           if (w == (uint32_t)SEG_MAX) {
             x = c.jseg[x];
-          } else {
+          } else {  // w steps along the successor words
             int rx, ry;
             edge_cell(g, x, rx, ry);
-            for (uint32_t i = 0; i < w && ok; ++i) {
-              const uint32_t d = c.nextd[succ_idx(g, rx, ry)];
-              if (d >= SUCC_TWO) { ok = false; break; }
-              rx += (int)(d % 5) - 2;
-              ry += (int)(d / 5) - 2;
+            bool ax = step_axis_y(c.kind, rx);
+            uint32_t word = WORD_END;
+            for (uint32_t i = 0; i < w; ++i) {
+              uint32_t q = word & 7u;
+              if (q == WORD_END) {
+                if (!word_cell_ok(g, rx, ry)) { ok = false; break; }
+                word = word_bits(c.wcode[succ_idx(g, rx, ry)]);
+                q = word & 7u;
+                if (q > 5u) { ok = false; break; }
+              }
+              word >>= 3;
+              step_apply(q, ax, rx, ry);
+              ax ^= q < 4u;
             }
             x = edge_id(g, rx, ry);
           }
@@ -678,44 +770,109 @@ __global__ void k_zip_blocks(DiscArgs a, ChainArgs c, const uint32_t *off) {
   }
 }
 
-// Pieces of at most SEG_MAX cells of one chain, stored straight at their
-// places in the disc.  A piece's cells are `alive` positions apart from its
-// first position (k_chain_segs), so a thread follows the 1-byte successor
-// offsets of the piece (read through the 8x8-vertex blocked layout of
-// succ_idx) and stores each cell as it reaches it; a successor code d is a
-// fixed packed cell id delta (a shared-memory table).  One piece per thread:
-// the walk is bound by the latency of its dependent loads, which more
-// resident threads hide better than more pieces per thread (measured).
-__global__ void __launch_bounds__(256) k_seg_place(DiscArgs a, ChainArgs c, long long nsegs, uint32_t *out,
-                                                   unsigned long long out_len) {
-  __shared__ int dcell[25];  // packed cell id delta of successor code d
+// Placement of the pieces' cells, one window of WIN disc positions per block.
+// A piece's cells are `alive` positions apart from its first position
+// (k_chain_segs).  Stored straight from the walking threads, every cell is a
+// separate 4-byte store to a different sector; instead, the block walks every
+// piece that has a cell inside its window (following the successor words,
+// one load per WORD_STEPS cells), puts the window's cells into shared memory
+// and stores the window out with 16-byte stores.  Positions of the window
+// that no piece fills (level-0 items, saddles with many chains, extremum
+// discs: other kernels write them) are left alone.  Discs are laid out in
+// critical-point order, so the pieces that reach a window are those of the
+// critical points from the one whose disc holds the window's first position
+// (k_win_first) to the one whose disc holds the next window's first position.
+constexpr int WIN = 4096, WIN_THREADS = 256;
+constexpr uint32_t WIN_EMPTY = 0xFFFFFFFFu;  // no packed cell id (coordinates are below 2^15)
+
+// first[w]: the critical point whose disc holds position w * WIN
+__global__ void k_win_first(uint32_t ncp, const uint32_t *__restrict__ off, uint32_t nwin, uint32_t *__restrict__ first) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < ncp; s += gridDim.x * blockDim.x) {
+    const unsigned long long a = off[s], b = off[s + 1];
+    if (b <= a) continue;
+    const unsigned long long w1 = (b - 1) / WIN;
+    for (unsigned long long w = (a + WIN - 1) / WIN; w <= w1 && w < nwin; ++w) first[w] = s;
+  }
+}
+
+__global__ void __launch_bounds__(WIN_THREADS) k_win_place(DiscArgs a, ChainArgs c, const uint32_t *__restrict__ first,
+                                                           uint32_t nwin, uint32_t *__restrict__ out,
+                                                           unsigned long long out_len) {
+  __shared__ __align__(16) uint32_t stage[WIN];
+  __shared__ uint32_t range[2];
   const GridGeom &g = a.g;
-  if (threadIdx.x < 25) dcell[threadIdx.x] = ((int)threadIdx.x / 5 - 2) * 65536 + ((int)threadIdx.x % 5 - 2);
-  __syncthreads();
   uint32_t st = 0;
-  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nsegs; k += (long long)gridDim.x * blockDim.x) {
-    const uint4 sg = c.segs[k];
-    const uint32_t w = sg.z & 0xffu, na = sg.z >> 8;
-    uint32_t pos = sg.y;
-    if (!w) continue;  // an unused slot
-    if (w > (uint32_t)SEG_MAX || na == 0 || na > (uint32_t)KMAX ||
-        (unsigned long long)pos + (unsigned long long)(w - 1) * na >= out_len) {
-      st |= ST_INVARIANT;
-      continue;
+  for (uint32_t w = blockIdx.x; w < nwin; w += gridDim.x) {
+    const unsigned long long P0 = (unsigned long long)w * WIN;
+    const unsigned long long P1 = P0 + WIN < out_len ? P0 + WIN : out_len;
+    for (int i = threadIdx.x; i < WIN; i += blockDim.x) stage[i] = WIN_EMPTY;
+    if (threadIdx.x == 0) {
+      const uint32_t sa = first[w], sb = w + 1 < nwin ? first[w + 1] : a.ncp - 1;
+      uint32_t lo = 0, hi = 0;
+      if (sa <= sb && sb < a.ncp) {
+        lo = c.csegoff[c.cbase[sa]];
+        hi = c.csegoff[c.cbase[sb + 1]];
+      } else {
+        st |= ST_INVARIANT;
+      }
+      range[0] = lo;
+      range[1] = hi;
     }
-    int rx, ry;
-    edge_cell(g, sg.x, rx, ry);
-    uint32_t cell = pack_cellid(g.ex0 + rx, g.ey0 + ry);
-    for (uint32_t i = 0;; ++i) {
-      const uint32_t d = i + 1 < w ? __ldg(c.nextd + succ_idx(g, rx, ry)) : 0u;  // the load first, then the store
-      __stcs(out + pos, cell);  // streaming: the disc is not read again here
-      if (i + 1 >= w) break;
-      pos += na;
-      if (d >= 25u) { st |= ST_INVARIANT; break; }
-      cell += (uint32_t)dcell[d];
-      rx = (int)(cell & 0xffffu) - g.ex0;
-      ry = (int)(cell >> 16) - g.ey0;
+    __syncthreads();
+    const uint32_t lo = range[0], hi = range[1];
+    for (uint32_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+      const uint4 sg = c.segs[k];
+      const uint32_t wl = sg.z & 0xffu, na = sg.z >> 8;
+      if (!wl) continue;  // an unused slot
+      unsigned long long pos = sg.y;
+      const unsigned long long last = pos + (unsigned long long)(wl - 1) * na;
+      if (wl > (uint32_t)SEG_MAX || na == 0 || na > (uint32_t)KMAX || last >= out_len) {
+        st |= ST_INVARIANT;
+        continue;
+      }
+      if (pos >= P1 || last < P0) continue;  // no cell in this window
+      int rx, ry;
+      edge_cell(g, sg.x, rx, ry);
+      if (!word_cell_ok(g, rx, ry)) {
+        st |= ST_INVARIANT;
+        continue;
+      }
+      uint32_t cell = pack_cellid(g.ex0 + rx, g.ey0 + ry);
+      bool ax = step_axis_y(c.kind, rx);
+      uint32_t word = wl > 1 ? word_bits(__ldg(c.wcode + succ_idx(g, rx, ry))) : WORD_END;
+      for (uint32_t i = 0;; ++i) {
+        if (pos >= P0) stage[pos - P0] = cell;
+        if (i + 1 >= wl || pos + na >= P1) break;
+        pos += na;
+        uint32_t q = word & 7u;
+        if (q == WORD_END) {  // the word is used up (or ended at a tile exit): the current cell's word
+          rx = (int)(cell & 0xffffu) - g.ex0;
+          ry = (int)(cell >> 16) - g.ey0;
+          if (!word_cell_ok(g, rx, ry)) { st |= ST_INVARIANT; break; }
+          word = word_bits(__ldg(c.wcode + succ_idx(g, rx, ry)));
+          q = word & 7u;
+          if (q > 5u) { st |= ST_INVARIANT; break; }
+        }
+        word >>= 3;
+        cell += step_delta(q, ax);
+        ax ^= q < 4u;
+      }
     }
+    __syncthreads();
+    // the window out: four positions per thread, one 16-byte store where all four are filled
+    const int nw = (int)(P1 - P0);
+    for (int i = 4 * threadIdx.x; i < nw; i += 4 * blockDim.x) {
+      const uint4 v = *reinterpret_cast<const uint4 *>(stage + i);
+      if (i + 4 <= nw && v.x != WIN_EMPTY && v.y != WIN_EMPTY && v.z != WIN_EMPTY && v.w != WIN_EMPTY) {
+        __stcs(reinterpret_cast<uint4 *>(out + P0 + i), v);
+      } else {
+        const uint32_t e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (i + q < nw && e[q] != WIN_EMPTY) __stcs(out + P0 + i + q, e[q]);
+      }
+    }
+    __syncthreads();  // the stage is refilled for the next window
   }
   if (st) atomicOr(a.status, st);
 }
@@ -880,7 +1037,7 @@ struct DiscShared {
   int gw[2];
   uint32_t *redir, *hop_to, *jseg, *gkey[2], *gval[2];
   uint16_t *hop_len;
-  uint8_t *nextd;
+  uint16_t *wcode;
 };
 
 // One disc kind (0 asc, 1 des) as a sequence of stages on its own stream;
@@ -896,7 +1053,7 @@ struct DiscKind {
   uint32_t *key = nullptr, *val = nullptr, *kt = nullptr, *vt = nullptr, *kc = nullptr, *mc = nullptr, *cbase = nullptr;
   uint8_t *big = nullptr;
   uint32_t *hbuf = nullptr;  // pinned host counts: [0] runs, [1] seeds, [2] chains, [3..5] totals
-  uint32_t *runbuf = nullptr, *chain_buf = nullptr;
+  uint32_t *runbuf = nullptr, *chain_buf = nullptr, *wfirst_buf = nullptr;
   uint4 *segs = nullptr, *blocks = nullptr;
   uint32_t *rp = nullptr, *rstart = nullptr;
   uint32_t nrun = 0, ns = 0, nch = 0, tot[2] = {0, 0};
@@ -910,7 +1067,8 @@ struct DiscKind {
     if (blocks) cudaFreeAsync(blocks, st);
     if (chain_buf) cudaFreeAsync(chain_buf, st);
     if (runbuf) cudaFreeAsync(runbuf, st);
-    segs = nullptr; blocks = nullptr; chain_buf = nullptr; runbuf = nullptr;
+    if (wfirst_buf) cudaFreeAsync(wfirst_buf, st);
+    segs = nullptr; blocks = nullptr; chain_buf = nullptr; runbuf = nullptr; wfirst_buf = nullptr;
   }
   // Runs the next stage; returns true while more stages remain (the caller
   // synchronises the stream before the next one).
@@ -982,7 +1140,7 @@ struct DiscKind {
           k_run_len<<<nb(ns), 256, 0, st>>>(ns, (uint32_t)ncp, key, sstart, scount, 0);
           DMSC_LAUNCHED(2);
         }
-        c.hop_to = S.hop_to; c.hop_len = S.hop_len; c.jseg = S.jseg; c.nextd = S.nextd;
+        c.hop_to = S.hop_to; c.hop_len = S.hop_len; c.jseg = S.jseg; c.wcode = S.wcode; c.kind = kind;
         c.kc = kc; c.mc = mc; c.big = big; c.cbase = cbase; c.limit = io.limit;
         k_chain_count<<<nb(ncp), 128, 0, st>>>(a, kind, SeedRuns{val, sstart, scount}, c);
         DMSC_LAUNCHED(1);
@@ -1040,9 +1198,18 @@ struct DiscKind {
           DMSC_LAUNCHED(1);
         }
         if (S.io->ev_place[kind][0]) L(cudaEventRecord(S.io->ev_place[kind][0], st));
-        if (tot[1]) {
-          k_seg_place<<<nb(tot[1]), 256, 0, st>>>(a, c, tot[1], ob->p, (unsigned long long)tot[0]);
-          DMSC_LAUNCHED(1);
+        if (tot[1] && tot[0]) {
+          const uint32_t nwin = (uint32_t)(((unsigned long long)tot[0] + WIN - 1) / WIN);
+          // the window starts reuse the per-saddle disc lengths (slen, ncp words, read
+          // by no later kernel); a complex with fewer critical points than windows allocates
+          uint32_t *wfirst = nwin <= (uint32_t)ncp ? slen : nullptr;
+          if (!wfirst) L(cudaMallocAsync((void **)&wfirst_buf, sizeof(uint32_t) * nwin, st));
+          if (e != cudaSuccess) return false;
+          if (!wfirst) wfirst = wfirst_buf;
+          k_win_first<<<nb(ncp), 256, 0, st>>>((uint32_t)ncp, offs, nwin, wfirst);
+          k_win_place<<<std::min<uint32_t>(nwin, 152u * 8u), WIN_THREADS, 0, st>>>(a, c, wfirst, nwin, ob->p,
+                                                                                  (unsigned long long)tot[0]);
+          DMSC_LAUNCHED(2);
         }
         k_level0<<<nb(ncp), 128, 0, st>>>(a, kind, sr, c, offs, ob->p);
         k_saddle_disc_write<<<nb(ncp), 128, 0, st>>>(a, kind, sr, big, offs, ob->p);
@@ -1080,11 +1247,11 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   S.gw[0] = (g.rx1 - g.rx0) / 2 + 1; S.gw[1] = (g.rx1 - g.rx0) / 2;
   const long long nE = 2ll * g.vnx * g.vny;  // edge ids of the ext window
   const bool seeds = !io.no_cancel;
-  // shared words: redir (ncp) | owner keys and run ids 2 (nV + nF) | hops 2.75 nE
+  // shared words: redir (ncp) | owner keys and run ids 2 (nV + nF) | hops 3 nE
   // per kind: cnt slen sstart scount (4 ncp) soff (ncp + 8) kc mc cbase (3 ncp + 1) big (ncp / 4 + 1)
   //           seed sort 4 nmax (only with seeds) | pinned counts
   const size_t kwords = (size_t)ncp * 8 + 16 + (size_t)ncp / 4 + 1 + (seeds ? 4 * (size_t)nmax : 0);
-  size_t words = (size_t)ncp + 8 + (size_t)(nV + nF) * 2 + 2 * (size_t)nE + (size_t)nE / 2 + succ_bytes(g) / 4 + 64 +
+  size_t words = (size_t)ncp + 8 + (size_t)(nV + nF) * 2 + 2 * (size_t)nE + (size_t)nE / 2 + succ_words(g) / 2 + 64 +
                  2 * kwords;
   uint32_t *buf = nullptr;
   cudaError_t e = hops_attr();
@@ -1101,7 +1268,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   S.hop_to = p; p += nE;
   S.jseg = p; p += nE;
   S.hop_len = (uint16_t *)p; p += nE / 2 + 1;
-  S.nextd = (uint8_t *)p; p += succ_bytes(g) / 4 + 1;
+  S.wcode = (uint16_t *)p; p += succ_words(g) / 2 + 1;
   DiscKind K[2];
   for (int k = 0; k < 2; ++k) {
     DiscKind &D = K[k];
@@ -1136,7 +1303,7 @@ cudaError_t fill_discs(DiscIO &io, cudaStream_t st) {
   }
   if (io.ev_hops[0]) L(cudaEventRecord(io.ev_hops[0], st));
   k_disc_hops<<<dim3(g.ntx, g.nty), HOP_THREADS, sizeof(HopSmem), st>>>(g, io.codes, S.hop_to, S.hop_len, S.jseg,
-                                                                        S.nextd, io.status);
+                                                                        S.wcode, io.status);
   DMSC_LAUNCHED(1);
   if (io.ev_hops[1]) L(cudaEventRecord(io.ev_hops[1], st));
   // extremum discs: vertices -> minima (asc_disc), faces -> maxima (des_disc),

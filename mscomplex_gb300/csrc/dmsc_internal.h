@@ -155,7 +155,7 @@ struct DiscIO {
   uint32_t *status = nullptr;
   unsigned long long limit = 1ull << 31;  // bound on one gradient chain (cells of the window)
   cudaEvent_t ev_hops[2] = {nullptr, nullptr};  // recorded around the hop kernel when set
-  cudaEvent_t ev_place[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // around k_seg_place, per kind, when set
+  cudaEvent_t ev_place[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // around the saddle-disc placement, per kind, when set
   bool no_cancel = false;  // the complex has no boundary-cancelable critical point
   long long nadisc = 0, nddisc = 0;
   // the des discs run on `aux` beside the asc discs on the caller's stream;
