@@ -782,7 +782,7 @@ __global__ void k_zip_blocks(DiscArgs a, ChainArgs c, const uint32_t *off) {
 // critical-point order, so the pieces that reach a window are those of the
 // critical points from the one whose disc holds the window's first position
 // (k_win_first) to the one whose disc holds the next window's first position.
-constexpr int WIN = 4096, WIN_THREADS = 256;
+constexpr int WIN = 8192, WIN_THREADS = 256;
 constexpr uint32_t WIN_EMPTY = 0xFFFFFFFFu;  // no packed cell id (coordinates are below 2^15)
 
 // first[w]: the critical point whose disc holds position w * WIN
