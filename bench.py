@@ -51,7 +51,8 @@ SIMPLIFY_HEAP_OPS = 2956808816 + 2954259461
 KERNEL_BYTES = {
     "gradient": (8.0, 0, 0, 0, 0),        # k_gradient: 4 B height read + 4 B gradient codes (1 B per cell)
     "labels_arcs": (16.0, 12, 8, 0, 0),   # k_labels: 16 B owner labels (4 B per cell), cp records, arcs
-    "disc_hops": (0.0, 0, 0, 0, 0),       # k_disc_hops: writes only the hop structure (intermediate)
+    "disc_hops": (4.0, 0, 0, 0, 0),       # k_disc_hops: reads the gradient codes (4 B/vertex); writes only the
+                                          # hop structure and successor words (intermediates, not counted)
     # the saddle discs of one kind: k_win_place (and the level-0 items and the discs of saddles with many
     # chains); 4 B per saddle disc cell written
     "seg_place_asc": (0.0, 0, 0, 4, 0),
