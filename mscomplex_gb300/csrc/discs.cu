@@ -800,12 +800,18 @@ __global__ void __launch_bounds__(WIN_THREADS) k_win_place(DiscArgs a, ChainArgs
                                                            unsigned long long out_len) {
   __shared__ __align__(16) uint32_t stage[WIN];
   __shared__ uint32_t range[2];
+  __shared__ int dtab[16];  // packed cell id delta of step code q: [8 * (axis y) + q]
   const GridGeom &g = a.g;
+  if (threadIdx.x < 16) {
+    const uint32_t q = threadIdx.x & 7u;
+    dtab[threadIdx.x] = q <= 5u ? (int)step_delta(q, threadIdx.x >= 8) : 0;
+  }
   uint32_t st = 0;
   for (uint32_t w = blockIdx.x; w < nwin; w += gridDim.x) {
     const unsigned long long P0 = (unsigned long long)w * WIN;
     const unsigned long long P1 = P0 + WIN < out_len ? P0 + WIN : out_len;
-    for (int i = threadIdx.x; i < WIN; i += blockDim.x) stage[i] = WIN_EMPTY;
+    for (int i = threadIdx.x; i < WIN / 4; i += blockDim.x)
+      reinterpret_cast<uint4 *>(stage)[i] = make_uint4(WIN_EMPTY, WIN_EMPTY, WIN_EMPTY, WIN_EMPTY);
     if (threadIdx.x == 0) {
       const uint32_t sa = first[w], sb = w + 1 < nwin ? first[w + 1] : a.ncp - 1;
       uint32_t lo = 0, hi = 0;
@@ -838,25 +844,36 @@ __global__ void __launch_bounds__(WIN_THREADS) k_win_place(DiscArgs a, ChainArgs
         continue;
       }
       uint32_t cell = pack_cellid(g.ex0 + rx, g.ey0 + ry);
-      bool ax = step_axis_y(c.kind, rx);
+      uint32_t axb = step_axis_y(c.kind, rx) ? 8u : 0u;
       uint32_t word = wl > 1 ? word_bits(__ldg(c.wcode + succ_idx(g, rx, ry))) : WORD_END;
-      for (uint32_t i = 0;; ++i) {
-        if (pos >= P0) stage[pos - P0] = cell;
-        if (i + 1 >= wl || pos + na >= P1) break;
-        pos += na;
+      uint32_t left = wl - 1;  // steps after the current cell
+      uint32_t p = (uint32_t)pos;
+      const uint32_t p0 = (uint32_t)P0, p1 = (uint32_t)P1;
+      auto advance = [&]() -> bool {  // one step along the successor words
         uint32_t q = word & 7u;
         if (q == WORD_END) {  // the word is used up (or ended at a tile exit): the current cell's word
           rx = (int)(cell & 0xffffu) - g.ex0;
           ry = (int)(cell >> 16) - g.ey0;
-          if (!word_cell_ok(g, rx, ry)) { st |= ST_INVARIANT; break; }
+          if (!word_cell_ok(g, rx, ry)) return false;
           word = word_bits(__ldg(c.wcode + succ_idx(g, rx, ry)));
           q = word & 7u;
-          if (q > 5u) { st |= ST_INVARIANT; break; }
+          if (q > 5u) return false;
         }
         word >>= 3;
-        cell += step_delta(q, ax);
-        ax ^= q < 4u;
+        cell += (uint32_t)dtab[axb | q];
+        axb ^= q < 4u ? 8u : 0u;
+        p += na;
+        --left;
+        return true;
+      };
+      bool ok = true;
+      while (ok && p < p0) ok = advance();  // cells before the window: walked, not stored
+      while (ok) {
+        stage[p - p0] = cell;
+        if (left == 0 || p + na >= p1) break;
+        ok = advance();
       }
+      if (!ok) st |= ST_INVARIANT;
     }
     __syncthreads();
     // the window out: four positions per thread, one 16-byte store where all four are filled

@@ -573,7 +573,9 @@ static unsigned grid_for(long long n, int threads) {
 // not depend on the claim order).  Segments of up to SEG_THREAD items are
 // sorted by one thread, up to SEG_BLOCK by one block in shared memory; a
 // longer one sets ST_CAPACITY and the caller falls back to the radix path.
-constexpr uint32_t SEG_THREAD = 32, SEG_BLOCK = 8192;
+// Segments of up to SEG_WARP items are sorted by one warp, taken from a queue
+// with an atomic counter, so that a few long segments do not hold the rest.
+constexpr uint32_t SEG_THREAD = 32, SEG_WARP = 256, SEG_BLOCK = 8192;
 
 __global__ void k_ext_scatter(long long ncp, const uint32_t *__restrict__ cellid, const uint32_t *__restrict__ des2,
                               const uint32_t *__restrict__ asc2, const uint32_t *__restrict__ aoff,
@@ -615,10 +617,12 @@ __global__ void k_saddle_lists(long long ncp, const uint32_t *__restrict__ celli
   }
 }
 
-// short extremum segments: insertion sort by one thread; longer ones queued
+// short extremum segments: insertion sort by one thread; longer ones queued,
+// up to SEG_WARP items in midq, longer in longq
 __global__ void k_seg_sort(long long ncp, const uint32_t *__restrict__ cellid, const uint32_t *__restrict__ aoff,
                            const uint32_t *__restrict__ doff, uint32_t *__restrict__ asc, uint32_t *__restrict__ des,
-                           uint32_t *__restrict__ longq, uint32_t *__restrict__ nlong, uint32_t *__restrict__ status) {
+                           uint32_t *__restrict__ midq, uint32_t *__restrict__ nmid, uint32_t *__restrict__ longq,
+                           uint32_t *__restrict__ nlong, uint32_t *__restrict__ status) {
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < ncp; k += (long long)gridDim.x * blockDim.x) {
     const int dim = cell_dim(cellid[k]);
     if (dim == 1) continue;
@@ -627,7 +631,8 @@ __global__ void k_seg_sort(long long ncp, const uint32_t *__restrict__ cellid, c
     if (n <= 1) continue;
     if (n > SEG_THREAD) {
       if (n > SEG_BLOCK) { atomicOr(status, ST_CAPACITY); continue; }
-      longq[atomicAdd(nlong, 1u)] = (uint32_t)k;
+      if (n <= SEG_WARP) midq[atomicAdd(nmid, 1u)] = (uint32_t)k;
+      else longq[atomicAdd(nlong, 1u)] = (uint32_t)k;
       continue;
     }
     uint32_t v[SEG_THREAD];
@@ -639,6 +644,46 @@ __global__ void k_seg_sort(long long ncp, const uint32_t *__restrict__ cellid, c
       v[j] = x;
     }
     for (uint32_t i = 0; i < n; ++i) seg[i] = v[i];
+  }
+}
+
+// queued segments of up to SEG_WARP items: one warp each, taken in turn from
+// the queue; each item's place is the count of items before it (value, then
+// position, so equal saddle indices keep distinct places)
+constexpr int SEG_WARP_THREADS = 256;
+__global__ void __launch_bounds__(SEG_WARP_THREADS) k_seg_sort_warp(const uint32_t *__restrict__ cellid,
+                                                                    const uint32_t *__restrict__ aoff,
+                                                                    const uint32_t *__restrict__ doff,
+                                                                    uint32_t *__restrict__ asc, uint32_t *__restrict__ des,
+                                                                    const uint32_t *__restrict__ midq,
+                                                                    const uint32_t *__restrict__ nmid,
+                                                                    uint32_t *__restrict__ taken) {
+  __shared__ uint32_t sh[SEG_WARP_THREADS / 32][SEG_WARP];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t *buf = sh[wid];
+  const uint32_t nq = *nmid;
+  for (;;) {
+    uint32_t q = 0;
+    if (lane == 0) q = atomicAdd(taken, 1u);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    if (q >= nq) break;
+    const uint32_t k = midq[q];
+    const int dim = cell_dim(cellid[k]);
+    uint32_t *seg = dim == 0 ? asc + aoff[k] : des + doff[k];
+    const uint32_t n = dim == 0 ? aoff[k + 1] - aoff[k] : doff[k + 1] - doff[k];
+    if (n > SEG_WARP) continue;  // queued by size: cannot happen
+    for (uint32_t i = lane; i < n; i += 32) buf[i] = seg[i];
+    __syncwarp();
+    for (uint32_t i = lane; i < n; i += 32) {
+      const uint32_t v = buf[i];
+      uint32_t r = 0;
+      for (uint32_t j = 0; j < n; ++j) {
+        const uint32_t u = buf[j];
+        r += (u < v) || (u == v && j < i);
+      }
+      seg[r] = v;
+    }
+    __syncwarp();
   }
 }
 
@@ -695,18 +740,20 @@ cudaError_t build_csr(long long ncp, const uint32_t *cellid, const uint32_t *des
                       uint32_t *status, cudaStream_t st) {
   if (ncp <= 0) return cudaSuccess;
   uint32_t *buf = nullptr;
-  cudaError_t e = cudaMallocAsync((void **)&buf, sizeof(uint32_t) * (3 * ncp + 8), st);
+  cudaError_t e = cudaMallocAsync((void **)&buf, sizeof(uint32_t) * (4 * ncp + 8), st);
   if (e != cudaSuccess) return e;
-  uint32_t *afill = buf, *dfill = buf + ncp, *longq = buf + 2 * ncp, *nlong = buf + 3 * ncp;
-  e = cudaMemsetAsync(afill, 0, sizeof(uint32_t) * 2 * ncp, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(nlong, 0, sizeof(uint32_t), st);
+  // afill dfill (2 ncp) | nlong nmid taken (3) | longq midq (2 ncp)
+  uint32_t *afill = buf, *dfill = buf + ncp, *nlong = buf + 2 * ncp, *nmid = nlong + 1, *taken = nlong + 2;
+  uint32_t *longq = buf + 2 * ncp + 8, *midq = longq + ncp;
+  e = cudaMemsetAsync(afill, 0, sizeof(uint32_t) * (2 * ncp + 8), st);
   if (e == cudaSuccess) {
     (void)out_cap;  // every write is bounded by its own segment of aoff/doff
     k_saddle_lists<<<grid_for(ncp, 256), 256, 0, st>>>(ncp, cellid, des2, asc2, aoff, doff, asc, des);
     k_ext_scatter<<<grid_for(ncp, 256), 256, 0, st>>>(ncp, cellid, des2, asc2, aoff, doff, asc, des, afill, dfill, status);
-    k_seg_sort<<<grid_for(ncp, 128), 128, 0, st>>>(ncp, cellid, aoff, doff, asc, des, longq, nlong, status);
+    k_seg_sort<<<grid_for(ncp, 128), 128, 0, st>>>(ncp, cellid, aoff, doff, asc, des, midq, nmid, longq, nlong, status);
+    k_seg_sort_warp<<<152 * 4, SEG_WARP_THREADS, 0, st>>>(cellid, aoff, doff, asc, des, midq, nmid, taken);
     k_seg_sort_block<<<152 * 2, 512, 0, st>>>(cellid, aoff, doff, asc, des, longq, nlong);
-    DMSC_LAUNCHED(4);
+    DMSC_LAUNCHED(5);
     e = cudaGetLastError();
   }
   cudaFreeAsync(buf, st);
