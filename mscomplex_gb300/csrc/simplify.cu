@@ -24,6 +24,7 @@
 #include "msc_graph.cuh"
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 namespace dmsc {
@@ -50,6 +51,43 @@ __host__ __device__ __forceinline__ float fsub_rn(float a, float b) {
   volatile float r = a - b;
   return r;
 #endif
+}
+
+__host__ __device__ __forceinline__ float bits_float(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+__host__ __device__ __forceinline__ uint32_t float_bits(float f) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(f);
+#else
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return u;
+#endif
+}
+// The loop stops at the first pair with (double)d / (double)max_persistence >
+// tresh (grid_mscomplex.cpp:446-447).  A correctly rounded division by a
+// fixed divisor is monotone in d, so over the persistences (non-negative,
+// finite floats, whose bit patterns order like their values) the test is
+// true exactly from one bit pattern on.  That pattern is found once here, by
+// bisection with the same double-precision test, and each pop compares bits:
+// the same outcome for every d, without a double division per pop (double
+// precision is slow on this part).  Returns 0x7F800001 if no finite d passes.
+__host__ __device__ inline uint32_t stop_bits(float max_persistence, double tresh) {
+  auto over = [&](uint32_t u) { return (double)bits_float(u) / (double)max_persistence > tresh; };
+  uint32_t lo = 0, hi = 0x7F800001u;  // the first passing pattern lies in [lo, hi]
+  while (lo < hi) {
+    const uint32_t mid = lo + (hi - lo) / 2;
+    if (over(mid)) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
 }
 
 struct SimpArgs {
@@ -114,19 +152,30 @@ struct Simp {
 
   // ---- heap (binary heap of the standard library, comparator d1 > d2) ----
   __host__ __device__ __forceinline__ static bool comp(const HeapEnt &x, const HeapEnt &y) { return x.d > y.d; }
-  __host__ __device__ void push_at(unsigned long long hole, unsigned long long topi, HeapEnt val) {
-    unsigned long long parent = (hole - 1) / 2;
-    while (hole > topi && comp(H(parent), val)) {
-      H(hole) = H(parent);
+  // __push_heap from position hole up to the root: the hole climbs while its
+  // parent is larger (comparator d1 > d2) -- in global memory while the hole
+  // is there, then in shared memory with 32-bit indices
+  __host__ __device__ void push_at(unsigned long long hole, HeapEnt val) {
+    while (hole >= ntop && hole > 0) {
+      const unsigned long long parent = (hole - 1) / 2;
+      const HeapEnt pe = H(parent);
+      if (!comp(pe, val)) { H(hole) = val; return; }
+      H(hole) = pe;
       hole = parent;
-      parent = (hole - 1) / 2;
     }
-    H(hole) = val;
+    if (hole >= ntop) { H(hole) = val; return; }  // the root itself is in global memory (no shared part)
+    uint32_t h = (uint32_t)hole;
+    while (h > 0) {
+      const uint32_t parent = (h - 1) >> 1;
+      if (!(top[parent].d > val.d)) break;
+      top[h] = top[parent];
+      h = parent;
+    }
+    top[h] = val;
   }
   __host__ __device__ void push_ent(const HeapEnt &x) {
     if (nheap >= A.heap_cap) { A.G.fail = true; return; }
-    H(nheap) = x;
-    push_at(nheap, 0, x);
+    push_at(nheap, x);
     ++nheap;
     ++n_push;
   }
@@ -167,29 +216,32 @@ struct Simp {
     float pkey[PMAX];
     int np = 0;
     {
-      unsigned long long h = 0;
+      // 32-bit indices: every index here is below ntop (at most HEAP_TOP); len
+      // is clamped, which keeps each comparison with it exact
+      const uint32_t nt = (uint32_t)ntop, ln = len > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)len;
+      uint32_t h = 0;
 #pragma unroll
       for (int q = 0; q < PMAX; q += 2) {
-        const unsigned long long l = 2 * h + 1;
-        if (l >= len || l + 1 >= ntop) break;
-        const unsigned long long ll = 2 * l + 1, rl = ll + 2;  // first child of l and of l + 1
-        const bool g_ok = rl + 1 < ntop;                      // all four grandchildren in `top`
-        const float dl = top[l].d, dr = l + 1 < len ? top[l + 1].d : 0.0f;
+        const uint32_t l = 2 * h + 1;
+        if (l >= ln || l + 1 >= nt) break;
+        const uint32_t ll = 2 * l + 1, rl = ll + 2;  // first child of l and of l + 1
+        const bool g_ok = rl + 1 < nt;              // all four grandchildren in `top`
+        const float dl = top[l].d, dr = l + 1 < ln ? top[l + 1].d : 0.0f;
         float g0 = 0, g1 = 0, g2 = 0, g3 = 0;
         if (g_ok) { g0 = top[ll].d; g1 = top[ll + 1].d; g2 = top[rl].d; g3 = top[rl + 1].d; }
-        const bool right = l + 1 < len && !(dr > dl);
-        const unsigned long long c = right ? l + 1 : l;
-        path[q] = (uint32_t)c;
+        const bool right = l + 1 < ln && !(dr > dl);
+        const uint32_t c = right ? l + 1 : l;
+        path[q] = c;
         pkey[q] = right ? dr : dl;
         np = q + 1;
         h = c;
         if (q + 1 >= PMAX || !g_ok) break;
-        const unsigned long long l2 = 2 * c + 1;
-        if (l2 >= len) break;
+        const uint32_t l2 = 2 * c + 1;
+        if (l2 >= ln) break;
         const float el = right ? g2 : g0, er = right ? g3 : g1;
-        const bool right2 = l2 + 1 < len && !(er > el);
-        const unsigned long long c2 = right2 ? l2 + 1 : l2;
-        path[q + 1] = (uint32_t)c2;
+        const bool right2 = l2 + 1 < ln && !(er > el);
+        const uint32_t c2 = right2 ? l2 + 1 : l2;
+        path[q + 1] = c2;
         pkey[q + 1] = right2 ? er : el;
         np = q + 2;
         h = c2;
@@ -199,11 +251,15 @@ struct Simp {
 #pragma unroll
     for (int i = PMAX - 1; i >= 0; --i)
       if (i < np && pkey[i] > val.d) stop = i;
+    {
+      uint32_t hs = 0;  // the hole while it is in shared memory (32-bit)
 #pragma unroll
-    for (int i = 0; i < PMAX; ++i) {
-      if (i >= stop) break;
-      top[hole] = top[path[i]];
-      hole = path[i];
+      for (int i = 0; i < PMAX; ++i) {
+        if (i >= stop) break;
+        top[hs] = top[path[i]];
+        hs = path[i];
+      }
+      hole = hs;
     }
     if (stop < np) {  // the last element lands in shared memory
       top[hole] = val;
@@ -257,6 +313,7 @@ struct Simp {
     }
     for (unsigned long long q = 0; q < A.ninit && !G.fail; ++q) push_ent(A.init[q]);
     const float max_persistence = fsub_rn(max_val, min_val);
+    const uint32_t stop_at = stop_bits(max_persistence, A.tresh);
     while (nheap != 0 && !G.fail) {
       if (!G.tick()) break;
       // the entry on top and its pair's dynamic state (three independent
@@ -270,7 +327,7 @@ struct Simp {
       const uint8_t f1 = inside ? G.flags[v1] : 0, f2 = inside ? G.flags[v2] : 0;
       const uint32_t tot2 = inside ? G.L.total[2 * v2 + cp2_dim / 2] : 0;
       HeapEnt e = pop();
-      if ((double)e.d / (double)max_persistence > A.tresh) break;
+      if (float_bits(e.d) >= stop_at) break;  // (double)e.d / max_persistence > tresh
       if (!inside) { A.stats[4] |= ST_INVARIANT; continue; }  // a list entry outside the complex
       if ((f1 & F_CANCELLED) || (f2 & F_CANCELLED)) continue;
       const bool b1 = ent_boundary(w1), b2 = ent_boundary(w2);
