@@ -252,11 +252,16 @@ struct Simp {
     for (int i = PMAX - 1; i >= 0; --i)
       if (i < np && pkey[i] > val.d) stop = i;
     {
+      // the path's entries first (independent loads), then each one level up
+      HeapEnt mv[PMAX];
+#pragma unroll
+      for (int i = 0; i < PMAX; ++i)
+        if (i < stop) mv[i] = top[path[i]];
       uint32_t hs = 0;  // the hole while it is in shared memory (32-bit)
 #pragma unroll
       for (int i = 0; i < PMAX; ++i) {
         if (i >= stop) break;
-        top[hs] = top[path[i]];
+        top[hs] = mv[i];
         hs = path[i];
       }
       hole = hs;
