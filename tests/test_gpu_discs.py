@@ -43,6 +43,26 @@ def test_discs_quantized_simplified(gpu_lib, oracle):
     check_discs(gpu_lib, oracle, synth.bumps4096q(n=256), 0.01, "bumps256q t=0.01")
 
 
+def _bumps(ny, nx, bumps):
+    y, x = np.mgrid[0:ny, 0:nx].astype(np.float64)
+    f = np.zeros((ny, nx))
+    for cx, cy, s, amp in bumps:
+        f += amp * np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2 * s * s))
+    return f.astype(np.float32)
+
+
+@pytest.mark.parametrize("name,bumps,tresh", [
+    ("one bump", [(140.3, 121.7, 60.0, 1.0)], 0.0),
+    ("two bumps", [(80.3, 121.7, 40.0, 1.0), (220.3, 131.7, 35.0, 0.8)], 0.0),
+    ("two bumps simplified", [(80.3, 121.7, 40.0, 1.0), (220.3, 131.7, 35.0, 0.8)], 0.5),
+])
+def test_discs_few_critical_points(gpu_lib, oracle, name, bumps, tresh):
+    """Smooth 257x301 fields with 9-15 critical points and about 78K cells in each
+    disc array: fewer critical points than 8192-position windows of the saddle
+    placement, and long chains crossing many tiles."""
+    check_discs(gpu_lib, oracle, _bumps(257, 301, bumps), tresh, name)
+
+
 def test_discs_multi_tile(gpu_lib, oracle):
     check_discs(gpu_lib, oracle, smooth_field(150, 133, 9), 0.02, "smooth 150x133 t=0.02")
 

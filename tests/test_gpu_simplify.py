@@ -30,6 +30,17 @@ def test_simplify_ties(gpu_lib, oracle, seed):
     check_simplify(gpu_lib, oracle, f, 0.3, f"ties seed={seed}")
 
 
+@pytest.mark.parametrize("seed", range(2))
+@pytest.mark.parametrize("tresh", [0.25, 0.2499])
+def test_simplify_threshold_on_a_persistence(gpu_lib, oracle, seed, tresh):
+    """Heights on 5 integer levels: persistences are whole numbers and the range
+    is 4, so at tresh 0.25 a pair of persistence 1 sits exactly on the stop test
+    (persistence / range > tresh, strictly) and is still cancelled, while at
+    0.2499 it stops the loop (the oracle cancels 649 / 560 pairs for seed 0)."""
+    f = tie_field(40 + 7 * seed, 50 + 5 * seed, 5, seed)
+    check_simplify(gpu_lib, oracle, f, tresh, f"ties seed={seed} t={tresh}")
+
+
 def test_simplify_bumps256(gpu_lib, oracle):
     from mscomplex_gb300 import synth
     check_simplify(gpu_lib, oracle, synth.bumps256(), 0.05, "bumps256 t=0.05")
