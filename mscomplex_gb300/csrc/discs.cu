@@ -11,11 +11,13 @@
 // then appends every rect vertex (face) to the asc (des) disc of its owner
 // after one level of redirection (:1142-1187), and finally grows each
 // surviving saddle's discs breadth-first along the gradient (:1190-1228).
-// The device does the same in four passes: redirection per critical point,
-// a stable sort of the vertices and faces by owner (row-major order is the
-// append order), a stable sort of the cancelled-extremum seeds by saddle, and
-// one thread per surviving saddle that first counts and then writes its
-// breadth-first discs, using the output array as the queue.
+// The device does the same in four parts: redirection per critical point;
+// the extremum discs from runs of one owner along the rows, stably sorted by
+// owner (row-major order is the append order); a stable sort of the
+// cancelled-extremum seeds by saddle; and the saddle discs as interleaved
+// chains (section 4b below) placed window by window, with one thread per
+// saddle that first counts and then writes its breadth-first discs (the
+// output array as the queue) for the few saddles with more than KMAX chains.
 #include "dmsc_common.cuh"
 #include "dmsc_internal.h"
 #include "grid_types.h"
