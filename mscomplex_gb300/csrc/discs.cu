@@ -801,7 +801,7 @@ __global__ void __launch_bounds__(WIN_THREADS) k_win_place(DiscArgs a, ChainArgs
                                                            uint32_t nwin, uint32_t *__restrict__ out,
                                                            unsigned long long out_len) {
   __shared__ __align__(16) uint32_t stage[WIN];
-  __shared__ uint32_t range[2];
+  __shared__ uint32_t range[2], next_piece;
   __shared__ int dtab[16];  // packed cell id delta of step code q: [8 * (axis y) + q]
   const GridGeom &g = a.g;
   if (threadIdx.x < 16) {
@@ -825,10 +825,13 @@ __global__ void __launch_bounds__(WIN_THREADS) k_win_place(DiscArgs a, ChainArgs
       }
       range[0] = lo;
       range[1] = hi;
+      next_piece = lo + blockDim.x;
     }
     __syncthreads();
     const uint32_t lo = range[0], hi = range[1];
-    for (uint32_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+    // each thread's first piece by its index, the rest taken in turn from a
+    // shared counter, so that threads whose walks end early take more
+    for (uint32_t k = lo + threadIdx.x; k < hi; k = atomicAdd(&next_piece, 1u)) {
       const uint4 sg = c.segs[k];
       const uint32_t wl = sg.z & 0xffu, na = sg.z >> 8;
       if (!wl) continue;  // an unused slot
